@@ -1,0 +1,114 @@
+/*
+ * qll_gb300.h -- native API of libqll_gb300, beside the QLL drop-in API of
+ * qll.h.  These entry points have no counterpart in the reference; they
+ * expose what the GPU adds: several lattices at once (the reference keeps
+ * one geometry in process-global tables, lib/stagDslash.c:715-719), many
+ * right-hand sides per solve, mixed-precision solvers, status codes and a
+ * caller-chosen CUDA stream.
+ *
+ * Conventions: every int-returning call returns a negative value on failure
+ * and leaves a message in qllg_last_error(); nothing in the library calls
+ * exit().  Host arrays use the layout of qll.h (one lane, [site][nelem],
+ * even sites first).  Links of a staggered operator are 8 (one-hop) or 16
+ * (one-hop and Naik) slots; slot s = 4*mu + 2*backward + naik (with Naik) or
+ * 2*mu + backward (without), i.e. the order of createStaggeredLinks.
+ */
+#ifndef QLLG_QLL_GB300_H
+#define QLLG_QLL_GB300_H
+
+#include "qll.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+const char *qllg_last_error(void);
+void qllg_clear_error(void);
+const char *qllg_version(void);
+/* CUDA device and stream: the library launches all work on one stream,
+ * created at first use; qllg_set_stream hands it a cudaStream_t instead */
+int qllg_init(void);
+int qllg_set_stream(void *cuda_stream);
+void *qllg_get_stream(void);
+
+/* ----------------------------------------------------- input generator */
+/* SU(3) links U_mu(x) = exp(i eps H), H traceless Hermitian with Gaussian
+ * entries from a counter-based SplitMix64 keyed by (seed, site, mu,
+ * entry), optionally times the staggered phases
+ * eta_mu(x) = (-1)^(x_0+...+x_{mu-1}); u[mu] are [V][18] host arrays */
+int qllg_gen_gauge(const int dims[4], unsigned long long seed, double eps,
+                   int ks_phases, double *u[4]);
+/* Gaussian reals (unit variance) on the sites of sub ("even", "odd",
+ * "all"), nelem per site, zero elsewhere */
+int qllg_gen_source(const int dims[4], unsigned long long seed, int nelem,
+                    const char *sub, double *v);
+/* asqtad coefficients: 5/8, -1/16, 1/64, -1/384, -1/16, -1/24 */
+void qllg_asqtad_coeffs(Fat7Coeffs *c);
+
+/* ---------------------------------------------- staggered operator */
+typedef struct qllg_stag qllg_stag;
+
+enum {
+  QLLG_SOLVE_DOUBLE = 0,        /* FP64 everywhere (the reference's D path) */
+  QLLG_SOLVE_SINGLE = 1,        /* FP32 everywhere (the reference's F path) */
+  QLLG_SOLVE_MIXED_HALF = 2,    /* 16-bit storage, FP32 arithmetic, FP64
+                                   reliable updates */
+  QLLG_SOLVE_MIXED_SINGLE = 3   /* FP32 sloppy, FP64 reliable updates */
+};
+
+typedef struct {
+  int iters[16];          /* iterations per right-hand side */
+  double rsq[16];         /* final |r|^2/|b|^2 of the solver's recurrence */
+  double true_rsq[16];    /* |b - A x|^2/|b|^2 recomputed in FP64 */
+  int reliable_updates;
+  int total_iters;        /* iterations of the batch (max over rhs) */
+  double seconds;         /* device time of the solve */
+} qllg_solve_info;
+
+/* links: fat[8], lng[8] host arrays [V][18]; slot 2i of the reference's
+ * createStaggeredLinks is fat[i], slot 2i+1 is lng[i]; lng NULL means no
+ * Naik term.  The links are copied to the GPU. */
+qllg_stag *qllg_stag_create(const int dims[4], double *const fat[8], double *const lng[8]);
+qllg_stag *qllg_stag_create_f(const int dims[4], float *const fat[8], float *const lng[8]);
+void qllg_stag_destroy(qllg_stag *S);
+size_t qllg_stag_device_bytes(const qllg_stag *S);
+
+/* x = mass*y + D y on the sites of sub (dslash2 semantics; "even"/"odd"
+ * ignore the mass); host arrays [V][6] of the precision of the operator */
+int qllg_stag_dslash(qllg_stag *S, void *x, double mass, const void *y, const char *sub);
+
+/* solve (m_r^2 - D_eo D_oe) x_r = b_r on even sites for nrhs right-hand
+ * sides (nrhs <= 16) in the requested precision mode; host arrays of
+ * [V][6] reals of the operator's precision (only the even half is read and
+ * written); stops when |r|^2 < rsq |b|^2 or after maxits iterations. */
+int qllg_stag_solve(qllg_stag *S, int nrhs, void *const x[], void *const b[],
+                    const double mass[], double rsq, int maxits, int mode,
+                    qllg_solve_info *info);
+/* the same with device buffers: b and x are FP64 device arrays in the
+ * library's multi-rhs layout ([3][Vh][nrhs] double2), inputs resident */
+int qllg_stag_solve_device(qllg_stag *S, int nrhs, void *x_dev, const void *b_dev,
+                           const double mass[], double rsq, int maxits, int mode,
+                           qllg_solve_info *info);
+/* allocate / free a device even-site FP64 vector of nrhs rhs and fill it
+ * from host arrays (or copy it back) */
+void *qllg_stag_vec_alloc(qllg_stag *S, int nrhs);
+void qllg_stag_vec_free(void *v);
+int qllg_stag_vec_upload(qllg_stag *S, void *v_dev, int nrhs, void *const h[]);
+int qllg_stag_vec_download(qllg_stag *S, const void *v_dev, int nrhs, void *const h[]);
+
+/* neighbour table of slot s for the output sites of a parity, as QLL site
+ * indices (host int[V/2]); the GPU computes it with the Dslash kernel's own
+ * index arithmetic */
+int qllg_stag_nbr_table(const int dims[4], int parity, int slot, int *host_out);
+
+/* kernel timing: when enabled, launches of the named kernel family are
+ * bracketed by CUDA events on the library stream; read returns the count
+ * and total milliseconds since the last reset */
+void qllg_timing_enable(int on);
+void qllg_timing_reset(void);
+int qllg_timing_read(const char *name, int *count, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,540 @@
+// k_blas.cu -- streaming vector kernels of the solvers (sm_103a):
+// layout transposes between the reference's host layout and the device
+// layout, precision conversion, axpby, norms with the deterministic grid
+// reduction, and the fused CG update steps of cgSolveT (lib/cg.c:77-115).
+#include "kcommon.cuh"
+
+using namespace qk;
+
+namespace {
+
+constexpr int kT = 256;
+
+size_t g_max_grid = 0;
+
+int grid_for(size_t total, const void *fn, qllg_redbuf *rb)
+{
+  (void)fn;
+  if(!g_max_grid) g_max_grid = (size_t)qllg_num_sms()*8;
+  size_t need = (total + kT - 1)/kT;
+  size_t g = need < g_max_grid ? need : g_max_grid;
+  if(rb && g > (size_t)rb->maxblocks) g = rb->maxblocks;
+  return g < 1 ? 1 : (int)g;
+}
+
+#define GRID_LOOP(t, total) \
+  for(size_t t = (size_t)blockIdx.x*blockDim.x + threadIdx.x; t < (total); \
+      t += (size_t)gridDim.x*blockDim.x)
+
+// ------------------------------------------------------------ transposes
+template <int P, int NC, typename S>
+__global__ void from_aos(void *dev, const S *stage, int nsites, int nrhs, size_t rstride)
+{
+  typedef typename Real<P>::T T;
+  size_t total = (size_t)nsites*nrhs;
+  GRID_LOOP(t, total) {
+    int site = (int)(t / nrhs), rhs = (int)(t % nrhs);
+    const S *src = stage + rhs*rstride + (size_t)site*2*NC;
+    Cx<T> v[NC];
+#pragma unroll
+    for(int c=0; c<NC; c++) { v[c].r = (T)src[2*c]; v[c].i = (T)src[2*c+1]; }
+    SpinorIO<P,NC>::store(dev, total, t, v);
+  }
+}
+
+template <int P, int NC, typename S>
+__global__ void to_aos(const void *dev, S *stage, int nsites, int nrhs, size_t rstride)
+{
+  typedef typename Calc<P,P>::T T;
+  size_t total = (size_t)nsites*nrhs;
+  GRID_LOOP(t, total) {
+    int site = (int)(t / nrhs), rhs = (int)(t % nrhs);
+    S *dst = stage + rhs*rstride + (size_t)site*2*NC;
+    Cx<T> v[NC];
+    SpinorIO<P,NC>::load(dev, total, t, v);
+#pragma unroll
+    for(int c=0; c<NC; c++) { dst[2*c] = (S)v[c].r; dst[2*c+1] = (S)v[c].i; }
+  }
+}
+
+template <int PO, int PI, int NC>
+__global__ void convert_k(void *out, const void *in, int nsites, int nrhs, const int *active)
+{
+  typedef typename Calc<PO,PI>::T T;
+  size_t total = (size_t)nsites*nrhs;
+  GRID_LOOP(t, total) {
+    if(active && !active[t % nrhs]) continue;
+    Cx<T> v[NC];
+    SpinorIO<PI,NC>::load(in, total, t, v);
+    SpinorIO<PO,NC>::store(out, total, t, v);
+  }
+}
+
+// --------------------------------------------------------------- links
+template <typename S>
+__global__ void link_maxabs(const S *stage, int V, unsigned *mx)
+{
+  float m = 0.f;
+  size_t total = (size_t)V*18;
+  GRID_LOOP(t, total) m = fmaxf(m, fabsf((float)stage[t]));
+  for(int o=16; o>0; o>>=1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if((threadIdx.x & 31) == 0) atomicMax(mx, __float_as_uint(m));
+}
+
+template <int P, typename S>
+__global__ void link_from_aos(void *dev, const float *scale, const S *stage, int V)
+{
+  GRID_LOOP(i, (size_t)V) {
+    const S *m = stage + i*18;
+    if(P == QLLG_F64) {
+      double2 *d = (double2 *)dev;
+#pragma unroll
+      for(int k=0; k<9; k++) d[k*(size_t)V + i] = make_double2((double)m[2*k], (double)m[2*k+1]);
+    } else if(P == QLLG_F32) {
+      float2 *d = (float2 *)dev;
+#pragma unroll
+      for(int k=0; k<9; k++) d[k*(size_t)V + i] = make_float2((float)m[2*k], (float)m[2*k+1]);
+    } else {
+      float s = *scale;
+      float inv = s > 0.f ? 32767.0f/s : 0.f;
+      uint32_t w[9];
+#pragma unroll
+      for(int k=0; k<9; k++) w[k] = pack_s16((float)m[2*k]*inv, (float)m[2*k+1]*inv);
+      char *b = (char *)dev;
+      ((int4 *)b)[i] = make_int4((int)w[0], (int)w[1], (int)w[2], (int)w[3]);
+      ((int4 *)(b + 16*(size_t)V))[i] = make_int4((int)w[4], (int)w[5], (int)w[6], (int)w[7]);
+      ((int *)(b + 32*(size_t)V))[i] = (int)w[8];
+    }
+  }
+}
+
+template <typename S>
+__global__ void link_to_aos(const double *dev, S *stage, int V)
+{
+  const double2 *d = (const double2 *)dev;
+  GRID_LOOP(i, (size_t)V) {
+    S *m = stage + i*18;
+#pragma unroll
+    for(int k=0; k<9; k++) { double2 t = d[k*(size_t)V + i]; m[2*k] = (S)t.x; m[2*k+1] = (S)t.y; }
+  }
+}
+
+__global__ void link_f64_maxabs(const double *dev, int V, unsigned *mx)
+{
+  float m = 0.f;
+  GRID_LOOP(t, (size_t)V*18) m = fmaxf(m, (float)fabs(dev[t]));
+  for(int o=16; o>0; o>>=1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if((threadIdx.x & 31) == 0) atomicMax(mx, __float_as_uint(m));
+}
+
+template <int P>
+__global__ void link_from_f64(void *dev, const float *scale, const double *in, int V)
+{
+  const double2 *d = (const double2 *)in;
+  GRID_LOOP(i, (size_t)V) {
+    double2 e[9];
+#pragma unroll
+    for(int k=0; k<9; k++) e[k] = d[k*(size_t)V + i];
+    if(P == QLLG_F32) {
+      float2 *o = (float2 *)dev;
+#pragma unroll
+      for(int k=0; k<9; k++) o[k*(size_t)V + i] = make_float2((float)e[k].x, (float)e[k].y);
+    } else {
+      float s = *scale;
+      float inv = s > 0.f ? 32767.0f/s : 0.f;
+      uint32_t w[9];
+#pragma unroll
+      for(int k=0; k<9; k++) w[k] = pack_s16((float)e[k].x*inv, (float)e[k].y*inv);
+      char *b = (char *)dev;
+      ((int4 *)b)[i] = make_int4((int)w[0], (int)w[1], (int)w[2], (int)w[3]);
+      ((int4 *)(b + 16*(size_t)V))[i] = make_int4((int)w[4], (int)w[5], (int)w[6], (int)w[7]);
+      ((int *)(b + 32*(size_t)V))[i] = (int)w[8];
+    }
+  }
+}
+
+// ------------------------------------------------------------ axpby/norm
+template <int PY, int PX, int NC, int NR>
+__global__ void axpby_k(void *y, const void *x, const double *a, double a0,
+                        const double *b, double b0, int nsites, const int *active)
+{
+  typedef typename Calc<PY,PX>::T T;
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(active && !active[rhs]) return;
+  const T ca = (T)(a ? a[rhs] : a0), cb = (T)(b ? b[rhs] : b0);
+  GRID_LOOP(t, total) {
+    Cx<T> yv[NC], xv[NC];
+    SpinorIO<PX,NC>::load(x, total, t, xv);
+    if(ca != (T)0) {
+      SpinorIO<PY,NC>::load(y, total, t, yv);
+#pragma unroll
+      for(int c=0; c<NC; c++) { yv[c].r = fma(cb, xv[c].r, ca*yv[c].r); yv[c].i = fma(cb, xv[c].i, ca*yv[c].i); }
+    } else {
+#pragma unroll
+      for(int c=0; c<NC; c++) { yv[c].r = cb*xv[c].r; yv[c].i = cb*xv[c].i; }
+    }
+    SpinorIO<PY,NC>::store(y, total, t, yv);
+  }
+}
+
+// y = y + b x, the exact form of X_veq_X_plus_r_times_X (lib/vla.c:767-786)
+template <int P, int NC, int NR>
+__global__ void xpay_k(void *y, const void *x, const double *b, double b0, double bsign,
+                       int nsites, const int *active)
+{
+  typedef typename Calc<P,P>::T T;
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(active && !active[rhs]) return;
+  const T cb = (T)(bsign*(b ? b[rhs] : b0));
+  GRID_LOOP(t, total) {
+    Cx<T> yv[NC], xv[NC];
+    SpinorIO<P,NC>::load(x, total, t, xv);
+    SpinorIO<P,NC>::load(y, total, t, yv);
+#pragma unroll
+    for(int c=0; c<NC; c++) { yv[c].r = fma(cb, xv[c].r, yv[c].r); yv[c].i = fma(cb, xv[c].i, yv[c].i); }
+    SpinorIO<P,NC>::store(y, total, t, yv);
+  }
+}
+
+template <int P, int NC, int NR>
+__global__ void __launch_bounds__(kT) norm2_k(const void *x, int nsites, double *out,
+                                               double *partial, unsigned *counter)
+{
+  typedef typename Calc<P,P>::T T;
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  double red[1] = {0};
+  GRID_LOOP(t, total) {
+    Cx<T> v[NC];
+    SpinorIO<P,NC>::load(x, total, t, v);
+#pragma unroll
+    for(int c=0; c<NC; c++) red[0] += (double)v[c].r*v[c].r + (double)v[c].i*v[c].i;
+  }
+  double *res[1] = {out};
+  grid_reduce<1>(red, NR, threadIdx.x % NR, partial, counter, shm, res);
+}
+
+// --------------------------------------------------------------- CG steps
+template <int P, int NC, int NR>
+__global__ void __launch_bounds__(kT) cg_init_k(void *x, void *r, void *p, const void *b,
+                                                 int nsites, qllg_cg_scalars *s,
+                                                 double *partial, unsigned *counter)
+{
+  typedef typename Calc<P,P>::T T;
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  double red[1] = {0};
+  GRID_LOOP(t, total) {
+    Cx<T> v[NC], z[NC];
+    SpinorIO<P,NC>::load(b, total, t, v);
+#pragma unroll
+    for(int c=0; c<NC; c++) { z[c].r = 0; z[c].i = 0; red[0] += (double)v[c].r*v[c].r + (double)v[c].i*v[c].i; }
+    SpinorIO<P,NC>::store(r, total, t, v);
+    SpinorIO<P,NC>::store(x, total, t, z);
+    SpinorIO<P,NC>::store(p, total, t, z);
+  }
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, threadIdx.x % NR, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int any = 0;
+      for(int q=0; q<NR; q++) {
+        double bs = s->tmp[q];
+        s->bsq[q] = bs;
+        s->rsq[q] = bs;
+        s->rsq_stop[q] *= bs;
+        s->iters[q] = 0;
+        s->active[q] = (bs > 0 && s->maxits > 0) ? 1 : 0;
+        any |= s->active[q];
+      }
+      s->done = !any;
+      s->count = 0;
+    }
+  }
+}
+
+template <int P, int NC, int NR>
+__global__ void __launch_bounds__(kT) cg_xr_k(void *x, void *r, const void *p, const void *Ap,
+                                               int nsites, qllg_cg_scalars *s,
+                                               double *partial, unsigned *counter)
+{
+  typedef typename Calc<P,P>::T T;
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  const bool skip = *(volatile int *)&s->done;
+  double red[1] = {0};
+  if(!skip && s->active[rhs]) {
+    const T alpha = (T)(1.0/(s->mass2[rhs]*s->pnorm[rhs] + s->vnorm[rhs]));
+    GRID_LOOP(t, total) {
+      Cx<T> xv[NC], rv[NC], pv[NC], av[NC];
+      SpinorIO<P,NC>::load(x, total, t, xv);
+      SpinorIO<P,NC>::load(r, total, t, rv);
+      SpinorIO<P,NC>::load(p, total, t, pv);
+      SpinorIO<P,NC>::load(Ap, total, t, av);
+#pragma unroll
+      for(int c=0; c<NC; c++) {
+        xv[c].r = fma(alpha, pv[c].r, xv[c].r); xv[c].i = fma(alpha, pv[c].i, xv[c].i);
+        rv[c].r = fma(-alpha, av[c].r, rv[c].r); rv[c].i = fma(-alpha, av[c].i, rv[c].i);
+        red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
+      }
+      SpinorIO<P,NC>::store(x, total, t, xv);
+      SpinorIO<P,NC>::store(r, total, t, rv);
+    }
+  }
+  if(skip) return;   // uniform over the grid
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int any = 0;
+      for(int q=0; q<NR; q++) {
+        if(s->active[q]) {
+          s->rsq[q] = s->tmp[q];
+          s->iters[q]++;
+          if(!(s->rsq[q] >= s->rsq_stop[q] && s->iters[q] < s->maxits)) s->active[q] = 0;
+        }
+        any |= s->active[q];
+      }
+      s->done = !any;
+      s->count++;
+    }
+  }
+}
+
+template <int P, int NC, int NR>
+__global__ void cg_p_k(void *p, const void *r, int nsites, qllg_cg_scalars *s)
+{
+  typedef typename Calc<P,P>::T T;
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->done || !s->active[rhs]) return;
+  const T beta = (T)(1.0/s->rsq[rhs]);
+  GRID_LOOP(t, total) {
+    Cx<T> pv[NC], rv[NC];
+    SpinorIO<P,NC>::load(p, total, t, pv);
+    SpinorIO<P,NC>::load(r, total, t, rv);
+#pragma unroll
+    for(int c=0; c<NC; c++) { pv[c].r = fma(beta, rv[c].r, pv[c].r); pv[c].i = fma(beta, rv[c].i, pv[c].i); }
+    SpinorIO<P,NC>::store(p, total, t, pv);
+  }
+}
+
+// ---------------------------------------------------------- dispatch
+#define NR_SWITCH(nrhs, ...) \
+  switch(nrhs) { \
+  case 1: { constexpr int NR = 1; __VA_ARGS__; } break; \
+  case 2: { constexpr int NR = 2; __VA_ARGS__; } break; \
+  case 4: { constexpr int NR = 4; __VA_ARGS__; } break; \
+  case 8: { constexpr int NR = 8; __VA_ARGS__; } break; \
+  case 16: { constexpr int NR = 16; __VA_ARGS__; } break; \
+  default: qllg_set_error("nrhs %d not in {1,2,4,8,16}", nrhs); return -1; }
+
+// precision x colour count for kernels on one field type
+#define PN_SWITCH(prec, ncomp, ...) \
+  if(prec == QLLG_F64 && ncomp == 3) { constexpr int P = QLLG_F64, NC = 3; __VA_ARGS__; } \
+  else if(prec == QLLG_F32 && ncomp == 3) { constexpr int P = QLLG_F32, NC = 3; __VA_ARGS__; } \
+  else if(prec == QLLG_I16 && ncomp == 3) { constexpr int P = QLLG_I16, NC = 3; __VA_ARGS__; } \
+  else if(prec == QLLG_F64 && ncomp == 12) { constexpr int P = QLLG_F64, NC = 12; __VA_ARGS__; } \
+  else if(prec == QLLG_F32 && ncomp == 12) { constexpr int P = QLLG_F32, NC = 12; __VA_ARGS__; } \
+  else { qllg_set_error("unsupported precision %d / components %d", prec, ncomp); return -1; }
+
+int done(const char *what) { return qllg_check_cuda(cudaGetLastError(), what); }
+
+} // namespace
+
+extern "C" int
+qllg_k_spinor_from_aos(int prec, void *dev, const void *stage, int dbl, int nsites, int ncomp,
+                       int nrhs, size_t rs)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, 0);
+  cudaStream_t st = qllg_stream();
+  PN_SWITCH(prec, ncomp, {
+    if(dbl) from_aos<P,NC,double><<<g,kT,0,st>>>(dev, (const double *)stage, nsites, nrhs, rs);
+    else from_aos<P,NC,float><<<g,kT,0,st>>>(dev, (const float *)stage, nsites, nrhs, rs);
+  });
+  return done("from_aos");
+}
+
+extern "C" int
+qllg_k_spinor_to_aos(int prec, const void *dev, void *stage, int dbl, int nsites, int ncomp,
+                     int nrhs, size_t rs)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, 0);
+  cudaStream_t st = qllg_stream();
+  PN_SWITCH(prec, ncomp, {
+    if(dbl) to_aos<P,NC,double><<<g,kT,0,st>>>(dev, (double *)stage, nsites, nrhs, rs);
+    else to_aos<P,NC,float><<<g,kT,0,st>>>(dev, (float *)stage, nsites, nrhs, rs);
+  });
+  return done("to_aos");
+}
+
+extern "C" int
+qllg_k_spinor_convert(int po, void *out, int pi, const void *in, int nsites, int ncomp,
+                      int nrhs, const int *active)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, 0);
+  cudaStream_t st = qllg_stream();
+#define CONV(A,B) if(po == A && pi == B) { \
+    if(ncomp == 3) convert_k<A,B,3><<<g,kT,0,st>>>(out, in, nsites, nrhs, active); \
+    else if(ncomp == 12 && A != QLLG_I16 && B != QLLG_I16) \
+      convert_k<(A==QLLG_I16?QLLG_F32:A),(B==QLLG_I16?QLLG_F32:B),12><<<g,kT,0,st>>>(out, in, nsites, nrhs, active); \
+    else { qllg_set_error("convert: components %d", ncomp); return -1; } \
+    return done("convert"); }
+  CONV(QLLG_F64, QLLG_F64) CONV(QLLG_F64, QLLG_F32) CONV(QLLG_F64, QLLG_I16)
+  CONV(QLLG_F32, QLLG_F64) CONV(QLLG_F32, QLLG_F32) CONV(QLLG_F32, QLLG_I16)
+  CONV(QLLG_I16, QLLG_F64) CONV(QLLG_I16, QLLG_F32) CONV(QLLG_I16, QLLG_I16)
+#undef CONV
+  qllg_set_error("convert: precisions %d <- %d", po, pi);
+  return -1;
+}
+
+extern "C" int
+qllg_k_link_from_aos(int prec, void *dev, float *scale, const void *stage, int dbl, int V)
+{
+  cudaStream_t st = qllg_stream();
+  int g = grid_for((size_t)V, 0, 0);
+  if(prec == QLLG_I16) {
+    if(qllg_check_cuda(cudaMemsetAsync(scale, 0, sizeof(float), st), "memset")) return -1;
+    int g2 = grid_for((size_t)V*18, 0, 0);
+    if(dbl) link_maxabs<double><<<g2,kT,0,st>>>((const double *)stage, V, (unsigned *)scale);
+    else link_maxabs<float><<<g2,kT,0,st>>>((const float *)stage, V, (unsigned *)scale);
+  }
+#define LF(P) if(prec == P) { \
+    if(dbl) link_from_aos<P,double><<<g,kT,0,st>>>(dev, scale, (const double *)stage, V); \
+    else link_from_aos<P,float><<<g,kT,0,st>>>(dev, scale, (const float *)stage, V); \
+    return done("link_from_aos"); }
+  LF(QLLG_F64) LF(QLLG_F32) LF(QLLG_I16)
+#undef LF
+  qllg_set_error("link_from_aos: precision %d", prec);
+  return -1;
+}
+
+extern "C" int
+qllg_k_link_to_aos(const double *dev, void *stage, int dbl, int V)
+{
+  int g = grid_for((size_t)V, 0, 0);
+  if(dbl) link_to_aos<double><<<g,kT,0,qllg_stream()>>>(dev, (double *)stage, V);
+  else link_to_aos<float><<<g,kT,0,qllg_stream()>>>(dev, (float *)stage, V);
+  return done("link_to_aos");
+}
+
+extern "C" int
+qllg_k_link_convert(int prec, void *out, float *scale, const double *in, int V)
+{
+  cudaStream_t st = qllg_stream();
+  int g = grid_for((size_t)V, 0, 0);
+  if(prec == QLLG_F32) {
+    link_from_f64<QLLG_F32><<<g,kT,0,st>>>(out, scale, in, V);
+  } else if(prec == QLLG_I16) {
+    if(qllg_check_cuda(cudaMemsetAsync(scale, 0, sizeof(float), st), "memset")) return -1;
+    link_f64_maxabs<<<grid_for((size_t)V*18, 0, 0),kT,0,st>>>(in, V, (unsigned *)scale);
+    link_from_f64<QLLG_I16><<<g,kT,0,st>>>(out, scale, in, V);
+  } else {
+    qllg_set_error("link_convert: precision %d", prec);
+    return -1;
+  }
+  return done("link_convert");
+}
+
+extern "C" int
+qllg_k_axpby(int py, void *y, int px, const void *x, const double *a, double a0,
+             const double *b, double b0, int nsites, int ncomp, int nrhs, const int *active)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, 0);
+  cudaStream_t st = qllg_stream();
+#define AX(A,B) if(py == A && px == B) { \
+    if(ncomp == 3) { NR_SWITCH(nrhs, (axpby_k<A,B,3,NR><<<g,kT,0,st>>>(y, x, a, a0, b, b0, nsites, active))); } \
+    else if(ncomp == 12 && A != QLLG_I16 && B != QLLG_I16) { \
+      NR_SWITCH(nrhs, (axpby_k<(A==QLLG_I16?QLLG_F32:A),(B==QLLG_I16?QLLG_F32:B),12,NR><<<g,kT,0,st>>>(y, x, a, a0, b, b0, nsites, active))); } \
+    else { qllg_set_error("axpby: components %d", ncomp); return -1; } \
+    return done("axpby"); }
+  AX(QLLG_F64, QLLG_F64) AX(QLLG_F64, QLLG_F32) AX(QLLG_F32, QLLG_F32)
+  AX(QLLG_F32, QLLG_F64) AX(QLLG_I16, QLLG_I16) AX(QLLG_F32, QLLG_I16) AX(QLLG_I16, QLLG_F32)
+#undef AX
+  qllg_set_error("axpby: precisions %d <- %d", py, px);
+  return -1;
+}
+
+extern "C" int
+qllg_k_xpay(int prec, void *y, const void *x, const double *b, double b0, double bsign,
+            int nsites, int ncomp, int nrhs, const int *active)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, 0);
+  cudaStream_t st = qllg_stream();
+  PN_SWITCH(prec, ncomp, {
+    NR_SWITCH(nrhs, (xpay_k<P,NC,NR><<<g,kT,0,st>>>(y, x, b, b0, bsign, nsites, active)));
+  });
+  return done("xpay");
+}
+
+extern "C" int
+qllg_k_norm2(int prec, const void *x, int nsites, int ncomp, int nrhs, double *out,
+             qllg_redbuf *rb)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, rb);
+  cudaStream_t st = qllg_stream();
+  PN_SWITCH(prec, ncomp, {
+    NR_SWITCH(nrhs, (norm2_k<P,NC,NR><<<g,kT,0,st>>>(x, nsites, out, rb->partial, rb->counter)));
+  });
+  return done("norm2");
+}
+
+extern "C" int
+qllg_k_zero(int prec, void *x, int nsites, int ncomp, int nrhs)
+{
+  return qllg_k_axpby(prec, x, prec, x, NULL, 0.0, NULL, 0.0, nsites, ncomp, nrhs, NULL);
+}
+
+extern "C" int
+qllg_k_copy(int prec, void *y, const void *x, int nsites, int ncomp, int nrhs)
+{
+  return qllg_k_axpby(prec, y, prec, x, NULL, 0.0, NULL, 1.0, nsites, ncomp, nrhs, NULL);
+}
+
+extern "C" int
+qllg_k_cg_init(int prec, void *x, void *r, void *p, const void *b, int nsites, int ncomp,
+               int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, rb);
+  cudaStream_t st = qllg_stream();
+  PN_SWITCH(prec, ncomp, {
+    NR_SWITCH(nrhs, (cg_init_k<P,NC,NR><<<g,kT,0,st>>>(x, r, p, b, nsites, s, rb->partial, rb->counter)));
+  });
+  return done("cg_init");
+}
+
+extern "C" int
+qllg_k_cg_update_xr(int prec, void *x, void *r, const void *p, const void *Ap, int nsites,
+                    int ncomp, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, rb);
+  cudaStream_t st = qllg_stream();
+  PN_SWITCH(prec, ncomp, {
+    NR_SWITCH(nrhs, (cg_xr_k<P,NC,NR><<<g,kT,0,st>>>(x, r, p, Ap, nsites, s, rb->partial, rb->counter)));
+  });
+  return done("cg_update_xr");
+}
+
+extern "C" int
+qllg_k_cg_update_p(int prec, void *p, const void *r, int nsites, int ncomp, int nrhs,
+                   qllg_cg_scalars *s)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, 0);
+  cudaStream_t st = qllg_stream();
+  PN_SWITCH(prec, ncomp, {
+    NR_SWITCH(nrhs, (cg_p_k<P,NC,NR><<<g,kT,0,st>>>(p, r, nsites, s)));
+  });
+  return done("cg_update_p");
+}

@@ -1,0 +1,279 @@
+// k_mixed.cu -- kernels of the mixed-precision (reliable-update) CG:
+// the sloppy recurrence runs in 16-bit or FP32 storage with FP32
+// arithmetic, and the flagged right-hand sides periodically replace the
+// sloppy residual by the FP64 true residual b - A x (Clark et al., "Solving
+// Lattice QCD systems of equations using mixed precision solvers on GPUs",
+// Comput. Phys. Commun. 181 (2010) 1517, the reliable-update scheme of
+// Sleijpen and van der Vorst).  The recurrence itself is cgSolveT's scaled
+// form (lib/cg.c:77-115): p += r/|r|^2, a = 1/<p,Ap>.
+#include "kcommon.cuh"
+
+using namespace qk;
+
+namespace {
+
+constexpr int kT = 256;
+
+#define GRID_LOOP(t, total) \
+  for(size_t t = (size_t)blockIdx.x*blockDim.x + threadIdx.x; t < (total); \
+      t += (size_t)gridDim.x*blockDim.x)
+
+int grid_for(size_t total, qllg_redbuf *rb)
+{
+  size_t g = (total + kT - 1)/kT, m = (size_t)qllg_num_sms()*8;
+  if(g > m) g = m;
+  if(rb && g > (size_t)rb->maxblocks) g = rb->maxblocks;
+  return g < 1 ? 1 : (int)g;
+}
+
+template <int PX, int PS, int NR>
+__global__ void __launch_bounds__(kT)
+mcg_init_k(void *x64, void *r64, void *xs, void *rs, void *p, const void *b, int nsites,
+           qllg_cg_scalars *s, double *partial, unsigned *counter)
+{
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  double red[1] = {0};
+  GRID_LOOP(t, total) {
+    Cx<double> v[3], z[3];
+    SpinorIO<QLLG_F64,3>::load(b, total, t, v);
+#pragma unroll
+    for(int c=0; c<3; c++) { z[c].r = 0; z[c].i = 0; red[0] += v[c].r*v[c].r + v[c].i*v[c].i; }
+    SpinorIO<QLLG_F64,3>::store(r64, total, t, v);
+    SpinorIO<QLLG_F64,3>::store(x64, total, t, z);
+    Cx<float> vf[3], zf[3];
+#pragma unroll
+    for(int c=0; c<3; c++) { vf[c].r = (float)v[c].r; vf[c].i = (float)v[c].i; zf[c].r = 0; zf[c].i = 0; }
+    SpinorIO<PS,3>::store(rs, total, t, vf);
+    SpinorIO<PX,3>::store(xs, total, t, zf);
+    SpinorIO<PS,3>::store(p, total, t, zf);
+  }
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, threadIdx.x % NR, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int any = 0;
+      for(int q=0; q<NR; q++) {
+        double bs = s->tmp[q];
+        s->bsq[q] = bs; s->rsq[q] = bs; s->maxr2[q] = bs;
+        s->rsq_stop[q] *= bs;
+        s->iters[q] = 0; s->ru[q] = 0; s->nru[q] = 0;
+        s->active[q] = (bs > 0 && s->maxits > 0) ? 1 : 0;
+        any |= s->active[q];
+      }
+      s->done = !any;
+      s->no_ru = 1;
+      s->count = 0;
+    }
+  }
+}
+
+template <int PS, int NR>
+__global__ void mcg_p_k(void *p, const void *rs, int nsites, qllg_cg_scalars *s)
+{
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->done || !s->active[rhs]) return;
+  const float beta = (float)(1.0/s->rsq[rhs]);
+  GRID_LOOP(t, total) {
+    Cx<float> pv[3], rv[3];
+    SpinorIO<PS,3>::load(p, total, t, pv);
+    SpinorIO<PS,3>::load(rs, total, t, rv);
+#pragma unroll
+    for(int c=0; c<3; c++) { pv[c].r = fmaf(beta, rv[c].r, pv[c].r); pv[c].i = fmaf(beta, rv[c].i, pv[c].i); }
+    SpinorIO<PS,3>::store(p, total, t, pv);
+  }
+}
+
+template <int PX, int PS, int NR>
+__global__ void __launch_bounds__(kT)
+mcg_update_k(void *xs, void *rs, const void *p, const void *Ap, int nsites,
+             qllg_cg_scalars *s, double *partial, unsigned *counter)
+{
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  const bool skip = *(volatile int *)&s->done;
+  if(skip) return;
+  double red[1] = {0};
+  if(s->active[rhs]) {
+    const float alpha = (float)(1.0/(s->mass2[rhs]*s->pnorm[rhs] + s->vnorm[rhs]));
+    GRID_LOOP(t, total) {
+      Cx<float> xv[3], rv[3], pv[3], av[3];
+      SpinorIO<PX,3>::load(xs, total, t, xv);
+      SpinorIO<PS,3>::load(rs, total, t, rv);
+      SpinorIO<PS,3>::load(p, total, t, pv);
+      SpinorIO<PS,3>::load(Ap, total, t, av);
+#pragma unroll
+      for(int c=0; c<3; c++) {
+        xv[c].r = fmaf(alpha, pv[c].r, xv[c].r); xv[c].i = fmaf(alpha, pv[c].i, xv[c].i);
+        rv[c].r = fmaf(-alpha, av[c].r, rv[c].r); rv[c].i = fmaf(-alpha, av[c].i, rv[c].i);
+        red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
+      }
+      SpinorIO<PX,3>::store(xs, total, t, xv);
+      SpinorIO<PS,3>::store(rs, total, t, rv);
+    }
+  }
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int anyru = 0;
+      for(int q=0; q<NR; q++) {
+        s->ru[q] = 0;
+        if(!s->active[q]) continue;
+        double r2 = s->tmp[q];
+        s->iters[q]++;
+        s->rsq[q] = r2;
+        if(r2 < s->delta2*s->maxr2[q] || r2 < s->rsq_stop[q] || s->iters[q] >= s->maxits ||
+           !(r2 == r2)) {
+          s->ru[q] = 1;
+          anyru = 1;
+        }
+      }
+      s->no_ru = !anyru;
+      s->count++;
+    }
+  }
+}
+
+template <int PX, int NR>
+__global__ void mcg_accum_k(void *x64, void *xs, int nsites, qllg_cg_scalars *s)
+{
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->no_ru || !s->ru[rhs]) return;
+  GRID_LOOP(t, total) {
+    Cx<double> xv[3];
+    Cx<float> sv[3], z[3];
+    SpinorIO<QLLG_F64,3>::load(x64, total, t, xv);
+    SpinorIO<PX,3>::load(xs, total, t, sv);
+#pragma unroll
+    for(int c=0; c<3; c++) { xv[c].r += sv[c].r; xv[c].i += sv[c].i; z[c].r = 0; z[c].i = 0; }
+    SpinorIO<QLLG_F64,3>::store(x64, total, t, xv);
+    SpinorIO<PX,3>::store(xs, total, t, z);
+  }
+}
+
+template <int PS, int NR>
+__global__ void __launch_bounds__(kT)
+mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites,
+               qllg_cg_scalars *s, double *partial, unsigned *counter)
+{
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->no_ru) return;   // uniform: written by the previous kernel
+  double red[1] = {0};
+  if(s->ru[rhs]) {
+    GRID_LOOP(t, total) {
+      Cx<double> bv[3], tv[3];
+      SpinorIO<QLLG_F64,3>::load(b, total, t, bv);
+      SpinorIO<QLLG_F64,3>::load(t64, total, t, tv);
+      Cx<float> f[3];
+#pragma unroll
+      for(int c=0; c<3; c++) {
+        tv[c].r = bv[c].r - tv[c].r; tv[c].i = bv[c].i - tv[c].i;
+        red[0] += tv[c].r*tv[c].r + tv[c].i*tv[c].i;
+        f[c].r = (float)tv[c].r; f[c].i = (float)tv[c].i;
+      }
+      SpinorIO<QLLG_F64,3>::store(r64, total, t, tv);
+      SpinorIO<PS,3>::store(rs, total, t, f);
+    }
+  }
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int any = 0;
+      for(int q=0; q<NR; q++) {
+        if(s->ru[q]) {
+          double r2 = s->tmp[q];
+          s->rsq[q] = r2;
+          s->maxr2[q] = r2;
+          s->nru[q]++;
+          if(!(r2 >= s->rsq_stop[q] && s->iters[q] < s->maxits)) s->active[q] = 0;
+          s->ru[q] = 0;
+        }
+        any |= s->active[q];
+      }
+      s->no_ru = 1;
+      s->done = !any;
+    }
+  }
+}
+
+#define NR_SWITCH(nrhs, ...) \
+  switch(nrhs) { \
+  case 1: { constexpr int NR = 1; __VA_ARGS__; } break; \
+  case 2: { constexpr int NR = 2; __VA_ARGS__; } break; \
+  case 4: { constexpr int NR = 4; __VA_ARGS__; } break; \
+  case 8: { constexpr int NR = 8; __VA_ARGS__; } break; \
+  case 16: { constexpr int NR = 16; __VA_ARGS__; } break; \
+  default: qllg_set_error("nrhs %d not in {1,2,4,8,16}", nrhs); return -1; }
+
+#define PXS_SWITCH(px, ps, ...) \
+  if(px == QLLG_F32 && ps == QLLG_I16) { constexpr int PX = QLLG_F32, PS = QLLG_I16; __VA_ARGS__; } \
+  else if(px == QLLG_F32 && ps == QLLG_F32) { constexpr int PX = QLLG_F32, PS = QLLG_F32; __VA_ARGS__; } \
+  else if(px == QLLG_I16 && ps == QLLG_I16) { constexpr int PX = QLLG_I16, PS = QLLG_I16; __VA_ARGS__; } \
+  else { qllg_set_error("mixed CG: precisions %d/%d", px, ps); return -1; }
+
+int done(const char *w) { return qllg_check_cuda(cudaGetLastError(), w); }
+
+} // namespace
+
+extern "C" int
+qllg_k_mcg_init(int px, int ps, void *x64, void *r64, void *xs, void *rs, void *p,
+                const void *b, int nsites, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  PXS_SWITCH(px, ps, NR_SWITCH(nrhs, (mcg_init_k<PX,PS,NR><<<g,kT,0,st>>>(x64, r64, xs, rs, p, b,
+                                      nsites, s, rb->partial, rb->counter))));
+  return done("mcg_init");
+}
+
+extern "C" int
+qllg_k_mcg_update_p(int ps, void *p, const void *rs, int nsites, int nrhs, qllg_cg_scalars *s)
+{
+  int g = grid_for((size_t)nsites*nrhs, 0);
+  cudaStream_t st = qllg_stream();
+  if(ps == QLLG_I16) { NR_SWITCH(nrhs, (mcg_p_k<QLLG_I16,NR><<<g,kT,0,st>>>(p, rs, nsites, s))); }
+  else if(ps == QLLG_F32) { NR_SWITCH(nrhs, (mcg_p_k<QLLG_F32,NR><<<g,kT,0,st>>>(p, rs, nsites, s))); }
+  else { qllg_set_error("mcg_update_p: precision %d", ps); return -1; }
+  return done("mcg_update_p");
+}
+
+extern "C" int
+qllg_k_mcg_update(int px, int ps, void *xs, void *rs, const void *p, const void *Ap,
+                  int nsites, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  PXS_SWITCH(px, ps, NR_SWITCH(nrhs, (mcg_update_k<PX,PS,NR><<<g,kT,0,st>>>(xs, rs, p, Ap, nsites,
+                                      s, rb->partial, rb->counter))));
+  return done("mcg_update");
+}
+
+extern "C" int
+qllg_k_mcg_accum(int px, void *x64, void *xs, int nsites, int nrhs, qllg_cg_scalars *s)
+{
+  int g = grid_for((size_t)nsites*nrhs, 0);
+  cudaStream_t st = qllg_stream();
+  if(px == QLLG_F32) { NR_SWITCH(nrhs, (mcg_accum_k<QLLG_F32,NR><<<g,kT,0,st>>>(x64, xs, nsites, s))); }
+  else if(px == QLLG_I16) { NR_SWITCH(nrhs, (mcg_accum_k<QLLG_I16,NR><<<g,kT,0,st>>>(x64, xs, nsites, s))); }
+  else { qllg_set_error("mcg_accum: precision %d", px); return -1; }
+  return done("mcg_accum");
+}
+
+extern "C" int
+qllg_k_mcg_residual(int ps, void *r64, void *rs, const void *b, const void *t64, int nsites,
+                    int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  if(ps == QLLG_I16) { NR_SWITCH(nrhs, (mcg_residual_k<QLLG_I16,NR><<<g,kT,0,st>>>(r64, rs, b, t64, nsites, s, rb->partial, rb->counter))); }
+  else if(ps == QLLG_F32) { NR_SWITCH(nrhs, (mcg_residual_k<QLLG_F32,NR><<<g,kT,0,st>>>(r64, rs, b, t64, nsites, s, rb->partial, rb->counter))); }
+  else { qllg_set_error("mcg_residual: precision %d", ps); return -1; }
+  return done("mcg_residual");
+}

@@ -1,0 +1,178 @@
+// k_stag.cu -- asqtad staggered half-Dslash kernels (sm_103a).
+//
+// One thread per (output site, right-hand side), rhs fastest, so the nrhs
+// threads of a site share every link load (a broadcast from L1) while the
+// spinor loads stay coalesced.  Neighbours are computed in-kernel from the
+// even-odd lexicographic site order (periodic in every direction), which
+// replaces the reference's gather tables (lib/shifts.c:516-736) and halo
+// exchange.  The slot order and the per-slot arithmetic follow dslash2T
+// (lib/stagDslash.c:316-328) and PeqM3AtimesV3o (lib/vla0.c.lua:193-213):
+// slot s = 4*mu + 2*backward + naik, acc += U_s(x) psi(x + d_s).
+#include "kcommon.cuh"
+
+using namespace qk;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <int PS, int PL, int NS, int NR>
+__global__ void __launch_bounds__(kThreads)
+stag_dslash(qllg_stag_args a)
+{
+  typedef typename Calc<PS, PL>::T T;
+  __shared__ double shm[2*kThreads];
+  const Geo G = make_geo(a.g);
+  const size_t V = (size_t)a.g.V;
+  const size_t total = (size_t)G.Vh * NR;
+  const int p = a.out_parity;
+  const size_t loff = p ? (size_t)G.Vh : 0;
+  const bool skip = a.done && *(volatile const int *)a.done;
+  double red[2] = {0.0, 0.0};
+  const int rhs = threadIdx.x % NR;
+  const bool act = !a.active || a.active[rhs];
+  const T ca = (T)(a.a ? a.a[rhs] : a.a0);
+  const T cb = (T)a.b;
+  if(!skip && act) {
+    for(size_t t = (size_t)blockIdx.x*blockDim.x + threadIdx.x; t < total;
+        t += (size_t)gridDim.x*blockDim.x) {
+      const int site = (int)(t / NR);
+      int x[4];
+      site_coords(G, p, site, x);
+      Cx<T> acc[3], self[3];
+      if(a.self) SpinorIO<PS,3>::load(a.self, total, t, self);
+      if(a.mode == 1) {
+#pragma unroll
+        for(int c=0; c<3; c++) { acc[c].r = ca*self[c].r; acc[c].i = ca*self[c].i; }
+      } else {
+#pragma unroll
+        for(int c=0; c<3; c++) { acc[c].r = 0; acc[c].i = 0; }
+      }
+#pragma unroll
+      for(int mu=0; mu<4; mu++) {
+#pragma unroll
+        for(int back=0; back<2; back++) {
+#pragma unroll
+          for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
+            const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
+            const int d = (nk ? 3 : 1)*(back ? -1 : 1);
+            const int k = nbr_index(G, x, mu, d);
+            Cx<T> U[9], v[3];
+            LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+            SpinorIO<PS,3>::load(a.in, total, (size_t)k*NR + rhs, v);
+#pragma unroll
+            for(int l=0; l<3; l++) {
+#pragma unroll
+              for(int j=0; j<3; j++) cmac(acc[j], U[3*l + j], v[l]);
+            }
+          }
+        }
+      }
+      Cx<T> out[3];
+      if(a.mode == 2) {
+#pragma unroll
+        for(int c=0; c<3; c++) {
+          T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
+          out[c].r = fma(cb, acc[c].r, sr);
+          out[c].i = fma(cb, acc[c].i, si);
+        }
+      } else {
+#pragma unroll
+        for(int c=0; c<3; c++) out[c] = acc[c];
+      }
+      SpinorIO<PS,3>::store(a.out, total, t, out);
+      if(a.norm_out) {
+#pragma unroll
+        for(int c=0; c<3; c++) red[0] += (double)out[c].r*out[c].r + (double)out[c].i*out[c].i;
+      }
+      if(a.norm_self && a.self) {
+#pragma unroll
+        for(int c=0; c<3; c++) red[1] += (double)self[c].r*self[c].r + (double)self[c].i*self[c].i;
+      }
+    }
+  }
+  if(a.norm_out || a.norm_self) {
+    double *res[2] = {a.norm_out, a.norm_self};
+    grid_reduce<2>(red, NR, rhs, a.rb->partial, a.rb->counter, shm, res);
+  }
+}
+
+__global__ void
+nbr_table(qllg_geom g, int p, int slot, int *out)
+{
+  const Geo G = make_geo(g);
+  int i = blockIdx.x*blockDim.x + threadIdx.x;
+  if(i >= G.Vh) return;
+  int x[4];
+  site_coords(G, p, i, x);
+  int mu = slot/4, back = (slot/2) & 1, nk = slot & 1;
+  int d = (nk ? 3 : 1)*(back ? -1 : 1);
+  out[i] = (1 - p)*G.Vh + nbr_index(G, x, mu, d);
+}
+
+template <int PS, int PL, int NS, int NR>
+int launch_t(const qllg_stag_args *a)
+{
+  static int blocks_per_sm = 0;
+  if(!blocks_per_sm) {
+    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &blocks_per_sm, stag_dslash<PS,PL,NS,NR>, kThreads, 0), "occupancy")) return -1;
+    if(blocks_per_sm < 1) blocks_per_sm = 1;
+  }
+  size_t total = (size_t)a->g.Vh * NR;
+  size_t need = (total + kThreads - 1)/kThreads;
+  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
+  if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
+  int grid = (int)(need < maxg ? need : maxg);
+  if(grid < 1) grid = 1;
+  stag_dslash<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
+  return qllg_check_cuda(cudaGetLastError(), "stag_dslash launch");
+}
+
+template <int PS, int PL, int NS>
+int launch_nr(const qllg_stag_args *a)
+{
+  switch(a->nrhs) {
+  case 1: return launch_t<PS,PL,NS,1>(a);
+  case 2: return launch_t<PS,PL,NS,2>(a);
+  case 4: return launch_t<PS,PL,NS,4>(a);
+  case 8: return launch_t<PS,PL,NS,8>(a);
+  case 16: return launch_t<PS,PL,NS,16>(a);
+  }
+  qllg_set_error("stag_dslash: nrhs %d not in {1,2,4,8,16}", a->nrhs);
+  return -1;
+}
+
+template <int PS, int PL>
+int launch_ns(const qllg_stag_args *a)
+{
+  if(a->nslots == 16) return launch_nr<PS,PL,16>(a);
+  if(a->nslots == 8) return launch_nr<PS,PL,8>(a);
+  qllg_set_error("stag_dslash: nslots %d not 8 or 16", a->nslots);
+  return -1;
+}
+
+} // namespace
+
+extern "C" int
+qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
+{
+  if((a->norm_out || a->norm_self) && !a->rb) {
+    qllg_set_error("stag_dslash: reduction requested without workspace");
+    return -1;
+  }
+  if(ps == QLLG_F64 && pl == QLLG_F64) return launch_ns<QLLG_F64, QLLG_F64>(a);
+  if(ps == QLLG_F32 && pl == QLLG_F32) return launch_ns<QLLG_F32, QLLG_F32>(a);
+  if(ps == QLLG_I16 && pl == QLLG_I16) return launch_ns<QLLG_I16, QLLG_I16>(a);
+  if(ps == QLLG_I16 && pl == QLLG_F32) return launch_ns<QLLG_I16, QLLG_F32>(a);
+  qllg_set_error("stag_dslash: unsupported precision pair %d/%d", ps, pl);
+  return -1;
+}
+
+extern "C" int
+qllg_k_stag_nbr_table(const qllg_geom *g, int parity, int slot, int *dev_out)
+{
+  int n = g->Vh;
+  nbr_table<<<(n + 255)/256, 256, 0, qllg_stream()>>>(*g, parity, slot, dev_out);
+  return qllg_check_cuda(cudaGetLastError(), "nbr_table launch");
+}

@@ -1,0 +1,225 @@
+// kcommon.cuh -- device helpers shared by the libqll_gb300 kernels:
+// lattice geometry of the even-odd site order, field loads/stores in the
+// three storage precisions, and the deterministic grid reduction.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "qllg_internal.h"
+
+namespace qk {
+
+// ------------------------------------------------------------- precisions
+template <int P> struct Real;
+template <> struct Real<QLLG_F64> { typedef double T; typedef double2 V2; };
+template <> struct Real<QLLG_F32> { typedef float T; typedef float2 V2; };
+template <> struct Real<QLLG_I16> { typedef float T; typedef float2 V2; };
+
+// arithmetic type of a kernel that reads precision A and writes B
+template <int A, int B> struct Calc { typedef float T; };
+template <int B> struct Calc<QLLG_F64, B> { typedef double T; };
+template <int A> struct Calc<A, QLLG_F64> { typedef double T; };
+template <> struct Calc<QLLG_F64, QLLG_F64> { typedef double T; };
+
+// ---------------------------------------------------------------- geometry
+struct Geo {
+  int L0, L1, L2, L3, X0h, Vh;
+};
+__host__ __device__ inline Geo make_geo(const qllg_geom &g) {
+  Geo r; r.L0 = g.L[0]; r.L1 = g.L[1]; r.L2 = g.L[2]; r.L3 = g.L[3];
+  r.X0h = g.L[0]/2; r.Vh = g.Vh; return r;
+}
+
+// coordinates of site i of parity p (x0 fastest; lexicographic index / 2)
+__device__ __forceinline__ void site_coords(const Geo &G, int p, int i, int x[4]) {
+  int x0h = i % G.X0h; int r = i / G.X0h;
+  x[1] = r % G.L1; r /= G.L1;
+  x[2] = r % G.L2; x[3] = r / G.L2;
+  x[0] = 2*x0h + ((p + x[1] + x[2] + x[3]) & 1);
+}
+
+// index within its parity block of the site x shifted by d along mu
+__device__ __forceinline__ int nbr_index(const Geo &G, const int x[4], int mu, int d) {
+  int y0 = x[0], y1 = x[1], y2 = x[2], y3 = x[3];
+  if(mu == 0)      { y0 += d; y0 += (y0 < 0) ? G.L0 : 0; y0 -= (y0 >= G.L0) ? G.L0 : 0; }
+  else if(mu == 1) { y1 += d; y1 += (y1 < 0) ? G.L1 : 0; y1 -= (y1 >= G.L1) ? G.L1 : 0; }
+  else if(mu == 2) { y2 += d; y2 += (y2 < 0) ? G.L2 : 0; y2 -= (y2 >= G.L2) ? G.L2 : 0; }
+  else             { y3 += d; y3 += (y3 < 0) ? G.L3 : 0; y3 -= (y3 >= G.L3) ? G.L3 : 0; }
+  return (y0 + G.L0*(y1 + G.L1*(y2 + G.L2*y3))) >> 1;
+}
+
+// -------------------------------------------------------------- complex
+template <typename T> struct Cx { T r, i; };
+
+template <typename T>
+__device__ __forceinline__ void cmac(Cx<T> &acc, const Cx<T> &m, const Cx<T> &v) {
+  acc.r = fma(m.r, v.r, acc.r); acc.i = fma(m.i, v.r, acc.i);
+  acc.r = fma(-m.i, v.i, acc.r); acc.i = fma(m.r, v.i, acc.i);
+}
+
+// ------------------------------------------------------------ spinor I/O
+// nc colour(-spin) complex components per site; idx = site*nrhs + rhs;
+// stride = nsites*nrhs (component-major for FP64/FP32)
+template <int P, int NC> struct SpinorIO;
+
+template <int NC> struct SpinorIO<QLLG_F64, NC> {
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, size_t stride, size_t idx, Cx<T> v[NC]) {
+    const double2 *p = (const double2 *)b;
+#pragma unroll
+    for(int c=0; c<NC; c++) { double2 t = __ldg(p + c*stride + idx); v[c].r = (T)t.x; v[c].i = (T)t.y; }
+  }
+  template <typename T>
+  static __device__ __forceinline__ void store(void *b, size_t stride, size_t idx, const Cx<T> v[NC]) {
+    double2 *p = (double2 *)b;
+#pragma unroll
+    for(int c=0; c<NC; c++) p[c*stride + idx] = make_double2((double)v[c].r, (double)v[c].i);
+  }
+};
+
+template <int NC> struct SpinorIO<QLLG_F32, NC> {
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, size_t stride, size_t idx, Cx<T> v[NC]) {
+    const float2 *p = (const float2 *)b;
+#pragma unroll
+    for(int c=0; c<NC; c++) { float2 t = __ldg(p + c*stride + idx); v[c].r = (T)t.x; v[c].i = (T)t.y; }
+  }
+  template <typename T>
+  static __device__ __forceinline__ void store(void *b, size_t stride, size_t idx, const Cx<T> v[NC]) {
+    float2 *p = (float2 *)b;
+#pragma unroll
+    for(int c=0; c<NC; c++) p[c*stride + idx] = make_float2((float)v[c].r, (float)v[c].i);
+  }
+};
+
+// exact int16 -> float: bias the value into the low mantissa bits of 2^23
+__device__ __forceinline__ float s16lo(uint32_t w) {
+  return __uint_as_float(0x4B000000u | ((w ^ 0x8000u) & 0xFFFFu)) - 8421376.0f;
+}
+__device__ __forceinline__ float s16hi(uint32_t w) {
+  return __uint_as_float(0x4B000000u | ((w >> 16) ^ 0x8000u)) - 8421376.0f;
+}
+__device__ __forceinline__ uint32_t pack_s16(float a, float b) {
+  int ia = __float2int_rn(a), ib = __float2int_rn(b);
+  return (uint32_t)(ia & 0xFFFF) | ((uint32_t)ib << 16);
+}
+
+// 16-bit spinor: three colour components in one int4 per (site,rhs)
+template <> struct SpinorIO<QLLG_I16, 3> {
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, size_t, size_t idx, Cx<T> v[3]) {
+    int4 w = __ldg((const int4 *)b + idx);
+    float s = __int_as_float(w.w) * (1.0f/32767.0f);
+    v[0].r = s16lo(w.x)*s; v[0].i = s16hi(w.x)*s;
+    v[1].r = s16lo(w.y)*s; v[1].i = s16hi(w.y)*s;
+    v[2].r = s16lo(w.z)*s; v[2].i = s16hi(w.z)*s;
+  }
+  template <typename T>
+  static __device__ __forceinline__ void store(void *b, size_t, size_t idx, const Cx<T> v[3]) {
+    float m = 0.f;
+#pragma unroll
+    for(int c=0; c<3; c++) { m = fmaxf(m, fabsf((float)v[c].r)); m = fmaxf(m, fabsf((float)v[c].i)); }
+    float inv = (m > 0.f) ? 32767.0f/m : 0.f;
+    int4 w;
+    w.x = (int)pack_s16((float)v[0].r*inv, (float)v[0].i*inv);
+    w.y = (int)pack_s16((float)v[1].r*inv, (float)v[1].i*inv);
+    w.z = (int)pack_s16((float)v[2].r*inv, (float)v[2].i*inv);
+    w.w = __float_as_int(m);
+    ((int4 *)b)[idx] = w;
+  }
+};
+
+// --------------------------------------------------------------- link I/O
+// slot-major stores; V = sites of the full lattice
+template <int P> struct LinkIO;
+
+template <> struct LinkIO<QLLG_F64> {
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, int slot, size_t V, size_t site, const float *, Cx<T> m[9]) {
+    const double2 *p = (const double2 *)b + (size_t)slot*9*V + site;
+#pragma unroll
+    for(int k=0; k<9; k++) { double2 t = __ldg(p + k*V); m[k].r = (T)t.x; m[k].i = (T)t.y; }
+  }
+};
+template <> struct LinkIO<QLLG_F32> {
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, int slot, size_t V, size_t site, const float *, Cx<T> m[9]) {
+    const float2 *p = (const float2 *)b + (size_t)slot*9*V + site;
+#pragma unroll
+    for(int k=0; k<9; k++) { float2 t = __ldg(p + k*V); m[k].r = (T)t.x; m[k].i = (T)t.y; }
+  }
+};
+// 16-bit link: per slot [V] int4 (entries 0..3), [V] int4 (4..7), [V] int (8)
+template <> struct LinkIO<QLLG_I16> {
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, int slot, size_t V, size_t site, const float *scale, Cx<T> m[9]) {
+    const char *base = (const char *)b + (size_t)slot*36*V;
+    int4 a = __ldg((const int4 *)base + site);
+    int4 c = __ldg((const int4 *)(base + 16*V) + site);
+    int e = __ldg((const int *)(base + 32*V) + site);
+    float s = __ldg(scale + slot) * (1.0f/32767.0f);
+    m[0].r = s16lo(a.x)*s; m[0].i = s16hi(a.x)*s;
+    m[1].r = s16lo(a.y)*s; m[1].i = s16hi(a.y)*s;
+    m[2].r = s16lo(a.z)*s; m[2].i = s16hi(a.z)*s;
+    m[3].r = s16lo(a.w)*s; m[3].i = s16hi(a.w)*s;
+    m[4].r = s16lo(c.x)*s; m[4].i = s16hi(c.x)*s;
+    m[5].r = s16lo(c.y)*s; m[5].i = s16hi(c.y)*s;
+    m[6].r = s16lo(c.z)*s; m[6].i = s16hi(c.z)*s;
+    m[7].r = s16lo(c.w)*s; m[7].i = s16hi(c.w)*s;
+    m[8].r = s16lo(e)*s;   m[8].i = s16hi(e)*s;
+  }
+};
+
+// ------------------------------------------------------------ reductions
+// Block partial sums per rhs, then the last block to finish folds the
+// partials of all blocks in a fixed order, so results are bitwise
+// repeatable for a fixed grid.  nr reductions of nrhs values each.
+template <int NR>
+__device__ __forceinline__ bool grid_reduce(double (&val)[NR], int nrhs, int rhs,
+                                            double *partial, unsigned *counter,
+                                            double *shm /* blockDim*NR */,
+                                            double *result[NR]) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+#pragma unroll
+  for(int q=0; q<NR; q++) shm[q*nt + tid] = val[q];
+  __syncthreads();
+  // fold threads of equal rhs: thread t holds rhs t % nrhs
+  if(tid < nrhs) {
+#pragma unroll
+    for(int q=0; q<NR; q++) {
+      double s = 0;
+      for(int t=tid; t<nt; t+=nrhs) s += shm[q*nt + t];
+      partial[(size_t)blockIdx.x*(2*QLLG_MAXRHS) + q*QLLG_MAXRHS + tid] = s;
+    }
+  }
+  __threadfence();
+  __shared__ bool last;
+  __syncthreads();
+  if(tid == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if(!last) return false;
+  __threadfence();
+  // all partials visible: K = NR*nrhs sums (a power of two dividing the
+  // block size); thread t adds blocks j, j+J, ... of sum c = t % K with
+  // j = t / K, then a fixed tree over j.
+  const int nb = gridDim.x;
+  const int K = NR*nrhs, J = nt / K;
+  const int c = tid % K, j = tid / K;
+  const int q = c / nrhs, r = c % nrhs;
+  double s = 0;
+  for(int b=j; b<nb; b+=J)
+    s += ((volatile double *)partial)[(size_t)b*(2*QLLG_MAXRHS) + q*QLLG_MAXRHS + r];
+  shm[tid] = s;
+  __syncthreads();
+  for(int w=J/2; w>0; w>>=1) {
+    if(j < w) shm[c + K*j] += shm[c + K*(j + w)];
+    __syncthreads();
+  }
+  if(j == 0) {
+#pragma unroll
+    for(int qq=0; qq<NR; qq++) if(qq == q && result[qq]) result[qq][r] = shm[c];
+  }
+  if(tid == 0) *counter = 0u;
+  return true;
+}
+
+} // namespace qk

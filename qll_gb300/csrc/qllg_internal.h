@@ -1,0 +1,201 @@
+/*
+ * qllg_internal.h -- internal interface between the C host code of
+ * libqll_gb300 and its CUDA kernels (kernel launchers are extern "C").
+ *
+ * Device data layout (all fields are split by parity; a parity block holds
+ * Vh = V/2 sites numbered as the reference's VLEN=1 layoutIndex does:
+ * lexicographic with x0 fastest, halved):
+ *
+ *  - spinor, FP64/FP32, nrhs right-hand sides: component-major
+ *    [3 colours][Vh sites][nrhs] of double2/float2 (re,im), so consecutive
+ *    threads (rhs fastest, then site) read consecutive 8/16-byte words;
+ *  - spinor, 16-bit: [Vh sites][nrhs] of int4 = six int16 (colour re/im,
+ *    fixed point, full scale 32767) plus the float scale max|component|:
+ *    one 128-bit load per site and rhs;
+ *  - Wilson spinor: as above with 12 colour-spin components (FP64/FP32
+ *    component-major [12][Vh][nrhs]);
+ *  - 3x3 link field slot s, FP64/FP32: [9 complex entries][V sites] of
+ *    double2/float2, entry k = 3*column + row (the reference's column-major
+ *    Mat3, lib/vla.c:9-11), sites in full-lattice order (even block then odd
+ *    block);
+ *  - link field, 16-bit: [V sites] x (int4, int4, int) = 18 int16 fixed
+ *    point with one float scale per slot.
+ */
+#ifndef QLLG_INTERNAL_H
+#define QLLG_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QLLG_MAXRHS 16
+
+typedef struct {
+  int L[4];   /* physical extents, all even and >= 4 */
+  int V;      /* sites */
+  int Vh;     /* sites per parity */
+} qllg_geom;
+
+enum { QLLG_F64 = 0, QLLG_F32 = 1, QLLG_I16 = 2 };
+
+/* ------------------------------------------------------------ geometry */
+struct Layout_s;
+int qllg_geom_from_dims(qllg_geom *g, const int dims[4]);
+void *qllg_stage(size_t bytes);          /* shared device staging buffer */
+void qllg_stage_release(void);
+/* bytes of one site and rhs of a spinor with ncomp complex components */
+static inline size_t qllg_spinor_bytes(int prec, int ncomp) {
+  return prec == QLLG_F64 ? 16u*ncomp : (prec == QLLG_F32 ? 8u*ncomp : 16u);
+}
+static inline size_t qllg_link_bytes(int prec) {
+  return prec == QLLG_F64 ? 144u : (prec == QLLG_F32 ? 72u : 36u);
+}
+
+/* ------------------------------------------------------------ runtime */
+int   qllg_runtime_init(void);                 /* 0 ok */
+cudaStream_t qllg_stream(void);                /* current library stream */
+void  qllg_set_error(const char *fmt, ...);
+int   qllg_check_cuda(cudaError_t e, const char *what);   /* 0 ok */
+void *qllg_dmalloc(size_t bytes);              /* NULL + error on failure */
+void  qllg_dfree(void *p);
+int   qllg_h2d(void *d, const void *h, size_t bytes);
+int   qllg_d2h(void *h, const void *d, size_t bytes);
+int   qllg_sync(void);
+int   qllg_num_sms(void);
+
+/* reduction workspace: block partials + completion counter + results */
+typedef struct {
+  double *partial;     /* [maxblocks][2*QLLG_MAXRHS] */
+  unsigned *counter;
+  int maxblocks;
+} qllg_redbuf;
+int  qllg_redbuf_init(qllg_redbuf *rb);
+void qllg_redbuf_free(qllg_redbuf *rb);
+
+/* ----------------------------------------------------- field transfers */
+/* stage: nrhs blocks of the reference's VLEN=1 host layout, each
+ * [nsites][2*ncomp] reals (double when stage_is_double, else float), already
+ * copied to device memory; converted to/from the device layout of prec.
+ * rhs_stride: reals between consecutive rhs blocks of stage. */
+int qllg_k_spinor_from_aos(int prec, void *dev, const void *stage, int stage_is_double,
+                           int nsites, int ncomp, int nrhs, size_t rhs_stride);
+int qllg_k_spinor_to_aos(int prec, const void *dev, void *stage, int stage_is_double,
+                         int nsites, int ncomp, int nrhs, size_t rhs_stride);
+/* y = convert(x) between precisions for the active rhs (active may be NULL) */
+int qllg_k_spinor_convert(int prec_out, void *out, int prec_in, const void *in,
+                          int nsites, int ncomp, int nrhs, const int *active);
+/* links: stage [V][18] reals (device copy of host data) -> device slot */
+int qllg_k_link_from_aos(int prec, void *dev, float *scale_dev, const void *stage,
+                         int stage_is_double, int V);
+/* device slot (FP64 layout) -> [V][18] reals stage */
+int qllg_k_link_to_aos(const double *dev, void *stage, int stage_is_double, int V);
+/* convert a device FP64 link slot to prec (FP32 or I16) */
+int qllg_k_link_convert(int prec, void *out, float *scale_dev, const double *in, int V);
+
+/* ----------------------------------------------------- staggered Dslash */
+typedef struct {
+  qllg_geom g;
+  int out_parity;        /* parity of the output sites */
+  int nrhs;              /* 1,2,4,8,16 */
+  int nslots;            /* 16 (fat+Naik) or 8 (one-hop only) */
+  const void *links;     /* device link store, prec_link */
+  const float *lscale;   /* per slot scale (I16 links) */
+  const void *in;        /* input spinor block of the opposite parity */
+  const void *self;      /* same-parity input for the epilogue or NULL */
+  void *out;
+  /* epilogue mode 0: out = acc
+   *          mode 1: acc starts at a0*self, out = acc (dslash2 mass term)
+   *          mode 2: out = a[rhs]*self + b*acc (a NULL: a0) */
+  int mode;
+  const double *a;       /* device [nrhs] or NULL */
+  double a0, b;
+  double *norm_out;      /* device [nrhs]: |out|^2, or NULL */
+  double *norm_self;     /* device [nrhs]: |self|^2, or NULL */
+  const int *active;     /* device [nrhs] mask or NULL */
+  const int *done;       /* device flag: skip everything when nonzero */
+  qllg_redbuf *rb;
+} qllg_stag_args;
+int qllg_k_stag_dslash(int prec_spinor, int prec_link, const qllg_stag_args *a);
+
+/* neighbour index of slot s for every output site of a parity, written as
+ * the full-lattice QLL site index (for the bit-exact table check) */
+int qllg_k_stag_nbr_table(const qllg_geom *g, int parity, int slot, int *dev_out);
+
+/* ------------------------------------------------------- CG kernels */
+/* scalars live on the device, per rhs (QLLG_MAXRHS each) */
+typedef struct {
+  double rsq[QLLG_MAXRHS];      /* current |r|^2 */
+  double rsq_stop[QLLG_MAXRHS]; /* stopping threshold */
+  double bsq[QLLG_MAXRHS];
+  double pnorm[QLLG_MAXRHS];    /* |p|^2 (even) */
+  double vnorm[QLLG_MAXRHS];    /* |D_oe p|^2 (odd) */
+  double mass2[QLLG_MAXRHS];    /* m^2 of the operator of each rhs */
+  double alpha[QLLG_MAXRHS];
+  double tmp[QLLG_MAXRHS];
+  double maxr2[QLLG_MAXRHS];    /* |r|^2 at the last reliable update */
+  double delta2;                /* reliable-update threshold, squared */
+  int active[QLLG_MAXRHS];
+  int iters[QLLG_MAXRHS];
+  int ru[QLLG_MAXRHS];          /* rhs that take a reliable update now */
+  int nru[QLLG_MAXRHS];         /* reliable updates taken per rhs */
+  int maxits;
+  int done;                     /* all rhs inactive */
+  int no_ru;                    /* no rhs takes a reliable update now */
+  int count;                    /* iterations issued */
+} qllg_cg_scalars;
+
+/* ------------------------------------------ mixed-precision CG kernels */
+/* start: r64 = b, x64 = 0, rs = b (sloppy prec ps), xs = 0 (prec px),
+ * p = 0; bsq = rsq = maxr2 = |b|^2; rsq_stop *= bsq */
+int qllg_k_mcg_init(int px, int ps, void *x64, void *r64, void *xs, void *rs, void *p,
+                    const void *b, int nsites, int nrhs, qllg_cg_scalars *s,
+                    qllg_redbuf *rb);
+/* sloppy step: xs += a p, rs -= a Ap, |rs|^2; flags rhs for a reliable
+ * update when |rs|^2 < delta2*maxr2, when |rs|^2 < rsq_stop, or at maxits */
+int qllg_k_mcg_update(int px, int ps, void *xs, void *rs, const void *p, const void *Ap,
+                      int nsites, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb);
+/* sloppy p += rs/rsq */
+int qllg_k_mcg_update_p(int ps, void *p, const void *rs, int nsites, int nrhs,
+                        qllg_cg_scalars *s);
+/* reliable update, part 1: x64 += xs, xs = 0 for the flagged rhs */
+int qllg_k_mcg_accum(int px, void *x64, void *xs, int nsites, int nrhs, qllg_cg_scalars *s);
+/* part 2 (after t64 = A x64): r64 = b - t64, rs = r64, |r64|^2; retires
+ * converged rhs and clears the flags */
+int qllg_k_mcg_residual(int ps, void *r64, void *rs, const void *b, const void *t64,
+                        int nsites, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb);
+
+/* r = b, x = 0, p = 0; bsq = rsq = |b|^2; rsq_stop *= bsq (rsq_stop holds
+ * the relative tolerance on entry); rhs with b = 0 start inactive */
+int qllg_k_cg_init(int prec, void *x, void *r, void *p, const void *b,
+                   int nsites, int ncomp, int nrhs, qllg_cg_scalars *s,
+                   qllg_redbuf *rb);
+/* x += alpha p, r -= alpha Ap with alpha = 1/(m^2 pnorm + vnorm);
+ * rsq = |r|^2; deactivate converged rhs and set done */
+int qllg_k_cg_update_xr(int prec, void *x, void *r, const void *p, const void *Ap,
+                        int nsites, int ncomp, int nrhs, qllg_cg_scalars *s,
+                        qllg_redbuf *rb);
+/* p = p + (1/rsq) r for active rhs */
+int qllg_k_cg_update_p(int prec, void *p, const void *r, int nsites, int ncomp,
+                       int nrhs, qllg_cg_scalars *s);
+/* rsq = |r|^2 etc for start-up: out[rhs] = |x|^2 */
+int qllg_k_norm2(int prec, const void *x, int nsites, int ncomp, int nrhs, double *out,
+                 qllg_redbuf *rb);
+/* y = a*y + b*x (per-rhs device coefficient arrays, or the scalar when the
+ * pointer is NULL; a == 0 does not read y), precisions of y and x may differ */
+int qllg_k_axpby(int py, void *y, int px, const void *x, const double *a, double a0,
+                 const double *b, double b0, int nsites, int ncomp, int nrhs,
+                 const int *active);
+/* y = y + (bsign*b) x, rounded like X_veq_X_plus_r_times_X */
+int qllg_k_xpay(int prec, void *y, const void *x, const double *b, double b0, double bsign,
+                int nsites, int ncomp, int nrhs, const int *active);
+int qllg_k_zero(int prec, void *x, int nsites, int ncomp, int nrhs);
+int qllg_k_copy(int prec, void *y, const void *x, int nsites, int ncomp, int nrhs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,200 @@
+/*
+ * runtime.c -- device context of libqll_gb300: one CUDA stream per
+ * process (replaceable by the caller), device allocation with error
+ * reporting, a reusable device staging buffer for host transfers, and the
+ * last-error string behind qllg_last_error().
+ *
+ * The reference library never reports errors (it calls exit(), e.g.
+ * lib/common.c:22-25, lib/layout.c:49,63); this library never exits: every
+ * failing call records a message here and returns a failure value.
+ */
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
+#include "qllg_internal.h"
+#include "qll_gb300.h"
+
+static char g_err[1024];
+static int g_inited = 0;
+static int g_nsm = 0;
+static cudaStream_t g_stream = 0;
+static int g_own_stream = 0;
+
+void
+qllg_set_error(const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  if(getenv("QLLG_VERBOSE")) fprintf(stderr, "qll_gb300: %s\n", g_err);
+}
+
+const char *
+qllg_last_error(void)
+{
+  return g_err;
+}
+
+void
+qllg_clear_error(void)
+{
+  g_err[0] = 0;
+}
+
+int
+qllg_check_cuda(cudaError_t e, const char *what)
+{
+  if(e == cudaSuccess) return 0;
+  qllg_set_error("%s: %s", what, cudaGetErrorString(e));
+  return -1;
+}
+
+int
+qllg_runtime_init(void)
+{
+  if(g_inited) return 0;
+  int n = 0;
+  if(qllg_check_cuda(cudaGetDeviceCount(&n), "cudaGetDeviceCount")) return -1;
+  if(n < 1) { qllg_set_error("no CUDA device"); return -1; }
+  int dev = 0;
+  if(qllg_check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return -1;
+  if(qllg_check_cuda(cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev),
+                     "cudaDeviceGetAttribute")) return -1;
+  if(!g_stream) {
+    if(qllg_check_cuda(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate")) return -1;
+    g_own_stream = 1;
+  }
+  g_inited = 1;
+  return 0;
+}
+
+int
+qllg_num_sms(void)
+{
+  if(!g_nsm) qllg_runtime_init();
+  return g_nsm ? g_nsm : 1;
+}
+
+cudaStream_t
+qllg_stream(void)
+{
+  return g_stream;
+}
+
+int
+qllg_set_stream(void *stream)
+{
+  if(qllg_runtime_init()) return -1;
+  if(g_own_stream && g_stream) {
+    cudaStreamSynchronize(g_stream);
+    cudaStreamDestroy(g_stream);
+    g_own_stream = 0;
+  }
+  g_stream = (cudaStream_t)stream;
+  return 0;
+}
+
+void *
+qllg_get_stream(void)
+{
+  return (void *)g_stream;
+}
+
+void *
+qllg_dmalloc(size_t bytes)
+{
+  if(qllg_runtime_init()) return NULL;
+  void *p = NULL;
+  if(bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if(e != cudaSuccess) {
+    qllg_set_error("cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    return NULL;
+  }
+  return p;
+}
+
+void
+qllg_dfree(void *p)
+{
+  if(p) cudaFree(p);
+}
+
+int
+qllg_h2d(void *d, const void *h, size_t bytes)
+{
+  return qllg_check_cuda(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g_stream),
+                         "copy host to device");
+}
+
+int
+qllg_d2h(void *h, const void *d, size_t bytes)
+{
+  if(qllg_check_cuda(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, g_stream),
+                     "copy device to host")) return -1;
+  return qllg_sync();
+}
+
+int
+qllg_sync(void)
+{
+  return qllg_check_cuda(cudaStreamSynchronize(g_stream), "stream synchronize");
+}
+
+int
+qllg_redbuf_init(qllg_redbuf *rb)
+{
+  rb->maxblocks = qllg_num_sms()*16;
+  rb->partial = qllg_dmalloc(sizeof(double)*2*QLLG_MAXRHS*(size_t)rb->maxblocks);
+  rb->counter = qllg_dmalloc(sizeof(unsigned)*4);
+  if(!rb->partial || !rb->counter) { qllg_redbuf_free(rb); return -1; }
+  return qllg_check_cuda(cudaMemsetAsync(rb->counter, 0, sizeof(unsigned)*4, g_stream),
+                         "memset counter");
+}
+
+void
+qllg_redbuf_free(qllg_redbuf *rb)
+{
+  qllg_dfree(rb->partial);
+  qllg_dfree(rb->counter);
+  rb->partial = NULL;
+  rb->counter = NULL;
+}
+
+/* one growing device staging buffer for host<->device layout transposes */
+static void *g_stage = NULL;
+static size_t g_stage_bytes = 0;
+
+void *
+qllg_stage(size_t bytes)
+{
+  if(bytes <= g_stage_bytes) return g_stage;
+  if(g_stage) { qllg_sync(); qllg_dfree(g_stage); }
+  g_stage = qllg_dmalloc(bytes);
+  g_stage_bytes = g_stage ? bytes : 0;
+  return g_stage;
+}
+
+void
+qllg_stage_release(void)
+{
+  if(g_stage) { qllg_sync(); qllg_dfree(g_stage); }
+  g_stage = NULL;
+  g_stage_bytes = 0;
+}
+
+int
+qllg_init(void)
+{
+  return qllg_runtime_init();
+}
+
+const char *
+qllg_version(void)
+{
+  return "qll_gb300 0.1 (sm_103a)";
+}

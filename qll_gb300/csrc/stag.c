@@ -1,0 +1,795 @@
+/*
+ * stag.c -- the asqtad staggered operator on the GPU: resident links,
+ * dslash2, the even-odd normal operator of dslashp2, CG (cgSolveT) and the
+ * drop-in entry points createStaggeredLinks / dslash2 /
+ * createStaggeredSolver / solve2 / freeStaggeredSolver
+ * (lib/stagDslash.c:422-657, lib/cg.c:8-136).
+ *
+ * A CG iteration is four launches: p += r/|r|^2; v = D_oe p with |v|^2;
+ * Ap = m^2 p - D_eo v with |p|^2; x += a p, r -= a Ap with |r|^2 (a =
+ * 1/(m^2|p|^2 + |v|^2), the fused <p,Ap> of dslashp2).  All scalars stay on
+ * the GPU; convergence is tested by the last kernel, which retires right-hand
+ * sides individually, and the host looks at the "done" flag once per batch
+ * of iterations, so the iteration count equals the reference's exactly.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
+#include "qll_gb300.h"
+#include "qllg_internal.h"
+
+void qllg_tm_begin(const char *name);
+void qllg_tm_end(void);
+int qllg_geom_from_layout(qllg_geom *g, const Layout *l);
+Layout *qllg_current_layout(void);
+
+enum { WS_X, WS_R, WS_P, WS_AP, WS_V, WS_B, WS_IO, WS_X64, WS_R64, WS_T64, WS_V64,
+       WS_PS, WS_OUT, WS_N };
+
+struct qllg_stag {
+  qllg_geom g;
+  int nslots;
+  int master;              /* precision of the links handed in */
+  void *links[3];          /* per precision, lazily derived from the master */
+  float *lscale;           /* 16-bit link scales [nslots] */
+  qllg_redbuf rb;
+  qllg_cg_scalars *sc;     /* device scalars */
+  qllg_cg_scalars *hsc;    /* pinned host copy */
+  void *ws[WS_N];
+  size_t ws_bytes[WS_N];
+  cudaEvent_t ev0, ev1;
+};
+
+/* ------------------------------------------------------------ helpers */
+
+static void *
+ws_get(qllg_stag *S, int id, size_t bytes)
+{
+  if(bytes <= S->ws_bytes[id]) return S->ws[id];
+  if(S->ws[id]) { qllg_sync(); qllg_dfree(S->ws[id]); }
+  S->ws[id] = qllg_dmalloc(bytes);
+  S->ws_bytes[id] = S->ws[id] ? bytes : 0;
+  return S->ws[id];
+}
+
+static size_t
+vec_bytes(const qllg_stag *S, int prec, int nrhs)
+{
+  return qllg_spinor_bytes(prec, 3)*(size_t)S->g.Vh*nrhs;
+}
+
+static int
+ensure_links(qllg_stag *S, int prec)
+{
+  if(S->links[prec]) return 0;
+  if(S->master != QLLG_F64) {
+    qllg_set_error("operator created from float links has no %s copy",
+                   prec == QLLG_F64 ? "FP64" : "16-bit");
+    return -1;
+  }
+  size_t per = qllg_link_bytes(prec)*(size_t)S->g.V;
+  S->links[prec] = qllg_dmalloc(per*S->nslots);
+  if(!S->links[prec]) return -1;
+  const double *src = S->links[QLLG_F64];
+  for(int s=0; s<S->nslots; s++) {
+    if(qllg_k_link_convert(prec, (char *)S->links[prec] + per*s, S->lscale + s,
+                           src + (size_t)s*18*S->g.V, S->g.V)) return -1;
+  }
+  return 0;
+}
+
+static qllg_stag *
+stag_create(const int dims[4], void *const fat[8], void *const lng[8], int dbl)
+{
+  if(qllg_runtime_init()) return NULL;
+  qllg_stag *S = calloc(1, sizeof(qllg_stag));
+  if(qllg_geom_from_dims(&S->g, dims)) { free(S); return NULL; }
+  S->nslots = lng ? 16 : 8;
+  S->master = dbl ? QLLG_F64 : QLLG_F32;
+  if(qllg_redbuf_init(&S->rb)) goto fail;
+  S->sc = qllg_dmalloc(sizeof(qllg_cg_scalars));
+  S->lscale = qllg_dmalloc(sizeof(float)*16);
+  if(!S->sc || !S->lscale) goto fail;
+  if(qllg_check_cuda(cudaMallocHost((void **)&S->hsc, sizeof(qllg_cg_scalars)), "cudaMallocHost"))
+    goto fail;
+  memset(S->hsc, 0, sizeof(qllg_cg_scalars));
+  cudaEventCreate(&S->ev0);
+  cudaEventCreate(&S->ev1);
+  {
+    int prec = S->master;
+    size_t per = qllg_link_bytes(prec)*(size_t)S->g.V;
+    size_t hbytes = (dbl ? 8 : 4)*18*(size_t)S->g.V;
+    S->links[prec] = qllg_dmalloc(per*S->nslots);
+    void *stage = qllg_stage(hbytes);
+    if(!S->links[prec] || !stage) goto fail;
+    for(int s=0; s<S->nslots; s++) {
+      const void *h = (S->nslots == 16) ? ((s & 1) ? lng[s/2] : fat[s/2]) : fat[s];
+      if(!h) { qllg_set_error("link slot %d is NULL", s); goto fail; }
+      if(qllg_h2d(stage, h, hbytes)) goto fail;
+      if(qllg_k_link_from_aos(prec, (char *)S->links[prec] + per*s, S->lscale + s, stage, dbl,
+                              S->g.V)) goto fail;
+    }
+    if(qllg_sync()) goto fail;
+  }
+  return S;
+fail:
+  qllg_stag_destroy(S);
+  return NULL;
+}
+
+qllg_stag *
+qllg_stag_create(const int dims[4], double *const fat[8], double *const lng[8])
+{
+  return stag_create(dims, (void *const *)fat, (void *const *)lng, 1);
+}
+
+qllg_stag *
+qllg_stag_create_f(const int dims[4], float *const fat[8], float *const lng[8])
+{
+  return stag_create(dims, (void *const *)fat, (void *const *)lng, 0);
+}
+
+void
+qllg_stag_destroy(qllg_stag *S)
+{
+  if(!S) return;
+  qllg_sync();
+  for(int p=0; p<3; p++) qllg_dfree(S->links[p]);
+  qllg_dfree(S->lscale);
+  qllg_dfree(S->sc);
+  if(S->hsc) cudaFreeHost(S->hsc);
+  qllg_redbuf_free(&S->rb);
+  for(int i=0; i<WS_N; i++) qllg_dfree(S->ws[i]);
+  if(S->ev0) cudaEventDestroy(S->ev0);
+  if(S->ev1) cudaEventDestroy(S->ev1);
+  free(S);
+}
+
+size_t
+qllg_stag_device_bytes(const qllg_stag *S)
+{
+  size_t b = 0;
+  for(int p=0; p<3; p++) if(S->links[p]) b += qllg_link_bytes(p)*(size_t)S->g.V*S->nslots;
+  for(int i=0; i<WS_N; i++) b += S->ws_bytes[i];
+  return b;
+}
+
+/* one half-Dslash launch */
+static int
+dslash_half(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *in,
+            const void *self, void *out, int mode, const double *a, double a0, double b,
+            double *norm_out, double *norm_self, const int *active, const int *done)
+{
+  if(ensure_links(S, pl)) return -1;
+  qllg_stag_args A;
+  memset(&A, 0, sizeof(A));
+  A.g = S->g;
+  A.out_parity = out_parity;
+  A.nrhs = nrhs;
+  A.nslots = S->nslots;
+  A.links = S->links[pl];
+  A.lscale = S->lscale;
+  A.in = in;
+  A.self = self;
+  A.out = out;
+  A.mode = mode;
+  A.a = a;
+  A.a0 = a0;
+  A.b = b;
+  A.norm_out = norm_out;
+  A.norm_self = norm_self;
+  A.active = active;
+  A.done = done;
+  A.rb = &S->rb;
+  qllg_tm_begin("stag_dslash");
+  int rc = qllg_k_stag_dslash(ps, pl, &A);
+  qllg_tm_end();
+  return rc;
+}
+
+/* host [V][6] parity block(s) <-> device single-rhs block */
+static int
+upload_block(qllg_stag *S, int prec, void *dev, const void *host, int dbl, int site0, int nsites)
+{
+  size_t bytes = (dbl ? 8 : 4)*6*(size_t)nsites;
+  void *stage = qllg_stage(bytes);
+  if(!stage) return -1;
+  if(qllg_h2d(stage, (const char *)host + (dbl ? 8 : 4)*6*(size_t)site0, bytes)) return -1;
+  return qllg_k_spinor_from_aos(prec, dev, stage, dbl, nsites, 3, 1, 0);
+}
+
+static int
+download_block(qllg_stag *S, int prec, const void *dev, void *host, int dbl, int site0, int nsites)
+{
+  size_t bytes = (dbl ? 8 : 4)*6*(size_t)nsites;
+  void *stage = qllg_stage(bytes);
+  if(!stage) return -1;
+  if(qllg_k_spinor_to_aos(prec, dev, stage, dbl, nsites, 3, 1, 0)) return -1;
+  return qllg_d2h((char *)host + (dbl ? 8 : 4)*6*(size_t)site0, stage, bytes);
+}
+
+/* ------------------------------------------------------------ dslash2 */
+
+int
+qllg_stag_dslash(qllg_stag *S, void *x, double mass, const void *y, const char *sub)
+{
+  int prec = S->master, dbl = (prec == QLLG_F64);
+  int Vh = S->g.Vh;
+  size_t vb = vec_bytes(S, prec, 1);
+  void *ye = ws_get(S, WS_IO, 4*vb);
+  if(!ye) return -1;
+  void *yo = (char *)ye + vb, *xe = (char *)ye + 2*vb, *xo = (char *)ye + 3*vb;
+  int doe = !(sub && sub[0] == 'o'), doo = !(sub && sub[0] == 'e');
+  int all = doe && doo;
+  /* inputs: the opposite parity of each output, plus self for the mass term */
+  if((doe && upload_block(S, prec, yo, y, dbl, Vh, Vh)) ||
+     (doo && upload_block(S, prec, ye, y, dbl, 0, Vh))) return -1;
+  if(all && mass != 0) {
+    /* x = mass*y + D y, accumulated onto mass*y like VeqRtimesV then the slots */
+    if(dslash_half(S, prec, prec, 0, 1, yo, ye, xe, 1, NULL, mass, 1, NULL, NULL, NULL, NULL) ||
+       dslash_half(S, prec, prec, 1, 1, ye, yo, xo, 1, NULL, mass, 1, NULL, NULL, NULL, NULL))
+      return -1;
+  } else {
+    if(doe && dslash_half(S, prec, prec, 0, 1, yo, NULL, xe, 0, NULL, 0, 1, NULL, NULL, NULL, NULL))
+      return -1;
+    if(doo && dslash_half(S, prec, prec, 1, 1, ye, NULL, xo, 0, NULL, 0, 1, NULL, NULL, NULL, NULL))
+      return -1;
+  }
+  if(doe && download_block(S, prec, xe, x, dbl, 0, Vh)) return -1;
+  if(doo && download_block(S, prec, xo, x, dbl, Vh, Vh)) return -1;
+  return 0;
+}
+
+/* ------------------------------------------------------------ CG */
+
+/* Ap = m^2 p - D_eo D_oe p (all rhs, masses from S->sc->mass2) */
+static int
+apply_normal(qllg_stag *S, int ps, int pl, int nrhs, const void *p, void *v, void *Ap,
+             double *vnorm, double *pnorm, const int *active, const int *done)
+{
+  if(dslash_half(S, ps, pl, 1, nrhs, p, NULL, v, 0, NULL, 0, 1, vnorm, NULL, active, done))
+    return -1;
+  return dslash_half(S, ps, pl, 0, nrhs, v, p, Ap, 2, S->sc->mass2, 0, -1, NULL, pnorm,
+                     active, done);
+}
+
+static int
+push_scalars(qllg_stag *S)
+{
+  return qllg_check_cuda(cudaMemcpyAsync(S->sc, S->hsc, sizeof(qllg_cg_scalars),
+                                         cudaMemcpyHostToDevice, qllg_stream()), "push scalars");
+}
+
+static int
+pull_scalars(qllg_stag *S)
+{
+  if(qllg_check_cuda(cudaMemcpyAsync(S->hsc, S->sc, sizeof(qllg_cg_scalars),
+                                     cudaMemcpyDeviceToHost, qllg_stream()), "pull scalars"))
+    return -1;
+  return qllg_sync();
+}
+
+static int
+pull_done(qllg_stag *S)
+{
+  if(qllg_check_cuda(cudaMemcpyAsync(&S->hsc->done, &S->sc->done, sizeof(int),
+                                     cudaMemcpyDeviceToHost, qllg_stream()), "pull done"))
+    return -1;
+  if(qllg_sync()) return -1;
+  return S->hsc->done;
+}
+
+/* plain CG of cgSolveT in one precision on device vectors x, b (even sites,
+ * nrhs rhs).  Returns the largest iteration count, fills hsc. */
+static int
+cg_plain(qllg_stag *S, int prec, int nrhs, void *x, const void *b, const double mass[],
+         double rsq, int maxits)
+{
+  if(ensure_links(S, prec)) return -1;
+  size_t vb = vec_bytes(S, prec, nrhs);
+  void *r = ws_get(S, WS_R, vb), *p = ws_get(S, WS_P, vb), *Ap = ws_get(S, WS_AP, vb);
+  void *v = ws_get(S, WS_V, vb);
+  if(!r || !p || !Ap || !v) return -1;
+  memset(S->hsc, 0, sizeof(qllg_cg_scalars));
+  for(int i=0; i<nrhs; i++) {
+    S->hsc->mass2[i] = mass[i]*mass[i];
+    S->hsc->rsq_stop[i] = rsq;
+  }
+  S->hsc->maxits = maxits;
+  if(push_scalars(S)) return -1;
+  int Vh = S->g.Vh;
+  qllg_cg_scalars *sc = S->sc;
+  if(qllg_k_cg_init(prec, x, r, p, b, Vh, 3, nrhs, sc, &S->rb)) return -1;
+  int issued = 0;
+  int batch = 8;
+  while(issued < maxits) {
+    int k = maxits - issued < batch ? maxits - issued : batch;
+    for(int it=0; it<k; it++) {
+      if(qllg_k_cg_update_p(prec, p, r, Vh, 3, nrhs, sc)) return -1;
+      if(apply_normal(S, prec, prec, nrhs, p, v, Ap, sc->vnorm, sc->pnorm, sc->active, &sc->done))
+        return -1;
+      if(qllg_k_cg_update_xr(prec, x, r, p, Ap, Vh, 3, nrhs, sc, &S->rb)) return -1;
+    }
+    issued += k;
+    int d = pull_done(S);
+    if(d < 0) return -1;
+    if(d) break;
+    if(batch < 64) batch *= 2;
+  }
+  if(pull_scalars(S)) return -1;
+  int its = 0;
+  for(int i=0; i<nrhs; i++) if(S->hsc->iters[i] > its) its = S->hsc->iters[i];
+  return its;
+}
+
+/* |b - A x|^2 / |b|^2 per rhs in FP64 (x, b FP64 device vectors) */
+static int
+true_residual(qllg_stag *S, int nrhs, const void *x, const void *b, double *out)
+{
+  if(ensure_links(S, QLLG_F64)) return -1;
+  size_t vb = vec_bytes(S, QLLG_F64, nrhs);
+  void *t = ws_get(S, WS_T64, vb), *v = ws_get(S, WS_V64, vb);
+  if(!t || !v) return -1;
+  if(apply_normal(S, QLLG_F64, QLLG_F64, nrhs, x, v, t, NULL, NULL, NULL, NULL)) return -1;
+  /* t = b - t */
+  if(qllg_k_axpby(QLLG_F64, t, QLLG_F64, b, NULL, -1.0, NULL, 1.0, S->g.Vh, 3, nrhs, NULL))
+    return -1;
+  double *dn = &S->sc->tmp[0];
+  if(qllg_k_norm2(QLLG_F64, t, S->g.Vh, 3, nrhs, dn, &S->rb)) return -1;
+  double num[QLLG_MAXRHS], den[QLLG_MAXRHS];
+  if(qllg_d2h(num, dn, sizeof(double)*nrhs)) return -1;
+  if(qllg_k_norm2(QLLG_F64, b, S->g.Vh, 3, nrhs, dn, &S->rb)) return -1;
+  if(qllg_d2h(den, dn, sizeof(double)*nrhs)) return -1;
+  for(int i=0; i<nrhs; i++) out[i] = den[i] > 0 ? num[i]/den[i] : 0;
+  return 0;
+}
+
+/* mixed-precision reliable-update CG on FP64 device vectors x64, b (even
+ * sites, nrhs rhs): sloppy vectors in ps storage (p, v, Ap, r) and px
+ * (solution increment), links in pl */
+static int
+cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *b,
+         const double mass[], double rsq, int maxits, double delta)
+{
+  if(ensure_links(S, pl) || ensure_links(S, QLLG_F64)) return -1;
+  size_t vs = vec_bytes(S, ps, nrhs), vx = vec_bytes(S, px, nrhs);
+  size_t v64 = vec_bytes(S, QLLG_F64, nrhs);
+  void *rs = ws_get(S, WS_R, vs), *p = ws_get(S, WS_P, vs), *Ap = ws_get(S, WS_AP, vs);
+  void *v = ws_get(S, WS_V, vs), *xs = ws_get(S, WS_X, vx);
+  void *r64 = ws_get(S, WS_R64, v64), *t64 = ws_get(S, WS_T64, v64), *w64 = ws_get(S, WS_V64, v64);
+  if(!rs || !p || !Ap || !v || !xs || !r64 || !t64 || !w64) return -1;
+  memset(S->hsc, 0, sizeof(qllg_cg_scalars));
+  for(int i=0; i<nrhs; i++) {
+    S->hsc->mass2[i] = mass[i]*mass[i];
+    S->hsc->rsq_stop[i] = rsq;
+  }
+  S->hsc->maxits = maxits;
+  S->hsc->delta2 = delta*delta;
+  if(push_scalars(S)) return -1;
+  int Vh = S->g.Vh;
+  qllg_cg_scalars *sc = S->sc;
+  if(qllg_k_mcg_init(px, ps, x64, r64, xs, rs, p, b, Vh, nrhs, sc, &S->rb)) return -1;
+  int issued = 0, batch = 8;
+  while(issued < maxits) {
+    int k = maxits - issued < batch ? maxits - issued : batch;
+    for(int it=0; it<k; it++) {
+      if(qllg_k_mcg_update_p(ps, p, rs, Vh, nrhs, sc)) return -1;
+      if(apply_normal(S, ps, pl, nrhs, p, v, Ap, sc->vnorm, sc->pnorm, sc->active, &sc->done))
+        return -1;
+      if(qllg_k_mcg_update(px, ps, xs, rs, p, Ap, Vh, nrhs, sc, &S->rb)) return -1;
+      /* reliable update of the flagged rhs; every launch returns at once
+       * when no rhs is flagged */
+      if(qllg_k_mcg_accum(px, x64, xs, Vh, nrhs, sc)) return -1;
+      if(apply_normal(S, QLLG_F64, QLLG_F64, nrhs, x64, w64, t64, NULL, NULL, sc->ru, &sc->no_ru))
+        return -1;
+      if(qllg_k_mcg_residual(ps, r64, rs, b, t64, Vh, nrhs, sc, &S->rb)) return -1;
+    }
+    issued += k;
+    int d = pull_done(S);
+    if(d < 0) return -1;
+    if(d) break;
+    if(batch < 64) batch *= 2;
+  }
+  if(pull_scalars(S)) return -1;
+  int its = 0;
+  for(int i=0; i<nrhs; i++) if(S->hsc->iters[i] > its) its = S->hsc->iters[i];
+  return its;
+}
+
+static int
+valid_nrhs(int nrhs)
+{
+  return nrhs == 1 || nrhs == 2 || nrhs == 4 || nrhs == 8 || nrhs == 16;
+}
+
+/* nrhs padded to the kernel batch sizes; padding rhs have b = 0 and start
+ * inactive */
+static int
+pad_nrhs(int nrhs)
+{
+  int n = 1;
+  while(n < nrhs) n *= 2;
+  return n;
+}
+
+static int
+solve_dev(qllg_stag *S, int nrhs, void *x, const void *b, const double mass[], double rsq,
+          int maxits, int mode, qllg_solve_info *info)
+{
+  if(!valid_nrhs(nrhs)) { qllg_set_error("solve: nrhs %d not in {1,2,4,8,16}", nrhs); return -1; }
+  if(rsq < 0) rsq = -rsq;
+  cudaEventRecord(S->ev0, qllg_stream());
+  int its;
+  switch(mode) {
+  case QLLG_SOLVE_DOUBLE:
+    its = cg_plain(S, QLLG_F64, nrhs, x, b, mass, rsq, maxits);
+    break;
+  case QLLG_SOLVE_SINGLE:
+    its = cg_plain(S, QLLG_F32, nrhs, x, b, mass, rsq, maxits);
+    break;
+  case QLLG_SOLVE_MIXED_HALF:
+    its = cg_mixed(S, QLLG_I16, QLLG_F32, QLLG_I16, nrhs, x, b, mass, rsq, maxits, 0.1);
+    break;
+  case QLLG_SOLVE_MIXED_SINGLE:
+    its = cg_mixed(S, QLLG_F32, QLLG_F32, QLLG_F32, nrhs, x, b, mass, rsq, maxits, 0.1);
+    break;
+  default:
+    qllg_set_error("solve: unknown mode %d", mode);
+    return -1;
+  }
+  cudaEventRecord(S->ev1, qllg_stream());
+  if(its < 0) return -1;
+  if(info) {
+    memset(info, 0, sizeof(*info));
+    cudaEventSynchronize(S->ev1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, S->ev0, S->ev1);
+    info->seconds = ms*1e-3;
+    info->total_iters = its;
+    for(int i=0; i<nrhs; i++) {
+      info->iters[i] = S->hsc->iters[i];
+      info->rsq[i] = S->hsc->bsq[i] > 0 ? S->hsc->rsq[i]/S->hsc->bsq[i] : 0;
+      info->reliable_updates += S->hsc->nru[i];
+    }
+  }
+  return its;
+}
+
+int
+qllg_stag_solve_device(qllg_stag *S, int nrhs, void *x_dev, const void *b_dev,
+                       const double mass[], double rsq, int maxits, int mode,
+                       qllg_solve_info *info)
+{
+  if(S->master != QLLG_F64 && mode != QLLG_SOLVE_SINGLE) {
+    qllg_set_error("solve_device: a float operator supports QLLG_SOLVE_SINGLE only");
+    return -1;
+  }
+  if(mode == QLLG_SOLVE_SINGLE) {
+    /* device API vectors are FP64: convert around an FP32 solve */
+    size_t v32 = vec_bytes(S, QLLG_F32, nrhs);
+    void *b32 = ws_get(S, WS_B, v32), *x32 = ws_get(S, WS_OUT, v32);
+    if(!b32 || !x32) return -1;
+    if(qllg_k_spinor_convert(QLLG_F32, b32, QLLG_F64, b_dev, S->g.Vh, 3, nrhs, NULL)) return -1;
+    int its = solve_dev(S, nrhs, x32, b32, mass, rsq, maxits, mode, info);
+    if(its < 0) return -1;
+    if(qllg_k_spinor_convert(QLLG_F64, x_dev, QLLG_F32, x32, S->g.Vh, 3, nrhs, NULL)) return -1;
+    return its;
+  }
+  int its = solve_dev(S, nrhs, x_dev, b_dev, mass, rsq, maxits, mode, info);
+  if(its >= 0 && info && S->master == QLLG_F64) {
+    if(true_residual(S, nrhs, x_dev, b_dev, info->true_rsq)) return -1;
+  }
+  return its;
+}
+
+void *
+qllg_stag_vec_alloc(qllg_stag *S, int nrhs)
+{
+  return qllg_dmalloc(vec_bytes(S, QLLG_F64, nrhs));
+}
+
+void
+qllg_stag_vec_free(void *v)
+{
+  qllg_sync();
+  qllg_dfree(v);
+}
+
+/* host arrays [V][6] of the operator's precision, even half */
+static int
+vec_upload(qllg_stag *S, int prec, void *v_dev, int nrhs, void *const h[], int dbl)
+{
+  int Vh = S->g.Vh;
+  size_t blk = (dbl ? 8 : 4)*6*(size_t)Vh;
+  char *stage = qllg_stage(blk*nrhs);
+  if(!stage) return -1;
+  for(int r=0; r<nrhs; r++) if(qllg_h2d(stage + blk*r, h[r], blk)) return -1;
+  return qllg_k_spinor_from_aos(prec, v_dev, stage, dbl, Vh, 3, nrhs, 6*(size_t)Vh);
+}
+
+static int
+vec_download(qllg_stag *S, int prec, const void *v_dev, int nrhs, void *const h[], int dbl)
+{
+  int Vh = S->g.Vh;
+  size_t blk = (dbl ? 8 : 4)*6*(size_t)Vh;
+  char *stage = qllg_stage(blk*nrhs);
+  if(!stage) return -1;
+  if(qllg_k_spinor_to_aos(prec, v_dev, stage, dbl, Vh, 3, nrhs, 6*(size_t)Vh)) return -1;
+  for(int r=0; r<nrhs; r++)
+    if(qllg_check_cuda(cudaMemcpyAsync(h[r], stage + blk*r, blk, cudaMemcpyDeviceToHost,
+                                       qllg_stream()), "copy device to host")) return -1;
+  return qllg_sync();
+}
+
+int
+qllg_stag_vec_upload(qllg_stag *S, void *v_dev, int nrhs, void *const h[])
+{
+  return vec_upload(S, QLLG_F64, v_dev, nrhs, h, S->master == QLLG_F64);
+}
+
+int
+qllg_stag_vec_download(qllg_stag *S, const void *v_dev, int nrhs, void *const h[])
+{
+  return vec_download(S, QLLG_F64, v_dev, nrhs, h, S->master == QLLG_F64);
+}
+
+/* host-array solve; post_scale: x *= mass (solve2's scaling) when set */
+static int
+stag_solve_host(qllg_stag *S, int nrhs, void *const x[], void *const b[], const double mass[],
+                double rsq, int maxits, int mode, qllg_solve_info *info, int post_scale,
+                const double *scale_real)
+{
+  if(nrhs < 1 || nrhs > QLLG_MAXRHS) { qllg_set_error("solve: nrhs %d", nrhs); return -1; }
+  int n = pad_nrhs(nrhs);
+  int dbl = S->master == QLLG_F64;
+  int prec = (mode == QLLG_SOLVE_SINGLE) ? QLLG_F32 : QLLG_F64;
+  if(!dbl && mode != QLLG_SOLVE_SINGLE) {
+    qllg_set_error("solve: a float operator supports QLLG_SOLVE_SINGLE only");
+    return -1;
+  }
+  size_t vb = vec_bytes(S, prec, n);
+  void *bd = ws_get(S, WS_B, vb), *xd = ws_get(S, WS_OUT, vb);
+  if(!bd || !xd) return -1;
+  void *hb[QLLG_MAXRHS];
+  double m[QLLG_MAXRHS];
+  for(int r=0; r<n; r++) { hb[r] = b[r < nrhs ? r : 0]; m[r] = mass[r < nrhs ? r : 0]; }
+  if(vec_upload(S, prec, bd, n, hb, dbl)) return -1;
+  if(n > nrhs) {   /* zero the padding rhs: they start inactive */
+    double zero[QLLG_MAXRHS], one[QLLG_MAXRHS];
+    for(int r=0; r<n; r++) { zero[r] = 0; one[r] = r < nrhs ? 1 : 0; }
+    double *dcoef = S->sc->tmp;
+    if(qllg_h2d(dcoef, one, sizeof(double)*n)) return -1;
+    if(qllg_k_axpby(prec, bd, prec, bd, NULL, 0.0, dcoef, 0.0, S->g.Vh, 3, n, NULL)) return -1;
+    (void)zero;
+  }
+  int its = solve_dev(S, n, xd, bd, m, rsq, maxits, mode, info);
+  if(its < 0) return -1;
+  if(info && dbl && prec == QLLG_F64) {
+    if(true_residual(S, n, xd, bd, info->true_rsq)) return -1;
+  }
+  if(post_scale) {
+    double sc[QLLG_MAXRHS];
+    for(int r=0; r<n; r++) sc[r] = scale_real[r < nrhs ? r : 0];
+    double *dcoef = S->sc->tmp;
+    if(qllg_h2d(dcoef, sc, sizeof(double)*n)) return -1;
+    if(qllg_k_axpby(prec, xd, prec, xd, NULL, 0.0, dcoef, 0.0, S->g.Vh, 3, n, NULL)) return -1;
+  }
+  void *hx[QLLG_MAXRHS];
+  char *scratch = NULL;
+  for(int r=0; r<n; r++) hx[r] = r < nrhs ? x[r] : NULL;
+  if(n > nrhs) {
+    scratch = malloc((dbl ? 8 : 4)*6*(size_t)S->g.Vh);
+    for(int r=nrhs; r<n; r++) hx[r] = scratch;
+  }
+  int rc = vec_download(S, prec, xd, n, hx, dbl);
+  free(scratch);
+  return rc ? -1 : its;
+}
+
+int
+qllg_stag_solve(qllg_stag *S, int nrhs, void *const x[], void *const b[], const double mass[],
+                double rsq, int maxits, int mode, qllg_solve_info *info)
+{
+  return stag_solve_host(S, nrhs, x, b, mass, rsq, maxits, mode, info, 0, NULL);
+}
+
+int
+qllg_stag_nbr_table(const int dims[4], int parity, int slot, int *host_out)
+{
+  qllg_geom g;
+  if(qllg_runtime_init() || qllg_geom_from_dims(&g, dims)) return -1;
+  int *d = qllg_dmalloc(sizeof(int)*g.Vh);
+  if(!d) return -1;
+  int rc = qllg_k_stag_nbr_table(&g, parity, slot, d);
+  if(!rc) rc = qllg_d2h(host_out, d, sizeof(int)*g.Vh);
+  qllg_dfree(d);
+  return rc;
+}
+
+/* ------------------------------------------------- QLL drop-in layer */
+
+/* private block behind StaggeredLinks.t: the Transporter records the
+ * reference fills, then the device operator; t points at its start */
+typedef struct {
+  char t[16][sizeof(TransporterD)];
+  qllg_stag *S;
+  int own;          /* destroy S with this link set */
+  int parity;       /* -1 all, 0 even, 1 odd */
+} links_priv;
+
+static int
+sub_parity(const char *sub)
+{
+  return (sub && sub[0] == 'e') ? 0 : ((sub && sub[0] == 'o') ? 1 : -1);
+}
+
+static const char *
+parity_sub(int p)
+{
+  return p == 0 ? "even" : (p == 1 ? "odd" : "all");
+}
+
+#define DEFINE_STAG_DROPIN(S_, real, DBL)                                          \
+static void                                                                       \
+links_fill##S_(StaggeredLinks##S_ *sl, Layout *l, real *u[], real *u3[], char *sub,\
+               qllg_stag *S, int own, int fb)                                     \
+{                                                                                 \
+  links_priv *pv = calloc(1, sizeof(links_priv));                                 \
+  pv->S = S;                                                                      \
+  pv->own = own;                                                                  \
+  pv->parity = sub_parity(sub);                                                   \
+  int n = S ? S->nslots : (u3 ? 16 : 8);                                          \
+  Transporter##S_ *t = (Transporter##S_ *)pv->t;                                  \
+  for(int i=0; i<n; i++) {                                                        \
+    t[i].u = u3 ? ((i & 1) ? u3[i/2] : u[i/2]) : u[i];                            \
+    t[i].nelem = 6;                                                               \
+    t[i].nc = 3;                                                                  \
+    layoutSubset(&t[i].sub, l, sub);                                              \
+    t[i].backward = 0;                                                            \
+  }                                                                               \
+  sl->t = t;                                                                      \
+  sl->n = n;                                                                      \
+  sl->massFac = (pv->parity >= 0) ? 0 : 1;                                        \
+  sl->fb = fb;                                                                    \
+}                                                                                 \
+                                                                                  \
+static qllg_stag *                                                                \
+links_op##S_(StaggeredLinks##S_ *sl)                                              \
+{                                                                                 \
+  return sl && sl->t ? ((links_priv *)(void *)sl->t)->S : NULL;                   \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+createStaggeredLinks##S_(StaggeredLinks##S_ *sl, Layout *l, real *u[], real *u3[],\
+                         char *sub)                                               \
+{                                                                                 \
+  qllg_geom g;                                                                    \
+  memset(sl, 0, sizeof(*sl));                                                     \
+  if(qllg_geom_from_layout(&g, l)) return;                                        \
+  qllg_stag *S = DBL ? qllg_stag_create(g.L, (double *const *)u, (double *const *)u3) \
+                     : qllg_stag_create_f(g.L, (float *const *)u, (float *const *)u3); \
+  if(!S) return;                                                                  \
+  links_fill##S_(sl, l, u, u3, sub, S, 1, 0);                                     \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+freeStaggeredLinks##S_(StaggeredLinks##S_ *sl)                                    \
+{                                                                                 \
+  if(!sl || !sl->t) return;                                                       \
+  links_priv *pv = (links_priv *)(void *)sl->t;                                   \
+  if(pv->own) qllg_stag_destroy(pv->S);                                           \
+  free(pv);                                                                       \
+  sl->t = NULL;                                                                   \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+dslash2##S_(StaggeredLinks##S_ *d, real *x, real mass, real *y)                   \
+{                                                                                 \
+  qllg_stag *S = links_op##S_(d);                                                 \
+  if(!S) { qllg_set_error("dslash2: links not created"); return; }               \
+  mass *= d->massFac;                                                             \
+  links_priv *pv = (links_priv *)(void *)d->t;                                    \
+  qllg_stag_dslash(S, x, (double)mass, y, parity_sub(pv->parity));                \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+createStaggeredSolver##S_(StaggeredSolver##S_ *ss, Layout *l, real *u[],          \
+                          real *u3[], char *sub)                                  \
+{                                                                                 \
+  (void)sub;                                                                      \
+  memset(ss, 0, sizeof(*ss));                                                     \
+  qllg_geom g;                                                                    \
+  if(qllg_geom_from_layout(&g, l)) return;                                        \
+  qllg_stag *S = DBL ? qllg_stag_create(g.L, (double *const *)u, (double *const *)u3) \
+                     : qllg_stag_create_f(g.L, (float *const *)u, (float *const *)u3); \
+  if(!S) return;                                                                  \
+  links_fill##S_(&ss->sle, l, u, u3, "even", S, 1, 0);                            \
+  links_fill##S_(&ss->slo, l, u, u3, "odd", S, 0, 0);                             \
+  ss->v = NULL;                                                                   \
+  cglsInit##S_(&ss->cgls, 6*l->nEvenOuter);                                       \
+  layoutSubset(&ss->sube, l, "even");                                             \
+  layoutSubset(&ss->subo, l, "odd");                                              \
+  ss->noscale = 0;                                                                \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+freeStaggeredSolver##S_(StaggeredSolver##S_ *ss)                                  \
+{                                                                                 \
+  cglsFree##S_(&ss->cgls);                                                        \
+  freeStaggeredLinks##S_(&ss->slo);                                               \
+  freeStaggeredLinks##S_(&ss->sle);                                               \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+solve2##S_(StaggeredSolver##S_ *ss, real *x, real mass, real *y, double rsq,      \
+           int maxits, char *sub)                                                 \
+{                                                                                 \
+  (void)sub;                                                                      \
+  qllg_stag *S = links_op##S_(&ss->sle);                                          \
+  if(!S) { qllg_set_error("solve2: solver not created"); return -1; }             \
+  ss->mass = mass;                                                                \
+  if(rsq < 0) { ss->cgls.verbose = 3; rsq = -rsq; }                               \
+  double m = ss->mass, sc = (double)mass;                                         \
+  void *xa[1] = {x}, *ya[1] = {y};                                                \
+  int its = stag_solve_host(S, 1, xa, ya, &m, rsq, maxits,                        \
+                            DBL ? QLLG_SOLVE_DOUBLE : QLLG_SOLVE_SINGLE, NULL,    \
+                            !ss->noscale, &sc);                                   \
+  ss->its = its;                                                                  \
+  return its;                                                                     \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+solve##S_(real *x, real *u[8], real *u3[8], real mass, real *y, double rsq,       \
+          char *sub)                                                              \
+{                                                                                 \
+  Layout *l = qllg_current_layout();                                              \
+  if(!l) { qllg_set_error("solve: call stagDslashSetup first"); return -1; }      \
+  StaggeredSolver##S_ ss;                                                         \
+  createStaggeredSolver##S_(&ss, l, u, u3, sub);                                  \
+  if(!ss.sle.t) return -1;                                                        \
+  int its = solve2##S_(&ss, x, mass, y, rsq, 1000000, sub);                       \
+  freeStaggeredSolver##S_(&ss);                                                   \
+  return its;                                                                     \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+cglsInit##S_(Cgls##S_ *cgls, int nelem)                                           \
+{                                                                                 \
+  memset(cgls, 0, sizeof(*cgls));                                                 \
+  cgls->nelem = nelem;                                                            \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+cglsFree##S_(Cgls##S_ *cgls)                                                      \
+{                                                                                 \
+  (void)cgls;                                                                     \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+stagLinop##S_(real *Ax, real *x, LinopInfo *li, void *args, ThreadCtx *TC)        \
+{                                                                                 \
+  (void)Ax; (void)x; (void)li; (void)args; (void)TC;                              \
+  qllg_set_error("stagLinop runs inside cgSolve/cgmsSolve only");                 \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+cgSolve##S_(Cgls##S_ *cgls, real *x, real *b, Linop##S_ *Aop, void *Aargs,        \
+            Linop##S_ *Mop, void *Margs, double rsq, int itnlim)                  \
+{                                                                                 \
+  (void)cgls; (void)Margs;                                                        \
+  if(Aop != stagLinop##S_ || Mop) {                                               \
+    qllg_set_error("cgSolve: the operator must be stagLinop with no preconditioner"); \
+    return -1;                                                                    \
+  }                                                                               \
+  StaggeredSolver##S_ *ss = (StaggeredSolver##S_ *)Aargs;                         \
+  qllg_stag *S = links_op##S_(&ss->sle);                                          \
+  if(!S) { qllg_set_error("cgSolve: solver not created"); return -1; }            \
+  double m = ss->mass;                                                            \
+  void *xa[1] = {x}, *ba[1] = {b};                                                \
+  return stag_solve_host(S, 1, xa, ba, &m, rsq, itnlim,                           \
+                         DBL ? QLLG_SOLVE_DOUBLE : QLLG_SOLVE_SINGLE, NULL, 0, NULL); \
+}
+
+DEFINE_STAG_DROPIN(D, double, 1)
+DEFINE_STAG_DROPIN(F, float, 0)

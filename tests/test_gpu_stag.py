@@ -1,0 +1,162 @@
+"""GPU parity of the asqtad staggered path against the CPU oracle, through
+the C-ABI: neighbour tables (bit-exact), dslash2 (FP64 1e-12, FP32 1e-5
+relative), solve2 (same iteration count in FP64; solutions within 10x the
+solver tolerance), multi-rhs and mixed-precision solves (true residual
+1e-8 in FP64)."""
+import ctypes
+from ctypes import byref, c_double, c_float, c_int
+
+import numpy as np
+import pytest
+
+import oracle_lib as orc
+from inputs import as_dtype, asqtad_links, relerr
+from qll_gb300 import qll
+
+pytestmark = pytest.mark.gpu
+
+DIMS = (4, 4, 6, 8)
+TOL = {"D": 1e-12, "F": 1e-5}
+DT = {"D": np.float64, "F": np.float32}
+CT = {"D": c_double, "F": c_float}
+
+
+def _links(prec, dims=DIMS):
+    u, u3 = asqtad_links(dims)
+    return as_dtype(u, DT[prec]), as_dtype(u3, DT[prec])
+
+
+@pytest.mark.parametrize("dims", [(4, 4, 6, 8), (8, 4, 4, 6)])
+def test_neighbour_tables_bit_exact(dims):
+    L = qll.load()
+    V = int(np.prod(dims))
+    Vh = V//2
+    for parity in (0, 1):
+        for slot in range(16):
+            out = np.zeros(Vh, dtype=np.int32)
+            rc = L.qllg_stag_nbr_table(qll.dims_c(dims), parity, slot, qll.ptr(out))
+            assert rc == 0, qll.last_error()
+            ref = orc.stag_slot_table(dims, slot, 1, parity)
+            assert np.array_equal(out, ref[parity*Vh:(parity+1)*Vh]), (parity, slot)
+
+
+@pytest.mark.parametrize("prec", ["D", "F"])
+@pytest.mark.parametrize("sub", ["all", "even", "odd"])
+def test_dslash2_matches_oracle(prec, sub):
+    L = qll.load()
+    lay = qll.setup_layout(DIMS, prec)
+    u, u3 = _links(prec)
+    S = qll.D if prec == "D" else qll.F
+    sl = S["StaggeredLinks"]()
+    getattr(L, "createStaggeredLinks" + prec)(byref(sl), byref(lay), qll.ptr_array(u, CT[prec]),
+                                              qll.ptr_array(u3, CT[prec]), sub.encode())
+    assert sl.t, qll.last_error()
+    y = qll.gen_source(DIMS, 31, 6, "all").astype(DT[prec])
+    x = np.full_like(y, 7.0)
+    getattr(L, "dslash2" + prec)(byref(sl), qll.ptr(x), CT[prec](0.25), qll.ptr(y))
+    assert not qll.last_error(), qll.last_error()
+    ref = orc.dslash(DIMS, u, u3, 0.25, y, sub)
+    Vh = x.shape[0]//2
+    rng = {"all": slice(0, 2*Vh), "even": slice(0, Vh), "odd": slice(Vh, 2*Vh)}[sub]
+    assert relerr(x[rng], ref[rng]) < TOL[prec]
+    # sites outside the subset are not written
+    if sub != "all":
+        other = slice(Vh, 2*Vh) if sub == "even" else slice(0, Vh)
+        assert np.all(x[other] == 7.0)
+    getattr(L, "freeStaggeredLinks" + prec)(byref(sl))
+
+
+def _make_solver(prec, dims=DIMS):
+    L = qll.load()
+    lay = qll.setup_layout(dims, prec)
+    u, u3 = _links(prec, dims)
+    S = qll.D if prec == "D" else qll.F
+    ss = S["StaggeredSolver"]()
+    getattr(L, "createStaggeredSolver" + prec)(byref(ss), byref(lay), qll.ptr_array(u, CT[prec]),
+                                               qll.ptr_array(u3, CT[prec]), b"even")
+    assert ss.sle.t, qll.last_error()
+    return L, lay, ss, u, u3
+
+
+@pytest.mark.parametrize("prec", ["D", "F"])
+def test_solve2_matches_oracle(prec):
+    L, lay, ss, u, u3 = _make_solver(prec)
+    b = qll.gen_source(DIMS, 2001, 6, "even").astype(DT[prec])
+    rsq = 1e-16 if prec == "D" else 1e-10
+    x = np.zeros_like(b)
+    its = getattr(L, "solve2" + prec)(byref(ss), qll.ptr(x), CT[prec](0.1), qll.ptr(b), rsq,
+                                      2000, b"even")
+    assert its > 0, qll.last_error()
+    assert ss.its == its
+    its_o, xo, _ = orc.solve2(DIMS, u, u3, 0.1, b, rsq, 2000)
+    Vh = b.shape[0]//2
+    if prec == "D":
+        assert abs(its - its_o) <= 1
+        assert relerr(x[:Vh], xo[:Vh]) < 10*np.sqrt(rsq)
+    else:
+        assert abs(its - its_o) <= 3
+        assert relerr(x[:Vh], xo[:Vh]) < 1e-4
+    assert np.all(x[Vh:] == 0)
+    getattr(L, "freeStaggeredSolver" + prec)(byref(ss))
+
+
+def test_solve2_noscale_and_mass_zero_scaling():
+    L, lay, ss, u, u3 = _make_solver("D")
+    b = qll.gen_source(DIMS, 2002, 6, "even")
+    x1 = np.zeros_like(b)
+    ss.noscale = 1
+    L.solve2D(byref(ss), qll.ptr(x1), 0.2, qll.ptr(b), 1e-18, 2000, b"even")
+    ss.noscale = 0
+    x2 = np.zeros_like(b)
+    L.solve2D(byref(ss), qll.ptr(x2), 0.2, qll.ptr(b), 1e-18, 2000, b"even")
+    Vh = b.shape[0]//2
+    assert relerr(x2[:Vh], 0.2*x1[:Vh]) < 1e-14
+    L.freeStaggeredSolverD(byref(ss))
+
+
+def _native(dims=DIMS):
+    L = qll.load()
+    u, u3 = asqtad_links(dims)
+    S = L.qllg_stag_create(qll.dims_c(dims), qll.vp_array(u), qll.vp_array(u3))
+    assert S, qll.last_error()
+    return L, S, u, u3
+
+
+@pytest.mark.parametrize("nrhs", [1, 3, 4, 16])
+def test_multi_rhs_double_matches_single(nrhs):
+    L, S, u, u3 = _native()
+    masses = [0.1 + 0.05*k for k in range(nrhs)]
+    bs = [qll.gen_source(DIMS, 3000 + k, 6, "even") for k in range(nrhs)]
+    xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+    info = qll.SolveInfo()
+    its = L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs),
+                            (c_double*nrhs)(*masses), 1e-16, 3000, qll.SOLVE_DOUBLE, byref(info))
+    assert its > 0, qll.last_error()
+    Vh = bs[0].shape[0]//2
+    for k in range(nrhs):
+        its_o, xo, _ = orc.solve2(DIMS, u, u3, masses[k], bs[k], 1e-16, 3000, noscale=1)
+        assert abs(info.iters[k] - its_o) <= 1
+        assert relerr(xs[k][:Vh], xo[:Vh]) < 1e-7
+        assert info.true_rsq[k] < 1e-15
+    L.qllg_stag_destroy(S)
+
+
+@pytest.mark.parametrize("mode", [qll.SOLVE_MIXED_HALF, qll.SOLVE_MIXED_SINGLE])
+@pytest.mark.parametrize("nrhs", [1, 8])
+def test_mixed_precision_reaches_fp64_residual(mode, nrhs):
+    L, S, u, u3 = _native()
+    masses = [0.05 + 0.01*k for k in range(nrhs)]
+    bs = [qll.gen_source(DIMS, 4000 + k, 6, "even") for k in range(nrhs)]
+    xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+    info = qll.SolveInfo()
+    its = L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs),
+                            (c_double*nrhs)(*masses), 1e-16, 5000, mode, byref(info))
+    assert its > 0, qll.last_error()
+    assert info.reliable_updates > 0
+    Vh = bs[0].shape[0]//2
+    for k in range(nrhs):
+        # true residual of the FP64 operator, recomputed in FP64
+        assert info.true_rsq[k] < 1e-16*1.0001, (k, info.true_rsq[k])
+        its_o, xo, _ = orc.solve2(DIMS, u, u3, masses[k], bs[k], 1e-16, 5000, noscale=1)
+        assert relerr(xs[k][:Vh], xo[:Vh]) < 1e-7
+    L.qllg_stag_destroy(S)
