@@ -1,0 +1,385 @@
+"""Benchmark of the asqtad CG hot path on GB300.
+
+Workload (the configuration the headline metric is quoted on): 32^3 x 64
+lattice, SU(3) links exp(i 0.4 H) with staggered phases, fat7/asqtad
+smearing on the GPU, m = 0.01, a block of 16 Gaussian sources solved
+together to |r|^2 < 1e-16 |b|^2 (true residual 1e-8) by the mixed-precision
+CG: 16-bit storage with per-site scale, FP32 arithmetic, FP64 reliable
+updates, multi-rhs Dslash reusing each link load across the 16 sources.
+A step is one such 16-source solve; value = solves per second.
+
+--impl reference times the reference's algorithm on the host CPU cores: the
+reference cannot be compiled here, so it is the CPU oracle (a C restatement
+of QLL's FP64 solve2/cgSolveT), run for a bounded number of CG iterations
+and scaled to a full solve by the iteration count of the FP64 CG.
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+For N > 1 each rank solves its own block (replicas; no collective in the
+data path); the timed region is bracketed by a barrier and the max over
+ranks is reported.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = (32, 32, 32, 64)
+EPS = 0.4
+MASS = 0.01
+NRHS = 16
+RSQ = 1e-16
+MAXITS = 20000
+SEED_GAUGE = 1004
+SEED_SRC = 2400
+WORKLOAD = "asqtad_cg_32^3x64_m0.01_eps0.4_16rhs_mixed16_tol1e-8"
+METRIC = "mixed-precision multi-RHS asqtad CG solves/s at 1e-8 true residual"
+# iterations of the FP64 CG (cgSolveT) on this workload, measured with the
+# library's FP64 solver on GB300 (same recurrence as the reference)
+FP64_ITERS_MEASURED = None
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region"""
+
+    def __init__(self, out):
+        self.out = out
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.out, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self, gpu_index=0):
+        try:
+            rows = [r.split(",") for r in open(self.out).read().strip().splitlines()]
+        except OSError:
+            return None
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        rows = [r for r in rows if r[0] == str(gpu_index)] or rows
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from qll_gb300 import qll
+    L = qll.load()
+    L.qllg_stag_create_asqtad.restype = ctypes.c_void_p
+    L.qllg_stag_create_asqtad.argtypes = [ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_void_p),
+                                          ctypes.POINTER(qll.Fat7Coeffs)]
+    L.qllg_launch_count.restype = ctypes.c_ulonglong
+    L.qllg_stag_get_links.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+    L.qllg_stag_device_bytes.restype = ctypes.c_size_t
+    stream = torch.cuda.current_stream()
+    L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
+
+    t0 = time.time()
+    thin = qll.gen_gauge(DIMS, SEED_GAUGE + 17*rank, EPS, ks=True)
+    coef = qll.asqtad_coeffs()
+    S = L.qllg_stag_create_asqtad(qll.dims_c(DIMS), qll.vp_array(thin), ctypes.byref(coef))
+    if not S:
+        raise RuntimeError(qll.last_error())
+    S = ctypes.c_void_p(S)
+    del thin
+    srcs = [qll.gen_source(DIMS, SEED_SRC + 100*rank + r, 6, "even") for r in range(NRHS)]
+    xs = [np.zeros_like(srcs[0]) for _ in range(NRHS)]
+    masses = (ctypes.c_double*NRHS)(*([MASS]*NRHS))
+    b_dev = L.qllg_stag_vec_alloc(S, NRHS)
+    x_dev = L.qllg_stag_vec_alloc(S, NRHS)
+    if L.qllg_stag_vec_upload(S, b_dev, NRHS, qll.vp_array(srcs)):
+        raise RuntimeError(qll.last_error())
+    log("setup %.1fs (gauge, GPU fat7, sources)" % (time.time() - t0))
+
+    info = qll.SolveInfo()
+
+    def solve(mode=qll.SOLVE_MIXED_HALF, nrhs=NRHS, x=x_dev, b=b_dev):
+        its = L.qllg_stag_solve_device(S, nrhs, x, b, masses, RSQ, MAXITS, mode,
+                                       ctypes.byref(info))
+        if its < 0:
+            raise RuntimeError(qll.last_error())
+        return its
+
+    # plain FP64 single-rhs GPU CG: the comparison the target is stated on
+    b1 = L.qllg_stag_vec_alloc(S, 1)
+    x1 = L.qllg_stag_vec_alloc(S, 1)
+    L.qllg_stag_vec_upload(S, b1, 1, qll.vp_array(srcs[:1]))
+    torch.cuda.synchronize()
+    t1 = time.time()
+    its64 = solve(qll.SOLVE_DOUBLE, 1, x1, b1)
+    torch.cuda.synchronize()
+    fp64_s = time.time() - t1
+    fp64_true = info.true_rsq[0]
+    log("FP64 single-rhs CG: %d iterations, %.3fs, true rsq %.2e" % (its64, fp64_s, fp64_true))
+
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    L.qllg_timing_enable(1)
+    L.qllg_timing_reset()
+    n0 = L.qllg_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters, truer = [], []
+    with Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                             else "/tmp", "bench_clocks_r%d.csv" % rank)) as clk:
+        torch.cuda.nvtx.range_push("timed")
+        ev0.record(stream)
+        for _ in range(args.steps):
+            iters.append(solve())
+            truer.append(max(info.true_rsq[r] for r in range(NRHS)))
+        ev1.record(stream)
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+    nlaunch = int(L.qllg_launch_count() - n0)
+    ms = ev0.elapsed_time(ev1)
+    cnt, tot = ctypes.c_int(), ctypes.c_double()
+    L.qllg_timing_read(b"stag_dslash_i16_n16", ctypes.byref(cnt), ctypes.byref(tot))
+    L.qllg_timing_enable(0)
+    t_max = ms
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = ws*NRHS*args.steps/(t_max*1e-3)
+
+    # end to end through the host-array API: H2D of the sources and D2H of
+    # the solutions are inside the timed region
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    te = time.time()
+    for _ in range(e2e_steps):
+        its = L.qllg_stag_solve(S, NRHS, qll.vp_array(xs), qll.vp_array(srcs), masses, RSQ,
+                                MAXITS, qll.SOLVE_MIXED_HALF, ctypes.byref(info))
+        if its < 0:
+            raise RuntimeError(qll.last_error())
+    torch.cuda.synchronize()
+    te = time.time() - te
+    if ws > 1:
+        t = torch.tensor([te], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    e2e = ws*NRHS*e2e_steps/te
+    Vh = srcs[0].shape[0]//2
+    bytes_io = NRHS*Vh*6*8
+
+    # roofline of the dominant kernel: the 16-rhs 16-bit asqtad half-Dslash
+    # algorithmic bytes per output site and rhs (16 neighbour spinors + 1
+    # store, links shared by the 16 rhs): (8*18*2 + 8*18*2)/16 + 17*(6*2+4)
+    per_site_rhs = (8*18*2 + 8*18*2)/16 + 17*(6*2 + 4)
+    launch_bytes = per_site_rhs*Vh*NRHS
+    avg_ms = tot.value/max(cnt.value, 1)
+    achieved = launch_bytes/(avg_ms*1e-3)/1e9
+    pk = peaks()
+    peak = pk.get("hbm_gbs")
+    compulsory = (8*18*2 + 8*18*2)/16 + 2*(6*2 + 4)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max/args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16-storage(int16+scale)/fp32/fp64-reliable",
+        "data": "synthetic (seeded SU(3) gauge, fat7 on GPU, Gaussian sources)",
+        "config": {"workload": WORKLOAD, "lattice": list(DIMS), "mass": MASS, "eps": EPS,
+                   "nrhs": NRHS, "tol_true_residual": 1e-8, "parallelism": "replicas",
+                   "l2": "inputs larger than L2 (links 1.2 GB 16-bit + 4.8 GB FP64)"},
+        "iters_per_solve": iters, "max_true_rsq": max(truer),
+        "fp64_single_rhs": {"solves_per_s": 1/fp64_s, "iters": its64, "true_rsq": fp64_true,
+                            "speedup_of_value": value/ws*fp64_s},
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": bytes_io,
+                "d2h_bytes_per_step": bytes_io},
+        "roofline": {"kernel": "stag_dslash<i16,i16,16 slots,16 rhs>", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved/peak if peak else None,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else None,
+                     "algorithmic_bytes_per_launch": launch_bytes,
+                     "avg_launch_ms": avg_ms, "launches_timed": cnt.value,
+                     "compulsory_frac": compulsory*Vh*NRHS/(avg_ms*1e-3)/1e9/peak if peak else None,
+                     "traffic": None},
+        "gpu_launches": nlaunch,
+        "clocks": clk.summary(local),
+        "device_bytes": int(L.qllg_stag_device_bytes(S)),
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(L, S, its64, bounded_iters=args.cpu_iters)
+    L.qllg_stag_vec_free(b_dev)
+    L.qllg_stag_vec_free(x_dev)
+    L.qllg_stag_vec_free(b1)
+    L.qllg_stag_vec_free(x1)
+    L.qllg_stag_destroy(S)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------- CPU baseline
+def _oracle():
+    from ctypes import POINTER
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "liboracle.so"))
+    lib.or_solve2D.restype = ctypes.c_int
+    lib.or_num_threads.restype = ctypes.c_int
+    return lib, POINTER
+
+
+def cpu_time_iters(u16, src, iters):
+    """seconds per FP64 CG iteration of the oracle (cgSolveT restated) on
+    the host cores, from a bounded run of `iters` iterations"""
+    lib, POINTER = _oracle()
+    PA = (POINTER(ctypes.c_double)*8)
+    u = PA(*[u16[2*i].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
+    u3 = PA(*[u16[2*i+1].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
+    x = np.zeros_like(src)
+    fr = ctypes.c_double()
+    lib.or_solve2D((ctypes.c_int*4)(*DIMS), x.ctypes.data_as(POINTER(ctypes.c_double)), u, u3,
+                   ctypes.c_double(MASS), src.ctypes.data_as(POINTER(ctypes.c_double)),
+                   ctypes.c_double(RSQ), 2, 1, ctypes.byref(fr))       # warm caches
+    t = time.time()
+    its = lib.or_solve2D((ctypes.c_int*4)(*DIMS), x.ctypes.data_as(POINTER(ctypes.c_double)),
+                         u, u3, ctypes.c_double(MASS),
+                         src.ctypes.data_as(POINTER(ctypes.c_double)), ctypes.c_double(RSQ),
+                         iters, 1, ctypes.byref(fr))
+    dt = time.time() - t
+    return dt/its, lib.or_num_threads()
+
+
+def cpu_baseline(L, S, its64, bounded_iters=30):
+    from qll_gb300 import qll
+    V = int(np.prod(DIMS))
+    links = [np.zeros((V, 18)) for _ in range(16)]
+    if L.qllg_stag_get_links(S, qll.vp_array(links)):
+        raise RuntimeError(qll.last_error())
+    src = qll.gen_source(DIMS, SEED_SRC, 6, "even")
+    per_it, cores = cpu_time_iters(links, src, bounded_iters)
+    return {"value": 1.0/(per_it*its64), "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": "%d FP64 CG iterations (oracle restatement of cgSolveT + dslash2) on the "
+                      "32^3x64 links, %.3f s/iteration, scaled by the %d iterations the FP64 CG "
+                      "needs to converge; one source per solve" % (bounded_iters, per_it, its64)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from qll_gb300 import qll
+    # host-only inputs: thin links, oracle fat7, negative-adjoint backward links
+    lib, POINTER = _oracle()
+    thin = qll.gen_gauge(DIMS, SEED_GAUGE, EPS, ks=True)
+    V = int(np.prod(DIMS))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as orc
+    fl, ll = orc.smear_fat7(DIMS, thin, qll.asqtad_coeffs())
+    links = []
+    for mu in range(4):
+        links += [fl[mu], ll[mu], orc.negadj_back(DIMS, fl[mu], mu, 1),
+                  orc.negadj_back(DIMS, ll[mu], mu, 3)]
+    # links in slot order 4mu+2b+naik -> u[2mu+b], u3[2mu+b]
+    order = []
+    for mu in range(4):
+        order += [links[4*mu], links[4*mu+1], links[4*mu+2], links[4*mu+3]]
+    src = qll.gen_source(DIMS, SEED_SRC, 6, "even")
+    its64 = FP64_ITERS_MEASURED or args.fp64_iters
+    vals = []
+    for _ in range(args.warmup):
+        cpu_time_iters(order, src, args.cpu_iters)
+    for _ in range(args.steps):
+        per_it, cores = cpu_time_iters(order, src, args.cpu_iters)
+        vals.append(1.0/(per_it*its64))
+    value = statistics.median(vals)
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+           "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded SU(3) gauge, oracle fat7, Gaussian source)",
+           "config": {"workload": WORKLOAD, "lattice": list(DIMS), "mass": MASS, "eps": EPS,
+                      "nrhs": NRHS, "tol_true_residual": 1e-8, "parallelism": "host threads"},
+           "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                            "sample": "%d FP64 CG iterations per step (oracle restatement of "
+                                      "cgSolveT/dslash2; the reference needs Lua-generated "
+                                      "sources and QMP and does not compile here), scaled by "
+                                      "%d iterations to convergence" % (args.cpu_iters, its64)},
+           "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-iters", type=int, default=30)
+    ap.add_argument("--fp64-iters", type=int, default=2000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -72,6 +72,9 @@ qllg_stag *qllg_stag_create(const int dims[4], double *const fat[8], double *con
 qllg_stag *qllg_stag_create_f(const int dims[4], float *const fat[8], float *const lng[8]);
 void qllg_stag_destroy(qllg_stag *S);
 size_t qllg_stag_device_bytes(const qllg_stag *S);
+int qllg_stag_nslots(const qllg_stag *S);
+/* copy the FP64 link slots back to host arrays [V][18] (out[nslots]) */
+int qllg_stag_get_links(qllg_stag *S, double *const out[16]);
 
 /* x = mass*y + D y on the sites of sub (dslash2 semantics; "even"/"odd"
  * ignore the mass); host arrays [V][6] of the precision of the operator */
@@ -101,10 +104,42 @@ int qllg_stag_vec_download(qllg_stag *S, const void *v_dev, int nrhs, void *cons
  * index arithmetic */
 int qllg_stag_nbr_table(const int dims[4], int parity, int slot, int *host_out);
 
+/* ------------------------------------------ link preparation (GPU) */
+/* fat7/asqtad smearing of thin links u (and ulong for the Naik term, NULL
+ * = u), host [V][18] FP64 arrays (smearFat7 of lib/gauge.c:264-416) */
+int qllg_smear_fat7(const int dims[4], double *const fl[4], double *const ll[4],
+                    const Fat7Coeffs *coef, double *const u[4], double *const ulong_[4]);
+/* thin links -> fat7 -> the 16 slots (with -F^dagger(x-mu), -L^dagger(x-3mu)
+ * backward links) of a resident FP64 operator, built on the GPU */
+qllg_stag *qllg_stag_create_asqtad(const int dims[4], double *const thin[4],
+                                   const Fat7Coeffs *coef);
+/* the six plaquettes of gaugePlaq (normalised by 3V) */
+int qllg_plaq(const int dims[4], double *const u[4], double plaqs[6]);
+
+/* -------------------------------------------------- Wilson operator */
+typedef struct qllg_wilson qllg_wilson;
+/* u[8]: slot 2mu forward link, 2mu+1 backward link (host [V][18]) */
+qllg_wilson *qllg_wilson_create(const int dims[4], double *const u[8]);
+qllg_wilson *qllg_wilson_create_f(const int dims[4], float *const u[8]);
+void qllg_wilson_destroy(qllg_wilson *W);
+/* x = massp*y + W y on sub (massp already massFac*(4+m)); dag: g5 W g5 */
+int qllg_wilson_dslash(qllg_wilson *W, void *x, double massp, const void *y, const char *sub,
+                       int dag);
+/* even-odd normal-equation solve of the Schur complement
+ * S = (4+m) - W_eo W_oe/(4+m): CG on S^dagger S x = S^dagger b, stopping at
+ * |r|^2 < rsq |S^dagger b|^2; mode QLLG_SOLVE_DOUBLE or
+ * QLLG_SOLVE_MIXED_SINGLE; x, b host [V][24] FP64, even half; info->true_rsq
+ * is |b - S x|^2/|b|^2 in FP64 */
+int qllg_wilson_solve(qllg_wilson *W, void *x, const void *b, double mass, double rsq,
+                      int maxits, int mode, qllg_solve_info *info);
+
 /* kernel timing: when enabled, launches of the named kernel family are
  * bracketed by CUDA events on the library stream; read returns the count
- * and total milliseconds since the last reset */
+ * and total milliseconds since the last reset.  Families:
+ * "stag_dslash_<f64|f32|i16>_n<nrhs>", "wilson_dslash" */
 void qllg_timing_enable(int on);
+/* number of kernels the library has launched since load */
+unsigned long long qllg_launch_count(void);
 void qllg_timing_reset(void);
 int qllg_timing_read(const char *name, int *count, double *ms);
 

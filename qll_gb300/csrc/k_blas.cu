@@ -108,14 +108,14 @@ __global__ void link_from_aos(void *dev, const float *scale, const S *stage, int
   }
 }
 
-template <typename S>
-__global__ void link_to_aos(const double *dev, S *stage, int V)
+template <typename D2, typename S>
+__global__ void link_to_aos(const void *dev, S *stage, int V)
 {
-  const double2 *d = (const double2 *)dev;
+  const D2 *d = (const D2 *)dev;
   GRID_LOOP(i, (size_t)V) {
     S *m = stage + i*18;
 #pragma unroll
-    for(int k=0; k<9; k++) { double2 t = d[k*(size_t)V + i]; m[2*k] = (S)t.x; m[2*k+1] = (S)t.y; }
+    for(int k=0; k<9; k++) { D2 t = d[k*(size_t)V + i]; m[2*k] = (S)t.x; m[2*k+1] = (S)t.y; }
   }
 }
 
@@ -341,7 +341,7 @@ __global__ void cg_p_k(void *p, const void *r, int nsites, qllg_cg_scalars *s)
   else if(prec == QLLG_F32 && ncomp == 12) { constexpr int P = QLLG_F32, NC = 12; __VA_ARGS__; } \
   else { qllg_set_error("unsupported precision %d / components %d", prec, ncomp); return -1; }
 
-int done(const char *what) { return qllg_check_cuda(cudaGetLastError(), what); }
+int done(const char *what) { return qllg_launched(what); }
 
 } // namespace
 
@@ -416,11 +416,17 @@ qllg_k_link_from_aos(int prec, void *dev, float *scale, const void *stage, int d
 }
 
 extern "C" int
-qllg_k_link_to_aos(const double *dev, void *stage, int dbl, int V)
+qllg_k_link_to_aos(int prec, const void *dev, void *stage, int dbl, int V)
 {
   int g = grid_for((size_t)V, 0, 0);
-  if(dbl) link_to_aos<double><<<g,kT,0,qllg_stream()>>>(dev, (double *)stage, V);
-  else link_to_aos<float><<<g,kT,0,qllg_stream()>>>(dev, (float *)stage, V);
+  cudaStream_t st = qllg_stream();
+  if(prec == QLLG_F64) {
+    if(dbl) link_to_aos<double2,double><<<g,kT,0,st>>>(dev, (double *)stage, V);
+    else link_to_aos<double2,float><<<g,kT,0,st>>>(dev, (float *)stage, V);
+  } else if(prec == QLLG_F32) {
+    if(dbl) link_to_aos<float2,double><<<g,kT,0,st>>>(dev, (double *)stage, V);
+    else link_to_aos<float2,float><<<g,kT,0,st>>>(dev, (float *)stage, V);
+  } else { qllg_set_error("link_to_aos: precision %d", prec); return -1; }
   return done("link_to_aos");
 }
 

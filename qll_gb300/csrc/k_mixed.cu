@@ -137,27 +137,27 @@ mcg_update_k(void *xs, void *rs, const void *p, const void *Ap, int nsites,
   }
 }
 
-template <int PX, int NR>
+template <int PX, int NC, int NR>
 __global__ void mcg_accum_k(void *x64, void *xs, int nsites, qllg_cg_scalars *s)
 {
   size_t total = (size_t)nsites*NR;
   const int rhs = threadIdx.x % NR;
   if(*(volatile int *)&s->no_ru || !s->ru[rhs]) return;
   GRID_LOOP(t, total) {
-    Cx<double> xv[3];
-    Cx<float> sv[3], z[3];
-    SpinorIO<QLLG_F64,3>::load(x64, total, t, xv);
-    SpinorIO<PX,3>::load(xs, total, t, sv);
+    Cx<double> xv[NC];
+    Cx<float> sv[NC], z[NC];
+    SpinorIO<QLLG_F64,NC>::load(x64, total, t, xv);
+    SpinorIO<PX,NC>::load(xs, total, t, sv);
 #pragma unroll
-    for(int c=0; c<3; c++) { xv[c].r += sv[c].r; xv[c].i += sv[c].i; z[c].r = 0; z[c].i = 0; }
-    SpinorIO<QLLG_F64,3>::store(x64, total, t, xv);
-    SpinorIO<PX,3>::store(xs, total, t, z);
+    for(int c=0; c<NC; c++) { xv[c].r += sv[c].r; xv[c].i += sv[c].i; z[c].r = 0; z[c].i = 0; }
+    SpinorIO<QLLG_F64,NC>::store(x64, total, t, xv);
+    SpinorIO<PX,NC>::store(xs, total, t, z);
   }
 }
 
-template <int PS, int NR>
+template <int PS, int NC, int NR>
 __global__ void __launch_bounds__(kT)
-mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites,
+mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites, int stdform,
                qllg_cg_scalars *s, double *partial, unsigned *counter)
 {
   __shared__ double shm[kT];
@@ -167,18 +167,18 @@ mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites,
   double red[1] = {0};
   if(s->ru[rhs]) {
     GRID_LOOP(t, total) {
-      Cx<double> bv[3], tv[3];
-      SpinorIO<QLLG_F64,3>::load(b, total, t, bv);
-      SpinorIO<QLLG_F64,3>::load(t64, total, t, tv);
-      Cx<float> f[3];
+      Cx<double> bv[NC], tv[NC];
+      SpinorIO<QLLG_F64,NC>::load(b, total, t, bv);
+      SpinorIO<QLLG_F64,NC>::load(t64, total, t, tv);
+      Cx<float> f[NC];
 #pragma unroll
-      for(int c=0; c<3; c++) {
+      for(int c=0; c<NC; c++) {
         tv[c].r = bv[c].r - tv[c].r; tv[c].i = bv[c].i - tv[c].i;
         red[0] += tv[c].r*tv[c].r + tv[c].i*tv[c].i;
         f[c].r = (float)tv[c].r; f[c].i = (float)tv[c].i;
       }
-      SpinorIO<QLLG_F64,3>::store(r64, total, t, tv);
-      SpinorIO<PS,3>::store(rs, total, t, f);
+      SpinorIO<QLLG_F64,NC>::store(r64, total, t, tv);
+      SpinorIO<PS,NC>::store(rs, total, t, f);
     }
   }
   double *res[1] = {s->tmp};
@@ -189,6 +189,7 @@ mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites,
       for(int q=0; q<NR; q++) {
         if(s->ru[q]) {
           double r2 = s->tmp[q];
+          if(stdform) s->alpha[q] = r2/s->prev[q];
           s->rsq[q] = r2;
           s->maxr2[q] = r2;
           s->nru[q]++;
@@ -218,7 +219,7 @@ mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites,
   else if(px == QLLG_I16 && ps == QLLG_I16) { constexpr int PX = QLLG_I16, PS = QLLG_I16; __VA_ARGS__; } \
   else { qllg_set_error("mixed CG: precisions %d/%d", px, ps); return -1; }
 
-int done(const char *w) { return qllg_check_cuda(cudaGetLastError(), w); }
+int done(const char *w) { return qllg_launched(w); }
 
 } // namespace
 
@@ -256,24 +257,191 @@ qllg_k_mcg_update(int px, int ps, void *xs, void *rs, const void *p, const void 
 }
 
 extern "C" int
-qllg_k_mcg_accum(int px, void *x64, void *xs, int nsites, int nrhs, qllg_cg_scalars *s)
+qllg_k_mcg_accum(int px, void *x64, void *xs, int nsites, int ncomp, int nrhs, qllg_cg_scalars *s)
 {
   int g = grid_for((size_t)nsites*nrhs, 0);
   cudaStream_t st = qllg_stream();
-  if(px == QLLG_F32) { NR_SWITCH(nrhs, (mcg_accum_k<QLLG_F32,NR><<<g,kT,0,st>>>(x64, xs, nsites, s))); }
-  else if(px == QLLG_I16) { NR_SWITCH(nrhs, (mcg_accum_k<QLLG_I16,NR><<<g,kT,0,st>>>(x64, xs, nsites, s))); }
-  else { qllg_set_error("mcg_accum: precision %d", px); return -1; }
+  if(px == QLLG_F32 && ncomp == 3) { NR_SWITCH(nrhs, (mcg_accum_k<QLLG_F32,3,NR><<<g,kT,0,st>>>(x64, xs, nsites, s))); }
+  else if(px == QLLG_I16 && ncomp == 3) { NR_SWITCH(nrhs, (mcg_accum_k<QLLG_I16,3,NR><<<g,kT,0,st>>>(x64, xs, nsites, s))); }
+  else if(px == QLLG_F32 && ncomp == 12) { NR_SWITCH(nrhs, (mcg_accum_k<QLLG_F32,12,NR><<<g,kT,0,st>>>(x64, xs, nsites, s))); }
+  else { qllg_set_error("mcg_accum: precision %d components %d", px, ncomp); return -1; }
   return done("mcg_accum");
 }
 
 extern "C" int
 qllg_k_mcg_residual(int ps, void *r64, void *rs, const void *b, const void *t64, int nsites,
-                    int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+                    int ncomp, int nrhs, int stdform, qllg_cg_scalars *s, qllg_redbuf *rb)
 {
   int g = grid_for((size_t)nsites*nrhs, rb);
   cudaStream_t st = qllg_stream();
-  if(ps == QLLG_I16) { NR_SWITCH(nrhs, (mcg_residual_k<QLLG_I16,NR><<<g,kT,0,st>>>(r64, rs, b, t64, nsites, s, rb->partial, rb->counter))); }
-  else if(ps == QLLG_F32) { NR_SWITCH(nrhs, (mcg_residual_k<QLLG_F32,NR><<<g,kT,0,st>>>(r64, rs, b, t64, nsites, s, rb->partial, rb->counter))); }
-  else { qllg_set_error("mcg_residual: precision %d", ps); return -1; }
+  if(ps == QLLG_I16 && ncomp == 3) { NR_SWITCH(nrhs, (mcg_residual_k<QLLG_I16,3,NR><<<g,kT,0,st>>>(r64, rs, b, t64, nsites, stdform, s, rb->partial, rb->counter))); }
+  else if(ps == QLLG_F32 && ncomp == 3) { NR_SWITCH(nrhs, (mcg_residual_k<QLLG_F32,3,NR><<<g,kT,0,st>>>(r64, rs, b, t64, nsites, stdform, s, rb->partial, rb->counter))); }
+  else if(ps == QLLG_F32 && ncomp == 12) { NR_SWITCH(nrhs, (mcg_residual_k<QLLG_F32,12,NR><<<g,kT,0,st>>>(r64, rs, b, t64, nsites, stdform, s, rb->partial, rb->counter))); }
+  else { qllg_set_error("mcg_residual: precision %d components %d", ps, ncomp); return -1; }
   return done("mcg_residual");
+}
+
+// ----------------------------------------------------- standard-form CG
+namespace {
+
+template <int PX, int PS, int NC, int NR>
+__global__ void __launch_bounds__(kT)
+scg_init_k(void *x, void *r, void *p, const void *b64, void *x64, void *r64, int nsites,
+           qllg_cg_scalars *s, double *partial, unsigned *counter)
+{
+  typedef typename Calc<PX, PS>::T T;
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  double red[1] = {0};
+  GRID_LOOP(t, total) {
+    Cx<double> bv[NC], z[NC];
+    SpinorIO<QLLG_F64,NC>::load(b64, total, t, bv);
+    Cx<T> bt[NC], zt[NC];
+#pragma unroll
+    for(int c=0; c<NC; c++) {
+      red[0] += bv[c].r*bv[c].r + bv[c].i*bv[c].i;
+      z[c].r = 0; z[c].i = 0; zt[c].r = 0; zt[c].i = 0;
+      bt[c].r = (T)bv[c].r; bt[c].i = (T)bv[c].i;
+    }
+    SpinorIO<PX,NC>::store(x, total, t, zt);
+    SpinorIO<PS,NC>::store(r, total, t, bt);
+    SpinorIO<PS,NC>::store(p, total, t, bt);
+    if(x64) SpinorIO<QLLG_F64,NC>::store(x64, total, t, z);
+    if(r64) SpinorIO<QLLG_F64,NC>::store(r64, total, t, bv);
+  }
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, threadIdx.x % NR, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int any = 0;
+      for(int q=0; q<NR; q++) {
+        double bs = s->tmp[q];
+        s->bsq[q] = bs; s->rsq[q] = bs; s->maxr2[q] = bs; s->prev[q] = bs;
+        s->rsq_stop[q] *= bs;
+        s->iters[q] = 0; s->ru[q] = 0; s->nru[q] = 0;
+        s->active[q] = (bs > 0 && s->maxits > 0) ? 1 : 0;
+        any |= s->active[q];
+      }
+      s->done = !any;
+      s->no_ru = 1;
+      s->count = 0;
+    }
+  }
+}
+
+template <int PX, int PS, int NC, int NR>
+__global__ void __launch_bounds__(kT)
+scg_xr_k(void *x, void *r, const void *p, const void *Ap, int nsites, qllg_cg_scalars *s,
+         double *partial, unsigned *counter)
+{
+  typedef typename Calc<PX, PS>::T T;
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->done) return;
+  double red[1] = {0};
+  if(s->active[rhs]) {
+    const T alpha = (T)(s->rsq[rhs]/s->pnorm[rhs]);
+    GRID_LOOP(t, total) {
+      Cx<T> xv[NC], rv[NC], pv[NC], av[NC];
+      SpinorIO<PX,NC>::load(x, total, t, xv);
+      SpinorIO<PS,NC>::load(r, total, t, rv);
+      SpinorIO<PS,NC>::load(p, total, t, pv);
+      SpinorIO<PS,NC>::load(Ap, total, t, av);
+#pragma unroll
+      for(int c=0; c<NC; c++) {
+        xv[c].r = fma(alpha, pv[c].r, xv[c].r); xv[c].i = fma(alpha, pv[c].i, xv[c].i);
+        rv[c].r = fma(-alpha, av[c].r, rv[c].r); rv[c].i = fma(-alpha, av[c].i, rv[c].i);
+        red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
+      }
+      SpinorIO<PX,NC>::store(x, total, t, xv);
+      SpinorIO<PS,NC>::store(r, total, t, rv);
+    }
+  }
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int anyru = 0, any = 0;
+      const bool mixed = s->delta2 > 0;
+      for(int q=0; q<NR; q++) {
+        s->ru[q] = 0;
+        if(s->active[q]) {
+          double r2 = s->tmp[q];
+          s->iters[q]++;
+          s->prev[q] = s->rsq[q];
+          s->rsq[q] = r2;
+          s->alpha[q] = r2/s->prev[q];
+          if(mixed) {
+            if(r2 < s->delta2*s->maxr2[q] || r2 < s->rsq_stop[q] || s->iters[q] >= s->maxits ||
+               !(r2 == r2)) { s->ru[q] = 1; anyru = 1; }
+          } else if(!(r2 >= s->rsq_stop[q] && s->iters[q] < s->maxits)) {
+            s->active[q] = 0;
+          }
+        }
+        any |= s->active[q];
+      }
+      s->no_ru = !anyru;
+      s->done = !any;
+      s->count++;
+    }
+  }
+}
+
+template <int PS, int NC, int NR>
+__global__ void scg_p_k(void *p, const void *r, int nsites, qllg_cg_scalars *s)
+{
+  typedef typename Calc<PS, PS>::T T;
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->done || !s->active[rhs]) return;
+  const T beta = (T)s->alpha[rhs];
+  GRID_LOOP(t, total) {
+    Cx<T> pv[NC], rv[NC];
+    SpinorIO<PS,NC>::load(p, total, t, pv);
+    SpinorIO<PS,NC>::load(r, total, t, rv);
+#pragma unroll
+    for(int c=0; c<NC; c++) { pv[c].r = fma(beta, pv[c].r, rv[c].r); pv[c].i = fma(beta, pv[c].i, rv[c].i); }
+    SpinorIO<PS,NC>::store(p, total, t, pv);
+  }
+}
+
+} // namespace
+
+#define SCG_SWITCH(px, ps, ncomp, ...) \
+  if(px == QLLG_F64 && ps == QLLG_F64 && ncomp == 3) { constexpr int PX = QLLG_F64, PS = QLLG_F64, NC = 3; __VA_ARGS__; } \
+  else if(px == QLLG_F64 && ps == QLLG_F64 && ncomp == 12) { constexpr int PX = QLLG_F64, PS = QLLG_F64, NC = 12; __VA_ARGS__; } \
+  else if(px == QLLG_F32 && ps == QLLG_F32 && ncomp == 3) { constexpr int PX = QLLG_F32, PS = QLLG_F32, NC = 3; __VA_ARGS__; } \
+  else if(px == QLLG_F32 && ps == QLLG_F32 && ncomp == 12) { constexpr int PX = QLLG_F32, PS = QLLG_F32, NC = 12; __VA_ARGS__; } \
+  else if(px == QLLG_F32 && ps == QLLG_I16 && ncomp == 3) { constexpr int PX = QLLG_F32, PS = QLLG_I16, NC = 3; __VA_ARGS__; } \
+  else { qllg_set_error("standard CG: precisions %d/%d components %d", px, ps, ncomp); return -1; }
+
+extern "C" int
+qllg_k_scg_init(int px, int ps, void *x, void *r, void *p, const void *b64, void *x64,
+                void *r64, int nsites, int ncomp, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  SCG_SWITCH(px, ps, ncomp, NR_SWITCH(nrhs, (scg_init_k<PX,PS,NC,NR><<<g,kT,0,st>>>(x, r, p, b64, x64, r64, nsites, s, rb->partial, rb->counter))));
+  return done("scg_init");
+}
+
+extern "C" int
+qllg_k_scg_update_xr(int px, int ps, void *x, void *r, const void *p, const void *Ap, int nsites,
+                     int ncomp, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  SCG_SWITCH(px, ps, ncomp, NR_SWITCH(nrhs, (scg_xr_k<PX,PS,NC,NR><<<g,kT,0,st>>>(x, r, p, Ap, nsites, s, rb->partial, rb->counter))));
+  return done("scg_update_xr");
+}
+
+extern "C" int
+qllg_k_scg_update_p(int prec, void *p, const void *r, int nsites, int ncomp, int nrhs,
+                    qllg_cg_scalars *s)
+{
+  int g = grid_for((size_t)nsites*nrhs, 0);
+  cudaStream_t st = qllg_stream();
+  SCG_SWITCH(prec, prec, ncomp, NR_SWITCH(nrhs, (scg_p_k<PS,NC,NR><<<g,kT,0,st>>>(p, r, nsites, s))));
+  return done("scg_update_p");
 }

@@ -40,7 +40,7 @@ stag_dslash(qllg_stag_args a)
       int x[4];
       site_coords(G, p, site, x);
       Cx<T> acc[3], self[3];
-      if(a.self) SpinorIO<PS,3>::load(a.self, total, t, self);
+      if(a.self && a.mode == 1) SpinorIO<PS,3>::load(a.self, total, t, self);
       if(a.mode == 1) {
 #pragma unroll
         for(int c=0; c<3; c++) { acc[c].r = ca*self[c].r; acc[c].i = ca*self[c].i; }
@@ -68,6 +68,7 @@ stag_dslash(qllg_stag_args a)
           }
         }
       }
+      if(a.self && a.mode != 1) SpinorIO<PS,3>::load(a.self, total, t, self);
       Cx<T> out[3];
       if(a.mode == 2) {
 #pragma unroll
@@ -126,7 +127,7 @@ int launch_t(const qllg_stag_args *a)
   int grid = (int)(need < maxg ? need : maxg);
   if(grid < 1) grid = 1;
   stag_dslash<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
-  return qllg_check_cuda(cudaGetLastError(), "stag_dslash launch");
+  return qllg_launched("stag_dslash launch");
 }
 
 template <int PS, int PL, int NS>
@@ -174,5 +175,5 @@ qllg_k_stag_nbr_table(const qllg_geom *g, int parity, int slot, int *dev_out)
 {
   int n = g->Vh;
   nbr_table<<<(n + 255)/256, 256, 0, qllg_stream()>>>(*g, parity, slot, dev_out);
-  return qllg_check_cuda(cudaGetLastError(), "nbr_table launch");
+  return qllg_launched("nbr_table launch");
 }

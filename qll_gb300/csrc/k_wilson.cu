@@ -1,0 +1,184 @@
+// k_wilson.cu -- Wilson half-Dslash (sm_103a): per slot project the
+// neighbour spinor to two spin components, multiply by the link, and
+// reconstruct (the half-spinor form of lib/vlaw0.c.lua:545-652 with the
+// DeGrand-Rossi gamma matrices of lib/Gamma.lua:5-26):
+//   out = mode-dependent mass term - sum_mu [ (1 - g_mu) U_2mu(x) psi(x+mu)
+//                                           + (1 + g_mu) U_2mu+1(x) psi(x-mu) ]
+// dag = 1 flips the projector signs, which is gamma5 D gamma5.
+#include "kcommon.cuh"
+
+using namespace qk;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// one nonzero per row of gamma_mu (DeGrand-Rossi): its column and phase
+// (0:+1 1:+i 2:-1 3:-i); compile-time so the unrolled loops index registers
+//   mu=0: cols 3,2,1,0 phases  i, i,-i,-i     mu=1: cols 3,2,1,0 phases -1,1,1,-1
+//   mu=2: cols 2,3,0,1 phases  i,-i,-i, i     mu=3: cols 2,3,0,1 phases  1,1,1, 1
+__device__ __forceinline__ constexpr int gcol(int mu, int row) {
+  return mu < 2 ? 3 - row : (row ^ 2);
+}
+__device__ __forceinline__ constexpr int gph(int mu, int row) {
+  return mu == 0 ? (row < 2 ? 1 : 3)
+       : mu == 1 ? ((row == 0 || row == 3) ? 2 : 0)
+       : mu == 2 ? ((row == 0 || row == 3) ? 1 : 3) : 0;
+}
+
+template <typename T>
+__device__ __forceinline__ Cx<T> phase(const Cx<T> &z, int code) {
+  Cx<T> r;
+  switch(code & 3) {
+  case 0: r = z; break;
+  case 1: r.r = -z.i; r.i = z.r; break;
+  case 2: r.r = -z.r; r.i = -z.i; break;
+  default: r.r = z.i; r.i = -z.r; break;
+  }
+  return r;
+}
+
+template <int PS, int PL, int NR>
+__global__ void __launch_bounds__(kThreads)
+wilson_dslash(qllg_stag_args a)
+{
+  typedef typename Calc<PS, PL>::T T;
+  __shared__ double shm[2*kThreads];
+  const Geo G = make_geo(a.g);
+  const size_t V = (size_t)a.g.V;
+  const size_t total = (size_t)G.Vh * NR;
+  const int p = a.out_parity;
+  const size_t loff = p ? (size_t)G.Vh : 0;
+  const bool skip = a.done && *(volatile const int *)a.done;
+  double red[2] = {0.0, 0.0};
+  const int rhs = threadIdx.x % NR;
+  const bool act = !a.active || a.active[rhs];
+  const T ca = (T)(a.a ? a.a[rhs] : a.a0);
+  const T cb = (T)a.b;
+  if(!skip && act) {
+    for(size_t t = (size_t)blockIdx.x*blockDim.x + threadIdx.x; t < total;
+        t += (size_t)gridDim.x*blockDim.x) {
+      const int site = (int)(t / NR);
+      int x[4];
+      site_coords(G, p, site, x);
+      Cx<T> acc[12], self[12];
+      if(a.self && a.mode == 1) SpinorIO<PS,12>::load(a.self, total, t, self);
+#pragma unroll
+      for(int c=0; c<12; c++) {
+        if(a.mode == 1) { acc[c].r = ca*self[c].r; acc[c].i = ca*self[c].i; }
+        else { acc[c].r = 0; acc[c].i = 0; }
+      }
+#pragma unroll
+      for(int mu=0; mu<4; mu++) {
+#pragma unroll
+        for(int back=0; back<2; back++) {
+          // slot 2mu: (1 - g_mu) from x+mu; slot 2mu+1: (1 + g_mu) from x-mu
+          const int sgn = (back ? 1 : -1)*(a.dag ? -1 : 1);
+          const int k = nbr_index(G, x, mu, back ? -1 : 1);
+          Cx<T> U[9], f[12];
+          LinkIO<PL>::load(a.links, 2*mu + back, V, loff + site, a.lscale, U);
+          SpinorIO<PS,12>::load(a.in, total, (size_t)k*NR + rhs, f);
+#pragma unroll
+          for(int hk=0; hk<2; hk++) {
+            const int col = gcol(mu, hk);
+            const int ph = gph(mu, hk) + (sgn < 0 ? 2 : 0);
+            Cx<T> h[3], tt[3];
+#pragma unroll
+            for(int c=0; c<3; c++) {
+              Cx<T> y = phase(f[3*col + c], ph);
+              h[c].r = f[3*hk + c].r + y.r; h[c].i = f[3*hk + c].i + y.i;
+              tt[c].r = 0; tt[c].i = 0;
+            }
+#pragma unroll
+            for(int l=0; l<3; l++) {
+#pragma unroll
+              for(int j=0; j<3; j++) cmac(tt[j], U[3*l + j], h[l]);
+            }
+            // r_hk -= t; r_a -= sgn*phase_a*t for the lower row a fed by hk
+#pragma unroll
+            for(int c=0; c<3; c++) { acc[3*hk + c].r -= tt[c].r; acc[3*hk + c].i -= tt[c].i; }
+#pragma unroll
+            for(int ar=2; ar<4; ar++) {
+              if(gcol(mu, ar) == hk) {
+                const int pa = gph(mu, ar) + (sgn < 0 ? 0 : 2);   // minus sign folded in
+#pragma unroll
+                for(int c=0; c<3; c++) {
+                  Cx<T> y = phase(tt[c], pa);
+                  acc[3*ar + c].r += y.r; acc[3*ar + c].i += y.i;
+                }
+              }
+            }
+          }
+        }
+      }
+      if(a.self && a.mode != 1) SpinorIO<PS,12>::load(a.self, total, t, self);
+      Cx<T> out[12];
+#pragma unroll
+      for(int c=0; c<12; c++) {
+        if(a.mode == 2) {
+          T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
+          out[c].r = fma(cb, acc[c].r, sr); out[c].i = fma(cb, acc[c].i, si);
+        } else out[c] = acc[c];
+      }
+      SpinorIO<PS,12>::store(a.out, total, t, out);
+      if(a.norm_out) {
+#pragma unroll
+        for(int c=0; c<12; c++) red[0] += (double)out[c].r*out[c].r + (double)out[c].i*out[c].i;
+      }
+      if(a.norm_self && a.self) {
+#pragma unroll
+        for(int c=0; c<12; c++) red[1] += (double)self[c].r*self[c].r + (double)self[c].i*self[c].i;
+      }
+    }
+  }
+  if(a.norm_out || a.norm_self) {
+    double *res[2] = {a.norm_out, a.norm_self};
+    grid_reduce<2>(red, NR, rhs, a.rb->partial, a.rb->counter, shm, res);
+  }
+}
+
+template <int PS, int PL, int NR>
+int launch_t(const qllg_stag_args *a)
+{
+  static int bps = 0;
+  if(!bps) {
+    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &bps, wilson_dslash<PS,PL,NR>, kThreads, 0), "occupancy")) return -1;
+    if(bps < 1) bps = 1;
+  }
+  size_t total = (size_t)a->g.Vh * NR;
+  size_t need = (total + kThreads - 1)/kThreads;
+  size_t maxg = (size_t)qllg_num_sms()*bps;
+  if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
+  int grid = (int)(need < maxg ? need : maxg);
+  if(grid < 1) grid = 1;
+  wilson_dslash<PS,PL,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
+  return qllg_launched("wilson_dslash launch");
+}
+
+template <int PS, int PL>
+int launch_nr(const qllg_stag_args *a)
+{
+  switch(a->nrhs) {
+  case 1: return launch_t<PS,PL,1>(a);
+  case 2: return launch_t<PS,PL,2>(a);
+  case 4: return launch_t<PS,PL,4>(a);
+  }
+  qllg_set_error("wilson_dslash: nrhs %d not in {1,2,4}", a->nrhs);
+  return -1;
+}
+
+} // namespace
+
+extern "C" int
+qllg_k_wilson_dslash(int ps, int pl, const qllg_stag_args *a)
+{
+  if((a->norm_out || a->norm_self) && !a->rb) {
+    qllg_set_error("wilson_dslash: reduction requested without workspace");
+    return -1;
+  }
+  if(ps == QLLG_F64 && pl == QLLG_F64) return launch_nr<QLLG_F64, QLLG_F64>(a);
+  if(ps == QLLG_F32 && pl == QLLG_F32) return launch_nr<QLLG_F32, QLLG_F32>(a);
+  qllg_set_error("wilson_dslash: unsupported precision pair %d/%d", ps, pl);
+  return -1;
+}

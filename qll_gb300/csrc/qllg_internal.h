@@ -66,6 +66,8 @@ int   qllg_h2d(void *d, const void *h, size_t bytes);
 int   qllg_d2h(void *h, const void *d, size_t bytes);
 int   qllg_sync(void);
 int   qllg_num_sms(void);
+/* after a kernel launch: count it and check the launch error */
+int   qllg_launched(const char *what);
 
 /* reduction workspace: block partials + completion counter + results */
 typedef struct {
@@ -91,8 +93,8 @@ int qllg_k_spinor_convert(int prec_out, void *out, int prec_in, const void *in,
 /* links: stage [V][18] reals (device copy of host data) -> device slot */
 int qllg_k_link_from_aos(int prec, void *dev, float *scale_dev, const void *stage,
                          int stage_is_double, int V);
-/* device slot (FP64 layout) -> [V][18] reals stage */
-int qllg_k_link_to_aos(const double *dev, void *stage, int stage_is_double, int V);
+/* device slot (FP64 or FP32 layout) -> [V][18] reals stage */
+int qllg_k_link_to_aos(int prec, const void *dev, void *stage, int stage_is_double, int V);
 /* convert a device FP64 link slot to prec (FP32 or I16) */
 int qllg_k_link_convert(int prec, void *out, float *scale_dev, const double *in, int V);
 
@@ -118,8 +120,13 @@ typedef struct {
   const int *active;     /* device [nrhs] mask or NULL */
   const int *done;       /* device flag: skip everything when nonzero */
   qllg_redbuf *rb;
+  int dag;               /* Wilson only: gamma5 D gamma5 (projector signs flipped) */
 } qllg_stag_args;
 int qllg_k_stag_dslash(int prec_spinor, int prec_link, const qllg_stag_args *a);
+
+/* Wilson half-Dslash with the same argument block (nslots = 8, spinors of
+ * 12 colour-spin components, FP64 or FP32) */
+int qllg_k_wilson_dslash(int prec_spinor, int prec_link, const qllg_stag_args *a);
 
 /* neighbour index of slot s for every output site of a parity, written as
  * the full-lattice QLL site index (for the bit-exact table check) */
@@ -137,6 +144,7 @@ typedef struct {
   double alpha[QLLG_MAXRHS];
   double tmp[QLLG_MAXRHS];
   double maxr2[QLLG_MAXRHS];    /* |r|^2 at the last reliable update */
+  double prev[QLLG_MAXRHS];     /* |r|^2 before the current iteration */
   double delta2;                /* reliable-update threshold, squared */
   int active[QLLG_MAXRHS];
   int iters[QLLG_MAXRHS];
@@ -162,11 +170,14 @@ int qllg_k_mcg_update(int px, int ps, void *xs, void *rs, const void *p, const v
 int qllg_k_mcg_update_p(int ps, void *p, const void *rs, int nsites, int nrhs,
                         qllg_cg_scalars *s);
 /* reliable update, part 1: x64 += xs, xs = 0 for the flagged rhs */
-int qllg_k_mcg_accum(int px, void *x64, void *xs, int nsites, int nrhs, qllg_cg_scalars *s);
+int qllg_k_mcg_accum(int px, void *x64, void *xs, int nsites, int ncomp, int nrhs,
+                     qllg_cg_scalars *s);
 /* part 2 (after t64 = A x64): r64 = b - t64, rs = r64, |r64|^2; retires
- * converged rhs and clears the flags */
+ * converged rhs and clears the flags; standard_form also resets the
+ * direction coefficient to |r64|^2/prev (standard-form CG) */
 int qllg_k_mcg_residual(int ps, void *r64, void *rs, const void *b, const void *t64,
-                        int nsites, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb);
+                        int nsites, int ncomp, int nrhs, int standard_form,
+                        qllg_cg_scalars *s, qllg_redbuf *rb);
 
 /* r = b, x = 0, p = 0; bsq = rsq = |b|^2; rsq_stop *= bsq (rsq_stop holds
  * the relative tolerance on entry); rhs with b = 0 start inactive */
@@ -194,6 +205,78 @@ int qllg_k_xpay(int prec, void *y, const void *x, const double *b, double b0, do
                 int nsites, int ncomp, int nrhs, const int *active);
 int qllg_k_zero(int prec, void *x, int nsites, int ncomp, int nrhs);
 int qllg_k_copy(int prec, void *y, const void *x, int nsites, int ncomp, int nrhs);
+
+/* ------------------------------------------ standard-form CG kernels */
+/* x += alpha p, r -= alpha Ap with alpha = rsq/pnorm (pnorm = <p,Ap>
+ * from the operator), then prev = rsq, rsq = |r|^2, alpha[] = rsq/prev (the
+ * next direction coefficient); retires converged rhs.  With
+ * s->delta2 > 0 (mixed precision: x in px, r/p/Ap in ps) rhs are flagged
+ * for a reliable update instead of retiring, as in qllg_k_mcg_update. */
+int qllg_k_scg_update_xr(int px, int ps, void *x, void *r, const void *p, const void *Ap,
+                         int nsites, int ncomp, int nrhs, qllg_cg_scalars *s,
+                         qllg_redbuf *rb);
+/* p = r + alpha[] p for active rhs */
+int qllg_k_scg_update_p(int prec, void *p, const void *r, int nsites, int ncomp, int nrhs,
+                        qllg_cg_scalars *s);
+/* start of the standard-form CG: x = 0, r = b, p = b (precision prec,
+ * converted from the FP64 b), rsq = bsq = maxr2 = |b|^2, rsq_stop *= bsq;
+ * x64/r64 (FP64) set to 0 and b when not NULL */
+int qllg_k_scg_init(int px, int ps, void *x, void *r, void *p, const void *b64,
+                    void *x64, void *r64, int nsites, int ncomp, int nrhs,
+                    qllg_cg_scalars *s, qllg_redbuf *rb);
+
+/* ------------------------------------------------ matrix fields */
+/* full-lattice 3x3 fields [9][V] of prec (F64/F32):
+ * out = op(A)(x) op(B)(x + len*mu) (len 0: no shift), kind 0: A B,
+ * 1: A B^dagger, 2: A^dagger B; acc adds to out */
+int qllg_k_mat_mul(int prec, void *out, const void *A, const void *B, const qllg_geom *g,
+                   int kind, int mu, int len, int acc);
+/* out(x) = sgn * in(x + len*mu), or its adjoint when adj */
+int qllg_k_mat_shift(int prec, void *out, const void *in, const qllg_geom *g, int mu, int len,
+                     int adj, double sgn);
+/* out = a*out + c*in over nreal reals (a = 0 does not read out) */
+int qllg_k_mat_axpy(int prec, void *out, const void *in, double a, double c, size_t nreal);
+/* out = out + c*in, X_vpeq_r_times_X */
+int qllg_k_mat_peq(int prec, void *out, const void *in, double c, size_t nreal);
+/* sum_x Re tr[(U_i(x)U_j(x+i))^dagger U_j(x)U_i(x+j)] into *out */
+int qllg_k_plaq(int prec, const void *ui, const void *uj, const qllg_geom *g, int i, int j,
+                double *out, qllg_redbuf *rb);
+
+/* ------------------------------------------- host-layout (AoS) fields */
+/* fields in the reference's host layout [V][nelem] on the device */
+int qllg_k_aos_shift(int prec, void *out, const void *in, int nelem, const qllg_geom *g,
+                     int mu, int len);
+/* out(x) += U(x) in(x + len*mu) column by column (nelem = 6*columns), U [V][18] */
+int qllg_k_aos_transport(int prec, void *out, const void *u, const void *in, int nelem,
+                         const qllg_geom *g, int mu, int len);
+/* sum of squares (sq = 1) or of values over sites [s0, s1) */
+int qllg_k_aos_sum(int prec, const void *x, int nelem, int s0, int s1, int sq, double *out,
+                   qllg_redbuf *rb);
+
+/* ------------------------------------------------- multishift CG */
+#define QLLG_MAXSHIFT 64
+/* cgmsSolveT's scalar state (lib/cgms.c:12-17), kept on the GPU */
+typedef struct {
+  double a[QLLG_MAXSHIFT], b[QLLG_MAXSHIFT], s[QLLG_MAXSHIFT], bo[QLLG_MAXSHIFT];
+  double z[QLLG_MAXSHIFT], zo[QLLG_MAXSHIFT], zn[QLLG_MAXSHIFT], shifts[QLLG_MAXSHIFT];
+  double rsq, oldrsq, rsqstop, pkp;
+  double mass2;                 /* m_0^2 of the operator */
+  double pnorm, vnorm;          /* |p_0|^2, |D_oe p_0|^2 from the Dslash pair */
+  int n, iteration, itnlim, done;
+} qllg_cgms_scalars;
+
+/* start of an iteration: shift (bo,zo,z) <- (b,z,zn) after the first one;
+ * oldrsq = rsq */
+int qllg_k_cgms_pre(qllg_cgms_scalars *s);
+/* pkp, b, zn of lib/cgms.c:71-89 (one thread); stops on pkp <= 0 */
+int qllg_k_cgms_coef(qllg_cgms_scalars *s);
+/* out_i += b_i s_i p_i, r -= b_0 s_0 Ap, rsq = |r|^2, stop test, a_i
+ * (lib/cgms.c:91-135); ps and out hold n single-rhs fields back to back */
+int qllg_k_cgms_update_xr(int prec, void *out, void *r, const void *ps, const void *Ap,
+                          int nsites, qllg_cgms_scalars *s, qllg_redbuf *rb);
+/* p_0 = a_0 p_0 + r, p_i = a_i p_i + zn_i r (lib/cgms.c:137-161) */
+int qllg_k_cgms_update_p(int prec, void *ps, const void *r, int nsites,
+                         qllg_cgms_scalars *s);
 
 #ifdef __cplusplus
 }

@@ -52,6 +52,21 @@ qllg_check_cuda(cudaError_t e, const char *what)
   return -1;
 }
 
+static unsigned long long g_launches = 0;
+
+int
+qllg_launched(const char *what)
+{
+  g_launches++;
+  return qllg_check_cuda(cudaGetLastError(), what);
+}
+
+unsigned long long
+qllg_launch_count(void)
+{
+  return g_launches;
+}
+
 int
 qllg_runtime_init(void)
 {

@@ -36,6 +36,8 @@ struct qllg_stag {
   qllg_redbuf rb;
   qllg_cg_scalars *sc;     /* device scalars */
   qllg_cg_scalars *hsc;    /* pinned host copy */
+  qllg_cgms_scalars *cs;   /* multishift scalars, device */
+  qllg_cgms_scalars *hcs;  /* pinned host copy */
   void *ws[WS_N];
   size_t ws_bytes[WS_N];
   cudaEvent_t ev0, ev1;
@@ -93,6 +95,10 @@ stag_create(const int dims[4], void *const fat[8], void *const lng[8], int dbl)
   if(!S->sc || !S->lscale) goto fail;
   if(qllg_check_cuda(cudaMallocHost((void **)&S->hsc, sizeof(qllg_cg_scalars)), "cudaMallocHost"))
     goto fail;
+  S->cs = qllg_dmalloc(sizeof(qllg_cgms_scalars));
+  if(!S->cs) goto fail;
+  if(qllg_check_cuda(cudaMallocHost((void **)&S->hcs, sizeof(qllg_cgms_scalars)), "cudaMallocHost"))
+    goto fail;
   memset(S->hsc, 0, sizeof(qllg_cg_scalars));
   cudaEventCreate(&S->ev0);
   cudaEventCreate(&S->ev1);
@@ -118,6 +124,41 @@ fail:
   return NULL;
 }
 
+/* an operator whose links are attached later (device-built links) */
+qllg_stag *
+qllg_stag_alloc(const int dims[4], int nslots, int prec)
+{
+  if(qllg_runtime_init()) return NULL;
+  qllg_stag *S = calloc(1, sizeof(qllg_stag));
+  if(qllg_geom_from_dims(&S->g, dims)) { free(S); return NULL; }
+  S->nslots = nslots;
+  S->master = prec;
+  if(qllg_redbuf_init(&S->rb)) goto fail;
+  S->sc = qllg_dmalloc(sizeof(qllg_cg_scalars));
+  S->lscale = qllg_dmalloc(sizeof(float)*16);
+  S->cs = qllg_dmalloc(sizeof(qllg_cgms_scalars));
+  if(!S->sc || !S->lscale || !S->cs) goto fail;
+  if(qllg_check_cuda(cudaMallocHost((void **)&S->hsc, sizeof(qllg_cg_scalars)), "cudaMallocHost") ||
+     qllg_check_cuda(cudaMallocHost((void **)&S->hcs, sizeof(qllg_cgms_scalars)), "cudaMallocHost"))
+    goto fail;
+  cudaEventCreate(&S->ev0);
+  cudaEventCreate(&S->ev1);
+  return S;
+fail:
+  qllg_stag_destroy(S);
+  return NULL;
+}
+
+/* hand a device link array [nslots][9][V] of prec to the operator, which
+ * owns it from now on */
+int
+qllg_stag_attach_links(qllg_stag *S, int prec, void *links)
+{
+  if(S->links[prec]) qllg_dfree(S->links[prec]);
+  S->links[prec] = links;
+  return 0;
+}
+
 qllg_stag *
 qllg_stag_create(const int dims[4], double *const fat[8], double *const lng[8])
 {
@@ -139,11 +180,34 @@ qllg_stag_destroy(qllg_stag *S)
   qllg_dfree(S->lscale);
   qllg_dfree(S->sc);
   if(S->hsc) cudaFreeHost(S->hsc);
+  qllg_dfree(S->cs);
+  if(S->hcs) cudaFreeHost(S->hcs);
   qllg_redbuf_free(&S->rb);
   for(int i=0; i<WS_N; i++) qllg_dfree(S->ws[i]);
   if(S->ev0) cudaEventDestroy(S->ev0);
   if(S->ev1) cudaEventDestroy(S->ev1);
   free(S);
+}
+
+/* copy the operator's FP64 link slots to host arrays [V][18] */
+int
+qllg_stag_get_links(qllg_stag *S, double *const out[16])
+{
+  if(ensure_links(S, QLLG_F64)) return -1;
+  size_t per = qllg_link_bytes(QLLG_F64)*(size_t)S->g.V, hb = 8*18*(size_t)S->g.V;
+  void *st = qllg_stage(hb);
+  if(!st) return -1;
+  for(int s=0; s<S->nslots; s++) {
+    if(qllg_k_link_to_aos(QLLG_F64, (char *)S->links[QLLG_F64] + per*s, st, 1, S->g.V)) return -1;
+    if(qllg_d2h(out[s], st, hb)) return -1;
+  }
+  return 0;
+}
+
+int
+qllg_stag_nslots(const qllg_stag *S)
+{
+  return S->nslots;
 }
 
 size_t
@@ -182,7 +246,10 @@ dslash_half(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *
   A.active = active;
   A.done = done;
   A.rb = &S->rb;
-  qllg_tm_begin("stag_dslash");
+  static const char *pn[3] = {"f64", "f32", "i16"};
+  char fam[32];
+  snprintf(fam, sizeof(fam), "stag_dslash_%s_n%d", pn[ps], nrhs);
+  qllg_tm_begin(fam);
   int rc = qllg_k_stag_dslash(ps, pl, &A);
   qllg_tm_end();
   return rc;
@@ -380,10 +447,10 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
       if(qllg_k_mcg_update(px, ps, xs, rs, p, Ap, Vh, nrhs, sc, &S->rb)) return -1;
       /* reliable update of the flagged rhs; every launch returns at once
        * when no rhs is flagged */
-      if(qllg_k_mcg_accum(px, x64, xs, Vh, nrhs, sc)) return -1;
+      if(qllg_k_mcg_accum(px, x64, xs, Vh, 3, nrhs, sc)) return -1;
       if(apply_normal(S, QLLG_F64, QLLG_F64, nrhs, x64, w64, t64, NULL, NULL, sc->ru, &sc->no_ru))
         return -1;
-      if(qllg_k_mcg_residual(ps, r64, rs, b, t64, Vh, nrhs, sc, &S->rb)) return -1;
+      if(qllg_k_mcg_residual(ps, r64, rs, b, t64, Vh, 3, nrhs, 0, sc, &S->rb)) return -1;
     }
     issued += k;
     int d = pull_done(S);
@@ -607,6 +674,133 @@ qllg_stag_nbr_table(const int dims[4], int parity, int slot, int *host_out)
   return rc;
 }
 
+/* ------------------------------------------------- multishift CG */
+
+/* cgmsSolveT (lib/cgms.c:6-179) with Aop = the normal operator of mass0,
+ * on device fields: in (single rhs), out (n fields back to back) */
+static int
+cgms_run(qllg_stag *S, int prec, void *out, const void *in, const double shifts[], int n,
+         double mass0, double rsqin, int itnlim)
+{
+  if(n < 1 || n > QLLG_MAXSHIFT) { qllg_set_error("cgms: %d shifts (1..%d)", n, QLLG_MAXSHIFT); return -1; }
+  if(ensure_links(S, prec)) return -1;
+  size_t vb = vec_bytes(S, prec, 1);
+  void *r = ws_get(S, WS_R, vb), *Ap = ws_get(S, WS_AP, vb), *v = ws_get(S, WS_V, vb);
+  void *ps = ws_get(S, WS_PS, vb*n);
+  if(!r || !Ap || !v || !ps) return -1;
+  int Vh = S->g.Vh;
+  qllg_cgms_scalars *cs = S->cs, *h = S->hcs;
+  if(qllg_k_norm2(prec, in, Vh, 3, 1, &cs->pkp, &S->rb)) return -1;
+  double insq;
+  if(qllg_d2h(&insq, &cs->pkp, sizeof(double))) return -1;
+  if(qllg_k_zero(prec, out, Vh*n, 3, 1)) return -1;
+  if(insq == 0) return qllg_sync() ? -1 : 0;
+  memset(h, 0, sizeof(*h));
+  h->n = n;
+  for(int i=0; i<n; i++) {
+    h->shifts[i] = shifts[i];
+    h->zo[i] = h->z[i] = 1;
+    h->bo[i] = -1;
+    h->a[i] = 0;
+    h->s[i] = 1;
+  }
+  h->rsqstop = rsqin*insq;
+  h->rsq = insq;
+  h->mass2 = mass0*mass0;
+  h->itnlim = itnlim;
+  if(qllg_check_cuda(cudaMemcpyAsync(cs, h, sizeof(*h), cudaMemcpyHostToDevice, qllg_stream()),
+                     "push cgms scalars")) return -1;
+  if(qllg_k_copy(prec, r, in, Vh, 3, 1)) return -1;
+  for(int i=0; i<n; i++)
+    if(qllg_k_copy(prec, (char *)ps + vb*i, r, Vh, 3, 1)) return -1;
+  int batch = 8;
+  for(;;) {
+    for(int it=0; it<batch; it++) {
+      if(qllg_k_cgms_pre(cs)) return -1;
+      if(dslash_half(S, prec, prec, 1, 1, ps, NULL, v, 0, NULL, 0, 1, &cs->vnorm, NULL, NULL,
+                     &cs->done)) return -1;
+      if(dslash_half(S, prec, prec, 0, 1, v, ps, Ap, 2, &cs->mass2, 0, -1, NULL, &cs->pnorm,
+                     NULL, &cs->done)) return -1;
+      if(qllg_k_cgms_coef(cs)) return -1;
+      if(qllg_k_cgms_update_xr(prec, out, r, ps, Ap, Vh, cs, &S->rb)) return -1;
+      if(qllg_k_cgms_update_p(prec, ps, r, Vh, cs)) return -1;
+    }
+    int d;
+    if(qllg_check_cuda(cudaMemcpyAsync(&h->done, &cs->done, sizeof(int), cudaMemcpyDeviceToHost,
+                                       qllg_stream()), "pull done") || qllg_sync()) return -1;
+    d = h->done;
+    if(d) break;
+    if(batch < 64) batch *= 2;
+  }
+  if(qllg_check_cuda(cudaMemcpyAsync(h, cs, sizeof(*h), cudaMemcpyDeviceToHost, qllg_stream()),
+                     "pull cgms scalars") || qllg_sync()) return -1;
+  return h->iteration;
+}
+
+/* host wrapper: in = y (even half), out[i] = x[i] (even half), optional
+ * scaling by scale[i] as solveMulti2 does */
+static int
+cgms_host(qllg_stag *S, void *const x[], const void *y, const double shifts[], int n,
+          double mass0, double rsq, int itnlim, const double *scale)
+{
+  int dbl = S->master == QLLG_F64;
+  int prec = S->master;
+  size_t vb = vec_bytes(S, prec, 1);
+  if(n < 1 || n > QLLG_MAXSHIFT) { qllg_set_error("cgms: %d shifts (1..%d)", n, QLLG_MAXSHIFT); return -1; }
+  void *b = ws_get(S, WS_B, vb), *out = ws_get(S, WS_OUT, vb*n);
+  if(!b || !out) return -1;
+  void *ya[1] = {(void *)y};
+  if(vec_upload(S, prec, b, 1, ya, dbl)) return -1;
+  int its = cgms_run(S, prec, out, b, shifts, n, mass0, rsq, itnlim);
+  if(its < 0) return -1;
+  for(int i=0; i<n; i++) {
+    void *oi = (char *)out + vb*i;
+    if(scale && qllg_k_axpby(prec, oi, prec, oi, NULL, 0.0, NULL, scale[i], S->g.Vh, 3, 1, NULL))
+      return -1;
+    void *xa[1] = {x[i]};
+    if(vec_download(S, prec, oi, 1, xa, dbl)) return -1;
+  }
+  return its;
+}
+
+/* createStaggeredLinksFb (lib/stagDslash.c:464-519): only the forward
+ * links u[2mu] (and u3[2mu]) are read; the backward slots -U^dagger(x-mu)
+ * and -U3^dagger(x-3mu) that dslashFb2T applies on the fly
+ * (V_vmeq_xMap_times_xVp, lib/vla.c:1368-1393) are built once on the GPU */
+int qllg_k_mat_shift(int prec, void *out, const void *in, const qllg_geom *g, int mu, int len,
+                     int adj, double sgn);
+
+static qllg_stag *
+stag_create_fb(const int dims[4], void *const u[8], void *const u3[8], int dbl)
+{
+  qllg_geom g;
+  if(qllg_runtime_init() || qllg_geom_from_dims(&g, dims)) return NULL;
+  int nslots = u3 ? 16 : 8, prec = dbl ? QLLG_F64 : QLLG_F32;
+  size_t per = qllg_link_bytes(prec)*(size_t)g.V, hb = (dbl ? 8 : 4)*18*(size_t)g.V;
+  char *links = qllg_dmalloc(per*nslots);
+  void *stage = qllg_stage(hb);
+  if(!links || !stage) { qllg_dfree(links); return NULL; }
+  for(int mu=0; mu<4; mu++) {
+    for(int nk=0; nk<(u3 ? 2 : 1); nk++) {
+      int fs = u3 ? 4*mu + nk : 2*mu;              /* forward slot */
+      int bs = u3 ? 4*mu + 2 + nk : 2*mu + 1;      /* backward slot */
+      const void *h = nk ? u3[2*mu] : u[2*mu];
+      if(!h || qllg_h2d(stage, h, hb) ||
+         qllg_k_link_from_aos(prec, links + per*fs, NULL, stage, dbl, g.V) ||
+         qllg_k_mat_shift(prec, links + per*bs, links + per*fs, &g, mu, nk ? -3 : -1, 1, -1.0)) {
+        qllg_sync();
+        qllg_dfree(links);
+        return NULL;
+      }
+    }
+  }
+  if(qllg_sync()) { qllg_dfree(links); return NULL; }
+  qllg_stag *S = qllg_stag_alloc(dims, nslots, prec);
+  if(!S) { qllg_dfree(links); return NULL; }
+  qllg_stag_attach_links(S, prec, links);
+  return S;
+}
+
 /* ------------------------------------------------- QLL drop-in layer */
 
 /* private block behind StaggeredLinks.t: the Transporter records the
@@ -674,6 +868,18 @@ createStaggeredLinks##S_(StaggeredLinks##S_ *sl, Layout *l, real *u[], real *u3[
 }                                                                                 \
                                                                                   \
 void                                                                              \
+createStaggeredLinksFb##S_(StaggeredLinks##S_ *sl, Layout *l, real *u[], real *u3[],\
+                           char *sub)                                             \
+{                                                                                 \
+  qllg_geom g;                                                                    \
+  memset(sl, 0, sizeof(*sl));                                                     \
+  if(qllg_geom_from_layout(&g, l)) return;                                        \
+  qllg_stag *S = stag_create_fb(g.L, (void *const *)u, (void *const *)u3, DBL);   \
+  if(!S) return;                                                                  \
+  links_fill##S_(sl, l, u, u3, sub, S, 1, 1);                                     \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
 freeStaggeredLinks##S_(StaggeredLinks##S_ *sl)                                    \
 {                                                                                 \
   if(!sl || !sl->t) return;                                                       \
@@ -737,6 +943,61 @@ solve2##S_(StaggeredSolver##S_ *ss, real *x, real mass, real *y, double rsq,    
                             !ss->noscale, &sc);                                   \
   ss->its = its;                                                                  \
   return its;                                                                     \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+solveMulti2##S_(StaggeredSolver##S_ *ss, real *x[], double masses[], int nmasses, \
+                real *y, double rsq, int maxits, char *sub)                       \
+{                                                                                 \
+  (void)sub;                                                                      \
+  qllg_stag *S = links_op##S_(&ss->sle);                                          \
+  if(!S) { qllg_set_error("solveMulti2: solver not created"); return -1; }        \
+  if(nmasses < 1 || nmasses > QLLG_MAXSHIFT) {                                    \
+    qllg_set_error("solveMulti2: %d masses (1..%d)", nmasses, QLLG_MAXSHIFT);     \
+    return -1;                                                                    \
+  }                                                                               \
+  ss->mass = masses[0];                                                           \
+  if(rsq < 0) { ss->cgls.verbose = 3; rsq = -rsq; }                               \
+  double m2[QLLG_MAXSHIFT], sc[QLLG_MAXSHIFT];                                    \
+  for(int i=0; i<nmasses; i++) {                                                  \
+    m2[i] = masses[i]*masses[i] - masses[0]*masses[0];                            \
+    sc[i] = (double)(real)masses[i];                                              \
+  }                                                                               \
+  int its = cgms_host(S, (void *const *)x, y, m2, nmasses, masses[0], rsq, maxits,\
+                      ss->noscale ? NULL : sc);                                   \
+  ss->its = its;                                                                  \
+  return its;                                                                     \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+solveMulti##S_(real *x[], real *u[8], real *u3[8], double masses[], int nmasses,  \
+               real *y, double rsq, char *sub)                                    \
+{                                                                                 \
+  Layout *l = qllg_current_layout();                                              \
+  if(!l) { qllg_set_error("solveMulti: call stagDslashSetup first"); return -1; } \
+  StaggeredSolver##S_ ss;                                                         \
+  createStaggeredSolver##S_(&ss, l, u, u3, sub);                                  \
+  if(!ss.sle.t) return -1;                                                        \
+  int its = solveMulti2##S_(&ss, x, masses, nmasses, y, rsq, 1000000, sub);       \
+  freeStaggeredSolver##S_(&ss);                                                   \
+  return its;                                                                     \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+cgmsSolve##S_(Cgls##S_ *cgls, real *x[], real *b, double shifts[], int nshifts,   \
+              Linop##S_ *Aop, void *Aargs, Linop##S_ *Mop, void *Margs,           \
+              double rsqs[], int itnlim)                                          \
+{                                                                                 \
+  (void)cgls; (void)Margs;                                                        \
+  if(Aop != stagLinop##S_ || Mop) {                                               \
+    qllg_set_error("cgmsSolve: the operator must be stagLinop with no preconditioner"); \
+    return -1;                                                                    \
+  }                                                                               \
+  StaggeredSolver##S_ *ss = (StaggeredSolver##S_ *)Aargs;                         \
+  qllg_stag *S = links_op##S_(&ss->sle);                                          \
+  if(!S) { qllg_set_error("cgmsSolve: solver not created"); return -1; }          \
+  return cgms_host(S, (void *const *)x, b, shifts, nshifts, ss->mass, rsqs[0],    \
+                   itnlim, NULL);                                                 \
 }                                                                                 \
                                                                                   \
 int                                                                               \

@@ -1,0 +1,497 @@
+/*
+ * wilson.c -- the Wilson operator on the GPU: resident links,
+ * wilsonDslash (lib/wilsonDslash.c:272-285), the reference's wilsonSolve
+ * (:318-364) and the even-odd preconditioned normal-equation solver.
+ *
+ * Conventions of the reference: x = (4+m) y - sum_mu [(1-g_mu) u_2mu(x)
+ * y(x+mu) + (1+g_mu) u_2mu+1(x) y(x-mu)] with caller-supplied backward links
+ * (testwilson.c uses +U(x-mu)^dagger); the e/o subsets drop the mass term;
+ * sign is ignored.
+ *
+ * Normal-equation solver (no counterpart in the reference, whose
+ * wilsonSolve is not a valid CG for the Wilson matrix): with a = 4+m and W
+ * the massless half-Dslash, the Schur complement on even sites is
+ * S = a - W_eo W_oe / a, S^dagger = g5 S g5, and CG runs on
+ * S^dagger S x = S^dagger b (CGNR).  Precision modes: FP64 throughout, or
+ * FP32 iterations with FP64 reliable updates (x accumulated in FP64, the
+ * residual periodically recomputed from the FP64 operator).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
+#include "qll_gb300.h"
+#include "qllg_internal.h"
+
+void qllg_tm_begin(const char *name);
+void qllg_tm_end(void);
+int qllg_geom_from_layout(qllg_geom *g, const Layout *l);
+Layout *qllg_current_layout(void);
+
+enum { WW_X, WW_R, WW_P, WW_AP, WW_S, WW_V, WW_B, WW_X64, WW_R64, WW_T64, WW_S64, WW_V64,
+       WW_IO, WW_N };
+
+struct qllg_wilson {
+  qllg_geom g;
+  int master;
+  void *links[2];          /* FP64, FP32: [8][9][V] */
+  qllg_redbuf rb;
+  qllg_cg_scalars *sc, *hsc;
+  void *ws[WW_N];
+  size_t ws_bytes[WW_N];
+  cudaEvent_t ev0, ev1;
+};
+
+static void *
+wws(qllg_wilson *W, int id, size_t bytes)
+{
+  if(bytes <= W->ws_bytes[id]) return W->ws[id];
+  if(W->ws[id]) { qllg_sync(); qllg_dfree(W->ws[id]); }
+  W->ws[id] = qllg_dmalloc(bytes);
+  W->ws_bytes[id] = W->ws[id] ? bytes : 0;
+  return W->ws[id];
+}
+
+static size_t
+wvec(const qllg_wilson *W, int prec)
+{
+  return qllg_spinor_bytes(prec, 12)*(size_t)W->g.Vh;
+}
+
+static int
+wlinks(qllg_wilson *W, int prec)
+{
+  if(W->links[prec]) return 0;
+  if(W->master != QLLG_F64) { qllg_set_error("Wilson operator from float links has no FP64 copy"); return -1; }
+  size_t per = qllg_link_bytes(prec)*(size_t)W->g.V;
+  if(!(W->links[prec] = qllg_dmalloc(per*8))) return -1;
+  for(int s=0; s<8; s++)
+    if(qllg_k_link_convert(prec, (char *)W->links[prec] + per*s, NULL,
+                           (const double *)W->links[QLLG_F64] + (size_t)s*18*W->g.V, W->g.V))
+      return -1;
+  return 0;
+}
+
+void
+qllg_wilson_destroy(qllg_wilson *W)
+{
+  if(!W) return;
+  qllg_sync();
+  for(int p=0; p<2; p++) qllg_dfree(W->links[p]);
+  qllg_dfree(W->sc);
+  if(W->hsc) cudaFreeHost(W->hsc);
+  qllg_redbuf_free(&W->rb);
+  for(int i=0; i<WW_N; i++) qllg_dfree(W->ws[i]);
+  if(W->ev0) cudaEventDestroy(W->ev0);
+  if(W->ev1) cudaEventDestroy(W->ev1);
+  free(W);
+}
+
+static qllg_wilson *
+wilson_create(const int dims[4], void *const u[8], int dbl)
+{
+  if(qllg_runtime_init()) return NULL;
+  qllg_wilson *W = calloc(1, sizeof(qllg_wilson));
+  if(qllg_geom_from_dims(&W->g, dims)) { free(W); return NULL; }
+  W->master = dbl ? QLLG_F64 : QLLG_F32;
+  if(qllg_redbuf_init(&W->rb)) goto fail;
+  if(!(W->sc = qllg_dmalloc(sizeof(qllg_cg_scalars)))) goto fail;
+  if(qllg_check_cuda(cudaMallocHost((void **)&W->hsc, sizeof(qllg_cg_scalars)), "cudaMallocHost"))
+    goto fail;
+  cudaEventCreate(&W->ev0);
+  cudaEventCreate(&W->ev1);
+  {
+    int prec = W->master;
+    size_t per = qllg_link_bytes(prec)*(size_t)W->g.V;
+    size_t hb = (dbl ? 8 : 4)*18*(size_t)W->g.V;
+    void *st = qllg_stage(hb);
+    if(!(W->links[prec] = qllg_dmalloc(per*8)) || !st) goto fail;
+    for(int s=0; s<8; s++) {
+      if(!u[s]) { qllg_set_error("Wilson link %d is NULL", s); goto fail; }
+      if(qllg_h2d(st, u[s], hb) ||
+         qllg_k_link_from_aos(prec, (char *)W->links[prec] + per*s, NULL, st, dbl, W->g.V))
+        goto fail;
+    }
+    if(qllg_sync()) goto fail;
+  }
+  return W;
+fail:
+  qllg_wilson_destroy(W);
+  return NULL;
+}
+
+qllg_wilson *
+qllg_wilson_create(const int dims[4], double *const u[8])
+{
+  return wilson_create(dims, (void *const *)u, 1);
+}
+
+qllg_wilson *
+qllg_wilson_create_f(const int dims[4], float *const u[8])
+{
+  return wilson_create(dims, (void *const *)u, 0);
+}
+
+static int
+whalf(qllg_wilson *W, int prec, int out_parity, const void *in, const void *self, void *out,
+      int mode, double a0, double b, double *norm_out, double *norm_self, const int *active,
+      const int *done, int dag)
+{
+  if(wlinks(W, prec)) return -1;
+  qllg_stag_args A;
+  memset(&A, 0, sizeof(A));
+  A.g = W->g;
+  A.out_parity = out_parity;
+  A.nrhs = 1;
+  A.nslots = 8;
+  A.links = W->links[prec];
+  A.in = in;
+  A.self = self;
+  A.out = out;
+  A.mode = mode;
+  A.a0 = a0;
+  A.b = b;
+  A.norm_out = norm_out;
+  A.norm_self = norm_self;
+  A.active = active;
+  A.done = done;
+  A.rb = &W->rb;
+  A.dag = dag;
+  qllg_tm_begin("wilson_dslash");
+  int rc = qllg_k_wilson_dslash(prec, prec, &A);
+  qllg_tm_end();
+  return rc;
+}
+
+static int
+wup(qllg_wilson *W, int prec, void *dev, const void *host, int dbl, int site0)
+{
+  int Vh = W->g.Vh;
+  size_t bytes = (dbl ? 8 : 4)*24*(size_t)Vh;
+  void *st = qllg_stage(bytes);
+  if(!st || qllg_h2d(st, (const char *)host + (dbl ? 8 : 4)*24*(size_t)site0, bytes)) return -1;
+  return qllg_k_spinor_from_aos(prec, dev, st, dbl, Vh, 12, 1, 0);
+}
+
+static int
+wdown(qllg_wilson *W, int prec, const void *dev, void *host, int dbl, int site0)
+{
+  int Vh = W->g.Vh;
+  size_t bytes = (dbl ? 8 : 4)*24*(size_t)Vh;
+  void *st = qllg_stage(bytes);
+  if(!st || qllg_k_spinor_to_aos(prec, dev, st, dbl, Vh, 12, 1, 0)) return -1;
+  return qllg_d2h((char *)host + (dbl ? 8 : 4)*24*(size_t)site0, st, bytes);
+}
+
+/* x = mass'*y + W y on the sites of sub (wilsonDslash with the mass
+ * already combined as massFac*(4+m)); dag applies g5 D g5 */
+int
+qllg_wilson_dslash(qllg_wilson *W, void *x, double massp, const void *y, const char *sub, int dag)
+{
+  int prec = W->master, dbl = prec == QLLG_F64;
+  int Vh = W->g.Vh;
+  size_t vb = wvec(W, prec);
+  char *io = wws(W, WW_IO, 4*vb);
+  if(!io) return -1;
+  void *ye = io, *yo = io + vb, *xe = io + 2*vb, *xo = io + 3*vb;
+  int doe = !(sub && sub[0] == 'o'), doo = !(sub && sub[0] == 'e');
+  if((doe && wup(W, prec, yo, y, dbl, Vh)) || (doo && wup(W, prec, ye, y, dbl, 0))) return -1;
+  int m = (doe && doo && massp != 0) ? 1 : 0;
+  if(doe && whalf(W, prec, 0, yo, m ? ye : NULL, xe, m, massp, 1, NULL, NULL, NULL, NULL, dag))
+    return -1;
+  if(doo && whalf(W, prec, 1, ye, m ? yo : NULL, xo, m, massp, 1, NULL, NULL, NULL, NULL, dag))
+    return -1;
+  if(doe && wdown(W, prec, xe, x, dbl, 0)) return -1;
+  if(doo && wdown(W, prec, xo, x, dbl, Vh)) return -1;
+  return 0;
+}
+
+/* ------------------------------------------- reference wilsonSolve */
+
+static int
+wpush(qllg_wilson *W)
+{
+  return qllg_check_cuda(cudaMemcpyAsync(W->sc, W->hsc, sizeof(qllg_cg_scalars),
+                                         cudaMemcpyHostToDevice, qllg_stream()), "push scalars");
+}
+
+static int
+wpull(qllg_wilson *W, int all)
+{
+  size_t n = all ? sizeof(qllg_cg_scalars) : sizeof(int);
+  void *h = all ? (void *)W->hsc : (void *)&W->hsc->done;
+  void *d = all ? (void *)W->sc : (void *)&W->sc->done;
+  if(qllg_check_cuda(cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, qllg_stream()), "pull"))
+    return -1;
+  return qllg_sync();
+}
+
+/* cgSolveT with the Wilson dslashp2 (lib/wilsonDslash.c:287-316): A x =
+ * m^2 x - W_e W_o x, <x,Ax> = m^2|x|^2 + |W_o x|^2 over all 24 reals */
+static int
+wilson_ref_cg(qllg_wilson *W, void *x, const void *b, double mass, double rsq, int maxits)
+{
+  int prec = W->master;
+  size_t vb = wvec(W, prec);
+  void *r = wws(W, WW_R, vb), *p = wws(W, WW_P, vb), *Ap = wws(W, WW_AP, vb), *v = wws(W, WW_V, vb);
+  if(!r || !p || !Ap || !v) return -1;
+  memset(W->hsc, 0, sizeof(qllg_cg_scalars));
+  W->hsc->mass2[0] = mass*mass;
+  W->hsc->rsq_stop[0] = rsq;
+  W->hsc->maxits = maxits;
+  if(wpush(W)) return -1;
+  int Vh = W->g.Vh;
+  qllg_cg_scalars *sc = W->sc;
+  if(qllg_k_cg_init(prec, x, r, p, b, Vh, 12, 1, sc, &W->rb)) return -1;
+  int issued = 0, batch = 8;
+  while(issued < maxits) {
+    int k = maxits - issued < batch ? maxits - issued : batch;
+    for(int it=0; it<k; it++) {
+      if(qllg_k_cg_update_p(prec, p, r, Vh, 12, 1, sc)) return -1;
+      if(whalf(W, prec, 1, p, NULL, v, 0, 0, 1, sc->vnorm, NULL, sc->active, &sc->done, 0))
+        return -1;
+      /* Ap = m^2 p - W_e v, with |p|^2 */
+      if(whalf(W, prec, 0, v, p, Ap, 2, mass*mass, -1, NULL, sc->pnorm, sc->active, &sc->done, 0))
+        return -1;
+      if(qllg_k_cg_update_xr(prec, x, r, p, Ap, Vh, 12, 1, sc, &W->rb)) return -1;
+    }
+    issued += k;
+    if(wpull(W, 0)) return -1;
+    if(W->hsc->done) break;
+    if(batch < 64) batch *= 2;
+  }
+  if(wpull(W, 1)) return -1;
+  return W->hsc->iters[0];
+}
+
+/* ---------------------------------------------------- CGNR on S */
+
+/* out = S in (dag: S^dagger); tmp: odd scratch; |out|^2 into norm */
+static int
+apply_schur(qllg_wilson *W, int prec, const void *in, void *out, void *tmp, double a, int dag,
+            double *norm, const int *active, const int *done)
+{
+  if(whalf(W, prec, 1, in, NULL, tmp, 0, 0, 1, NULL, NULL, active, done, dag)) return -1;
+  return whalf(W, prec, 0, tmp, in, out, 2, a, -1.0/a, norm, NULL, active, done, dag);
+}
+
+static int
+wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq, int maxits,
+            int mode)
+{
+  double a = 4 + mass;
+  size_t v64 = wvec(W, QLLG_F64);
+  void *bp = wws(W, WW_B, v64), *s64 = wws(W, WW_S64, v64), *vv64 = wws(W, WW_V64, v64);
+  void *t64 = wws(W, WW_T64, v64), *r64 = wws(W, WW_R64, v64);
+  if(!bp || !s64 || !vv64 || !t64 || !r64) return -1;
+  int Vh = W->g.Vh;
+  /* b' = S^dagger b in FP64 */
+  if(apply_schur(W, QLLG_F64, b64, bp, vv64, a, 1, NULL, NULL, NULL)) return -1;
+  int ps = (mode == QLLG_SOLVE_DOUBLE) ? QLLG_F64 : QLLG_F32;
+  size_t vs = wvec(W, ps);
+  void *xs = (ps == QLLG_F64) ? x64 : wws(W, WW_X, vs);
+  void *r = wws(W, WW_R, vs), *p = wws(W, WW_P, vs), *Ap = wws(W, WW_AP, vs);
+  void *Sp = wws(W, WW_S, vs), *v = wws(W, WW_V, vs);
+  if(!xs || !r || !p || !Ap || !Sp || !v) return -1;
+  memset(W->hsc, 0, sizeof(qllg_cg_scalars));
+  W->hsc->rsq_stop[0] = rsq;
+  W->hsc->maxits = maxits;
+  W->hsc->delta2 = (ps == QLLG_F64) ? 0 : 0.01;
+  if(wpush(W)) return -1;
+  qllg_cg_scalars *sc = W->sc;
+  if(qllg_k_scg_init(ps, ps, xs, r, p, bp, ps == QLLG_F64 ? NULL : x64,
+                     ps == QLLG_F64 ? NULL : r64, Vh, 12, 1, sc, &W->rb)) return -1;
+  int issued = 0, batch = 8;
+  while(issued < maxits) {
+    int k = maxits - issued < batch ? maxits - issued : batch;
+    for(int it=0; it<k; it++) {
+      if(apply_schur(W, ps, p, Sp, v, a, 0, sc->pnorm, sc->active, &sc->done)) return -1;
+      if(apply_schur(W, ps, Sp, Ap, v, a, 1, NULL, sc->active, &sc->done)) return -1;
+      if(qllg_k_scg_update_xr(ps, ps, xs, r, p, Ap, Vh, 12, 1, sc, &W->rb)) return -1;
+      if(ps != QLLG_F64) {
+        if(qllg_k_mcg_accum(ps, x64, xs, Vh, 12, 1, sc)) return -1;
+        if(apply_schur(W, QLLG_F64, x64, s64, vv64, a, 0, NULL, sc->ru, &sc->no_ru)) return -1;
+        if(apply_schur(W, QLLG_F64, s64, t64, vv64, a, 1, NULL, sc->ru, &sc->no_ru)) return -1;
+        if(qllg_k_mcg_residual(ps, r64, r, bp, t64, Vh, 12, 1, 1, sc, &W->rb)) return -1;
+      }
+      if(qllg_k_scg_update_p(ps, p, r, Vh, 12, 1, sc)) return -1;
+    }
+    issued += k;
+    if(wpull(W, 0)) return -1;
+    if(W->hsc->done) break;
+    if(batch < 64) batch *= 2;
+  }
+  if(wpull(W, 1)) return -1;
+  return W->hsc->iters[0];
+}
+
+/* native: solve S x = b_e by CGNR; x, b host [V][24] (even half) */
+int
+qllg_wilson_solve(qllg_wilson *W, void *x, const void *b, double mass, double rsq, int maxits,
+                  int mode, qllg_solve_info *info)
+{
+  if(W->master != QLLG_F64) { qllg_set_error("wilson_solve: needs an FP64 operator"); return -1; }
+  if(mode != QLLG_SOLVE_DOUBLE && mode != QLLG_SOLVE_MIXED_SINGLE) {
+    qllg_set_error("wilson_solve: mode %d (DOUBLE or MIXED_SINGLE)", mode);
+    return -1;
+  }
+  if(rsq < 0) rsq = -rsq;
+  size_t v64 = wvec(W, QLLG_F64);
+  void *bd = wws(W, WW_IO, 2*v64);
+  if(!bd) return -1;
+  void *xd = (char *)bd + v64;
+  if(wup(W, QLLG_F64, bd, b, 1, 0)) return -1;
+  cudaEventRecord(W->ev0, qllg_stream());
+  int its = wilson_cgnr(W, xd, bd, mass, rsq, maxits, mode);
+  cudaEventRecord(W->ev1, qllg_stream());
+  if(its < 0) return -1;
+  if(info) {
+    memset(info, 0, sizeof(*info));
+    cudaEventSynchronize(W->ev1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, W->ev0, W->ev1);
+    info->seconds = ms*1e-3;
+    info->iters[0] = its;
+    info->total_iters = its;
+    info->reliable_updates = W->hsc->nru[0];
+    info->rsq[0] = W->hsc->bsq[0] > 0 ? W->hsc->rsq[0]/W->hsc->bsq[0] : 0;
+    /* true residual of S x = b in FP64 */
+    void *t = wws(W, WW_T64, v64), *vv = wws(W, WW_V64, v64);
+    double a = 4 + mass;
+    if(!t || !vv || apply_schur(W, QLLG_F64, xd, t, vv, a, 0, NULL, NULL, NULL)) return -1;
+    if(qllg_k_axpby(QLLG_F64, t, QLLG_F64, bd, NULL, -1.0, NULL, 1.0, W->g.Vh, 12, 1, NULL)) return -1;
+    double *dn = W->sc->tmp, num, den;
+    if(qllg_k_norm2(QLLG_F64, t, W->g.Vh, 12, 1, dn, &W->rb) || qllg_d2h(&num, dn, 8)) return -1;
+    if(qllg_k_norm2(QLLG_F64, bd, W->g.Vh, 12, 1, dn, &W->rb) || qllg_d2h(&den, dn, 8)) return -1;
+    info->true_rsq[0] = den > 0 ? num/den : 0;
+  }
+  if(wdown(W, QLLG_F64, xd, x, 1, 0)) return -1;
+  return its;
+}
+
+/* ------------------------------------------------- drop-in layer */
+
+typedef struct {
+  char t[8][sizeof(TransporterD)];
+  qllg_wilson *W;
+  int own;
+  int parity;
+} wlinks_priv;
+
+static int
+wsub_parity(const char *sub)
+{
+  return (sub && sub[0] == 'e') ? 0 : ((sub && sub[0] == 'o') ? 1 : -1);
+}
+
+#define DEFINE_WILSON_DROPIN(S_, real, DBL)                                       \
+static void                                                                       \
+wfill##S_(WilsonLinks##S_ *sl, Layout *l, real *u[], char *sub, qllg_wilson *W, int own) \
+{                                                                                 \
+  wlinks_priv *pv = calloc(1, sizeof(wlinks_priv));                               \
+  pv->W = W;                                                                      \
+  pv->own = own;                                                                  \
+  pv->parity = wsub_parity(sub);                                                  \
+  Transporter##S_ *t = (Transporter##S_ *)pv->t;                                  \
+  for(int i=0; i<8; i++) {                                                        \
+    t[i].u = u[i];                                                                \
+    t[i].nelem = 24;                                                              \
+    t[i].nc = 3;                                                                  \
+    layoutSubset(&t[i].sub, l, sub);                                              \
+  }                                                                               \
+  sl->t = t;                                                                      \
+  sl->n = 8;                                                                      \
+  sl->massFac = pv->parity >= 0 ? 0 : 1;                                          \
+  sl->fb = 0;                                                                     \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+createWilsonLinks##S_(WilsonLinks##S_ *sl, Layout *l, real *u[], char *sub)       \
+{                                                                                 \
+  memset(sl, 0, sizeof(*sl));                                                     \
+  qllg_geom g;                                                                    \
+  if(qllg_geom_from_layout(&g, l)) return;                                        \
+  qllg_wilson *W = wilson_create(g.L, (void *const *)u, DBL);                     \
+  if(W) wfill##S_(sl, l, u, sub, W, 1);                                           \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+freeWilsonLinks##S_(WilsonLinks##S_ *sl)                                          \
+{                                                                                 \
+  if(!sl || !sl->t) return;                                                       \
+  wlinks_priv *pv = (wlinks_priv *)(void *)sl->t;                                 \
+  if(pv->own) qllg_wilson_destroy(pv->W);                                         \
+  free(pv);                                                                       \
+  sl->t = NULL;                                                                   \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+wilsonDslash##S_(WilsonLinks##S_ *d, real *x, real mass, int sign, real *y)       \
+{                                                                                 \
+  (void)sign;                                                                     \
+  if(!d || !d->t) { qllg_set_error("wilsonDslash: links not created"); return; }  \
+  wlinks_priv *pv = (wlinks_priv *)(void *)d->t;                                  \
+  mass = d->massFac*(4 + mass);                                                   \
+  qllg_wilson_dslash(pv->W, x, (double)mass, y,                                   \
+                     pv->parity == 0 ? "even" : (pv->parity == 1 ? "odd" : "all"), 0); \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+createWilsonSolver##S_(WilsonSolver##S_ *ss, Layout *l, real *u[], char *sub)     \
+{                                                                                 \
+  (void)sub;                                                                      \
+  memset(ss, 0, sizeof(*ss));                                                     \
+  qllg_geom g;                                                                    \
+  if(qllg_geom_from_layout(&g, l)) return;                                        \
+  qllg_wilson *W = wilson_create(g.L, (void *const *)u, DBL);                     \
+  if(!W) return;                                                                  \
+  wfill##S_(&ss->sle, l, u, "even", W, 1);                                        \
+  wfill##S_(&ss->slo, l, u, "odd", W, 0);                                         \
+  cglsInit##S_(&ss->cgls, 24*l->nEvenOuter);                                      \
+  layoutSubset(&ss->sube, l, "even");                                             \
+  layoutSubset(&ss->subo, l, "odd");                                              \
+}                                                                                 \
+                                                                                  \
+void                                                                              \
+freeWilsonSolver##S_(WilsonSolver##S_ *ss)                                        \
+{                                                                                 \
+  freeWilsonLinks##S_(&ss->slo);                                                  \
+  freeWilsonLinks##S_(&ss->sle);                                                  \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+wilsonSolve##S_(WilsonSolver##S_ *ss, real *x, real mass, real *y, double rsq,    \
+                int maxits, char *sub)                                            \
+{                                                                                 \
+  (void)sub;                                                                      \
+  if(!ss->sle.t) { qllg_set_error("wilsonSolve: solver not created"); return -1; }\
+  qllg_wilson *W = ((wlinks_priv *)(void *)ss->sle.t)->W;                         \
+  ss->mass = mass;                                                                \
+  if(rsq < 0) { ss->cgls.verbose = 3; rsq = -rsq; }                               \
+  int prec = W->master;                                                           \
+  size_t vb = wvec(W, prec);                                                      \
+  char *io = wws(W, WW_IO, 2*vb);                                                 \
+  if(!io) return -1;                                                              \
+  if(wup(W, prec, io, y, DBL, 0)) return -1;                                      \
+  int its = wilson_ref_cg(W, io + vb, io, ss->mass, rsq, maxits);                 \
+  ss->its = its;                                                                  \
+  if(its < 0) return -1;                                                          \
+  if(!ss->noscale &&                                                              \
+     qllg_k_axpby(prec, io + vb, prec, io + vb, NULL, 0.0, NULL, (double)mass,    \
+                  W->g.Vh, 12, 1, NULL)) return -1;                               \
+  if(wdown(W, prec, io + vb, x, DBL, 0)) return -1;                               \
+  return its;                                                                     \
+}                                                                                 \
+                                                                                  \
+int                                                                               \
+wilsonSolveMulti##S_(WilsonSolver##S_ *ss, real *x[], double masses[], int nmasses,\
+                     real *y, double rsq, int maxits, char *sub)                  \
+{                                                                                 \
+  (void)ss; (void)x; (void)masses; (void)nmasses; (void)y; (void)rsq;             \
+  (void)maxits; (void)sub;                                                        \
+  qllg_set_error("wilsonSolveMulti: not available (the reference's body is disabled)"); \
+  return -1;                                                                      \
+}
+
+DEFINE_WILSON_DROPIN(D, double, 1)
+DEFINE_WILSON_DROPIN(F, float, 0)

@@ -32,3 +32,16 @@ def as_dtype(arrs, dtype):
 def relerr(a, b):
     n = np.linalg.norm(b)
     return np.linalg.norm(a - b)/(n if n > 0 else 1.0)
+
+
+@functools.lru_cache(maxsize=4)
+def wilson_links(dims, seed=1201, eps=0.3, half=True):
+    """8 Wilson links: u[2mu] = c U_mu(x), u[2mu+1] = c U_mu(x-mu)^dagger with
+    c = 1/2 (the hopping normalisation of the standard Wilson matrix)."""
+    th = qll.gen_gauge(dims, seed, eps, ks=False)
+    c = 0.5 if half else 1.0
+    u = [None]*8
+    for mu in range(4):
+        u[2*mu] = c*th[mu]
+        u[2*mu+1] = c*orc.doublestore(dims, th[mu], mu, -1)
+    return tuple(u)

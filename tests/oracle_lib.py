@@ -182,6 +182,28 @@ def wilson_schur(dims, u, mass, y, dag):
     return out
 
 
+def wilson_solve_ref(dims, u, mass, b, rsq, maxits, noscale=0):
+    s = sfx(b)
+    ct = realtype(b.dtype)
+    x = np.zeros_like(b)
+    its = getattr(lib(), "or_wilson_solve" + s)(dims_c(dims), P(x), PA(u, ct), ct(mass), P(b),
+                                                c_double(rsq), maxits, noscale)
+    return its, x
+
+
+def transport(dims, dest, u, src, nelem, mu, fwd):
+    s = sfx(src)
+    getattr(lib(), "or_transport" + s)(dims_c(dims), P(dest), P(u), P(src), nelem, mu, fwd)
+    return dest
+
+
+def shift(dims, y, nelem, d, length):
+    s = sfx(y)
+    x = np.zeros_like(y)
+    getattr(lib(), "or_shift" + s)(dims_c(dims), P(x), P(y), nelem, d, length)
+    return x
+
+
 def gamma(d):
     g = (c_double*32)()
     lib().or_gamma(d, g)
