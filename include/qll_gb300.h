@@ -133,6 +133,11 @@ int qllg_wilson_dslash(qllg_wilson *W, void *x, double massp, const void *y, con
 int qllg_wilson_solve(qllg_wilson *W, void *x, const void *b, double mass, double rsq,
                       int maxits, int mode, qllg_solve_info *info);
 
+/* solver parameters: "reliable_delta" (0.1), "reortho" (1), "graph" (1),
+ * "poll" (8); returns -1 for an unknown name */
+int qllg_set_param(const char *name, double value);
+double qllg_get_param(const char *name);
+
 /* kernel timing: when enabled, launches of the named kernel family are
  * bracketed by CUDA events on the library stream; read returns the count
  * and total milliseconds since the last reset.  Families:

@@ -497,7 +497,10 @@ qllg_k_norm2(int prec, const void *x, int nsites, int ncomp, int nrhs, double *o
 extern "C" int
 qllg_k_zero(int prec, void *x, int nsites, int ncomp, int nrhs)
 {
-  return qllg_k_axpby(prec, x, prec, x, NULL, 0.0, NULL, 0.0, nsites, ncomp, nrhs, NULL);
+  /* all-zero bits are 0.0 in every storage format (the 16-bit one has a
+   * zero scale); never read x, which may hold stale NaN patterns */
+  size_t bytes = (prec == QLLG_I16 ? 16u : (prec == QLLG_F64 ? 16u : 8u)*ncomp)*(size_t)nsites*nrhs;
+  return qllg_check_cuda(cudaMemsetAsync(x, 0, bytes, qllg_stream()), "zero");
 }
 
 extern "C" int

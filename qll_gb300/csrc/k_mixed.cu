@@ -194,13 +194,70 @@ mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites, 
           s->maxr2[q] = r2;
           s->nru[q]++;
           if(!(r2 >= s->rsq_stop[q] && s->iters[q] < s->maxits)) s->active[q] = 0;
-          s->ru[q] = 0;
         }
         any |= s->active[q];
       }
-      s->no_ru = 1;
+      /* ru[] and no_ru stay set for the re-orthogonalisation that follows;
+       * the next sloppy update clears them (or, once every rhs is done,
+       * nothing else runs) */
       s->done = !any;
+      if(!any) s->no_ru = 1;
     }
+  }
+}
+
+template <int PS, int NR>
+__global__ void __launch_bounds__(kT)
+mcg_orth_dot_k(const void *p, const void *rs, int nsites, qllg_cg_scalars *s,
+               double *partial, unsigned *counter)
+{
+  __shared__ double shm[2*kT];
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->no_ru) return;
+  double red[2] = {0, 0};
+  if(s->ru[rhs]) {
+    GRID_LOOP(t, total) {
+      Cx<float> pv[3], rv[3];
+      SpinorIO<PS,3>::load(p, total, t, pv);
+      SpinorIO<PS,3>::load(rs, total, t, rv);
+#pragma unroll
+      for(int c=0; c<3; c++) {
+        red[0] += (double)rv[c].r*pv[c].r + (double)rv[c].i*pv[c].i;
+        red[1] += (double)rv[c].r*pv[c].i - (double)rv[c].i*pv[c].r;
+      }
+    }
+  }
+  double *res[2] = {s->orth_re, s->orth_im};
+  if(grid_reduce<2>(red, NR, rhs, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      for(int q=0; q<NR; q++) {
+        double r2 = s->rsq[q];
+        s->orth_re[q] = (s->ru[q] && r2 > 0) ? s->orth_re[q]/r2 : 0;
+        s->orth_im[q] = (s->ru[q] && r2 > 0) ? s->orth_im[q]/r2 : 0;
+      }
+    }
+  }
+}
+
+template <int PS, int NR>
+__global__ void mcg_orth_axpy_k(void *p, const void *rs, int nsites, qllg_cg_scalars *s)
+{
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->no_ru || !s->ru[rhs]) return;
+  const float cr = (float)s->orth_re[rhs], ci = (float)s->orth_im[rhs];
+  GRID_LOOP(t, total) {
+    Cx<float> pv[3], rv[3];
+    SpinorIO<PS,3>::load(p, total, t, pv);
+    SpinorIO<PS,3>::load(rs, total, t, rv);
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      pv[c].r -= cr*rv[c].r - ci*rv[c].i;
+      pv[c].i -= cr*rv[c].i + ci*rv[c].r;
+    }
+    SpinorIO<PS,3>::store(p, total, t, pv);
   }
 }
 
@@ -222,6 +279,24 @@ mcg_residual_k(void *r64, void *rs, const void *b, const void *t64, int nsites, 
 int done(const char *w) { return qllg_launched(w); }
 
 } // namespace
+
+extern "C" int
+qllg_k_mcg_reortho(int ps, void *p, const void *rs, int nsites, int nrhs, qllg_cg_scalars *s,
+                   qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  if(ps == QLLG_I16) {
+    NR_SWITCH(nrhs, (mcg_orth_dot_k<QLLG_I16,NR><<<g,kT,0,st>>>(p, rs, nsites, s, rb->partial, rb->counter)));
+    if(done("mcg_orth_dot")) return -1;
+    NR_SWITCH(nrhs, (mcg_orth_axpy_k<QLLG_I16,NR><<<g,kT,0,st>>>(p, rs, nsites, s)));
+  } else if(ps == QLLG_F32) {
+    NR_SWITCH(nrhs, (mcg_orth_dot_k<QLLG_F32,NR><<<g,kT,0,st>>>(p, rs, nsites, s, rb->partial, rb->counter)));
+    if(done("mcg_orth_dot")) return -1;
+    NR_SWITCH(nrhs, (mcg_orth_axpy_k<QLLG_F32,NR><<<g,kT,0,st>>>(p, rs, nsites, s)));
+  } else { qllg_set_error("mcg_reortho: precision %d", ps); return -1; }
+  return done("mcg_orth_axpy");
+}
 
 extern "C" int
 qllg_k_mcg_init(int px, int ps, void *x64, void *r64, void *xs, void *rs, void *p,

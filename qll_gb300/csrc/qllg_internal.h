@@ -68,6 +68,7 @@ int   qllg_sync(void);
 int   qllg_num_sms(void);
 /* after a kernel launch: count it and check the launch error */
 int   qllg_launched(const char *what);
+double qllg_get_param(const char *name);
 
 /* reduction workspace: block partials + completion counter + results */
 typedef struct {
@@ -148,6 +149,8 @@ typedef struct {
   double delta2;                /* reliable-update threshold, squared */
   int active[QLLG_MAXRHS];
   int iters[QLLG_MAXRHS];
+  double orth_re[QLLG_MAXRHS];  /* <r,p>/|r|^2 after a reliable update */
+  double orth_im[QLLG_MAXRHS];
   int ru[QLLG_MAXRHS];          /* rhs that take a reliable update now */
   int nru[QLLG_MAXRHS];         /* reliable updates taken per rhs */
   int maxits;
@@ -224,6 +227,11 @@ int qllg_k_scg_update_p(int prec, void *p, const void *r, int nsites, int ncomp,
 int qllg_k_scg_init(int px, int ps, void *x, void *r, void *p, const void *b64,
                     void *x64, void *r64, int nsites, int ncomp, int nrhs,
                     qllg_cg_scalars *s, qllg_redbuf *rb);
+
+/* after a reliable update (flagged rhs): restore the orthogonality of the
+ * search direction to the new residual, p -= (<r,p>/|r|^2) r */
+int qllg_k_mcg_reortho(int ps, void *p, const void *rs, int nsites, int nrhs,
+                       qllg_cg_scalars *s, qllg_redbuf *rb);
 
 /* ------------------------------------------------ matrix fields */
 /* full-lattice 3x3 fields [9][V] of prec (F64/F32):

@@ -213,3 +213,28 @@ qllg_version(void)
 {
   return "qll_gb300 0.1 (sm_103a)";
 }
+
+/* tunable solver parameters (qllg_set_param) */
+static struct { const char *name; double value; } g_params[] = {
+  {"reliable_delta", 0.1},   /* reliable update when |r| < delta * |r at last update| */
+  {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
+  {"graph", 1},              /* run solver iterations as one CUDA graph launch */
+  {"poll", 8},               /* first batch of iterations between host checks */
+};
+
+int
+qllg_set_param(const char *name, double value)
+{
+  for(size_t i=0; i<sizeof(g_params)/sizeof(g_params[0]); i++)
+    if(!strcmp(g_params[i].name, name)) { g_params[i].value = value; return 0; }
+  qllg_set_error("unknown parameter %s", name);
+  return -1;
+}
+
+double
+qllg_get_param(const char *name)
+{
+  for(size_t i=0; i<sizeof(g_params)/sizeof(g_params[0]); i++)
+    if(!strcmp(g_params[i].name, name)) return g_params[i].value;
+  return 0;
+}

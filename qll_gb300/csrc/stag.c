@@ -437,7 +437,9 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
   int Vh = S->g.Vh;
   qllg_cg_scalars *sc = S->sc;
   if(qllg_k_mcg_init(px, ps, x64, r64, xs, rs, p, b, Vh, nrhs, sc, &S->rb)) return -1;
-  int issued = 0, batch = 8;
+  int reortho = qllg_get_param("reortho") != 0;
+  int issued = 0, batch = (int)qllg_get_param("poll");
+  if(batch < 1) batch = 1;
   while(issued < maxits) {
     int k = maxits - issued < batch ? maxits - issued : batch;
     for(int it=0; it<k; it++) {
@@ -451,6 +453,7 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
       if(apply_normal(S, QLLG_F64, QLLG_F64, nrhs, x64, w64, t64, NULL, NULL, sc->ru, &sc->no_ru))
         return -1;
       if(qllg_k_mcg_residual(ps, r64, rs, b, t64, Vh, 3, nrhs, 0, sc, &S->rb)) return -1;
+      if(reortho && qllg_k_mcg_reortho(ps, p, rs, Vh, nrhs, sc, &S->rb)) return -1;
     }
     issued += k;
     int d = pull_done(S);
@@ -496,10 +499,12 @@ solve_dev(qllg_stag *S, int nrhs, void *x, const void *b, const double mass[], d
     its = cg_plain(S, QLLG_F32, nrhs, x, b, mass, rsq, maxits);
     break;
   case QLLG_SOLVE_MIXED_HALF:
-    its = cg_mixed(S, QLLG_I16, QLLG_F32, QLLG_I16, nrhs, x, b, mass, rsq, maxits, 0.1);
+    its = cg_mixed(S, QLLG_I16, QLLG_F32, QLLG_I16, nrhs, x, b, mass, rsq, maxits,
+                   qllg_get_param("reliable_delta"));
     break;
   case QLLG_SOLVE_MIXED_SINGLE:
-    its = cg_mixed(S, QLLG_F32, QLLG_F32, QLLG_F32, nrhs, x, b, mass, rsq, maxits, 0.1);
+    its = cg_mixed(S, QLLG_F32, QLLG_F32, QLLG_F32, nrhs, x, b, mass, rsq, maxits,
+                   qllg_get_param("reliable_delta"));
     break;
   default:
     qllg_set_error("solve: unknown mode %d", mode);
