@@ -22,8 +22,9 @@
 /* neighbour tables are built once per (dims, displacement) and kept, like
  * the static shift tables of lib/stagDslash.c:715-719 */
 typedef struct { int dims[4]; int disp[4]; int *t; } OFN(tcache_t);
-static OFN(tcache_t) OFN(tcache)[128];
-static int OFN(ntcache) = 0;
+#define OR_NCACHE 512
+static OFN(tcache_t) OFN(tcache)[OR_NCACHE];
+static int OFN(ntcache) = 0, OFN(next_evict) = 0;
 
 static const int *
 OFN(table)(const int dims[4], const int disp[4])
@@ -33,11 +34,15 @@ OFN(table)(const int dims[4], const int disp[4])
     if(!memcmp(c->dims, dims, sizeof(int)*4) && !memcmp(c->disp, disp, sizeof(int)*4))
       return c->t;
   }
-  if(OFN(ntcache) == 128) {   /* full: drop everything */
-    for(int i=0; i<128; i++) free(OFN(tcache)[i].t);
-    OFN(ntcache) = 0;
+  /* full: replace the oldest entry only, so tables handed out earlier in
+   * the same call (at most 16) stay valid */
+  OFN(tcache_t) *c;
+  if(OFN(ntcache) < OR_NCACHE) c = &OFN(tcache)[OFN(ntcache)++];
+  else {
+    c = &OFN(tcache)[OFN(next_evict)];
+    OFN(next_evict) = (OFN(next_evict) + 1) % OR_NCACHE;
+    free(c->t);
   }
-  OFN(tcache_t) *c = &OFN(tcache)[OFN(ntcache)++];
   memcpy(c->dims, dims, sizeof(int)*4);
   memcpy(c->disp, disp, sizeof(int)*4);
   c->t = malloc(sizeof(int)*or_nsites(dims));

@@ -322,6 +322,36 @@ __global__ void cg_p_k(void *p, const void *r, int nsites, qllg_cg_scalars *s)
   }
 }
 
+template <int P, int NR>
+__global__ void __launch_bounds__(kT)
+cg_p_norm_k(void *p, const void *r, int nsites, qllg_cg_scalars *s, double *partial,
+            unsigned *counter)
+{
+  typedef typename Calc<P,P>::T T;
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  if(*(volatile int *)&s->done) return;        // uniform
+  double red[1] = {0};
+  if(s->active[rhs]) {
+    const T beta = (T)(1.0/s->rsq[rhs]);
+    GRID_LOOP(t, total) {
+      Cx<T> pv[3], rv[3];
+      SpinorIO<P,3>::load(p, total, t, pv);
+      SpinorIO<VecPrec<P>::value,3>::load(r, total, t, rv);
+#pragma unroll
+      for(int c=0; c<3; c++) {
+        pv[c].r = fma(beta, rv[c].r, pv[c].r); pv[c].i = fma(beta, rv[c].i, pv[c].i);
+      }
+      SpinorIO<P,3>::store(p, total, t, pv);
+#pragma unroll
+      for(int c=0; c<3; c++) red[0] += (double)pv[c].r*pv[c].r + (double)pv[c].i*pv[c].i;
+    }
+  }
+  double *res[1] = {s->pnorm};
+  grid_reduce<1>(red, NR, rhs, partial, counter, shm, res);
+}
+
 // ---------------------------------------------------------- dispatch
 #define NR_SWITCH(nrhs, ...) \
   switch(nrhs) { \
@@ -546,4 +576,18 @@ qllg_k_cg_update_p(int prec, void *p, const void *r, int nsites, int ncomp, int 
     NR_SWITCH(nrhs, (cg_p_k<P,NC,NR><<<g,kT,0,st>>>(p, r, nsites, s)));
   });
   return done("cg_update_p");
+}
+
+extern "C" int
+qllg_k_cg_update_p_norm(int prec, void *p, const void *r, int nsites, int nrhs,
+                        qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  size_t total = (size_t)nsites*nrhs;
+  int g = grid_for(total, 0, rb);
+  cudaStream_t st = qllg_stream();
+  if(prec == QLLG_F64) { NR_SWITCH(nrhs, (cg_p_norm_k<QLLG_F64,NR><<<g,kT,0,st>>>(p, r, nsites, s, rb->partial, rb->counter))); }
+  else if(prec == QLLG_F32) { NR_SWITCH(nrhs, (cg_p_norm_k<QLLG_F32,NR><<<g,kT,0,st>>>(p, r, nsites, s, rb->partial, rb->counter))); }
+  else if(prec == QLLG_I16) { NR_SWITCH(nrhs, (cg_p_norm_k<QLLG_I16,NR><<<g,kT,0,st>>>(p, r, nsites, s, rb->partial, rb->counter))); }
+  else { qllg_set_error("cg_update_p_norm: precision %d", prec); return -1; }
+  return done("cg_update_p_norm");
 }

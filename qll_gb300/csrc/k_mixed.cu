@@ -44,7 +44,7 @@ mcg_init_k(void *x64, void *r64, void *xs, void *rs, void *p, const void *b, int
     Cx<float> vf[3], zf[3];
 #pragma unroll
     for(int c=0; c<3; c++) { vf[c].r = (float)v[c].r; vf[c].i = (float)v[c].i; zf[c].r = 0; zf[c].i = 0; }
-    SpinorIO<PS,3>::store(rs, total, t, vf);
+    SpinorIO<VecPrec<PS>::value,3>::store(rs, total, t, vf);
     SpinorIO<PX,3>::store(xs, total, t, zf);
     SpinorIO<PS,3>::store(p, total, t, zf);
   }
@@ -220,7 +220,7 @@ mcg_orth_dot_k(const void *p, const void *rs, int nsites, qllg_cg_scalars *s,
     GRID_LOOP(t, total) {
       Cx<float> pv[3], rv[3];
       SpinorIO<PS,3>::load(p, total, t, pv);
-      SpinorIO<PS,3>::load(rs, total, t, rv);
+      SpinorIO<VecPrec<PS>::value,3>::load(rs, total, t, rv);
 #pragma unroll
       for(int c=0; c<3; c++) {
         red[0] += (double)rv[c].r*pv[c].r + (double)rv[c].i*pv[c].i;
@@ -251,7 +251,7 @@ __global__ void mcg_orth_axpy_k(void *p, const void *rs, int nsites, qllg_cg_sca
   GRID_LOOP(t, total) {
     Cx<float> pv[3], rv[3];
     SpinorIO<PS,3>::load(p, total, t, pv);
-    SpinorIO<PS,3>::load(rs, total, t, rv);
+    SpinorIO<VecPrec<PS>::value,3>::load(rs, total, t, rv);
 #pragma unroll
     for(int c=0; c<3; c++) {
       pv[c].r -= cr*rv[c].r - ci*rv[c].i;

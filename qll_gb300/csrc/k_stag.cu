@@ -33,6 +33,10 @@ stag_dslash(qllg_stag_args a)
   const bool act = !a.active || a.active[rhs];
   const T ca = (T)(a.a ? a.a[rhs] : a.a0);
   const T cb = (T)a.b;
+  constexpr int PX = VecPrec<PS>::value;   // x and r of the fused CG epilogue
+  T alpha = 0;
+  if(a.mode == 3 && act)
+    alpha = (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs]));
   if(!skip && act) {
     for(size_t t = (size_t)blockIdx.x*blockDim.x + threadIdx.x; t < total;
         t += (size_t)gridDim.x*blockDim.x) {
@@ -70,6 +74,22 @@ stag_dslash(qllg_stag_args a)
       }
       if(a.self && a.mode != 1) SpinorIO<PS,3>::load(a.self, total, t, self);
       Cx<T> out[3];
+      if(a.mode == 3) {
+        // Ap = m^2 p - D v; x += alpha p; r -= alpha Ap (cgSolveT, lib/cg.c:101-105)
+        Cx<T> xv[3], rv[3];
+        SpinorIO<PX,3>::load(a.x, total, t, xv);
+        SpinorIO<PX,3>::load(a.r, total, t, rv);
+#pragma unroll
+        for(int c=0; c<3; c++) {
+          T apr = fma(cb, acc[c].r, ca*self[c].r), api = fma(cb, acc[c].i, ca*self[c].i);
+          xv[c].r = fma(alpha, self[c].r, xv[c].r); xv[c].i = fma(alpha, self[c].i, xv[c].i);
+          rv[c].r = fma(-alpha, apr, rv[c].r); rv[c].i = fma(-alpha, api, rv[c].i);
+          red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
+        }
+        SpinorIO<PX,3>::store(a.x, total, t, xv);
+        SpinorIO<PX,3>::store(a.r, total, t, rv);
+        continue;
+      }
       if(a.mode == 2) {
 #pragma unroll
         for(int c=0; c<3; c++) {
@@ -92,7 +112,17 @@ stag_dslash(qllg_stag_args a)
       }
     }
   }
-  if(a.norm_out || a.norm_self) {
+  if(a.mode == 3) {
+    if(skip) return;   // uniform: the flag was set before this launch
+    double *res[2] = {a.sc->tmp, NULL};
+    if(grid_reduce<2>(red, NR, rhs, a.rb->partial, a.rb->counter, shm, res)) {
+      __syncthreads();
+      if(threadIdx.x == 0) {
+        if(a.mixed) cg_finish_mixed(a.sc, NR);
+        else cg_finish_plain(a.sc, NR);
+      }
+    }
+  } else if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
     grid_reduce<2>(red, NR, rhs, a.rb->partial, a.rb->counter, shm, res);
   }
@@ -158,14 +188,14 @@ int launch_ns(const qllg_stag_args *a)
 extern "C" int
 qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
 {
-  if((a->norm_out || a->norm_self) && !a->rb) {
+  if((a->norm_out || a->norm_self || a->mode == 3) && !a->rb) {
     qllg_set_error("stag_dslash: reduction requested without workspace");
     return -1;
   }
   if(ps == QLLG_F64 && pl == QLLG_F64) return launch_ns<QLLG_F64, QLLG_F64>(a);
   if(ps == QLLG_F32 && pl == QLLG_F32) return launch_ns<QLLG_F32, QLLG_F32>(a);
   if(ps == QLLG_I16 && pl == QLLG_I16) return launch_ns<QLLG_I16, QLLG_I16>(a);
-  if(ps == QLLG_I16 && pl == QLLG_F32) return launch_ns<QLLG_I16, QLLG_F32>(a);
+
   qllg_set_error("stag_dslash: unsupported precision pair %d/%d", ps, pl);
   return -1;
 }

@@ -14,6 +14,10 @@ template <> struct Real<QLLG_F64> { typedef double T; typedef double2 V2; };
 template <> struct Real<QLLG_F32> { typedef float T; typedef float2 V2; };
 template <> struct Real<QLLG_I16> { typedef float T; typedef float2 V2; };
 
+// storage of the residual/solution vectors that go with Dslash operands of
+// precision P: 16-bit Dslash operands keep FP32 recurrence vectors
+template <int P> struct VecPrec { static constexpr int value = (P == QLLG_F64) ? QLLG_F64 : QLLG_F32; };
+
 // arithmetic type of a kernel that reads precision A and writes B
 template <int A, int B> struct Calc { typedef float T; };
 template <int B> struct Calc<QLLG_F64, B> { typedef double T; };
@@ -220,6 +224,43 @@ __device__ __forceinline__ bool grid_reduce(double (&val)[NR], int nrhs, int rhs
   }
   if(tid == 0) *counter = 0u;
   return true;
+}
+
+// ------------------------------------------------ CG bookkeeping (last block)
+// plain CG (cgSolveT's loop test, lib/cg.c:115): keep iterating while
+// |r|^2 >= rsq_stop and iters < maxits; the new |r|^2 of each rhs is in tmp
+__device__ inline void cg_finish_plain(qllg_cg_scalars *s, int nr) {
+  int any = 0;
+  for(int q=0; q<nr; q++) {
+    if(s->active[q]) {
+      s->rsq[q] = s->tmp[q];
+      s->iters[q]++;
+      if(!(s->rsq[q] >= s->rsq_stop[q] && s->iters[q] < s->maxits)) s->active[q] = 0;
+    }
+    any |= s->active[q];
+  }
+  s->done = !any;
+  s->count++;
+}
+
+// mixed CG: flag a reliable update when the sloppy residual fell by delta
+// since the last one, passed the target, hit maxits or is not a number
+__device__ inline void cg_finish_mixed(qllg_cg_scalars *s, int nr) {
+  int anyru = 0;
+  for(int q=0; q<nr; q++) {
+    s->ru[q] = 0;
+    if(!s->active[q]) continue;
+    double r2 = s->tmp[q];
+    s->iters[q]++;
+    s->rsq[q] = r2;
+    if(r2 < s->delta2*s->maxr2[q] || r2 < s->rsq_stop[q] || s->iters[q] >= s->maxits ||
+       !(r2 == r2)) {
+      s->ru[q] = 1;
+      anyru = 1;
+    }
+  }
+  s->no_ru = !anyru;
+  s->count++;
 }
 
 } // namespace qk

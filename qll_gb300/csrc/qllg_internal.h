@@ -122,6 +122,14 @@ typedef struct {
   const int *done;       /* device flag: skip everything when nonzero */
   qllg_redbuf *rb;
   int dag;               /* Wilson only: gamma5 D gamma5 (projector signs flipped) */
+  /* mode 3 (staggered CG, fused): Ap = a[rhs]*self - acc stays in registers,
+   * then x += alpha self, r -= alpha Ap with alpha = 1/(a pnorm + vnorm) and
+   * |r|^2 reduced; the last block does the iteration's bookkeeping (mixed:
+   * reliable-update flags).  x is FP64 for FP64 spinors, else FP32; r has
+   * the spinor precision. */
+  void *x, *r;
+  struct qllg_cg_scalars_s *sc;
+  int mixed;
 } qllg_stag_args;
 int qllg_k_stag_dslash(int prec_spinor, int prec_link, const qllg_stag_args *a);
 
@@ -135,7 +143,7 @@ int qllg_k_stag_nbr_table(const qllg_geom *g, int parity, int slot, int *dev_out
 
 /* ------------------------------------------------------- CG kernels */
 /* scalars live on the device, per rhs (QLLG_MAXRHS each) */
-typedef struct {
+typedef struct qllg_cg_scalars_s {
   double rsq[QLLG_MAXRHS];      /* current |r|^2 */
   double rsq_stop[QLLG_MAXRHS]; /* stopping threshold */
   double bsq[QLLG_MAXRHS];

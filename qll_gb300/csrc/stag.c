@@ -321,6 +321,48 @@ apply_normal(qllg_stag *S, int ps, int pl, int nrhs, const void *p, void *v, voi
                      active, done);
 }
 
+/* one CG iteration in three launches (cgSolveT, lib/cg.c:77-115):
+ *   p += r/|r|^2 with |p|^2;  v = D_oe p with |v|^2;
+ *   Ap = m^2 p - D_eo v in registers, x += a p, r -= a Ap, |r|^2, bookkeeping
+ * ps: precision of p, v, r; pl: of the links; x is FP64 for FP64 spinors,
+ * else FP32; mixed selects the reliable-update bookkeeping */
+static int
+cg_iteration(qllg_stag *S, int ps, int pl, int nrhs, void *x, void *r, void *p, void *v, int mixed)
+{
+  qllg_cg_scalars *sc = S->sc;
+  if(qllg_k_cg_update_p_norm(ps, p, r, S->g.Vh, nrhs, sc, &S->rb)) return -1;
+  if(dslash_half(S, ps, pl, 1, nrhs, p, NULL, v, 0, NULL, 0, 1, sc->vnorm, NULL, sc->active,
+                 &sc->done)) return -1;
+  if(ensure_links(S, pl)) return -1;
+  qllg_stag_args A;
+  memset(&A, 0, sizeof(A));
+  A.g = S->g;
+  A.out_parity = 0;
+  A.nrhs = nrhs;
+  A.nslots = S->nslots;
+  A.links = S->links[pl];
+  A.lscale = S->lscale;
+  A.in = v;
+  A.self = p;
+  A.mode = 3;
+  A.a = sc->mass2;
+  A.b = -1;
+  A.active = sc->active;
+  A.done = &sc->done;
+  A.rb = &S->rb;
+  A.x = x;
+  A.r = r;
+  A.sc = sc;
+  A.mixed = mixed;
+  static const char *pn[3] = {"f64", "f32", "i16"};
+  char fam[32];
+  snprintf(fam, sizeof(fam), "stag_dslash_%s_n%d", pn[ps], nrhs);
+  qllg_tm_begin(fam);
+  int rc = qllg_k_stag_dslash(ps, pl, &A);
+  qllg_tm_end();
+  return rc;
+}
+
 static int
 push_scalars(qllg_stag *S)
 {
@@ -355,9 +397,9 @@ cg_plain(qllg_stag *S, int prec, int nrhs, void *x, const void *b, const double 
 {
   if(ensure_links(S, prec)) return -1;
   size_t vb = vec_bytes(S, prec, nrhs);
-  void *r = ws_get(S, WS_R, vb), *p = ws_get(S, WS_P, vb), *Ap = ws_get(S, WS_AP, vb);
+  void *r = ws_get(S, WS_R, vb), *p = ws_get(S, WS_P, vb);
   void *v = ws_get(S, WS_V, vb);
-  if(!r || !p || !Ap || !v) return -1;
+  if(!r || !p || !v) return -1;
   memset(S->hsc, 0, sizeof(qllg_cg_scalars));
   for(int i=0; i<nrhs; i++) {
     S->hsc->mass2[i] = mass[i]*mass[i];
@@ -373,10 +415,7 @@ cg_plain(qllg_stag *S, int prec, int nrhs, void *x, const void *b, const double 
   while(issued < maxits) {
     int k = maxits - issued < batch ? maxits - issued : batch;
     for(int it=0; it<k; it++) {
-      if(qllg_k_cg_update_p(prec, p, r, Vh, 3, nrhs, sc)) return -1;
-      if(apply_normal(S, prec, prec, nrhs, p, v, Ap, sc->vnorm, sc->pnorm, sc->active, &sc->done))
-        return -1;
-      if(qllg_k_cg_update_xr(prec, x, r, p, Ap, Vh, 3, nrhs, sc, &S->rb)) return -1;
+      if(cg_iteration(S, prec, prec, nrhs, x, r, p, v, 0)) return -1;
     }
     issued += k;
     int d = pull_done(S);
@@ -420,12 +459,14 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
          const double mass[], double rsq, int maxits, double delta)
 {
   if(ensure_links(S, pl) || ensure_links(S, QLLG_F64)) return -1;
-  size_t vs = vec_bytes(S, ps, nrhs), vx = vec_bytes(S, px, nrhs);
+  /* p, v: Dslash operands in ps; r and the solution increment in FP32 */
+  size_t vs = vec_bytes(S, ps, nrhs), vx = vec_bytes(S, QLLG_F32, nrhs);
   size_t v64 = vec_bytes(S, QLLG_F64, nrhs);
-  void *rs = ws_get(S, WS_R, vs), *p = ws_get(S, WS_P, vs), *Ap = ws_get(S, WS_AP, vs);
+  void *rs = ws_get(S, WS_R, vx), *p = ws_get(S, WS_P, vs);
   void *v = ws_get(S, WS_V, vs), *xs = ws_get(S, WS_X, vx);
   void *r64 = ws_get(S, WS_R64, v64), *t64 = ws_get(S, WS_T64, v64), *w64 = ws_get(S, WS_V64, v64);
-  if(!rs || !p || !Ap || !v || !xs || !r64 || !t64 || !w64) return -1;
+  if(!rs || !p || !v || !xs || !r64 || !t64 || !w64) return -1;
+  (void)px;
   memset(S->hsc, 0, sizeof(qllg_cg_scalars));
   for(int i=0; i<nrhs; i++) {
     S->hsc->mass2[i] = mass[i]*mass[i];
@@ -436,23 +477,20 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
   if(push_scalars(S)) return -1;
   int Vh = S->g.Vh;
   qllg_cg_scalars *sc = S->sc;
-  if(qllg_k_mcg_init(px, ps, x64, r64, xs, rs, p, b, Vh, nrhs, sc, &S->rb)) return -1;
+  if(qllg_k_mcg_init(QLLG_F32, ps, x64, r64, xs, rs, p, b, Vh, nrhs, sc, &S->rb)) return -1;
   int reortho = qllg_get_param("reortho") != 0;
   int issued = 0, batch = (int)qllg_get_param("poll");
   if(batch < 1) batch = 1;
   while(issued < maxits) {
     int k = maxits - issued < batch ? maxits - issued : batch;
     for(int it=0; it<k; it++) {
-      if(qllg_k_mcg_update_p(ps, p, rs, Vh, nrhs, sc)) return -1;
-      if(apply_normal(S, ps, pl, nrhs, p, v, Ap, sc->vnorm, sc->pnorm, sc->active, &sc->done))
-        return -1;
-      if(qllg_k_mcg_update(px, ps, xs, rs, p, Ap, Vh, nrhs, sc, &S->rb)) return -1;
+      if(cg_iteration(S, ps, pl, nrhs, xs, rs, p, v, 1)) return -1;
       /* reliable update of the flagged rhs; every launch returns at once
        * when no rhs is flagged */
-      if(qllg_k_mcg_accum(px, x64, xs, Vh, 3, nrhs, sc)) return -1;
+      if(qllg_k_mcg_accum(QLLG_F32, x64, xs, Vh, 3, nrhs, sc)) return -1;
       if(apply_normal(S, QLLG_F64, QLLG_F64, nrhs, x64, w64, t64, NULL, NULL, sc->ru, &sc->no_ru))
         return -1;
-      if(qllg_k_mcg_residual(ps, r64, rs, b, t64, Vh, 3, nrhs, 0, sc, &S->rb)) return -1;
+      if(qllg_k_mcg_residual(QLLG_F32, r64, rs, b, t64, Vh, 3, nrhs, 0, sc, &S->rb)) return -1;
       if(reortho && qllg_k_mcg_reortho(ps, p, rs, Vh, nrhs, sc, &S->rb)) return -1;
     }
     issued += k;
