@@ -4,9 +4,13 @@ Workload (the configuration the headline metric is quoted on): 32^3 x 64
 lattice, SU(3) links exp(i 0.4 H) with staggered phases, fat7/asqtad
 smearing on the GPU, m = 0.01, a block of 16 Gaussian sources solved
 together to |r|^2 < 1e-16 |b|^2 (true residual 1e-8) by the mixed-precision
-CG: 16-bit storage with per-site scale, FP32 arithmetic, FP64 reliable
-updates, multi-rhs Dslash reusing each link load across the 16 sources.
-A step is one such 16-source solve; value = solves per second.
+CG: FP32 Krylov vectors and links in the sloppy iterations, FP64 reliable
+updates (true residual recomputed from the FP64 operator, solution
+accumulated in FP64), multi-rhs Dslash reusing each link load across the 16
+sources.  A step is one such 16-source solve; value = solves per second.
+The 16-bit-storage mode (per-site scale) is also run once and reported: at
+m = 0.01 its quantisation noise swamps the low modes and it needs about 3x
+the iterations, so FP32 sloppy storage is the faster choice here.
 
 --impl reference times the reference's algorithm on the host CPU cores: the
 reference cannot be compiled here, so it is the CPU oracle (a C restatement
@@ -40,7 +44,7 @@ RSQ = 1e-16
 MAXITS = 20000
 SEED_GAUGE = 1004
 SEED_SRC = 2400
-WORKLOAD = "asqtad_cg_32^3x64_m0.01_eps0.4_16rhs_mixed16_tol1e-8"
+WORKLOAD = "asqtad_cg_32^3x64_m0.01_eps0.4_16rhs_mixed_fp32_fp64_tol1e-8"
 METRIC = "mixed-precision multi-RHS asqtad CG solves/s at 1e-8 true residual"
 # iterations of the FP64 CG (cgSolveT) on this workload, measured with the
 # library's FP64 solver on GB300 (same recurrence as the reference)
@@ -150,7 +154,7 @@ def run_gpu(args):
 
     info = qll.SolveInfo()
 
-    def solve(mode=qll.SOLVE_MIXED_HALF, nrhs=NRHS, x=x_dev, b=b_dev):
+    def solve(mode=qll.SOLVE_MIXED_SINGLE, nrhs=NRHS, x=x_dev, b=b_dev):
         its = L.qllg_stag_solve_device(S, nrhs, x, b, masses, RSQ, MAXITS, mode,
                                        ctypes.byref(info))
         if its < 0:
@@ -194,7 +198,9 @@ def run_gpu(args):
     nlaunch = int(L.qllg_launch_count() - n0)
     ms = ev0.elapsed_time(ev1)
     cnt, tot = ctypes.c_int(), ctypes.c_double()
-    L.qllg_timing_read(b"stag_dslash_i16_n16", ctypes.byref(cnt), ctypes.byref(tot))
+    L.qllg_timing_read(b"stag_dslash_f32_n16", ctypes.byref(cnt), ctypes.byref(tot))
+    fcnt, ftot = ctypes.c_int(), ctypes.c_double()
+    L.qllg_timing_read(b"stag_cg_fused_f32_n16", ctypes.byref(fcnt), ctypes.byref(ftot))
     L.qllg_timing_enable(0)
     t_max = ms
     if ws > 1:
@@ -213,7 +219,7 @@ def run_gpu(args):
     te = time.time()
     for _ in range(e2e_steps):
         its = L.qllg_stag_solve(S, NRHS, qll.vp_array(xs), qll.vp_array(srcs), masses, RSQ,
-                                MAXITS, qll.SOLVE_MIXED_HALF, ctypes.byref(info))
+                                MAXITS, qll.SOLVE_MIXED_SINGLE, ctypes.byref(info))
         if its < 0:
             raise RuntimeError(qll.last_error())
     torch.cuda.synchronize()
@@ -226,32 +232,47 @@ def run_gpu(args):
     Vh = srcs[0].shape[0]//2
     bytes_io = NRHS*Vh*6*8
 
-    # roofline of the dominant kernel: the 16-rhs 16-bit asqtad half-Dslash
-    # algorithmic bytes per output site and rhs (16 neighbour spinors + 1
-    # store, links shared by the 16 rhs): (8*18*2 + 8*18*2)/16 + 17*(6*2+4)
-    per_site_rhs = (8*18*2 + 8*18*2)/16 + 17*(6*2 + 4)
+    # roofline of the dominant kernel: the 16-rhs FP32 asqtad half-Dslash
+    # (D_oe p).  Algorithmic bytes per output site and rhs, SURVEY.md 8(d):
+    # 16 neighbour spinors + 1 store, links shared by the 16 rhs:
+    # (8*18*4 + 8*18*4)/16 + 17*(6*4) = 480 B
+    per_site_rhs = (8*18*4 + 8*18*4)/16 + 17*(6*4)
     launch_bytes = per_site_rhs*Vh*NRHS
     avg_ms = tot.value/max(cnt.value, 1)
     achieved = launch_bytes/(avg_ms*1e-3)/1e9
     pk = peaks()
     peak = pk.get("hbm_gbs")
-    compulsory = (8*18*2 + 8*18*2)/16 + 2*(6*2 + 4)
+    compulsory = (8*18*4 + 8*18*4)/16 + 2*(6*4)
+    # the fused D_eo + CG update: links + 16 neighbours + self + x and r
+    # read and written
+    fused_bytes = ((8*18*4 + 8*18*4)/16 + 17*(6*4) + 4*(6*4))*Vh*NRHS
+    favg = ftot.value/max(fcnt.value, 1)
+
+    # the 16-bit-storage mode, once (not timed in the headline)
+    t_h = time.time()
+    its_half = solve(qll.SOLVE_MIXED_HALF)
+    torch.cuda.synchronize()
+    t_h = time.time() - t_h
 
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max/args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp16-storage(int16+scale)/fp32/fp64-reliable",
+        "dtype": "fp32 (sloppy vectors and links) / fp64 (reliable updates, solution)",
         "data": "synthetic (seeded SU(3) gauge, fat7 on GPU, Gaussian sources)",
         "config": {"workload": WORKLOAD, "lattice": list(DIMS), "mass": MASS, "eps": EPS,
                    "nrhs": NRHS, "tol_true_residual": 1e-8, "parallelism": "replicas",
                    "l2": "inputs larger than L2 (links 1.2 GB 16-bit + 4.8 GB FP64)"},
         "iters_per_solve": iters, "max_true_rsq": max(truer),
+        "mixed_16bit_storage": {"solves_per_s": ws*NRHS/t_h, "iters": its_half,
+                                "note": "16-bit Krylov vectors with per-site scale; slower at m=0.01"},
         "fp64_single_rhs": {"solves_per_s": 1/fp64_s, "iters": its64, "true_rsq": fp64_true,
                             "speedup_of_value": value/ws*fp64_s},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io},
-        "roofline": {"kernel": "stag_dslash<i16,i16,16 slots,16 rhs>", "bound": "hbm",
+        "fused_cg_kernel": {"avg_launch_ms": favg, "launches": fcnt.value,
+                            "gbs": fused_bytes/(favg*1e-3)/1e9 if favg > 0 else None},
+        "roofline": {"kernel": "stag_dslash_mr<f32,f32,16 slots,16 rhs,4 rhs/thread>", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved/peak if peak else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else None,
@@ -365,6 +386,61 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_dslash_only(args):
+    """a few launches of the headline Dslash kernel on a chosen lattice, for
+    profiling: FP32, 16 rhs, device-resident random input"""
+    import torch
+    from qll_gb300 import qll
+    L = qll.load()
+    L.qllg_stag_create_asqtad.restype = ctypes.c_void_p
+    L.qllg_stag_create_asqtad.argtypes = [ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_void_p),
+                                          ctypes.POINTER(qll.Fat7Coeffs)]
+    L.qllg_stag_vec_bytes.restype = ctypes.c_size_t
+    L.qllg_stag_vec_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    L.qllg_stag_dslash_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    stream = torch.cuda.current_stream()
+    L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
+    dims = tuple(int(v) for v in args.dims.split(","))
+    prec = {"f64": 0, "f32": 1, "i16": 2}[args.prec]
+    thin = qll.gen_gauge(dims, SEED_GAUGE, EPS, ks=True)
+    coef = qll.asqtad_coeffs()
+    S = ctypes.c_void_p(L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(thin),
+                                                  ctypes.byref(coef)))
+    nb = L.qllg_stag_vec_bytes(S, prec, args.nrhs)
+    # random 4-byte words are valid input for FP32 layouts; the 16-bit layout
+    # gets scales of 1
+    src = torch.randn(nb//4, dtype=torch.float32, device="cuda")
+    if prec == 2:
+        src = src.view(-1, 4)
+        src[:, 3] = 1.0
+        src = src.reshape(-1)
+    if prec == 0:
+        src = torch.randn(nb//8, dtype=torch.float64, device="cuda")
+    dst = torch.empty_like(src)
+    for _ in range(3):
+        L.qllg_stag_dslash_device(S, prec, args.nrhs, 1, ctypes.c_void_p(dst.data_ptr()),
+                                  ctypes.c_void_p(src.data_ptr()))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.launches):
+        L.qllg_stag_dslash_device(S, prec, args.nrhs, 1, ctypes.c_void_p(dst.data_ptr()),
+                                  ctypes.c_void_p(src.data_ptr()))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)/args.launches
+    Vh = int(np.prod(dims))//2
+    bs = {0: 8, 1: 4, 2: 2}[prec]
+    ns = 4 if prec == 2 else 0
+    per = (8*18*bs + 8*18*bs)/args.nrhs + 17*(6*bs + ns)
+    print(json.dumps({"dslash_only": {"dims": dims, "nrhs": args.nrhs, "prec": args.prec,
+                                      "ms": ms, "algorithmic_gbs": per*Vh*args.nrhs/(ms*1e-3)/1e9,
+                                      "error": qll.last_error()}}), flush=True)
+    L.qllg_stag_destroy(S)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -374,8 +450,15 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=30)
     ap.add_argument("--fp64-iters", type=int, default=2000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--dslash-only", action="store_true")
+    ap.add_argument("--dims", default="32,32,32,64")
+    ap.add_argument("--prec", default="f32", choices=["f64", "f32", "i16"])
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--launches", type=int, default=20)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.dslash_only:
+        run_dslash_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

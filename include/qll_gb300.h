@@ -99,6 +99,13 @@ void qllg_stag_vec_free(void *v);
 int qllg_stag_vec_upload(qllg_stag *S, void *v_dev, int nrhs, void *const h[]);
 int qllg_stag_vec_download(qllg_stag *S, const void *v_dev, int nrhs, void *const h[]);
 
+/* the half Dslash out = D in (output sites of out_parity) on device vectors
+ * of nrhs rhs, precision prec (0 FP64, 1 FP32, 2 16-bit) in the library
+ * layout; links of that precision are derived from FP64 on first use */
+int qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *out_dev,
+                            const void *in_dev);
+size_t qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs);
+
 /* neighbour table of slot s for the output sites of a parity, as QLL site
  * indices (host int[V/2]); the GPU computes it with the Dslash kernel's own
  * index arithmetic */
@@ -141,7 +148,8 @@ double qllg_get_param(const char *name);
 /* kernel timing: when enabled, launches of the named kernel family are
  * bracketed by CUDA events on the library stream; read returns the count
  * and total milliseconds since the last reset.  Families:
- * "stag_dslash_<f64|f32|i16>_n<nrhs>", "wilson_dslash" */
+ * "stag_dslash_<f64|f32|i16>_n<nrhs>" (half Dslash), "stag_cg_fused_<...>_n<nrhs>"
+ * (D_eo with the fused CG update), "wilson_dslash" */
 void qllg_timing_enable(int on);
 /* number of kernels the library has launched since load */
 unsigned long long qllg_launch_count(void);

@@ -372,6 +372,9 @@ cg_p_norm_k(void *p, const void *r, int nsites, qllg_cg_scalars *s, double *part
   else { qllg_set_error("unsupported precision %d / components %d", prec, ncomp); return -1; }
 
 int done(const char *what) { return qllg_launched(what); }
+} // namespace
+static int done_check(const char *w) { return qllg_launched(w); }
+namespace {
 
 } // namespace
 
@@ -590,4 +593,22 @@ qllg_k_cg_update_p_norm(int prec, void *p, const void *r, int nsites, int nrhs,
   else if(prec == QLLG_I16) { NR_SWITCH(nrhs, (cg_p_norm_k<QLLG_I16,NR><<<g,kT,0,st>>>(p, r, nsites, s, rb->partial, rb->counter))); }
   else { qllg_set_error("cg_update_p_norm: precision %d", prec); return -1; }
   return done("cg_update_p_norm");
+}
+
+// the WHILE condition of a graph-captured solver loop: continue while the
+// done flag is clear and the iteration cap is not reached (the cap makes the
+// loop end even if a flag were never set)
+__global__ void loop_cond_k(cudaGraphConditionalHandle h, int *done, int *loops, const int *limit)
+{
+  if(threadIdx.x == 0) {
+    int n = ++*loops;
+    cudaGraphSetConditional(h, (!*(volatile int *)done && n < *limit) ? 1u : 0u);
+  }
+}
+
+extern "C" int
+qllg_k_loop_cond(unsigned long long handle, int *done, int *loops, const int *limit)
+{
+  loop_cond_k<<<1, 32, 0, qllg_stream()>>>((cudaGraphConditionalHandle)handle, done, loops, limit);
+  return done_check("loop_cond");
 }

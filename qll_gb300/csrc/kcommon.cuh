@@ -226,6 +226,61 @@ __device__ __forceinline__ bool grid_reduce(double (&val)[NR], int nrhs, int rhs
   return true;
 }
 
+// Same reduction when each thread holds R right-hand sides: thread t works
+// on rhs q*R + j (j < R) with q = t % Q and Q = nrhs/R threads per site.
+template <int NRED, int R>
+__device__ __forceinline__ bool grid_reduce_mr(double (&val)[NRED][R], int nrhs, int Q,
+                                               double *partial, unsigned *counter,
+                                               double *shm /* NRED*R*blockDim */,
+                                               double *result[NRED]) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+#pragma unroll
+  for(int n=0; n<NRED; n++)
+#pragma unroll
+    for(int j=0; j<R; j++) shm[(n*R + j)*nt + tid] = val[n][j];
+  __syncthreads();
+  {
+    const int K = NRED*nrhs, J = nt/K, c = tid % K, l = tid / K;
+    const int n = c / nrhs, r = c % nrhs, j = r % R, qq = r / R;
+    double s = 0;
+    for(int i=l; i<nt/Q; i+=J) s += shm[(n*R + j)*nt + qq + Q*i];
+    __syncthreads();
+    shm[tid] = s;
+    __syncthreads();
+    for(int w=J/2; w>0; w>>=1) {
+      if(l < w) shm[c + K*l] += shm[c + K*(l + w)];
+      __syncthreads();
+    }
+    if(l == 0) partial[(size_t)blockIdx.x*(2*QLLG_MAXRHS) + n*QLLG_MAXRHS + r] = shm[c];
+  }
+  __threadfence();
+  __shared__ bool last;
+  __syncthreads();
+  if(tid == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if(!last) return false;
+  __threadfence();
+  const int nb = gridDim.x;
+  const int K = NRED*nrhs, J = nt / K;
+  const int c = tid % K, l = tid / K;
+  const int q = c / nrhs, r = c % nrhs;
+  double s = 0;
+  for(int b=l; b<nb; b+=J)
+    s += ((volatile double *)partial)[(size_t)b*(2*QLLG_MAXRHS) + q*QLLG_MAXRHS + r];
+  shm[tid] = s;
+  __syncthreads();
+  for(int w=J/2; w>0; w>>=1) {
+    if(l < w) shm[c + K*l] += shm[c + K*(l + w)];
+    __syncthreads();
+  }
+  if(l == 0) {
+#pragma unroll
+    for(int qq=0; qq<NRED; qq++) if(qq == q && result[qq]) result[qq][r] = shm[c];
+  }
+  if(tid == 0) *counter = 0u;
+  return true;
+}
+
 // ------------------------------------------------ CG bookkeeping (last block)
 // plain CG (cgSolveT's loop test, lib/cg.c:115): keep iterating while
 // |r|^2 >= rsq_stop and iters < maxits; the new |r|^2 of each rhs is in tmp

@@ -66,6 +66,12 @@ int   qllg_h2d(void *d, const void *h, size_t bytes);
 int   qllg_d2h(void *h, const void *d, size_t bytes);
 int   qllg_sync(void);
 int   qllg_num_sms(void);
+/* CUDA graph capture of library launches (graph bodies) */
+int   qllg_capturing(void);
+int   qllg_capture_begin(cudaGraph_t body);
+int   qllg_capture_end(cudaGraph_t body);
+/* last kernel of a graph-loop body: keep looping while work remains */
+int   qllg_k_loop_cond(unsigned long long handle, int *done, int *loops, const int *limit);
 /* after a kernel launch: count it and check the launch error */
 int   qllg_launched(const char *what);
 double qllg_get_param(const char *name);
@@ -165,6 +171,8 @@ typedef struct qllg_cg_scalars_s {
   int done;                     /* all rhs inactive */
   int no_ru;                    /* no rhs takes a reliable update now */
   int count;                    /* iterations issued */
+  int loops;                    /* graph-loop trips (safety cap) */
+  int loop_limit;
 } qllg_cg_scalars;
 
 /* ------------------------------------------ mixed-precision CG kernels */

@@ -94,10 +94,41 @@ qllg_num_sms(void)
   return g_nsm ? g_nsm : 1;
 }
 
+/* while a CUDA graph body is being captured, launches go to the capture
+ * stream instead of the library stream */
+static cudaStream_t g_cap = 0;
+static int g_capturing = 0;
+
 cudaStream_t
 qllg_stream(void)
 {
-  return g_stream;
+  return g_capturing ? g_cap : g_stream;
+}
+
+int
+qllg_capturing(void)
+{
+  return g_capturing;
+}
+
+int
+qllg_capture_begin(cudaGraph_t body)
+{
+  if(!g_cap && qllg_check_cuda(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking),
+                               "capture stream")) return -1;
+  if(qllg_check_cuda(cudaStreamBeginCaptureToGraph(g_cap, body, NULL, NULL, 0,
+                                                   cudaStreamCaptureModeRelaxed),
+                     "begin capture")) return -1;
+  g_capturing = 1;
+  return 0;
+}
+
+int
+qllg_capture_end(cudaGraph_t body)
+{
+  cudaGraph_t out = body;
+  g_capturing = 0;
+  return qllg_check_cuda(cudaStreamEndCapture(g_cap, &out), "end capture");
 }
 
 int
@@ -220,6 +251,7 @@ static struct { const char *name; double value; } g_params[] = {
   {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
   {"graph", 1},              /* run solver iterations as one CUDA graph launch */
   {"poll", 8},               /* first batch of iterations between host checks */
+  {"dslash_mr", 1},          /* multi-rhs Dslash: one thread per site and 4 rhs */
 };
 
 int

@@ -40,7 +40,13 @@ struct qllg_stag {
   qllg_cgms_scalars *hcs;  /* pinned host copy */
   void *ws[WS_N];
   size_t ws_bytes[WS_N];
+  unsigned ws_gen;         /* bumped when a workspace buffer moves */
   cudaEvent_t ev0, ev1;
+  struct {                 /* graph-captured solver loops */
+    long key[10];
+    cudaGraphExec_t exec;
+  } graphs[6];
+  int ngraph_next;
 };
 
 /* ------------------------------------------------------------ helpers */
@@ -52,6 +58,7 @@ ws_get(qllg_stag *S, int id, size_t bytes)
   if(S->ws[id]) { qllg_sync(); qllg_dfree(S->ws[id]); }
   S->ws[id] = qllg_dmalloc(bytes);
   S->ws_bytes[id] = S->ws[id] ? bytes : 0;
+  S->ws_gen++;
   return S->ws[id];
 }
 
@@ -184,6 +191,7 @@ qllg_stag_destroy(qllg_stag *S)
   if(S->hcs) cudaFreeHost(S->hcs);
   qllg_redbuf_free(&S->rb);
   for(int i=0; i<WS_N; i++) qllg_dfree(S->ws[i]);
+  for(int i=0; i<6; i++) if(S->graphs[i].exec) cudaGraphExecDestroy(S->graphs[i].exec);
   if(S->ev0) cudaEventDestroy(S->ev0);
   if(S->ev1) cudaEventDestroy(S->ev1);
   free(S);
@@ -355,8 +363,8 @@ cg_iteration(qllg_stag *S, int ps, int pl, int nrhs, void *x, void *r, void *p, 
   A.sc = sc;
   A.mixed = mixed;
   static const char *pn[3] = {"f64", "f32", "i16"};
-  char fam[32];
-  snprintf(fam, sizeof(fam), "stag_dslash_%s_n%d", pn[ps], nrhs);
+  char fam[40];
+  snprintf(fam, sizeof(fam), "stag_cg_fused_%s_n%d", pn[ps], nrhs);
   qllg_tm_begin(fam);
   int rc = qllg_k_stag_dslash(ps, pl, &A);
   qllg_tm_end();
@@ -389,6 +397,111 @@ pull_done(qllg_stag *S)
   return S->hsc->done;
 }
 
+/* ------------------------------------------------ solver loop driver */
+
+/* what one solver iteration launches */
+typedef struct {
+  int mixed;                 /* 0 plain CG, 1 mixed CG with reliable updates */
+  int ps, pl, nrhs, reortho;
+  void *x, *r, *p, *v;       /* sloppy (or only) vectors */
+  void *x64, *r64, *t64, *w64;
+  const void *b;
+} iter_ctx;
+
+static int
+issue_iteration(qllg_stag *S, const iter_ctx *c)
+{
+  qllg_cg_scalars *sc = S->sc;
+  int Vh = S->g.Vh;
+  if(cg_iteration(S, c->ps, c->pl, c->nrhs, c->x, c->r, c->p, c->v, c->mixed)) return -1;
+  if(!c->mixed) return 0;
+  /* reliable update of the flagged rhs; every launch returns at once when
+   * no rhs is flagged */
+  if(qllg_k_mcg_accum(QLLG_F32, c->x64, c->x, Vh, 3, c->nrhs, sc)) return -1;
+  if(apply_normal(S, QLLG_F64, QLLG_F64, c->nrhs, c->x64, c->w64, c->t64, NULL, NULL, sc->ru,
+                  &sc->no_ru)) return -1;
+  if(qllg_k_mcg_residual(QLLG_F32, c->r64, c->r, c->b, c->t64, Vh, 3, c->nrhs, 0, sc, &S->rb))
+    return -1;
+  if(c->reortho && qllg_k_mcg_reortho(c->ps, c->p, c->r, Vh, c->nrhs, sc, &S->rb)) return -1;
+  return 0;
+}
+
+/* a CUDA graph whose conditional WHILE node repeats one captured iteration
+ * until the done flag is set (or the trip cap is reached) */
+static cudaGraphExec_t
+loop_graph(qllg_stag *S, const iter_ctx *c)
+{
+  long key[10] = {c->mixed, c->ps, c->pl, c->nrhs, c->reortho, (long)c->x, (long)c->b,
+                  (long)c->x64, (long)S->ws_gen, 1};
+  for(int i=0; i<6; i++)
+    if(S->graphs[i].exec && !memcmp(S->graphs[i].key, key, sizeof(key))) return S->graphs[i].exec;
+  cudaGraph_t g = NULL;
+  cudaGraphExec_t exec = NULL;
+  cudaGraphConditionalHandle h;
+  cudaGraphNode_t node;
+  struct cudaGraphNodeParams np;
+  if(qllg_check_cuda(cudaGraphCreate(&g, 0), "graph create")) return NULL;
+  if(qllg_check_cuda(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault),
+                     "conditional handle")) goto fail;
+  memset(&np, 0, sizeof(np));
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  if(qllg_check_cuda(cudaGraphAddNode(&node, g, NULL, NULL, 0, &np), "conditional node")) goto fail;
+  if(qllg_capture_begin(np.conditional.phGraph_out[0])) goto fail;
+  {
+    int rc = issue_iteration(S, c);
+    rc |= qllg_k_loop_cond((unsigned long long)h, &S->sc->done, &S->sc->loops,
+                           &S->sc->loop_limit);
+    rc |= qllg_capture_end(np.conditional.phGraph_out[0]);
+    if(rc) goto fail;
+  }
+  if(qllg_check_cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate")) goto fail;
+  cudaGraphDestroy(g);
+  {
+    int i = S->ngraph_next;
+    S->ngraph_next = (i + 1) % 6;
+    if(S->graphs[i].exec) cudaGraphExecDestroy(S->graphs[i].exec);
+    memcpy(S->graphs[i].key, key, sizeof(key));
+    S->graphs[i].exec = exec;
+  }
+  return exec;
+fail:
+  if(qllg_capturing()) qllg_capture_end(np.conditional.phGraph_out[0]);
+  if(g) cudaGraphDestroy(g);
+  return NULL;
+}
+
+/* run iterations until every rhs is done: one graph launch, or (timing
+ * enabled, or graphs switched off) batches of launches with a host check of
+ * the done flag after each batch */
+int qllg_timing_on(void);
+
+static int
+run_loop(qllg_stag *S, const iter_ctx *c, int maxits)
+{
+  if(qllg_get_param("graph") != 0 && !qllg_timing_on()) {
+    /* one iteration launched directly first: every kernel of the body is
+     * then loaded before the capture starts */
+    if(issue_iteration(S, c)) return -1;
+    cudaGraphExec_t exec = loop_graph(S, c);
+    if(!exec) return -1;
+    return qllg_check_cuda(cudaGraphLaunch(exec, qllg_stream()), "graph launch");
+  }
+  int issued = 0, batch = (int)qllg_get_param("poll");
+  if(batch < 1) batch = 1;
+  while(issued < maxits + 2) {
+    for(int it=0; it<batch; it++) if(issue_iteration(S, c)) return -1;
+    issued += batch;
+    int d = pull_done(S);
+    if(d < 0) return -1;
+    if(d) break;
+    if(batch < 64) batch *= 2;
+  }
+  return 0;
+}
+
 /* plain CG of cgSolveT in one precision on device vectors x, b (even sites,
  * nrhs rhs).  Returns the largest iteration count, fills hsc. */
 static int
@@ -406,23 +519,18 @@ cg_plain(qllg_stag *S, int prec, int nrhs, void *x, const void *b, const double 
     S->hsc->rsq_stop[i] = rsq;
   }
   S->hsc->maxits = maxits;
+  S->hsc->loop_limit = maxits + 2;
   if(push_scalars(S)) return -1;
   int Vh = S->g.Vh;
   qllg_cg_scalars *sc = S->sc;
   if(qllg_k_cg_init(prec, x, r, p, b, Vh, 3, nrhs, sc, &S->rb)) return -1;
-  int issued = 0;
-  int batch = 8;
-  while(issued < maxits) {
-    int k = maxits - issued < batch ? maxits - issued : batch;
-    for(int it=0; it<k; it++) {
-      if(cg_iteration(S, prec, prec, nrhs, x, r, p, v, 0)) return -1;
-    }
-    issued += k;
-    int d = pull_done(S);
-    if(d < 0) return -1;
-    if(d) break;
-    if(batch < 64) batch *= 2;
-  }
+  iter_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.ps = c.pl = prec;
+  c.nrhs = nrhs;
+  c.x = x; c.r = r; c.p = p; c.v = v;
+  c.b = b;
+  if(run_loop(S, &c, maxits)) return -1;
   if(pull_scalars(S)) return -1;
   int its = 0;
   for(int i=0; i<nrhs; i++) if(S->hsc->iters[i] > its) its = S->hsc->iters[i];
@@ -473,32 +581,21 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
     S->hsc->rsq_stop[i] = rsq;
   }
   S->hsc->maxits = maxits;
+  S->hsc->loop_limit = maxits + 2;
   S->hsc->delta2 = delta*delta;
   if(push_scalars(S)) return -1;
   int Vh = S->g.Vh;
   qllg_cg_scalars *sc = S->sc;
   if(qllg_k_mcg_init(QLLG_F32, ps, x64, r64, xs, rs, p, b, Vh, nrhs, sc, &S->rb)) return -1;
-  int reortho = qllg_get_param("reortho") != 0;
-  int issued = 0, batch = (int)qllg_get_param("poll");
-  if(batch < 1) batch = 1;
-  while(issued < maxits) {
-    int k = maxits - issued < batch ? maxits - issued : batch;
-    for(int it=0; it<k; it++) {
-      if(cg_iteration(S, ps, pl, nrhs, xs, rs, p, v, 1)) return -1;
-      /* reliable update of the flagged rhs; every launch returns at once
-       * when no rhs is flagged */
-      if(qllg_k_mcg_accum(QLLG_F32, x64, xs, Vh, 3, nrhs, sc)) return -1;
-      if(apply_normal(S, QLLG_F64, QLLG_F64, nrhs, x64, w64, t64, NULL, NULL, sc->ru, &sc->no_ru))
-        return -1;
-      if(qllg_k_mcg_residual(QLLG_F32, r64, rs, b, t64, Vh, 3, nrhs, 0, sc, &S->rb)) return -1;
-      if(reortho && qllg_k_mcg_reortho(ps, p, rs, Vh, nrhs, sc, &S->rb)) return -1;
-    }
-    issued += k;
-    int d = pull_done(S);
-    if(d < 0) return -1;
-    if(d) break;
-    if(batch < 64) batch *= 2;
-  }
+  iter_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.mixed = 1;
+  c.ps = ps; c.pl = pl; c.nrhs = nrhs;
+  c.reortho = qllg_get_param("reortho") != 0;
+  c.x = xs; c.r = rs; c.p = p; c.v = v;
+  c.x64 = x64; c.r64 = r64; c.t64 = t64; c.w64 = w64;
+  c.b = b;
+  if(run_loop(S, &c, maxits)) return -1;
   if(pull_scalars(S)) return -1;
   int its = 0;
   for(int i=0; i<nrhs; i++) if(S->hsc->iters[i] > its) its = S->hsc->iters[i];
@@ -702,6 +799,25 @@ qllg_stag_solve(qllg_stag *S, int nrhs, void *const x[], void *const b[], const 
                 double rsq, int maxits, int mode, qllg_solve_info *info)
 {
   return stag_solve_host(S, nrhs, x, b, mass, rsq, maxits, mode, info, 0, NULL);
+}
+
+/* out = D in on the output parity, device vectors of nrhs rhs in the
+ * library layout of precision prec (0 FP64, 1 FP32, 2 16-bit) */
+int
+qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *out_dev,
+                        const void *in_dev)
+{
+  if(!valid_nrhs(nrhs)) { qllg_set_error("dslash_device: nrhs %d", nrhs); return -1; }
+  if(prec < 0 || prec > 2) { qllg_set_error("dslash_device: precision %d", prec); return -1; }
+  return dslash_half(S, prec, prec, out_parity, nrhs, in_dev, NULL, out_dev, 0, NULL, 0, 1,
+                     NULL, NULL, NULL, NULL);
+}
+
+/* bytes of a device vector of nrhs rhs in precision prec (one parity) */
+size_t
+qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs)
+{
+  return vec_bytes(S, prec, nrhs);
 }
 
 int

@@ -83,10 +83,12 @@ qllg_timing_read(const char *name, int *count, double *ms)
 }
 
 /* bracket one launch; no-ops unless enabled */
+int qllg_capturing(void);
+
 void
 qllg_tm_begin(const char *name)
 {
-  if(!g_on) return;
+  if(!g_on || qllg_capturing()) return;
   if(g_npair == NPAIR) harvest();
   int f = fam_id(name);
   if(f < 0) return;
@@ -98,8 +100,14 @@ qllg_tm_begin(const char *name)
 void
 qllg_tm_end(void)
 {
-  if(!g_on || g_open < 0) return;
+  if(!g_on || g_open < 0 || qllg_capturing()) return;
   cudaEventRecord(g_ev[2*g_open+1], qllg_stream());
   g_npair = g_open + 1;
   g_open = -1;
+}
+
+int
+qllg_timing_on(void)
+{
+  return g_on;
 }

@@ -132,6 +132,7 @@ def _declare(L):
     vp, i, d = c_void_p, c_int, c_double
     sig = {
         "qllg_last_error": (c_char_p, []),
+        "qllg_clear_error": (None, []),
         "qllg_version": (c_char_p, []),
         "qllg_init": (i, []),
         "qllg_set_stream": (i, [vp]),

@@ -25,3 +25,12 @@ def _ensure_built():
 
 
 _ensure_built()
+
+
+@pytest.fixture(autouse=True)
+def _clear_library_error():
+    """qllg_last_error() keeps the last message until the next error; start
+    every test from a clean slate so a test sees only its own errors"""
+    from qll_gb300 import qll
+    qll.load().qllg_clear_error()
+    yield

@@ -160,3 +160,36 @@ def test_mixed_precision_reaches_fp64_residual(mode, nrhs):
         its_o, xo, _ = orc.solve2(DIMS, u, u3, masses[k], bs[k], 1e-16, 5000, noscale=1)
         assert relerr(xs[k][:Vh], xo[:Vh]) < 1e-7
     L.qllg_stag_destroy(S)
+
+
+@pytest.mark.parametrize("mode", [qll.SOLVE_DOUBLE, qll.SOLVE_MIXED_SINGLE])
+def test_graph_loop_matches_host_loop(mode):
+    """the CUDA-graph solver loop (conditional WHILE node) and the
+    host-polled loop launch the same kernels: identical iterations and
+    bitwise identical solutions"""
+    L, S, u, u3 = _native()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    nrhs = 4
+    masses = (c_double*nrhs)(0.05, 0.07, 0.1, 0.2)
+    bs = [qll.gen_source(DIMS, 5000 + k, 6, "even") for k in range(nrhs)]
+    out = {}
+    for graph in (1, 0):
+        L.qllg_set_param(b"graph", graph)
+        xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+        info = qll.SolveInfo()
+        its = L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), masses, 1e-16, 5000,
+                                mode, byref(info))
+        assert its > 0, qll.last_error()
+        out[graph] = (list(info.iters[:nrhs]), xs)
+    L.qllg_set_param(b"graph", 1)
+    assert out[0][0] == out[1][0]
+    for k in range(nrhs):
+        assert np.array_equal(out[0][1][k], out[1][1][k])
+    L.qllg_stag_destroy(S)
+
+
+def test_unknown_parameter_is_refused():
+    L = qll.load()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    assert L.qllg_set_param(b"no_such_knob", 1.0) == -1
+    assert "no_such_knob" in qll.last_error()
