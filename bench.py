@@ -48,7 +48,10 @@ WORKLOAD = "asqtad_cg_32^3x64_m0.01_eps0.4_16rhs_mixed_fp32_fp64_tol1e-8"
 METRIC = "mixed-precision multi-RHS asqtad CG solves/s at 1e-8 true residual"
 # iterations of the FP64 CG (cgSolveT) on this workload, measured with the
 # library's FP64 solver on GB300 (same recurrence as the reference)
-FP64_ITERS_MEASURED = None
+FP64_ITERS_MEASURED = 454
+# DRAM bytes (read + write) per even site of one 16-rhs FP32 half Dslash,
+# ncu capture at 24^3x48: 537.2 MB + 113.2 MB over 331,776 sites
+TRAFFIC_PER_SITE_BYTES = (537.198592e6 + 113.220096e6)/331776
 
 
 def log(*a):
@@ -279,7 +282,10 @@ def run_gpu(args):
                      "algorithmic_bytes_per_launch": launch_bytes,
                      "avg_launch_ms": avg_ms, "launches_timed": cnt.value,
                      "compulsory_frac": compulsory*Vh*NRHS/(avg_ms*1e-3)/1e9/peak if peak else None,
-                     "traffic": None},
+                     # dram read+write of one launch from an ncu capture at
+                     # 24^3x48 (650 MB), scaled by sites to this lattice
+                     "traffic": TRAFFIC_PER_SITE_BYTES*Vh,
+                     "traffic_source": "ncu dram__bytes_read+write at 24^3x48, scaled by sites"},
         "gpu_launches": nlaunch,
         "clocks": clk.summary(local),
         "device_bytes": int(L.qllg_stag_device_bytes(S)),
