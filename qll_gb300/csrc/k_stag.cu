@@ -117,7 +117,7 @@ stag_dslash(qllg_stag_args a)
   if(a.mode == 3) {
     if(skip) return;   // uniform: the flag was set before this launch
     double *res[2] = {a.sc->tmp, NULL};
-    if(grid_reduce<2>(red, NR, rhs, a.rb->partial, a.rb->counter, shm, res)) {
+    if(grid_reduce<2>(red, NR, rhs, a.partial, a.counter, shm, res)) {
       __syncthreads();
       if(threadIdx.x == 0) {
         if(a.mixed) cg_finish_mixed(a.sc, NR);
@@ -126,7 +126,7 @@ stag_dslash(qllg_stag_args a)
     }
   } else if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
-    grid_reduce<2>(red, NR, rhs, a.rb->partial, a.rb->counter, shm, res);
+    grid_reduce<2>(red, NR, rhs, a.partial, a.counter, shm, res);
   }
 }
 
@@ -259,7 +259,7 @@ stag_dslash_mr(qllg_stag_args a)
   if(a.mode == 3) {
     if(skip) return;
     double *res[2] = {a.sc->tmp, NULL};
-    if(grid_reduce_mr<2,R>(red, NR, Q, a.rb->partial, a.rb->counter, shm, res)) {
+    if(grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res)) {
       __syncthreads();
       if(threadIdx.x == 0) {
         if(a.mixed) cg_finish_mixed(a.sc, NR);
@@ -268,7 +268,7 @@ stag_dslash_mr(qllg_stag_args a)
     }
   } else if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
-    grid_reduce_mr<2,R>(red, NR, Q, a.rb->partial, a.rb->counter, shm, res);
+    grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res);
   }
 }
 
@@ -300,7 +300,10 @@ int launch_mr(const qllg_stag_args *a)
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
   int grid = (int)(need < maxg ? need : maxg);
   if(grid < 1) grid = 1;
-  stag_dslash_mr<PS,PL,NS,NR,R><<<grid, kThreads, 0, qllg_stream()>>>(*a);
+  qllg_stag_args A = *a;
+  A.partial = a->rb ? a->rb->partial : NULL;
+  A.counter = a->rb ? a->rb->counter : NULL;
+  stag_dslash_mr<PS,PL,NS,NR,R><<<grid, kThreads, 0, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash_mr launch");
 }
 
@@ -320,7 +323,10 @@ int launch_t(const qllg_stag_args *a)
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
   int grid = (int)(need < maxg ? need : maxg);
   if(grid < 1) grid = 1;
-  stag_dslash<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
+  qllg_stag_args A = *a;
+  A.partial = a->rb ? a->rb->partial : NULL;
+  A.counter = a->rb ? a->rb->counter : NULL;
+  stag_dslash<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash launch");
 }
 

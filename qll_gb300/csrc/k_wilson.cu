@@ -133,7 +133,7 @@ wilson_dslash(qllg_stag_args a)
   }
   if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
-    grid_reduce<2>(red, NR, rhs, a.rb->partial, a.rb->counter, shm, res);
+    grid_reduce<2>(red, NR, rhs, a.partial, a.counter, shm, res);
   }
 }
 
@@ -152,7 +152,10 @@ int launch_t(const qllg_stag_args *a)
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
   int grid = (int)(need < maxg ? need : maxg);
   if(grid < 1) grid = 1;
-  wilson_dslash<PS,PL,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
+  qllg_stag_args A = *a;
+  A.partial = a->rb ? a->rb->partial : NULL;
+  A.counter = a->rb ? a->rb->counter : NULL;
+  wilson_dslash<PS,PL,NR><<<grid, kThreads, 0, qllg_stream()>>>(A);
   return qllg_launched("wilson_dslash launch");
 }
 

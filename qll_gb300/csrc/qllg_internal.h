@@ -126,7 +126,10 @@ typedef struct {
   double *norm_self;     /* device [nrhs]: |self|^2, or NULL */
   const int *active;     /* device [nrhs] mask or NULL */
   const int *done;       /* device flag: skip everything when nonzero */
-  qllg_redbuf *rb;
+  qllg_redbuf *rb;        /* host struct; the launcher copies its device
+                            pointers into partial/counter below */
+  double *partial;        /* device block partials (from rb) */
+  unsigned *counter;      /* device last-block counter (from rb) */
   int dag;               /* Wilson only: gamma5 D gamma5 (projector signs flipped) */
   /* mode 3 (staggered CG, fused): Ap = a[rhs]*self - acc stays in registers,
    * then x += alpha self, r -= alpha Ap with alpha = 1/(a pnorm + vnorm) and
