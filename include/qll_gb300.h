@@ -104,6 +104,24 @@ int qllg_stag_vec_download(qllg_stag *S, const void *v_dev, int nrhs, void *cons
  * layout; links of that precision are derived from FP64 on first use */
 int qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *out_dev,
                             const void *in_dev);
+
+/* No counterpart in the reference (QLL takes its work memory from myalloc,
+ * lib/common.c:10, e.g. per call in cgmsSolve, lib/cgms.c:43).  The same
+ * half Dslash as qllg_stag_dslash_device, plus |out|^2 of each rhs written to the device
+ * array norm2_dev[nrhs], and no device memory allocated by the call: the
+ * grid reduction uses a fixed file-scope __device__ scratch of 262,400 B
+ * (partials of up to 1024 blocks x 16 rhs), and links not yet created in
+ * precision prec are refused, not derived.  It is for callers that cannot
+ * allocate: a serving loop holding a fixed HBM budget for admitted solves,
+ * or one whose concurrent streams a device-synchronising cudaMalloc/cudaFree
+ * would stall.  Limits: nrhs in {1,2,4,8,16}; anything else, or links of
+ * prec missing, returns -1 with qllg_last_error() saying why.  The first
+ * call on each device looks up the scratch's address (cudaGetSymbolAddress
+ * with that device current): make it before any stream capture.  The
+ * scratch is one per device, so calls that overlap in time (other host
+ * threads, other streams) race: serialise them. */
+int qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
+                                   void *out_dev, const void *in_dev, double *norm2_dev);
 size_t qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs);
 
 /* neighbour table of slot s for the output sites of a parity, as QLL site

@@ -84,6 +84,10 @@ typedef struct {
 } qllg_redbuf;
 int  qllg_redbuf_init(qllg_redbuf *rb);
 void qllg_redbuf_free(qllg_redbuf *rb);
+/* a redbuf over the fixed file-scope scratch of k_noalloc.cu (no
+ * allocation; the first call on a device looks up its address) */
+#define QLLG_NOALLOC_MAXBLOCKS 1024
+int  qllg_noalloc_redbuf(qllg_redbuf *rb);
 
 /* ----------------------------------------------------- field transfers */
 /* stage: nrhs blocks of the reference's VLEN=1 host layout, each

@@ -813,6 +813,63 @@ qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *
                      NULL, NULL, NULL, NULL);
 }
 
+/* out = D in as qllg_stag_dslash_device, plus |out|^2 of each rhs into
+ * norm2_dev, without allocating any device memory: the grid reduction runs
+ * in the fixed scratch of k_noalloc.cu instead of a workspace, and links
+ * that do not exist yet in precision prec are refused rather than derived
+ * (deriving them allocates).  For callers with a fixed device-memory budget
+ * (a serving loop that admits solves against HBM) or with other streams in
+ * flight that a device-synchronising cudaMalloc/cudaFree would stall.
+ * The first call on a device looks up the scratch's address; make it
+ * before any stream capture.  Calls that overlap in time share the scratch
+ * and race. */
+int
+qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
+                               void *out_dev, const void *in_dev, double *norm2_dev)
+{
+  if(!S || !out_dev || !in_dev || !norm2_dev) {
+    qllg_set_error("dslash_norm2_noalloc: null argument");
+    return -1;
+  }
+  if(!valid_nrhs(nrhs) || nrhs > QLLG_MAXRHS) {
+    qllg_set_error("dslash_norm2_noalloc: nrhs %d not in {1,2,4,8,16} (the fixed scratch holds "
+                   "partial sums of at most %d rhs)", nrhs, QLLG_MAXRHS);
+    return -1;
+  }
+  if(prec < 0 || prec > 2) { qllg_set_error("dslash_norm2_noalloc: precision %d", prec); return -1; }
+  if(out_parity != 0 && out_parity != 1) {
+    qllg_set_error("dslash_norm2_noalloc: parity %d", out_parity);
+    return -1;
+  }
+  if(!S->links[prec]) {
+    qllg_set_error("dslash_norm2_noalloc: links of precision %d not created yet (creating them "
+                   "allocates; one qllg_stag_dslash_device call of that precision does it)", prec);
+    return -1;
+  }
+  qllg_redbuf rb;
+  if(qllg_noalloc_redbuf(&rb)) return -1;
+  /* the last-block counter must start at zero (the last block also leaves
+   * it at zero); the partials are written before they are read and the
+   * norms are stored, not accumulated */
+  if(qllg_check_cuda(cudaMemsetAsync(rb.counter, 0, sizeof(unsigned), qllg_stream()),
+                     "dslash_norm2_noalloc: counter clear")) return -1;
+  qllg_stag_args A;
+  memset(&A, 0, sizeof(A));
+  A.g = S->g;
+  A.out_parity = out_parity;
+  A.nrhs = nrhs;
+  A.nslots = S->nslots;
+  A.links = S->links[prec];
+  A.lscale = S->lscale;
+  A.in = in_dev;
+  A.out = out_dev;
+  A.mode = 0;
+  A.b = 1;
+  A.norm_out = norm2_dev;
+  A.rb = &rb;
+  return qllg_k_stag_dslash(prec, prec, &A);
+}
+
 /* bytes of a device vector of nrhs rhs in precision prec (one parity) */
 size_t
 qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs)
