@@ -406,6 +406,11 @@ def run_dslash_only(args):
     L.qllg_stag_vec_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     L.qllg_stag_dslash_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    for kv in args.param:
+        k, v = kv.split("=")
+        if L.qllg_set_param(k.encode(), float(v)) != 0:
+            raise SystemExit(qll.last_error())
     stream = torch.cuda.current_stream()
     L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
     dims = tuple(int(v) for v in args.dims.split(","))
@@ -442,8 +447,55 @@ def run_dslash_only(args):
     ns = 4 if prec == 2 else 0
     per = (8*18*bs + 8*18*bs)/args.nrhs + 17*(6*bs + ns)
     print(json.dumps({"dslash_only": {"dims": dims, "nrhs": args.nrhs, "prec": args.prec,
+                                      "params": args.param,
                                       "ms": ms, "algorithmic_gbs": per*Vh*args.nrhs/(ms*1e-3)/1e9,
                                       "error": qll.last_error()}}), flush=True)
+    L.qllg_stag_destroy(S)
+
+
+def run_solve_only(args):
+    """a few multi-rhs solves of a chosen mode on a chosen lattice, for
+    profiling the solver's kernels (and sweeping its parameters with
+    --param name=value): prints iterations, reliable updates and time"""
+    from qll_gb300 import qll
+    L = qll.load()
+    L.qllg_stag_create_asqtad.restype = ctypes.c_void_p
+    L.qllg_stag_create_asqtad.argtypes = [ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_void_p),
+                                          ctypes.POINTER(qll.Fat7Coeffs)]
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    for kv in args.param:
+        k, v = kv.split("=")
+        if L.qllg_set_param(k.encode(), float(v)) != 0:
+            raise SystemExit(qll.last_error())
+    dims = tuple(int(v) for v in args.dims.split(","))
+    mode = {"double": qll.SOLVE_DOUBLE, "single": qll.SOLVE_SINGLE,
+            "mixed_half": qll.SOLVE_MIXED_HALF, "mixed_single": qll.SOLVE_MIXED_SINGLE}[args.mode]
+    thin = qll.gen_gauge(dims, SEED_GAUGE, EPS, ks=True)
+    coef = qll.asqtad_coeffs()
+    S = ctypes.c_void_p(L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(thin),
+                                                  ctypes.byref(coef)))
+    if not S.value:
+        raise SystemExit(qll.last_error())
+    nrhs = args.nrhs
+    srcs = [qll.gen_source(dims, SEED_SRC + r, 6, "even") for r in range(nrhs)]
+    b = L.qllg_stag_vec_alloc(S, nrhs)
+    x = L.qllg_stag_vec_alloc(S, nrhs)
+    L.qllg_stag_vec_upload(S, b, nrhs, qll.vp_array(srcs))
+    masses = (ctypes.c_double*nrhs)(*([MASS]*nrhs))
+    info = qll.SolveInfo()
+    for k in range(args.launches):
+        t = time.time()
+        its = L.qllg_stag_solve_device(S, nrhs, x, b, masses, RSQ, MAXITS, mode, ctypes.byref(info))
+        dt = time.time() - t
+        print(json.dumps({"solve_only": {"dims": dims, "nrhs": nrhs, "mode": args.mode,
+                                         "params": args.param, "iters": its,
+                                         "reliable_updates": info.reliable_updates,
+                                         "seconds": dt,
+                                         "max_true_rsq": max(info.true_rsq[r] for r in range(nrhs)),
+                                         "error": qll.last_error()}}), flush=True)
+    L.qllg_stag_vec_free(b)
+    L.qllg_stag_vec_free(x)
     L.qllg_stag_destroy(S)
 
 
@@ -461,9 +513,15 @@ def main():
     ap.add_argument("--prec", default="f32", choices=["f64", "f32", "i16"])
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--launches", type=int, default=20)
+    ap.add_argument("--solve-only", action="store_true")
+    ap.add_argument("--mode", default="mixed_single",
+                    choices=["double", "single", "mixed_half", "mixed_single"])
+    ap.add_argument("--param", action="append", default=[])
     args = ap.parse_args()
     if args.dslash_only:
         run_dslash_only(args)
+    elif args.solve_only:
+        run_solve_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -158,8 +158,11 @@ int qllg_wilson_dslash(qllg_wilson *W, void *x, double massp, const void *y, con
 int qllg_wilson_solve(qllg_wilson *W, void *x, const void *b, double mass, double rsq,
                       int maxits, int mode, qllg_solve_info *info);
 
-/* solver parameters: "reliable_delta" (0.1), "reortho" (1), "graph" (1),
- * "poll" (8); returns -1 for an unknown name */
+/* solver parameters: "reliable_delta" (0.1, 16-bit mixed mode),
+ * "reliable_delta_single" (0.01, FP32 mixed mode), "reortho" (1), "graph" (1),
+ * "poll" (8), "dslash_mr" (1: multi-rhs Dslash with 4 rhs per thread),
+ * "ru_compact" (1: the FP64 reliable update runs over the flagged rhs
+ * only); returns -1 for an unknown name */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);
 

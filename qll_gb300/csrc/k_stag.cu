@@ -134,7 +134,7 @@ stag_dslash(qllg_stag_args a)
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
 // sides, so each link is loaded and converted once per R rhs and the R
 // accumulator sets give independent FMA chains.  Same epilogues as above.
-template <int PS, int PL, int NS, int NR, int R>
+template <int PS, int PL, int NS, int NR, int R, bool V4>
 __global__ void __launch_bounds__(kThreads)
 stag_dslash_mr(qllg_stag_args a)
 {
@@ -152,13 +152,15 @@ stag_dslash_mr(qllg_stag_args a)
   const int q = threadIdx.x % Q;
   bool act[R];
   T ca[R], alpha[R];
-  bool anyact = false;
+  bool anyact = false, allact = true;
+  constexpr bool v4 = (R == 4) && V4 && PS == QLLG_F32;
   const T cb = (T)a.b;
 #pragma unroll
   for(int j=0; j<R; j++) {
     const int rhs = q*R + j;
     act[j] = !a.active || a.active[rhs];
     anyact |= act[j];
+    allact &= act[j];
     ca[j] = (T)(a.a ? a.a[rhs] : a.a0);
     alpha[j] = (a.mode == 3 && act[j])
       ? (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs])) : (T)0;
@@ -197,18 +199,93 @@ stag_dslash_mr(qllg_stag_args a)
             const size_t kb = (size_t)nbr_index(G, x, mu, d)*NR + q*R;
             Cx<T> U[9];
             LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+            if constexpr (v4) {
+              // two rhs per 16-byte load and colour
 #pragma unroll
-            for(int j=0; j<R; j++) {
-              if(!act[j]) continue;
-              Cx<T> v[3];
-              SpinorIO<PS,3>::load(a.in, total, kb + j, v);
+              for(int h=0; h<R/2; h++) {
+                if(!act[2*h] && !act[2*h + 1]) continue;
+                Cx<T> v[2][3];
+                Spinor4<PS>::load_half(a.in, total, kb, h, v);
 #pragma unroll
-              for(int l=0; l<3; l++) {
+                for(int jj=0; jj<2; jj++) {
 #pragma unroll
-                for(int c=0; c<3; c++) cmac(acc[j][c], U[3*l + c], v[l]);
+                  for(int l=0; l<3; l++) {
+#pragma unroll
+                    for(int c=0; c<3; c++) cmac(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
+                  }
+                }
+              }
+            } else {
+#pragma unroll
+              for(int j=0; j<R; j++) {
+                if(!act[j]) continue;
+                Cx<T> v[3];
+                SpinorIO<PS,3>::load(a.in, total, kb + j, v);
+#pragma unroll
+                for(int l=0; l<3; l++) {
+#pragma unroll
+                  for(int c=0; c<3; c++) cmac(acc[j][c], U[3*l + c], v[l]);
+                }
               }
             }
           }
+        }
+      }
+      // epilogue.  With v4 and all R rhs active, the R rhs of the site move
+      // as 16-byte vectors (inactive rhs must keep their old values, so a
+      // partly active group takes the per-rhs path)
+      if constexpr (v4) {
+        if(allact) {
+          // per pair of rhs (one 16-byte vector per colour) to keep few
+          // values live
+#pragma unroll
+          for(int h=0; h<R/2; h++) {
+            Cx<T> sv[2][3];
+            if(a.self) Spinor4<PS>::load_half(a.self, total, t0, h, sv);
+            if(a.mode == 3) {
+              Cx<T> xv[2][3], rv[2][3];
+              Spinor4<PX>::load_half(a.x, total, t0, h, xv);
+              Spinor4<PX>::load_half(a.r, total, t0, h, rv);
+#pragma unroll
+              for(int jj=0; jj<2; jj++) {
+                const int j = 2*h + jj;
+#pragma unroll
+                for(int c=0; c<3; c++) {
+                  T apr = fma(cb, acc[j][c].r, ca[j]*sv[jj][c].r);
+                  T api = fma(cb, acc[j][c].i, ca[j]*sv[jj][c].i);
+                  xv[jj][c].r = fma(alpha[j], sv[jj][c].r, xv[jj][c].r);
+                  xv[jj][c].i = fma(alpha[j], sv[jj][c].i, xv[jj][c].i);
+                  rv[jj][c].r = fma(-alpha[j], apr, rv[jj][c].r);
+                  rv[jj][c].i = fma(-alpha[j], api, rv[jj][c].i);
+                  red[0][j] += (double)rv[jj][c].r*rv[jj][c].r + (double)rv[jj][c].i*rv[jj][c].i;
+                }
+              }
+              Spinor4<PX>::store_half(a.x, total, t0, h, xv);
+              Spinor4<PX>::store_half(a.r, total, t0, h, rv);
+              continue;
+            }
+            Cx<T> ov[2][3];
+#pragma unroll
+            for(int jj=0; jj<2; jj++) {
+              const int j = 2*h + jj;
+#pragma unroll
+              for(int c=0; c<3; c++) {
+                if(a.mode == 2) {
+                  T sr = a.self ? ca[j]*sv[jj][c].r : (T)0, si = a.self ? ca[j]*sv[jj][c].i : (T)0;
+                  ov[jj][c].r = fma(cb, acc[j][c].r, sr);
+                  ov[jj][c].i = fma(cb, acc[j][c].i, si);
+                } else {
+                  ov[jj][c] = acc[j][c];
+                }
+                if(a.norm_out)
+                  red[0][j] += (double)ov[jj][c].r*ov[jj][c].r + (double)ov[jj][c].i*ov[jj][c].i;
+                if(a.norm_self && a.self)
+                  red[1][j] += (double)sv[jj][c].r*sv[jj][c].r + (double)sv[jj][c].i*sv[jj][c].i;
+              }
+            }
+            Spinor4<PS>::store_half(a.out, total, t0, h, ov);
+          }
+          continue;
         }
       }
 #pragma unroll
@@ -272,6 +349,101 @@ stag_dslash_mr(qllg_stag_args a)
   }
 }
 
+// Compacted variant for sparse masks (the FP64 reliable update of the
+// mixed solver, where one or a few rhs of the batch are flagged at a time):
+// work item w maps to (site, k-th flagged rhs), so the cost follows the
+// number of flagged rhs instead of running whole warps at the FP64 rate for
+// one of their lanes.  Modes 0 and 2 without norms.
+template <int PS, int PL, int NS, int NR>
+__global__ void __launch_bounds__(kThreads)
+stag_dslash_compact(qllg_stag_args a)
+{
+  typedef typename Calc<PS, PL>::T T;
+  __shared__ int list[NR];
+  __shared__ int nact_s;
+  if(a.done && *(volatile const int *)a.done) return;      // uniform
+  if(threadIdx.x == 0) {
+    int n = 0;
+    for(int r=0; r<NR; r++) if(a.active[r]) list[n++] = r;
+    nact_s = n;
+  }
+  __syncthreads();
+  const int nact = nact_s;
+  if(!nact) return;
+  const Geo G = make_geo(a.g);
+  const size_t V = (size_t)a.g.V;
+  const size_t total = (size_t)G.Vh * NR;
+  const size_t nwork = (size_t)G.Vh * nact;
+  const int p = a.out_parity;
+  const size_t loff = p ? (size_t)G.Vh : 0;
+  const T cb = (T)a.b;
+  for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < nwork;
+      w += (size_t)gridDim.x*blockDim.x) {
+    const int site = (int)(w / nact);
+    const int rhs = list[w % nact];
+    const size_t t = (size_t)site*NR + rhs;
+    int x[4];
+    site_coords(G, p, site, x);
+    Cx<T> acc[3];
+#pragma unroll
+    for(int c=0; c<3; c++) { acc[c].r = 0; acc[c].i = 0; }
+#pragma unroll
+    for(int mu=0; mu<4; mu++) {
+#pragma unroll
+      for(int back=0; back<2; back++) {
+#pragma unroll
+        for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
+          const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
+          const int d = (nk ? 3 : 1)*(back ? -1 : 1);
+          const int k = nbr_index(G, x, mu, d);
+          Cx<T> U[9], v[3];
+          LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+          SpinorIO<PS,3>::load(a.in, total, (size_t)k*NR + rhs, v);
+#pragma unroll
+          for(int l=0; l<3; l++) {
+#pragma unroll
+            for(int j=0; j<3; j++) cmac(acc[j], U[3*l + j], v[l]);
+          }
+        }
+      }
+    }
+    Cx<T> out[3];
+    if(a.mode == 2) {
+      const T ca = (T)(a.a ? a.a[rhs] : a.a0);
+      Cx<T> self[3];
+      if(a.self) SpinorIO<PS,3>::load(a.self, total, t, self);
+#pragma unroll
+      for(int c=0; c<3; c++) {
+        T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
+        out[c].r = fma(cb, acc[c].r, sr);
+        out[c].i = fma(cb, acc[c].i, si);
+      }
+    } else {
+#pragma unroll
+      for(int c=0; c<3; c++) out[c] = acc[c];
+    }
+    SpinorIO<PS,3>::store(a.out, total, t, out);
+  }
+}
+
+template <int PS, int PL, int NS, int NR>
+int launch_compact(const qllg_stag_args *a)
+{
+  static int blocks_per_sm = 0;
+  if(!blocks_per_sm) {
+    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &blocks_per_sm, stag_dslash_compact<PS,PL,NS,NR>, kThreads, 0), "occupancy")) return -1;
+    if(blocks_per_sm < 1) blocks_per_sm = 1;
+  }
+  // sized for one flagged rhs: with more, the grid-stride loop takes them
+  size_t need = ((size_t)a->g.Vh + kThreads - 1)/kThreads;
+  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
+  int grid = (int)(need < maxg ? need : maxg);
+  if(grid < 1) grid = 1;
+  stag_dslash_compact<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
+  return qllg_launched("stag_dslash_compact launch");
+}
+
 __global__ void
 nbr_table(qllg_geom g, int p, int slot, int *out)
 {
@@ -285,31 +457,46 @@ nbr_table(qllg_geom g, int p, int slot, int *out)
   out[i] = (1 - p)*G.Vh + nbr_index(G, x, mu, d);
 }
 
+// 16-byte vector access to the spinor buffers is allowed when every base
+// pointer the kernel touches is 16-byte aligned (per-colour strides and the
+// 4-rhs offsets keep that alignment)
+bool vec4_ok(const qllg_stag_args *a)
+{
+  const void *ptrs[5] = {a->in, a->self, a->out, a->x, a->r};
+  for(int i=0; i<5; i++) if(((uintptr_t)ptrs[i] & 15u) != 0) return false;
+  return true;
+}
+
 template <int PS, int PL, int NS, int NR, int R>
 int launch_mr(const qllg_stag_args *a)
 {
-  static int blocks_per_sm = 0;
-  if(!blocks_per_sm) {
+  const bool v4 = (R == 4) && PS == QLLG_F32 && qllg_get_param("dslash_vec4") != 0 &&
+                  vec4_ok(a);
+  static int blocks_per_sm[2] = {0, 0};
+  if(!blocks_per_sm[v4]) {
     if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm, stag_dslash_mr<PS,PL,NS,NR,R>, kThreads, 0), "occupancy")) return -1;
-    if(blocks_per_sm < 1) blocks_per_sm = 1;
+         &blocks_per_sm[v4], v4 ? stag_dslash_mr<PS,PL,NS,NR,R,true> : stag_dslash_mr<PS,PL,NS,NR,R,false>,
+         kThreads, 0), "occupancy")) return -1;
+    if(blocks_per_sm[v4] < 1) blocks_per_sm[v4] = 1;
   }
   size_t work = (size_t)a->g.Vh * (NR/R);
   size_t need = (work + kThreads - 1)/kThreads;
-  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
+  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm[v4];
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
   int grid = (int)(need < maxg ? need : maxg);
   if(grid < 1) grid = 1;
   qllg_stag_args A = *a;
   A.partial = a->rb ? a->rb->partial : NULL;
   A.counter = a->rb ? a->rb->counter : NULL;
-  stag_dslash_mr<PS,PL,NS,NR,R><<<grid, kThreads, 0, qllg_stream()>>>(A);
+  if(v4) stag_dslash_mr<PS,PL,NS,NR,R,true><<<grid, kThreads, 0, qllg_stream()>>>(A);
+  else stag_dslash_mr<PS,PL,NS,NR,R,false><<<grid, kThreads, 0, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash_mr launch");
 }
 
 template <int PS, int PL, int NS, int NR>
 int launch_t(const qllg_stag_args *a)
 {
+  if(a->compact) return launch_compact<PS,PL,NS,NR>(a);
   if(NR >= 4 && !qllg_mr_disabled()) return launch_mr<PS,PL,NS,NR,(NR >= 4 ? 4 : 1)>(a);
   static int blocks_per_sm = 0;
   if(!blocks_per_sm) {
@@ -358,6 +545,10 @@ int launch_ns(const qllg_stag_args *a)
 extern "C" int
 qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
 {
+  if(a->compact && (!a->active || a->norm_out || a->norm_self || a->mode == 1 || a->mode == 3)) {
+    qllg_set_error("stag_dslash: compacted launch needs a mask and takes modes 0 and 2 only");
+    return -1;
+  }
   if((a->norm_out || a->norm_self || a->mode == 3) && !a->rb) {
     qllg_set_error("stag_dslash: reduction requested without workspace");
     return -1;

@@ -132,6 +132,62 @@ template <> struct SpinorIO<QLLG_I16, 3> {
   }
 };
 
+// four consecutive rhs (idx0, a multiple of 4) of one site, all three
+// colours: FP32 as two 16-byte loads per colour (the buffer and stride must
+// keep idx0 16-byte aligned: the launchers check the base pointers); other
+// precisions one load per rhs
+template <int P> struct Spinor4 {
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, size_t stride, size_t idx0, Cx<T> v[4][3]) {
+#pragma unroll
+    for(int j=0; j<4; j++) SpinorIO<P,3>::load(b, stride, idx0 + j, v[j]);
+  }
+  template <typename T>
+  static __device__ __forceinline__ void store(void *b, size_t stride, size_t idx0, const Cx<T> v[4][3]) {
+#pragma unroll
+    for(int j=0; j<4; j++) SpinorIO<P,3>::store(b, stride, idx0 + j, v[j]);
+  }
+};
+template <> struct Spinor4<QLLG_F32> {
+  // rhs 2h and 2h+1 only: one 16-byte load per colour
+  template <typename T>
+  static __device__ __forceinline__ void load_half(const void *b, size_t stride, size_t idx0, int h,
+                                                   Cx<T> v[2][3]) {
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      float4 q = __ldg((const float4 *)((const float2 *)b + c*stride + idx0) + h);
+      v[0][c].r = q.x; v[0][c].i = q.y; v[1][c].r = q.z; v[1][c].i = q.w;
+    }
+  }
+  template <typename T>
+  static __device__ __forceinline__ void store_half(void *b, size_t stride, size_t idx0, int h,
+                                                    const Cx<T> v[2][3]) {
+#pragma unroll
+    for(int c=0; c<3; c++)
+      ((float4 *)((float2 *)b + c*stride + idx0))[h] =
+        make_float4((float)v[0][c].r, (float)v[0][c].i, (float)v[1][c].r, (float)v[1][c].i);
+  }
+  template <typename T>
+  static __device__ __forceinline__ void load(const void *b, size_t stride, size_t idx0, Cx<T> v[4][3]) {
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      const float4 *p = (const float4 *)((const float2 *)b + c*stride + idx0);
+      float4 lo = __ldg(p), hi = __ldg(p + 1);
+      v[0][c].r = lo.x; v[0][c].i = lo.y; v[1][c].r = lo.z; v[1][c].i = lo.w;
+      v[2][c].r = hi.x; v[2][c].i = hi.y; v[3][c].r = hi.z; v[3][c].i = hi.w;
+    }
+  }
+  template <typename T>
+  static __device__ __forceinline__ void store(void *b, size_t stride, size_t idx0, const Cx<T> v[4][3]) {
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      float4 *p = (float4 *)((float2 *)b + c*stride + idx0);
+      p[0] = make_float4((float)v[0][c].r, (float)v[0][c].i, (float)v[1][c].r, (float)v[1][c].i);
+      p[1] = make_float4((float)v[2][c].r, (float)v[2][c].i, (float)v[3][c].r, (float)v[3][c].i);
+    }
+  }
+};
+
 // --------------------------------------------------------------- link I/O
 // slot-major stores; V = sites of the full lattice
 template <int P> struct LinkIO;

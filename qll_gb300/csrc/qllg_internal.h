@@ -134,6 +134,8 @@ typedef struct {
                             pointers into partial/counter below */
   double *partial;        /* device block partials (from rb) */
   unsigned *counter;      /* device last-block counter (from rb) */
+  int compact;           /* threads over (site, flagged rhs of active) only;
+                            modes 0 and 2, no norms */
   int dag;               /* Wilson only: gamma5 D gamma5 (projector signs flipped) */
   /* mode 3 (staggered CG, fused): Ap = a[rhs]*self - acc stays in registers,
    * then x += alpha self, r -= alpha Ap with alpha = 1/(a pnorm + vnorm) and
@@ -218,6 +220,10 @@ int qllg_k_cg_update_xr(int prec, void *x, void *r, const void *p, const void *A
 /* p = p + (1/rsq) r for active rhs */
 int qllg_k_cg_update_p(int prec, void *p, const void *r, int nsites, int ncomp,
                        int nrhs, qllg_cg_scalars *s);
+/* the same for staggered fields, fused with pnorm = |p|^2 of the new p
+ * (r in VecPrec of prec) */
+int qllg_k_cg_update_p_norm(int prec, void *p, const void *r, int nsites, int nrhs,
+                            qllg_cg_scalars *s, qllg_redbuf *rb);
 /* rsq = |r|^2 etc for start-up: out[rhs] = |x|^2 */
 int qllg_k_norm2(int prec, const void *x, int nsites, int ncomp, int nrhs, double *out,
                  qllg_redbuf *rb);

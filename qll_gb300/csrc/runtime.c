@@ -247,11 +247,19 @@ qllg_version(void)
 
 /* tunable solver parameters (qllg_set_param) */
 static struct { const char *name; double value; } g_params[] = {
-  {"reliable_delta", 0.1},   /* reliable update when |r| < delta * |r at last update| */
+  {"reliable_delta", 0.1},   /* 16-bit mixed mode: reliable update when
+                                |r| < delta * |r at the last update| */
+  {"reliable_delta_single", 0.01}, /* the same for the FP32 mixed mode: FP32
+                                      sloppy iterations keep the CG recurrence
+                                      over two decades (measured: 455
+                                      iterations at 32^3x64, m=0.01, for 0.1
+                                      and 0.01; 464 at 0.003, 623 at 0.001) */
   {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
   {"graph", 1},              /* run solver iterations as one CUDA graph launch */
   {"poll", 8},               /* first batch of iterations between host checks */
   {"dslash_mr", 1},          /* multi-rhs Dslash: one thread per site and 4 rhs */
+  {"ru_compact", 1},         /* reliable-update Dslash over the flagged rhs only */
+  {"dslash_vec4", 1},        /* 16-byte loads of the 4 rhs of a thread (FP32) */
 };
 
 int

@@ -227,11 +227,13 @@ qllg_stag_device_bytes(const qllg_stag *S)
   return b;
 }
 
-/* one half-Dslash launch */
+/* one half-Dslash launch; compact: threads only over the rhs flagged in
+ * active (modes 0 and 2, no norms) */
 static int
-dslash_half(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *in,
-            const void *self, void *out, int mode, const double *a, double a0, double b,
-            double *norm_out, double *norm_self, const int *active, const int *done)
+dslash_half_x(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *in,
+              const void *self, void *out, int mode, const double *a, double a0, double b,
+              double *norm_out, double *norm_self, const int *active, const int *done,
+              int compact)
 {
   if(ensure_links(S, pl)) return -1;
   qllg_stag_args A;
@@ -254,6 +256,7 @@ dslash_half(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *
   A.active = active;
   A.done = done;
   A.rb = &S->rb;
+  A.compact = compact;
   static const char *pn[3] = {"f64", "f32", "i16"};
   char fam[32];
   snprintf(fam, sizeof(fam), "stag_dslash_%s_n%d", pn[ps], nrhs);
@@ -261,6 +264,15 @@ dslash_half(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *
   int rc = qllg_k_stag_dslash(ps, pl, &A);
   qllg_tm_end();
   return rc;
+}
+
+static int
+dslash_half(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *in,
+            const void *self, void *out, int mode, const double *a, double a0, double b,
+            double *norm_out, double *norm_self, const int *active, const int *done)
+{
+  return dslash_half_x(S, ps, pl, out_parity, nrhs, in, self, out, mode, a, a0, b, norm_out,
+                       norm_self, active, done, 0);
 }
 
 /* host [V][6] parity block(s) <-> device single-rhs block */
@@ -327,6 +339,19 @@ apply_normal(qllg_stag *S, int ps, int pl, int nrhs, const void *p, void *v, voi
     return -1;
   return dslash_half(S, ps, pl, 0, nrhs, v, p, Ap, 2, S->sc->mass2, 0, -1, NULL, pnorm,
                      active, done);
+}
+
+/* t = m^2 x - D_eo D_oe x for the rhs flagged in active only (the FP64
+ * reliable update: threads over the flagged rhs, so its cost follows how
+ * many are flagged); every launch returns at once when *done is set */
+static int
+apply_normal_flagged(qllg_stag *S, int prec, int nrhs, const void *x, void *w, void *t,
+                     const int *active, const int *done)
+{
+  if(dslash_half_x(S, prec, prec, 1, nrhs, x, NULL, w, 0, NULL, 0, 1, NULL, NULL, active, done,
+                   1)) return -1;
+  return dslash_half_x(S, prec, prec, 0, nrhs, w, x, t, 2, S->sc->mass2, 0, -1, NULL, NULL,
+                       active, done, 1);
 }
 
 /* one CG iteration in three launches (cgSolveT, lib/cg.c:77-115):
@@ -418,8 +443,11 @@ issue_iteration(qllg_stag *S, const iter_ctx *c)
   /* reliable update of the flagged rhs; every launch returns at once when
    * no rhs is flagged */
   if(qllg_k_mcg_accum(QLLG_F32, c->x64, c->x, Vh, 3, c->nrhs, sc)) return -1;
-  if(apply_normal(S, QLLG_F64, QLLG_F64, c->nrhs, c->x64, c->w64, c->t64, NULL, NULL, sc->ru,
-                  &sc->no_ru)) return -1;
+  if(qllg_get_param("ru_compact") != 0) {
+    if(apply_normal_flagged(S, QLLG_F64, c->nrhs, c->x64, c->w64, c->t64, sc->ru, &sc->no_ru))
+      return -1;
+  } else if(apply_normal(S, QLLG_F64, QLLG_F64, c->nrhs, c->x64, c->w64, c->t64, NULL, NULL,
+                         sc->ru, &sc->no_ru)) return -1;
   if(qllg_k_mcg_residual(QLLG_F32, c->r64, c->r, c->b, c->t64, Vh, 3, c->nrhs, 0, sc, &S->rb))
     return -1;
   if(c->reortho && qllg_k_mcg_reortho(c->ps, c->p, c->r, Vh, c->nrhs, sc, &S->rb)) return -1;
@@ -639,7 +667,7 @@ solve_dev(qllg_stag *S, int nrhs, void *x, const void *b, const double mass[], d
     break;
   case QLLG_SOLVE_MIXED_SINGLE:
     its = cg_mixed(S, QLLG_F32, QLLG_F32, QLLG_F32, nrhs, x, b, mass, rsq, maxits,
-                   qllg_get_param("reliable_delta"));
+                   qllg_get_param("reliable_delta_single"));
     break;
   default:
     qllg_set_error("solve: unknown mode %d", mode);

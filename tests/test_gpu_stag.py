@@ -188,6 +188,68 @@ def test_graph_loop_matches_host_loop(mode):
     L.qllg_stag_destroy(S)
 
 
+@pytest.mark.parametrize("mode", [qll.SOLVE_MIXED_SINGLE, qll.SOLVE_MIXED_HALF])
+def test_compact_reliable_update_matches_masked(mode):
+    """the reliable update over the flagged rhs only (threads compacted onto
+    them) and the masked multi-rhs launch compute the same FP64 residuals:
+    identical iterations and bitwise identical solutions"""
+    L, S, u, u3 = _native()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    nrhs = 8
+    masses = (c_double*nrhs)(*[0.05 + 0.02*k for k in range(nrhs)])
+    bs = [qll.gen_source(DIMS, 5100 + k, 6, "even") for k in range(nrhs)]
+    out = {}
+    for compact in (1, 0):
+        L.qllg_set_param(b"ru_compact", compact)
+        xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+        info = qll.SolveInfo()
+        its = L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), masses, 1e-16, 5000,
+                                mode, byref(info))
+        assert its > 0, qll.last_error()
+        assert info.reliable_updates > 0
+        out[compact] = (list(info.iters[:nrhs]), xs)
+    L.qllg_set_param(b"ru_compact", 1)
+    assert out[0][0] == out[1][0]
+    for k in range(nrhs):
+        assert np.array_equal(out[0][1][k], out[1][1][k])
+    L.qllg_stag_destroy(S)
+
+
+@pytest.mark.parametrize("nrhs", [4, 16])
+def test_vectorised_dslash_matches_per_rhs_loads(nrhs):
+    """FP32 multi-rhs Dslash with 16-byte spinor access, with per-rhs
+    access (parameter off), and on buffers offset by 8 bytes (the launcher
+    then falls back to per-rhs access): bitwise identical outputs"""
+    torch = pytest.importorskip("torch")
+    L, S, u, u3 = _native()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_stag_vec_bytes.restype = ctypes.c_size_t
+    L.qllg_stag_vec_bytes.argtypes = [ctypes.c_void_p, c_int, c_int]
+    L.qllg_stag_dslash_device.argtypes = [ctypes.c_void_p, c_int, c_int, c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    n = L.qllg_stag_vec_bytes(S, 1, nrhs)//4
+    g = torch.Generator(device="cuda").manual_seed(77 + nrhs)
+    src = torch.randn(n + 2, dtype=torch.float32, device="cuda", generator=g)
+    outs = []
+    for vec4, off in ((1, 0), (0, 0), (1, 2)):
+        L.qllg_set_param(b"dslash_vec4", vec4)
+        dst = torch.zeros(n + 2, dtype=torch.float32, device="cuda")
+        if off:
+            src[off:].copy_(src[:n].clone())
+        torch.cuda.synchronize()
+        for parity in (0, 1):
+            rc = L.qllg_stag_dslash_device(S, 1, nrhs, parity,
+                                           ctypes.c_void_p(dst[off:].data_ptr() + 0),
+                                           ctypes.c_void_p(src[off:].data_ptr()))
+            assert rc == 0, qll.last_error()
+            torch.cuda.synchronize()
+            outs.append(dst[off:off + n].clone())
+    L.qllg_set_param(b"dslash_vec4", 1)
+    assert torch.equal(outs[0], outs[2]) and torch.equal(outs[1], outs[3])
+    assert torch.equal(outs[0], outs[4]) and torch.equal(outs[1], outs[5])
+    L.qllg_stag_destroy(S)
+
+
 def test_unknown_parameter_is_refused():
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
