@@ -57,6 +57,39 @@ __global__ void to_aos(const void *dev, S *stage, int nsites, int nrhs, size_t r
   }
 }
 
+// one column (rhs col of nrhs) of an FP64 device vector <-> a contiguous
+// [nsites][6] double array (the continuous-batching solver moves requests
+// in and out of single columns while the others keep running)
+__global__ void column_from_aos_k(void *dev, const double *stage, int nsites, int nrhs, int col)
+{
+  const size_t total = (size_t)nsites*nrhs;
+  for(size_t s = (size_t)blockIdx.x*blockDim.x + threadIdx.x; s < (size_t)nsites;
+      s += (size_t)gridDim.x*blockDim.x) {
+    Cx<double> v[3];
+#pragma unroll
+    for(int c=0; c<3; c++) { v[c].r = stage[6*s + 2*c]; v[c].i = stage[6*s + 2*c + 1]; }
+    SpinorIO<QLLG_F64,3>::store(dev, total, s*nrhs + col, v);
+  }
+}
+
+__global__ void column_to_aos_k(const void *dev, double *stage, int nsites, int nrhs, int col)
+{
+  const size_t total = (size_t)nsites*nrhs;
+  for(size_t s = (size_t)blockIdx.x*blockDim.x + threadIdx.x; s < (size_t)nsites;
+      s += (size_t)gridDim.x*blockDim.x) {
+    Cx<double> v[3];
+    SpinorIO<QLLG_F64,3>::load(dev, total, s*nrhs + col, v);
+#pragma unroll
+    for(int c=0; c<3; c++) { stage[6*s + 2*c] = v[c].r; stage[6*s + 2*c + 1] = v[c].i; }
+  }
+}
+
+// a chunk of a graph-captured solver loop: at most n more trips
+__global__ void chunk_limit_k(int *loops, int *limit, int n)
+{
+  if(threadIdx.x == 0 && blockIdx.x == 0) *limit = *loops + n;
+}
+
 template <int PO, int PI, int NC>
 __global__ void convert_k(void *out, const void *in, int nsites, int nrhs, const int *active)
 {
@@ -265,7 +298,7 @@ __global__ void __launch_bounds__(kT) cg_xr_k(void *x, void *r, const void *p, c
   size_t total = (size_t)nsites*NR;
   const int rhs = threadIdx.x % NR;
   const bool skip = *(volatile int *)&s->done;
-  double red[1] = {0};
+  Acc<T> acc;
   if(!skip && s->active[rhs]) {
     const T alpha = (T)(1.0/(s->mass2[rhs]*s->pnorm[rhs] + s->vnorm[rhs]));
     GRID_LOOP(t, total) {
@@ -278,13 +311,14 @@ __global__ void __launch_bounds__(kT) cg_xr_k(void *x, void *r, const void *p, c
       for(int c=0; c<NC; c++) {
         xv[c].r = fma(alpha, pv[c].r, xv[c].r); xv[c].i = fma(alpha, pv[c].i, xv[c].i);
         rv[c].r = fma(-alpha, av[c].r, rv[c].r); rv[c].i = fma(-alpha, av[c].i, rv[c].i);
-        red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
       }
+      acc.norm(rv);
       SpinorIO<P,NC>::store(x, total, t, xv);
       SpinorIO<P,NC>::store(r, total, t, rv);
     }
   }
   if(skip) return;   // uniform over the grid
+  double red[1] = {acc.get()};
   double *res[1] = {s->tmp};
   if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
     __syncthreads();
@@ -332,7 +366,7 @@ cg_p_norm_k(void *p, const void *r, int nsites, qllg_cg_scalars *s, double *part
   size_t total = (size_t)nsites*NR;
   const int rhs = threadIdx.x % NR;
   if(*(volatile int *)&s->done) return;        // uniform
-  double red[1] = {0};
+  Acc<T> acc;
   if(s->active[rhs]) {
     const T beta = (T)(1.0/s->rsq[rhs]);
     GRID_LOOP(t, total) {
@@ -344,10 +378,10 @@ cg_p_norm_k(void *p, const void *r, int nsites, qllg_cg_scalars *s, double *part
         pv[c].r = fma(beta, rv[c].r, pv[c].r); pv[c].i = fma(beta, rv[c].i, pv[c].i);
       }
       SpinorIO<P,3>::store(p, total, t, pv);
-#pragma unroll
-      for(int c=0; c<3; c++) red[0] += (double)pv[c].r*pv[c].r + (double)pv[c].i*pv[c].i;
+      acc.norm(pv);
     }
   }
+  double red[1] = {acc.get()};
   double *res[1] = {s->pnorm};
   grid_reduce<1>(red, NR, rhs, partial, counter, shm, res);
 }
@@ -404,6 +438,29 @@ qllg_k_spinor_to_aos(int prec, const void *dev, void *stage, int dbl, int nsites
     else to_aos<P,NC,float><<<g,kT,0,st>>>(dev, (float *)stage, nsites, nrhs, rs);
   });
   return done("to_aos");
+}
+
+extern "C" int
+qllg_k_column_from_aos(void *dev, const double *stage, int nsites, int nrhs, int col)
+{
+  column_from_aos_k<<<grid_for((size_t)nsites, 0, 0), kT, 0, qllg_stream()>>>(dev, stage, nsites,
+                                                                              nrhs, col);
+  return done("column_from_aos");
+}
+
+extern "C" int
+qllg_k_column_to_aos(const void *dev, double *stage, int nsites, int nrhs, int col)
+{
+  column_to_aos_k<<<grid_for((size_t)nsites, 0, 0), kT, 0, qllg_stream()>>>(dev, stage, nsites,
+                                                                            nrhs, col);
+  return done("column_to_aos");
+}
+
+extern "C" int
+qllg_k_chunk_limit(int *loops, int *limit, int n)
+{
+  chunk_limit_k<<<1, 32, 0, qllg_stream()>>>(loops, limit, n);
+  return done("chunk_limit");
 }
 
 extern "C" int

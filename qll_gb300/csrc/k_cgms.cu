@@ -63,7 +63,7 @@ cgms_xr_k(void *out, void *r, const void *ps, const void *Ap, int nsites, size_t
   __syncthreads();
   const T t0 = -(T)(s->b[0]*s->s[0]);
   const size_t total = (size_t)nsites;
-  double red[1] = {0};
+  Acc<T> acc;
   GRID_LOOP(t, total) {
     Cx<T> pv[3], ov[3];
     for(int i=0; i<n; i++) {
@@ -81,10 +81,11 @@ cgms_xr_k(void *out, void *r, const void *ps, const void *Ap, int nsites, size_t
 #pragma unroll
     for(int c=0; c<3; c++) {
       rv[c].r = fma(t0, av[c].r, rv[c].r); rv[c].i = fma(t0, av[c].i, rv[c].i);
-      red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
     }
+    acc.norm(rv);
     SpinorIO<P,3>::store(r, total, t, rv);
   }
+  double red[1] = {acc.get()};
   double rsq = 0;
   double *res[1] = {&s->pkp};   // scratch slot for the sum
   if(grid_reduce<1>(red, 1, 0, partial, counter, shm, res)) {

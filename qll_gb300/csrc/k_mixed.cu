@@ -68,6 +68,57 @@ mcg_init_k(void *x64, void *r64, void *xs, void *rs, void *p, const void *b, int
   }
 }
 
+// admit right-hand sides into columns of a running batch (continuous
+// batching): the admitted columns get x64 = xs = p = 0, r64 = rs = b and
+// fresh scalars; every other column, and its scalars, is left as it is.
+// A column's arithmetic never involves another column, so a request gives
+// the same result whichever columns run beside it.
+template <int PS, int NR>
+__global__ void __launch_bounds__(kT)
+mcg_admit_k(void *x64, void *r64, void *xs, void *rs, void *p, const void *b, int nsites,
+            qllg_cg_scalars *s, qllg_admit_args ad, double *partial, unsigned *counter)
+{
+  __shared__ double shm[kT];
+  size_t total = (size_t)nsites*NR;
+  const int rhs = threadIdx.x % NR;
+  double red[1] = {0};
+  if(ad.mask[rhs]) {
+    GRID_LOOP(t, total) {
+      Cx<double> v[3], z[3];
+      SpinorIO<QLLG_F64,3>::load(b, total, t, v);
+#pragma unroll
+      for(int c=0; c<3; c++) { z[c].r = 0; z[c].i = 0; red[0] += v[c].r*v[c].r + v[c].i*v[c].i; }
+      SpinorIO<QLLG_F64,3>::store(r64, total, t, v);
+      SpinorIO<QLLG_F64,3>::store(x64, total, t, z);
+      Cx<float> vf[3], zf[3];
+#pragma unroll
+      for(int c=0; c<3; c++) { vf[c].r = (float)v[c].r; vf[c].i = (float)v[c].i; zf[c].r = 0; zf[c].i = 0; }
+      SpinorIO<VecPrec<PS>::value,3>::store(rs, total, t, vf);
+      SpinorIO<QLLG_F32,3>::store(xs, total, t, zf);
+      SpinorIO<PS,3>::store(p, total, t, zf);
+    }
+  }
+  double *res[1] = {s->tmp};
+  if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int any = 0;
+      for(int q=0; q<NR; q++) {
+        if(ad.mask[q]) {
+          double bs = s->tmp[q];
+          s->bsq[q] = bs; s->rsq[q] = bs; s->maxr2[q] = bs; s->prev[q] = bs;
+          s->rsq_stop[q] = ad.tol2[q]*bs;
+          s->mass2[q] = ad.mass2[q];
+          s->iters[q] = 0; s->ru[q] = 0; s->nru[q] = 0;
+          s->active[q] = (bs > 0 && s->maxits > 0) ? 1 : 0;
+        }
+        any |= s->active[q];
+      }
+      s->done = !any;
+    }
+  }
+}
+
 template <int PS, int NR>
 __global__ void mcg_p_k(void *p, const void *rs, int nsites, qllg_cg_scalars *s)
 {
@@ -95,7 +146,7 @@ mcg_update_k(void *xs, void *rs, const void *p, const void *Ap, int nsites,
   const int rhs = threadIdx.x % NR;
   const bool skip = *(volatile int *)&s->done;
   if(skip) return;
-  double red[1] = {0};
+  Acc<float> acc;
   if(s->active[rhs]) {
     const float alpha = (float)(1.0/(s->mass2[rhs]*s->pnorm[rhs] + s->vnorm[rhs]));
     GRID_LOOP(t, total) {
@@ -108,12 +159,13 @@ mcg_update_k(void *xs, void *rs, const void *p, const void *Ap, int nsites,
       for(int c=0; c<3; c++) {
         xv[c].r = fmaf(alpha, pv[c].r, xv[c].r); xv[c].i = fmaf(alpha, pv[c].i, xv[c].i);
         rv[c].r = fmaf(-alpha, av[c].r, rv[c].r); rv[c].i = fmaf(-alpha, av[c].i, rv[c].i);
-        red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
       }
+      acc.norm(rv);
       SpinorIO<PX,3>::store(xs, total, t, xv);
       SpinorIO<PS,3>::store(rs, total, t, rv);
     }
   }
+  double red[1] = {acc.get()};
   double *res[1] = {s->tmp};
   if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
     __syncthreads();
@@ -215,19 +267,23 @@ mcg_orth_dot_k(const void *p, const void *rs, int nsites, qllg_cg_scalars *s,
   size_t total = (size_t)nsites*NR;
   const int rhs = threadIdx.x % NR;
   if(*(volatile int *)&s->no_ru) return;
-  double red[2] = {0, 0};
+  Acc<float> acc0, acc1;
   if(s->ru[rhs]) {
     GRID_LOOP(t, total) {
       Cx<float> pv[3], rv[3];
       SpinorIO<PS,3>::load(p, total, t, pv);
       SpinorIO<VecPrec<PS>::value,3>::load(rs, total, t, rv);
+      float re = 0, im = 0;
 #pragma unroll
       for(int c=0; c<3; c++) {
-        red[0] += (double)rv[c].r*pv[c].r + (double)rv[c].i*pv[c].i;
-        red[1] += (double)rv[c].r*pv[c].i - (double)rv[c].i*pv[c].r;
+        re = fmaf(rv[c].r, pv[c].r, re); re = fmaf(rv[c].i, pv[c].i, re);
+        im = fmaf(rv[c].r, pv[c].i, im); im = fmaf(-rv[c].i, pv[c].r, im);
       }
+      acc0.add(re);
+      acc1.add(im);
     }
   }
+  double red[2] = {acc0.get(), acc1.get()};
   double *res[2] = {s->orth_re, s->orth_im};
   if(grid_reduce<2>(red, NR, rhs, partial, counter, shm, res)) {
     __syncthreads();
@@ -307,6 +363,23 @@ qllg_k_mcg_init(int px, int ps, void *x64, void *r64, void *xs, void *rs, void *
   PXS_SWITCH(px, ps, NR_SWITCH(nrhs, (mcg_init_k<PX,PS,NR><<<g,kT,0,st>>>(x64, r64, xs, rs, p, b,
                                       nsites, s, rb->partial, rb->counter))));
   return done("mcg_init");
+}
+
+extern "C" int
+qllg_k_mcg_admit(int ps, void *x64, void *r64, void *xs, void *rs, void *p, const void *b,
+                 int nsites, int nrhs, qllg_cg_scalars *s, const qllg_admit_args *ad,
+                 qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  if(ps == QLLG_F32) {
+    NR_SWITCH(nrhs, (mcg_admit_k<QLLG_F32,NR><<<g,kT,0,st>>>(x64, r64, xs, rs, p, b, nsites, s, *ad,
+                                                           rb->partial, rb->counter)));
+  } else if(ps == QLLG_I16) {
+    NR_SWITCH(nrhs, (mcg_admit_k<QLLG_I16,NR><<<g,kT,0,st>>>(x64, r64, xs, rs, p, b, nsites, s, *ad,
+                                                           rb->partial, rb->counter)));
+  } else { qllg_set_error("mcg_admit: precision %d", ps); return -1; }
+  return done("mcg_admit");
 }
 
 extern "C" int
@@ -414,7 +487,7 @@ scg_xr_k(void *x, void *r, const void *p, const void *Ap, int nsites, qllg_cg_sc
   size_t total = (size_t)nsites*NR;
   const int rhs = threadIdx.x % NR;
   if(*(volatile int *)&s->done) return;
-  double red[1] = {0};
+  Acc<T> acc;
   if(s->active[rhs]) {
     const T alpha = (T)(s->rsq[rhs]/s->pnorm[rhs]);
     GRID_LOOP(t, total) {
@@ -427,12 +500,13 @@ scg_xr_k(void *x, void *r, const void *p, const void *Ap, int nsites, qllg_cg_sc
       for(int c=0; c<NC; c++) {
         xv[c].r = fma(alpha, pv[c].r, xv[c].r); xv[c].i = fma(alpha, pv[c].i, xv[c].i);
         rv[c].r = fma(-alpha, av[c].r, rv[c].r); rv[c].i = fma(-alpha, av[c].i, rv[c].i);
-        red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
       }
+      acc.norm(rv);
       SpinorIO<PX,NC>::store(x, total, t, xv);
       SpinorIO<PS,NC>::store(r, total, t, rv);
     }
   }
+  double red[1] = {acc.get()};
   double *res[1] = {s->tmp};
   if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
     __syncthreads();

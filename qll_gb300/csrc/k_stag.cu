@@ -30,7 +30,7 @@ stag_dslash(qllg_stag_args a)
   const int p = a.out_parity;
   const size_t loff = p ? (size_t)G.Vh : 0;
   const bool skip = a.done && *(volatile const int *)a.done;
-  double red[2] = {0.0, 0.0};
+  Acc<T> acc0, acc1;
   const int rhs = threadIdx.x % NR;
   const bool act = !a.active || a.active[rhs];
   const T ca = (T)(a.a ? a.a[rhs] : a.a0);
@@ -86,8 +86,8 @@ stag_dslash(qllg_stag_args a)
           T apr = fma(cb, acc[c].r, ca*self[c].r), api = fma(cb, acc[c].i, ca*self[c].i);
           xv[c].r = fma(alpha, self[c].r, xv[c].r); xv[c].i = fma(alpha, self[c].i, xv[c].i);
           rv[c].r = fma(-alpha, apr, rv[c].r); rv[c].i = fma(-alpha, api, rv[c].i);
-          red[0] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
         }
+        acc0.norm(rv);
         SpinorIO<PX,3>::store(a.x, total, t, xv);
         SpinorIO<PX,3>::store(a.r, total, t, rv);
         continue;
@@ -104,16 +104,11 @@ stag_dslash(qllg_stag_args a)
         for(int c=0; c<3; c++) out[c] = acc[c];
       }
       SpinorIO<PS,3>::store(a.out, total, t, out);
-      if(a.norm_out) {
-#pragma unroll
-        for(int c=0; c<3; c++) red[0] += (double)out[c].r*out[c].r + (double)out[c].i*out[c].i;
-      }
-      if(a.norm_self && a.self) {
-#pragma unroll
-        for(int c=0; c<3; c++) red[1] += (double)self[c].r*self[c].r + (double)self[c].i*self[c].i;
-      }
+      if(a.norm_out) acc0.norm(out);
+      if(a.norm_self && a.self) acc1.norm(self);
     }
   }
+  double red[2] = {acc0.get(), acc1.get()};
   if(a.mode == 3) {
     if(skip) return;   // uniform: the flag was set before this launch
     double *res[2] = {a.sc->tmp, NULL};
@@ -165,9 +160,7 @@ stag_dslash_mr(qllg_stag_args a)
     alpha[j] = (a.mode == 3 && act[j])
       ? (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs])) : (T)0;
   }
-  double red[2][R];
-#pragma unroll
-  for(int j=0; j<R; j++) { red[0][j] = 0; red[1][j] = 0; }
+  Acc<T> acc0[R], acc1[R];
   if(!skip && anyact) {
     for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < nwork;
         w += (size_t)gridDim.x*blockDim.x) {
@@ -257,8 +250,8 @@ stag_dslash_mr(qllg_stag_args a)
                   xv[jj][c].i = fma(alpha[j], sv[jj][c].i, xv[jj][c].i);
                   rv[jj][c].r = fma(-alpha[j], apr, rv[jj][c].r);
                   rv[jj][c].i = fma(-alpha[j], api, rv[jj][c].i);
-                  red[0][j] += (double)rv[jj][c].r*rv[jj][c].r + (double)rv[jj][c].i*rv[jj][c].i;
                 }
+                acc0[j].norm(rv[jj]);
               }
               Spinor4<PX>::store_half(a.x, total, t0, h, xv);
               Spinor4<PX>::store_half(a.r, total, t0, h, rv);
@@ -277,11 +270,9 @@ stag_dslash_mr(qllg_stag_args a)
                 } else {
                   ov[jj][c] = acc[j][c];
                 }
-                if(a.norm_out)
-                  red[0][j] += (double)ov[jj][c].r*ov[jj][c].r + (double)ov[jj][c].i*ov[jj][c].i;
-                if(a.norm_self && a.self)
-                  red[1][j] += (double)sv[jj][c].r*sv[jj][c].r + (double)sv[jj][c].i*sv[jj][c].i;
               }
+              if(a.norm_out) acc0[j].norm(ov[jj]);
+              if(a.norm_self && a.self) acc1[j].norm(sv[jj]);
             }
             Spinor4<PS>::store_half(a.out, total, t0, h, ov);
           }
@@ -303,8 +294,8 @@ stag_dslash_mr(qllg_stag_args a)
             T apr = fma(cb, acc[j][c].r, ca[j]*self[c].r), api = fma(cb, acc[j][c].i, ca[j]*self[c].i);
             xv[c].r = fma(alpha[j], self[c].r, xv[c].r); xv[c].i = fma(alpha[j], self[c].i, xv[c].i);
             rv[c].r = fma(-alpha[j], apr, rv[c].r); rv[c].i = fma(-alpha[j], api, rv[c].i);
-            red[0][j] += (double)rv[c].r*rv[c].r + (double)rv[c].i*rv[c].i;
           }
+          acc0[j].norm(rv);
           SpinorIO<PX,3>::store(a.x, total, t, xv);
           SpinorIO<PX,3>::store(a.r, total, t, rv);
           continue;
@@ -322,17 +313,14 @@ stag_dslash_mr(qllg_stag_args a)
           for(int c=0; c<3; c++) out[c] = acc[j][c];
         }
         SpinorIO<PS,3>::store(a.out, total, t, out);
-        if(a.norm_out) {
-#pragma unroll
-          for(int c=0; c<3; c++) red[0][j] += (double)out[c].r*out[c].r + (double)out[c].i*out[c].i;
-        }
-        if(a.norm_self && a.self) {
-#pragma unroll
-          for(int c=0; c<3; c++) red[1][j] += (double)self[c].r*self[c].r + (double)self[c].i*self[c].i;
-        }
+        if(a.norm_out) acc0[j].norm(out);
+        if(a.norm_self && a.self) acc1[j].norm(self);
       }
     }
   }
+  double red[2][R];
+#pragma unroll
+  for(int j=0; j<R; j++) { red[0][j] = acc0[j].get(); red[1][j] = acc1[j].get(); }
   if(a.mode == 3) {
     if(skip) return;
     double *res[2] = {a.sc->tmp, NULL};

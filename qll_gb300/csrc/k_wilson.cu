@@ -50,7 +50,7 @@ wilson_dslash(qllg_stag_args a)
   const int p = a.out_parity;
   const size_t loff = p ? (size_t)G.Vh : 0;
   const bool skip = a.done && *(volatile const int *)a.done;
-  double red[2] = {0.0, 0.0};
+  Acc<T> acc0, acc1;
   const int rhs = threadIdx.x % NR;
   const bool act = !a.active || a.active[rhs];
   const T ca = (T)(a.a ? a.a[rhs] : a.a0);
@@ -121,16 +121,11 @@ wilson_dslash(qllg_stag_args a)
         } else out[c] = acc[c];
       }
       SpinorIO<PS,12>::store(a.out, total, t, out);
-      if(a.norm_out) {
-#pragma unroll
-        for(int c=0; c<12; c++) red[0] += (double)out[c].r*out[c].r + (double)out[c].i*out[c].i;
-      }
-      if(a.norm_self && a.self) {
-#pragma unroll
-        for(int c=0; c<12; c++) red[1] += (double)self[c].r*self[c].r + (double)self[c].i*self[c].i;
-      }
+      if(a.norm_out) acc0.norm(out);
+      if(a.norm_self && a.self) acc1.norm(self);
     }
   }
+  double red[2] = {acc0.get(), acc1.get()};
   if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
     grid_reduce<2>(red, NR, rhs, a.partial, a.counter, shm, res);

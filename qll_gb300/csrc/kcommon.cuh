@@ -229,6 +229,41 @@ template <> struct LinkIO<QLLG_I16> {
   }
 };
 
+// ------------------------------------------------- per-thread accumulators
+// Sums of squares and dot products that a thread accumulates before the
+// block/grid tree (which is FP64).  FP64 data accumulate in FP64.  FP32
+// data accumulate in FP32 with Kahan compensation, one compensated add per
+// (site, rhs): the FP64 pipe of this part runs at a small fraction of the
+// FP32 rate, and converting every product to double made the norms of the
+// FP32 kernels FP64-bound.  The compensated sum keeps the thread's partial
+// to about one FP32 rounding of the total.
+template <typename T> struct Acc;
+template <> struct Acc<double> {
+  double s = 0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  template <int N> __device__ __forceinline__ void norm(const Cx<double> (&v)[N]) {
+#pragma unroll
+    for(int c=0; c<N; c++) s += v[c].r*v[c].r + v[c].i*v[c].i;
+  }
+  __device__ __forceinline__ double get() const { return s; }
+};
+template <> struct Acc<float> {
+  float s = 0, e = 0;
+  __device__ __forceinline__ void add(float x) {
+    float y = x - e;
+    float t = s + y;
+    e = (t - s) - y;
+    s = t;
+  }
+  template <int N> __device__ __forceinline__ void norm(const Cx<float> (&v)[N]) {
+    float q = 0;
+#pragma unroll
+    for(int c=0; c<N; c++) { q = fmaf(v[c].r, v[c].r, q); q = fmaf(v[c].i, v[c].i, q); }
+    add(q);
+  }
+  __device__ __forceinline__ double get() const { return (double)s - (double)e; }
+};
+
 // ------------------------------------------------------------ reductions
 // Block partial sums per rhs, then the last block to finish folds the
 // partials of all blocks in a fixed order, so results are bitwise

@@ -190,6 +190,34 @@ typedef struct qllg_cg_scalars_s {
 int qllg_k_mcg_init(int px, int ps, void *x64, void *r64, void *xs, void *rs, void *p,
                     const void *b, int nsites, int nrhs, qllg_cg_scalars *s,
                     qllg_redbuf *rb);
+/* continuous batching on an operator (stag.c): a fixed-width FP32 mixed
+ * CG whose columns are admitted and retired between chunks */
+struct qllg_stag;
+struct qllg_stag *qllg_stag_share(struct qllg_stag *S);
+size_t qllg_batch_bytes(const struct qllg_stag *S);
+int qllg_batch_init(struct qllg_stag *S, int maxits);
+int qllg_batch_admit(struct qllg_stag *S, int ncol, const int cols[], const double mass[],
+                     const double tol[], const double *const src[]);
+int qllg_batch_launch(struct qllg_stag *S, int iters);
+int qllg_batch_poll(struct qllg_stag *S);
+int qllg_batch_retire(struct qllg_stag *S, int col, double *out);
+const qllg_cg_scalars *qllg_batch_scalars(const struct qllg_stag *S);
+/* admission of right-hand sides into columns of a running mixed batch */
+typedef struct {
+  int mask[QLLG_MAXRHS];        /* columns admitted now */
+  double mass2[QLLG_MAXRHS];    /* their m^2 */
+  double tol2[QLLG_MAXRHS];     /* their stopping |r|^2/|b|^2 */
+} qllg_admit_args;
+int qllg_k_mcg_admit(int ps, void *x64, void *r64, void *xs, void *rs, void *p, const void *b,
+                     int nsites, int nrhs, qllg_cg_scalars *s, const qllg_admit_args *ad,
+                     qllg_redbuf *rb);
+/* one column of an FP64 [3][nsites][nrhs] device vector <-> a contiguous
+ * [nsites][6] device array */
+int qllg_k_column_from_aos(void *dev, const double *stage, int nsites, int nrhs, int col);
+int qllg_k_column_to_aos(const void *dev, double *stage, int nsites, int nrhs, int col);
+/* *limit = *loops + n on the stream (the next graph launch runs at most n
+ * more trips) */
+int qllg_k_chunk_limit(int *loops, int *limit, int n);
 /* sloppy step: xs += a p, rs -= a Ap, |rs|^2; flags rhs for a reliable
  * update when |rs|^2 < delta2*maxr2, when |rs|^2 < rsq_stop, or at maxits */
 int qllg_k_mcg_update(int px, int ps, void *xs, void *rs, const void *p, const void *Ap,

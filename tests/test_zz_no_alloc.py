@@ -5,9 +5,10 @@ same inputs.
 
 Tolerances: the output is produced by the same kernel instantiation as the
 allocating call, so it must be bit-identical; the per-rhs norms must match
-|out|^2 recomputed here in float64 to 1e-12 relative for FP64/FP32 spinors,
-and to 2e-4 for the 16-bit layout (the kernel sums the values before they
-are rounded to 16 bits).  Two calls in a row are checked, so a counter or
+|out|^2 recomputed here in float64 to 1e-12 relative for FP64 spinors, to
+1e-6 for FP32 spinors (each thread sums its squares in FP32 with Kahan
+compensation before the FP64 grid reduction) and to 2e-4 for the 16-bit
+layout (the kernel sums the values before they are rounded to 16 bits).  Two calls in a row are checked, so a counter or
 partial left over by the first call would show in the second.
 
 The file sorts last so it runs after every other test; it also passes
@@ -82,7 +83,7 @@ def _norm2(out, prec, nrhs):
 @pytest.mark.parametrize("nrhs", [1, 4, 16])
 def test_noalloc_matches_dslash_device(op, prec, nrhs):
     L, S = op
-    tol = 2e-4 if prec == 2 else 1e-12
+    tol = {0: 1e-12, 1: 1e-6, 2: 2e-4}[prec]
     for parity in (0, 1):
         src = _input(L, S, prec, nrhs, 17 + 3*prec + nrhs + parity)
         ref = torch.zeros_like(src)
@@ -134,7 +135,7 @@ def test_noalloc_with_the_grid_at_its_block_cap():
                                                         VP(nrm.data_ptr())) == 0, qll.last_error()
                 torch.cuda.synchronize()
                 assert torch.equal(out.view(torch.uint8), ref.view(torch.uint8))
-                assert abs(nrm.item() - want.item())/want.item() < 1e-12
+                assert abs(nrm.item() - want.item())/want.item() < (1e-12 if prec == 0 else 1e-6)
     finally:
         L.qllg_stag_destroy(S)
 
