@@ -297,10 +297,91 @@ def run_gpu(args):
     L.qllg_stag_vec_free(b1)
     L.qllg_stag_vec_free(x1)
     L.qllg_stag_destroy(S)
+    if rank == 0 and not args.no_serve:
+        ts = time.time()
+        out["serving"] = run_serving(args)
+        log("serving %.1fs" % (time.time() - ts))
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------- serving
+SERVE_LATTICES = [(16, 16, 16, 16), (24, 24, 24, 48), (32, 32, 32, 64)]
+SERVE_SEEDS = [5001, 5002, 5003]
+SERVE_EPS = [0.3, 0.3, 0.4]
+
+
+def run_serving(args):
+    """the request loop on the three resident lattices: the capacity with
+    every request queued at once, then Poisson arrivals at 70% of it
+    (seed 7): p50/p99 latency and solves/s; beside it the same kind of
+    requests solved one shift at a time by the plain FP64 single-rhs CG"""
+    from qll_gb300 import qll, serve
+    L = serve._lib()
+    ops = [serve.asqtad_operator(d, s, e) for d, s, e in zip(SERVE_LATTICES, SERVE_SEEDS, SERVE_EPS)]
+
+    def server():
+        V = serve.Server(int(args.serve_budget*(1 << 30)), chunk=args.serve_chunk, max_batches=2)
+        for S, d in zip(ops, SERVE_LATTICES):
+            V.add_lattice(S, d)
+        return V
+
+    # capacity: all requests queued at t = 0
+    V = server()
+    recs, t_sat = serve.poisson_load(V, SERVE_LATTICES, rate=1e9, nreq=args.serve_requests//2,
+                                     seed=11)
+    cap = len(recs)/t_sat
+    V.close()
+    # Poisson arrivals at 70% of the capacity
+    rate = 0.7*cap
+    V = server()
+    recs, t_run = serve.poisson_load(V, SERVE_LATTICES, rate=rate, nreq=args.serve_requests, seed=7)
+    st = V.stats()
+    V.close()
+    lat = np.array([r["latency_s"] for r in recs])
+    cols = sum(r["nshift"] for r in recs)
+    worst = max(r["max_true_rsq_over_tol2"] for r in recs)
+
+    # serial plain FP64 baseline on a sample: one request per lattice, each
+    # shift a separate single-rhs FP64 CG
+    info = qll.SolveInfo()
+    rng = np.random.default_rng(7)
+    t_serial, n_serial = 0.0, 0
+    for li, (S, d) in enumerate(zip(ops, SERVE_LATTICES)):
+        m = float(rng.uniform(0.005, 0.1))
+        ns = int(rng.integers(1, 17))
+        shifts = list(np.logspace(-4, 0, ns)) if ns > 1 else [1e-4]
+        b = qll.gen_source(d, 6000 + 100*li, 6, "even")
+        x = np.zeros_like(b)
+        t = time.time()
+        for sh in shifts:
+            ms = (ctypes.c_double*1)(float(np.sqrt(m*m + sh)))
+            if L.qllg_stag_solve(S, 1, qll.vp_array([x]), qll.vp_array([b]), ms, 1e-16, MAXITS,
+                                 qll.SOLVE_DOUBLE, ctypes.byref(info)) < 0:
+                raise RuntimeError(qll.last_error())
+        t_serial += time.time() - t
+        n_serial += 1
+    for S in ops:
+        L.qllg_stag_destroy(S)
+    return {
+        "workload": "C5: 16^4 + 24^3x48 + 32^3x64 resident; Poisson arrivals (seed 7) at 70% "
+                    "of the measured capacity; per request m~U[0.005,0.1], 1-16 shifts "
+                    "log-spaced in [1e-4,1], tolerance 1e-8 or 1e-10",
+        "requests": len(recs), "shift_solves": cols, "seconds": t_run,
+        "requests_per_s": len(recs)/t_run, "shift_solves_per_s": cols/t_run,
+        "capacity_requests_per_s": cap, "arrival_rate_per_s": rate,
+        "latency_p50_s": float(np.percentile(lat, 50)),
+        "latency_p99_s": float(np.percentile(lat, 99)),
+        "latency_max_s": float(lat.max()),
+        "max_true_rsq_over_tol2": worst,
+        "hbm_budget_bytes": st.budget_bytes, "hbm_used_bytes_end": st.used_bytes,
+        "chunk_iters": args.serve_chunk,
+        "serial_fp64_baseline": {"requests_per_s": n_serial/t_serial, "sample": "%d requests, "
+                                 "one per lattice, each shift a separate FP64 single-rhs CG"
+                                 % n_serial},
+    }
 
 
 # ---------------------------------------------------------- CPU baseline
@@ -517,11 +598,18 @@ def main():
     ap.add_argument("--mode", default="mixed_single",
                     choices=["double", "single", "mixed_half", "mixed_single"])
     ap.add_argument("--param", action="append", default=[])
+    ap.add_argument("--serve", action="store_true", help="only the serving benchmark")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=36)
+    ap.add_argument("--serve-budget", type=float, default=48.0, help="GiB")
+    ap.add_argument("--serve-chunk", type=int, default=20)
     args = ap.parse_args()
     if args.dslash_only:
         run_dslash_only(args)
     elif args.solve_only:
         run_solve_only(args)
+    elif args.serve:
+        print(json.dumps({"serving": run_serving(args)}), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

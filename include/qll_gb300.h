@@ -158,6 +158,54 @@ int qllg_wilson_dslash(qllg_wilson *W, void *x, double massp, const void *y, con
 int qllg_wilson_solve(qllg_wilson *W, void *x, const void *b, double mass, double rsq,
                       int maxits, int mode, qllg_solve_info *info);
 
+/* ------------------------------------------------------------ serving */
+/* No counterpart in the reference (its solvers run one call at a time).
+ * A server keeps the links of several lattices resident and runs solve
+ * requests as they arrive, with continuous batching: a request with n
+ * shifts occupies n columns of a 16-column FP32 mixed-precision batch
+ * (FP64 reliable updates; column k solves (m^2 + shift_k - D_eo D_oe) x_k
+ * = b); batches advance in chunks of chunk_iters iterations, and between
+ * two chunks finished columns are retired and queued requests admitted into
+ * free columns while the others continue.  Each batch has its own stream,
+ * so batches overlap on the device.  New batches are created only within
+ * hbm_budget bytes (resident links plus batch workspaces; idle batches are
+ * released when it is short).  A request's solution is bitwise the same
+ * whichever requests run beside it.  One host thread drives a server. */
+typedef struct qllg_server qllg_server;
+
+typedef struct {
+  int status;              /* 0 queued, 1 running, 2 done */
+  int ncol;                /* shifts (columns) of the request */
+  int iters[16];           /* iterations per shift */
+  double true_rsq[16];     /* |b - A x|^2/|b|^2 per shift, FP64 */
+  double seconds_queued;   /* submit -> admission (host clock) */
+  double seconds_total;    /* submit -> solution copied out */
+} qllg_request_info;
+
+typedef struct {
+  size_t budget_bytes, used_bytes;
+  int batches, busy_columns, requests, pending;
+  long long admitted_columns, chunks;
+} qllg_server_info;
+
+qllg_server *qllg_server_create(size_t hbm_budget, int chunk_iters, int max_batches_per_lattice);
+/* a resident operator (not owned; it must outlive the server); returns
+ * the lattice id */
+int qllg_server_add_lattice(qllg_server *V, qllg_stag *S);
+/* src: host [V/2][6] FP64 source on the even sites; out[k]: host [V/2][6]
+ * FP64 solution of shift k (nshift <= 0: one solve at mass), written when
+ * the request completes.  Both must stay valid until then.  Stops at
+ * |b - A x| < tol |b|.  Returns the request id. */
+int qllg_server_submit(qllg_server *V, int lattice, double mass, int nshift, const double *shifts,
+                       double tol, const double *src, double *const out[]);
+/* one scheduling pass (retire, admit, launch); never waits for the GPU.
+ * Returns the number of requests completed in this pass, or -1. */
+int qllg_server_step(qllg_server *V);
+int qllg_server_pending(const qllg_server *V);
+int qllg_server_request(const qllg_server *V, int id, qllg_request_info *info);
+int qllg_server_stats(const qllg_server *V, qllg_server_info *info);
+void qllg_server_destroy(qllg_server *V);
+
 /* solver parameters: "reliable_delta" (0.1, 16-bit mixed mode),
  * "reliable_delta_single" (0.01, FP32 mixed mode), "reortho" (1), "graph" (1),
  * "poll" (8), "dslash_mr" (1: multi-rhs Dslash with 4 rhs per thread),

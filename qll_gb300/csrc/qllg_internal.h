@@ -59,6 +59,7 @@ static inline size_t qllg_link_bytes(int prec) {
 int   qllg_runtime_init(void);                 /* 0 ok */
 cudaStream_t qllg_stream(void);                /* current library stream */
 void  qllg_set_error(const char *fmt, ...);
+cudaStream_t qllg_stream_swap(cudaStream_t s);
 int   qllg_check_cuda(cudaError_t e, const char *what);   /* 0 ok */
 void *qllg_dmalloc(size_t bytes);              /* NULL + error on failure */
 void  qllg_dfree(void *p);

@@ -144,6 +144,17 @@ qllg_set_stream(void *stream)
   return 0;
 }
 
+/* make s the library stream for a while and return the previous one (the
+ * server's batches each run on their own stream); unlike qllg_set_stream
+ * this never destroys the library's own stream */
+cudaStream_t
+qllg_stream_swap(cudaStream_t s)
+{
+  cudaStream_t old = g_stream;
+  g_stream = s;
+  return old;
+}
+
 void *
 qllg_get_stream(void)
 {

@@ -27,6 +27,15 @@ Layout *qllg_current_layout(void);
 enum { WS_X, WS_R, WS_P, WS_AP, WS_V, WS_B, WS_IO, WS_X64, WS_R64, WS_T64, WS_V64,
        WS_PS, WS_OUT, WS_N };
 
+/* what one solver iteration launches */
+typedef struct {
+  int mixed;                 /* 0 plain CG, 1 mixed CG with reliable updates */
+  int ps, pl, nrhs, reortho;
+  void *x, *r, *p, *v;       /* sloppy (or only) vectors */
+  void *x64, *r64, *t64, *w64;
+  const void *b;
+} iter_ctx;
+
 struct qllg_stag {
   qllg_geom g;
   int nslots;
@@ -47,6 +56,13 @@ struct qllg_stag {
     cudaGraphExec_t exec;
   } graphs[6];
   int ngraph_next;
+  unsigned char shared[3]; /* links[p] belong to another operator */
+  /* continuous batching (qllg_batch_*): a fixed-width mixed CG whose
+   * columns are admitted and retired independently */
+  int batch_on;
+  iter_ctx bctx;
+  void *bstage;            /* one column, [Vh][6] FP64, on the device */
+  cudaEvent_t bev;         /* end of the last chunk and its scalar copy */
 };
 
 /* ------------------------------------------------------------ helpers */
@@ -178,12 +194,36 @@ qllg_stag_create_f(const int dims[4], float *const fat[8], float *const lng[8])
   return stag_create(dims, (void *const *)fat, (void *const *)lng, 0);
 }
 
+/* a second operator on the same resident links: its own workspaces,
+ * scalars, reduction buffer and graphs, the links (FP64 and FP32, derived
+ * here if missing) shared with S.  S must outlive it. */
+qllg_stag *
+qllg_stag_share(qllg_stag *S)
+{
+  if(ensure_links(S, QLLG_F64) || ensure_links(S, QLLG_F32)) return NULL;
+  int dims[4] = {S->g.L[0], S->g.L[1], S->g.L[2], S->g.L[3]};
+  qllg_stag *T = qllg_stag_alloc(dims, S->nslots, S->master);
+  if(!T) return NULL;
+  for(int p=0; p<3; p++) {
+    T->links[p] = S->links[p];
+    T->shared[p] = S->links[p] != NULL;
+  }
+  if(qllg_check_cuda(cudaMemcpyAsync(T->lscale, S->lscale, sizeof(float)*16,
+                                     cudaMemcpyDeviceToDevice, qllg_stream()), "share scales")) {
+    qllg_stag_destroy(T);
+    return NULL;
+  }
+  return T;
+}
+
 void
 qllg_stag_destroy(qllg_stag *S)
 {
   if(!S) return;
   qllg_sync();
-  for(int p=0; p<3; p++) qllg_dfree(S->links[p]);
+  for(int p=0; p<3; p++) if(!S->shared[p]) qllg_dfree(S->links[p]);
+  qllg_dfree(S->bstage);
+  if(S->bev) cudaEventDestroy(S->bev);
   qllg_dfree(S->lscale);
   qllg_dfree(S->sc);
   if(S->hsc) cudaFreeHost(S->hsc);
@@ -222,8 +262,10 @@ size_t
 qllg_stag_device_bytes(const qllg_stag *S)
 {
   size_t b = 0;
-  for(int p=0; p<3; p++) if(S->links[p]) b += qllg_link_bytes(p)*(size_t)S->g.V*S->nslots;
+  for(int p=0; p<3; p++)
+    if(S->links[p] && !S->shared[p]) b += qllg_link_bytes(p)*(size_t)S->g.V*S->nslots;
   for(int i=0; i<WS_N; i++) b += S->ws_bytes[i];
+  if(S->bstage) b += 48*(size_t)S->g.Vh;
   return b;
 }
 
@@ -424,15 +466,6 @@ pull_done(qllg_stag *S)
 
 /* ------------------------------------------------ solver loop driver */
 
-/* what one solver iteration launches */
-typedef struct {
-  int mixed;                 /* 0 plain CG, 1 mixed CG with reliable updates */
-  int ps, pl, nrhs, reortho;
-  void *x, *r, *p, *v;       /* sloppy (or only) vectors */
-  void *x64, *r64, *t64, *w64;
-  const void *b;
-} iter_ctx;
-
 static int
 issue_iteration(qllg_stag *S, const iter_ctx *c)
 {
@@ -628,6 +661,144 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
   int its = 0;
   for(int i=0; i<nrhs; i++) if(S->hsc->iters[i] > its) its = S->hsc->iters[i];
   return its;
+}
+
+/* ---------------------------------------------- continuous batching */
+/* A batch is the FP32 mixed CG (FP64 reliable updates) over all
+ * QLLG_MAXRHS columns of the operator's workspaces.  Columns are admitted
+ * (x = 0, r = b, own mass and tolerance) and retired one by one between
+ * chunks; a chunk is one launch of the graph-captured iteration loop with a
+ * trip limit, so the columns already running never stop for an admission.
+ * Everything is asynchronous on the library stream except retire, which
+ * waits for its copy. */
+
+size_t
+qllg_batch_bytes(const qllg_stag *S)
+{
+  const int n = QLLG_MAXRHS;
+  /* rs, p, v, xs in FP32; r64, t64, w64, x64, b in FP64; one column of
+   * staging */
+  return 4*vec_bytes(S, QLLG_F32, n) + 5*vec_bytes(S, QLLG_F64, n) + 48*(size_t)S->g.Vh;
+}
+
+int
+qllg_batch_init(qllg_stag *S, int maxits)
+{
+  const int n = QLLG_MAXRHS;
+  if(ensure_links(S, QLLG_F32) || ensure_links(S, QLLG_F64)) return -1;
+  size_t vx = vec_bytes(S, QLLG_F32, n), v64 = vec_bytes(S, QLLG_F64, n);
+  iter_ctx *c = &S->bctx;
+  memset(c, 0, sizeof(*c));
+  c->mixed = 1;
+  c->ps = c->pl = QLLG_F32;
+  c->nrhs = n;
+  c->reortho = qllg_get_param("reortho") != 0;
+  c->r = ws_get(S, WS_R, vx);
+  c->p = ws_get(S, WS_P, vx);
+  c->v = ws_get(S, WS_V, vx);
+  c->x = ws_get(S, WS_X, vx);
+  c->r64 = ws_get(S, WS_R64, v64);
+  c->t64 = ws_get(S, WS_T64, v64);
+  c->w64 = ws_get(S, WS_V64, v64);
+  c->x64 = ws_get(S, WS_X64, v64);
+  c->b = ws_get(S, WS_B, v64);
+  if(!c->r || !c->p || !c->v || !c->x || !c->r64 || !c->t64 || !c->w64 || !c->x64 || !c->b)
+    return -1;
+  if(!S->bstage && !(S->bstage = qllg_dmalloc(48*(size_t)S->g.Vh))) return -1;
+  if(!S->bev && qllg_check_cuda(cudaEventCreateWithFlags(&S->bev, cudaEventDisableTiming),
+                                "batch event")) return -1;
+  void *zero[] = {c->r, c->p, c->v, c->x};
+  for(int i=0; i<4; i++)
+    if(qllg_check_cuda(cudaMemsetAsync(zero[i], 0, vx, qllg_stream()), "batch clear")) return -1;
+  void *zero64[] = {c->r64, c->t64, c->w64, c->x64, (void *)c->b};
+  for(int i=0; i<5; i++)
+    if(qllg_check_cuda(cudaMemsetAsync(zero64[i], 0, v64, qllg_stream()), "batch clear")) return -1;
+  double delta = qllg_get_param("reliable_delta_single");
+  memset(S->hsc, 0, sizeof(qllg_cg_scalars));
+  S->hsc->maxits = maxits;
+  S->hsc->delta2 = delta*delta;
+  S->hsc->done = 1;
+  S->hsc->no_ru = 1;
+  if(push_scalars(S)) return -1;
+  /* one iteration with every column idle (every launch returns at once)
+   * loads the loop body's kernels before the graph is captured */
+  if(issue_iteration(S, c)) return -1;
+  S->batch_on = 1;
+  return 0;
+}
+
+/* columns cols[i] take right-hand side src[i] (host, [Vh][6] FP64, the
+ * even sites) with mass mass[i] and stopping |r|/|b| < tol[i] */
+int
+qllg_batch_admit(qllg_stag *S, int ncol, const int cols[], const double mass[], const double tol[],
+                 const double *const src[])
+{
+  if(!S->batch_on) { qllg_set_error("batch_admit: batch not initialised"); return -1; }
+  const int Vh = S->g.Vh;
+  iter_ctx *c = &S->bctx;
+  qllg_admit_args ad;
+  memset(&ad, 0, sizeof(ad));
+  for(int i=0; i<ncol; i++) {
+    int col = cols[i];
+    if(col < 0 || col >= QLLG_MAXRHS) { qllg_set_error("batch_admit: column %d", col); return -1; }
+    if(qllg_check_cuda(cudaMemcpyAsync(S->bstage, src[i], 48*(size_t)Vh, cudaMemcpyHostToDevice,
+                                       qllg_stream()), "batch source")) return -1;
+    if(qllg_k_column_from_aos((void *)c->b, S->bstage, Vh, QLLG_MAXRHS, col)) return -1;
+    ad.mask[col] = 1;
+    ad.mass2[col] = mass[i]*mass[i];
+    ad.tol2[col] = tol[i]*tol[i];
+  }
+  return qllg_k_mcg_admit(QLLG_F32, c->x64, c->r64, c->x, c->r, c->p, c->b, Vh, QLLG_MAXRHS, S->sc,
+                          &ad, &S->rb);
+}
+
+/* at most iters more iterations of every running column; then the scalars
+ * are copied back and the chunk's event recorded */
+int
+qllg_batch_launch(qllg_stag *S, int iters)
+{
+  if(!S->batch_on) { qllg_set_error("batch_launch: batch not initialised"); return -1; }
+  if(qllg_k_chunk_limit(&S->sc->loops, &S->sc->loop_limit, iters)) return -1;
+  if(qllg_get_param("graph") != 0 && !qllg_timing_on()) {
+    cudaGraphExec_t exec = loop_graph(S, &S->bctx);
+    if(!exec) return -1;
+    if(qllg_check_cuda(cudaGraphLaunch(exec, qllg_stream()), "batch graph launch")) return -1;
+  } else {
+    for(int i=0; i<iters; i++) if(issue_iteration(S, &S->bctx)) return -1;
+  }
+  if(qllg_check_cuda(cudaMemcpyAsync(S->hsc, S->sc, sizeof(qllg_cg_scalars),
+                                     cudaMemcpyDeviceToHost, qllg_stream()), "batch scalars"))
+    return -1;
+  return qllg_check_cuda(cudaEventRecord(S->bev, qllg_stream()), "batch event");
+}
+
+/* 1 when the last chunk (and its scalar copy) has finished, 0 while it runs */
+int
+qllg_batch_poll(qllg_stag *S)
+{
+  cudaError_t e = cudaEventQuery(S->bev);
+  if(e == cudaSuccess) return 1;
+  if(e == cudaErrorNotReady) return 0;
+  return qllg_check_cuda(e, "batch poll") ? -1 : 0;
+}
+
+/* the scalars as of the last finished chunk (per column: active, iters,
+ * rsq, bsq, nru) */
+const qllg_cg_scalars *
+qllg_batch_scalars(const qllg_stag *S)
+{
+  return S->hsc;
+}
+
+/* copy column col's FP64 solution to out (host, [Vh][6]); waits for it */
+int
+qllg_batch_retire(qllg_stag *S, int col, double *out)
+{
+  const int Vh = S->g.Vh;
+  if(qllg_k_column_to_aos(S->bctx.x64, S->bstage, Vh, QLLG_MAXRHS, col)) return -1;
+  if(qllg_check_cuda(cudaMemcpyAsync(out, S->bstage, 48*(size_t)Vh, cudaMemcpyDeviceToHost,
+                                     qllg_stream()), "batch solution")) return -1;
+  return qllg_check_cuda(cudaStreamSynchronize(qllg_stream()), "batch retire");
 }
 
 static int
