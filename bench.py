@@ -299,12 +299,57 @@ def run_gpu(args):
     L.qllg_stag_destroy(S)
     if rank == 0 and not args.no_serve:
         ts = time.time()
+        out["multishift"] = run_multishift(args)
         out["serving"] = run_serving(args)
-        log("serving %.1fs" % (time.time() - ts))
+        log("multishift and serving %.1fs" % (time.time() - ts))
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------- multishift
+def run_multishift(args):
+    """C3: 24^3x48, m=0.02, 12 shifts log-spaced over 1e-4..1, 8 Gaussian
+    rhs, tolerance 1e-8 on every shift: the mixed multi-rhs solve (every
+    (rhs, shift) pair a column of the 16-wide FP32 mixed CG) against the
+    reference's FP64 multishift CG run rhs after rhs"""
+    from qll_gb300 import qll, serve
+    L = serve._lib()
+    L.qllg_stag_solve_multishift.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    dims, nrhs, mass = (24, 24, 24, 48), 8, 0.02
+    shifts = [10**(-4 + 4*k/11) for k in range(12)]
+    ns = len(shifts)
+    S = serve.asqtad_operator(dims, 1003, 0.3)
+    bs = [qll.gen_source(dims, 2300 + r, 6, "even") for r in range(nrhs)]
+    out = {"workload": "C3: asqtad multishift 24^3x48, m=0.02, eps=0.3, 12 shifts 1e-4..1, "
+                       "8 rhs, tolerance 1e-8 on every shift", "dims": list(dims)}
+    for name, mode in (("mixed", qll.SOLVE_MIXED_SINGLE), ("fp64_cgms", qll.SOLVE_DOUBLE)):
+        xs = [np.zeros_like(bs[0]) for _ in range(nrhs*ns)]
+        its = (ctypes.c_int*(nrhs*ns))()
+        tr = (ctypes.c_double*(nrhs*ns))()
+        reps = 1 if mode == qll.SOLVE_DOUBLE else 2
+        best = None
+        for _ in range(reps):
+            t = time.time()
+            rc = L.qllg_stag_solve_multishift(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), mass, ns,
+                                              (ctypes.c_double*ns)(*shifts), 1e-16, MAXITS, mode,
+                                              its, tr)
+            dt = time.time() - t
+            if rc < 0:
+                raise RuntimeError(qll.last_error())
+            best = dt if best is None else min(best, dt)
+        out[name] = {"seconds": best, "rhs_per_s": nrhs/best, "shift_solves_per_s": nrhs*ns/best,
+                     "max_iters": max(its), "max_true_rsq": max(tr[:]),
+                     "note": ("pairs packed 16 per launch, FP64 reliable updates"
+                              if mode == qll.SOLVE_MIXED_SINGLE else
+                              "reference algorithm (cgmsSolveT) in FP64, one rhs per call")}
+    out["speedup_mixed_over_fp64"] = out["fp64_cgms"]["seconds"]/out["mixed"]["seconds"]
+    L.qllg_stag_destroy(S)
+    return out
 
 
 # ---------------------------------------------------------------- serving
@@ -599,7 +644,8 @@ def main():
                     choices=["double", "single", "mixed_half", "mixed_single"])
     ap.add_argument("--param", action="append", default=[])
     ap.add_argument("--serve", action="store_true", help="only the serving benchmark")
-    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip multishift and serving")
+    ap.add_argument("--multishift", action="store_true", help="only the multishift benchmark")
     ap.add_argument("--serve-requests", type=int, default=36)
     ap.add_argument("--serve-budget", type=float, default=48.0, help="GiB")
     ap.add_argument("--serve-chunk", type=int, default=20)
@@ -610,6 +656,8 @@ def main():
         run_solve_only(args)
     elif args.serve:
         print(json.dumps({"serving": run_serving(args)}), flush=True)
+    elif args.multishift:
+        print(json.dumps({"multishift": run_multishift(args)}), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

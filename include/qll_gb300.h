@@ -92,6 +92,17 @@ int qllg_stag_solve(qllg_stag *S, int nrhs, void *const x[], void *const b[],
 int qllg_stag_solve_device(qllg_stag *S, int nrhs, void *x_dev, const void *b_dev,
                            const double mass[], double rsq, int maxits, int mode,
                            qllg_solve_info *info);
+/* multi-rhs multishift solve (solveMulti2 of lib/stagDslash.c:625-657 for
+ * many rhs): for every rhs r and shift k, (m^2 + shift_k - D_eo D_oe)
+ * x[r*nshift + k] = b[r] on the even sites, each to |r|^2 < rsq |b|^2.
+ * QLLG_SOLVE_DOUBLE runs the reference's FP64 multishift CG per rhs;
+ * QLLG_SOLVE_MIXED_SINGLE runs every (rhs, shift) pair as a column of the
+ * 16-wide FP32 mixed CG with FP64 reliable updates.  Host arrays [V][6]
+ * FP64; iters and true_rsq (FP64 |b - A_k x|^2/|b|^2) per pair, may be
+ * NULL.  Returns the largest iteration count. */
+int qllg_stag_solve_multishift(qllg_stag *S, int nrhs, void *const x[], void *const b[],
+                               double mass, int nshift, const double shifts[], double rsq,
+                               int maxits, int mode, int iters[], double true_rsq[]);
 /* allocate / free a device even-site FP64 vector of nrhs rhs and fill it
  * from host arrays (or copy it back) */
 void *qllg_stag_vec_alloc(qllg_stag *S, int nrhs);

@@ -67,7 +67,7 @@ def build(verbose=False, jobs=None):
         list(ex.map(run, todo))
     if todo or not os.path.exists(LIB):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + [
-            "-Xcompiler", "-fopenmp", "-lcudart", "-lgomp"]
+            "-Xcompiler", "-fopenmp", "-lcudart", "-lgomp", "-lm"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

@@ -12,6 +12,7 @@
  * sides individually, and the host looks at the "done" flag once per batch
  * of iterations, so the iteration count equals the reference's exactly.
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1176,6 +1177,103 @@ cgms_host(qllg_stag *S, void *const x[], const void *y, const double shifts[], i
     if(vec_download(S, prec, oi, 1, xa, dbl)) return -1;
   }
   return its;
+}
+
+/* ------------------------------------------------ multi-rhs multishift */
+/* For every rhs r and shift k: (m^2 + shift_k - D_eo D_oe) x[r*nshift + k]
+ * = b[r] on the even sites, stopping at |r_k|^2 < rsq |b_r|^2.
+ *  - QLLG_SOLVE_DOUBLE: the reference's multishift CG (cgmsSolveT,
+ *    lib/cgms.c:6-179) in FP64, all shifts of one rhs from one Krylov
+ *    space, one rhs after the other (solveMulti2 per rhs);
+ *  - QLLG_SOLVE_MIXED_SINGLE: every (rhs, shift) pair is a column of the
+ *    16-wide FP32 mixed CG with FP64 reliable updates (one multi-rhs Dslash
+ *    launch per half iteration serves 16 pairs, each link loaded once for
+ *    all of them); pairs go in order of shift, so a batch holds pairs of
+ *    similar iteration counts.
+ * Host arrays [V][6] FP64 (the even half is read and written).  iters and
+ * true_rsq (|b - A_k x|^2/|b|^2 in FP64) are per pair, optional. */
+int
+qllg_stag_solve_multishift(qllg_stag *S, int nrhs, void *const x[], void *const b[], double mass,
+                           int nshift, const double shifts[], double rsq, int maxits, int mode,
+                           int iters[], double true_rsq[])
+{
+  if(S->master != QLLG_F64) { qllg_set_error("multishift: needs an FP64 operator"); return -1; }
+  if(nrhs < 1 || nshift < 1 || nshift > QLLG_MAXSHIFT) {
+    qllg_set_error("multishift: %d rhs, %d shifts (1..%d)", nrhs, nshift, QLLG_MAXSHIFT);
+    return -1;
+  }
+  for(int k=0; k<nshift; k++)
+    if(!(mass*mass + shifts[k] > 0)) { qllg_set_error("multishift: shift %d", k); return -1; }
+  if(rsq < 0) rsq = -rsq;
+  const int Vh = S->g.Vh;
+  const size_t vb1 = vec_bytes(S, QLLG_F64, 1);
+  int maxit_seen = 0;
+  if(mode == QLLG_SOLVE_DOUBLE) {
+    /* cgmsSolveT iterates on its first system and takes the others as
+     * offsets from it (shift 0 is the base, lib/cgms.c): the smallest
+     * shift, the slowest system, goes first and the others relative to it */
+    int order[QLLG_MAXSHIFT], kmin = 0;
+    for(int k=1; k<nshift; k++) if(shifts[k] < shifts[kmin]) kmin = k;
+    double rel[QLLG_MAXSHIFT];
+    order[0] = kmin;
+    for(int k=0, j=1; k<nshift; k++) if(k != kmin) order[j++] = k;
+    for(int j=0; j<nshift; j++) rel[j] = shifts[order[j]] - shifts[kmin];
+    const double mass0 = sqrt(mass*mass + shifts[kmin]);
+    void *xs[QLLG_MAXSHIFT];
+    for(int r=0; r<nrhs; r++) {
+      for(int j=0; j<nshift; j++) xs[j] = x[r*nshift + order[j]];
+      int its = cgms_host(S, xs, b[r], rel, nshift, mass0, rsq, maxits, NULL);
+      if(its < 0) return -1;
+      if(its > maxit_seen) maxit_seen = its;
+      /* cgms_host leaves b in WS_B and the n solutions in WS_OUT */
+      for(int j=0; j<nshift; j++) {
+        int k = order[j];
+        if(iters) iters[r*nshift + k] = its;
+        if(!true_rsq) continue;
+        double m2 = mass*mass + shifts[k];
+        if(qllg_h2d(S->sc->mass2, &m2, sizeof(double))) return -1;
+        if(true_residual(S, 1, (char *)S->ws[WS_OUT] + vb1*j, S->ws[WS_B],
+                         &true_rsq[r*nshift + k])) return -1;
+      }
+    }
+    return maxit_seen;
+  }
+  if(mode != QLLG_SOLVE_MIXED_SINGLE) {
+    qllg_set_error("multishift: mode %d (QLLG_SOLVE_DOUBLE or QLLG_SOLVE_MIXED_SINGLE)", mode);
+    return -1;
+  }
+  const int npair = nrhs*nshift;
+  size_t vb = vec_bytes(S, QLLG_F64, QLLG_MAXRHS);
+  void *bd = ws_get(S, WS_B, vb), *xd = ws_get(S, WS_OUT, vb);
+  void *stage = qllg_stage(48*(size_t)Vh);
+  if(!bd || !xd || !stage) return -1;
+  for(int p0=0; p0<npair; p0+=QLLG_MAXRHS) {
+    int n = npair - p0 < QLLG_MAXRHS ? npair - p0 : QLLG_MAXRHS;
+    int nc = pad_nrhs(n);
+    double m[QLLG_MAXRHS], tr[QLLG_MAXRHS];
+    if(qllg_check_cuda(cudaMemsetAsync(bd, 0, vec_bytes(S, QLLG_F64, nc), qllg_stream()),
+                       "multishift clear")) return -1;
+    for(int j=0; j<nc; j++) {
+      int pr = p0 + (j < n ? j : 0), k = pr / nrhs, r = pr % nrhs;
+      m[j] = sqrt(mass*mass + shifts[k]);
+      if(j >= n) continue;            /* padding: b = 0, starts inactive */
+      if(qllg_h2d(stage, b[r], 48*(size_t)Vh) ||
+         qllg_k_column_from_aos(bd, stage, Vh, nc, j)) return -1;
+    }
+    qllg_solve_info info;
+    int its = solve_dev(S, nc, xd, bd, m, rsq, maxits, QLLG_SOLVE_MIXED_SINGLE, &info);
+    if(its < 0) return -1;
+    if(its > maxit_seen) maxit_seen = its;
+    if(true_rsq && true_residual(S, nc, xd, bd, tr)) return -1;
+    for(int j=0; j<n; j++) {
+      int pr = p0 + j, k = pr / nrhs, r = pr % nrhs;
+      if(qllg_k_column_to_aos(xd, stage, Vh, nc, j) ||
+         qllg_d2h(x[r*nshift + k], stage, 48*(size_t)Vh)) return -1;
+      if(iters) iters[r*nshift + k] = info.iters[j];
+      if(true_rsq) true_rsq[r*nshift + k] = tr[j];
+    }
+  }
+  return maxit_seen;
 }
 
 /* createStaggeredLinksFb (lib/stagDslash.c:464-519): only the forward

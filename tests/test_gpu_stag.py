@@ -250,6 +250,39 @@ def test_vectorised_dslash_matches_per_rhs_loads(nrhs):
     L.qllg_stag_destroy(S)
 
 
+@pytest.mark.parametrize("mode", [qll.SOLVE_DOUBLE, qll.SOLVE_MIXED_SINGLE])
+def test_multishift_multi_rhs_matches_oracle(mode):
+    """every (rhs, shift) pair reaches the FP64 true residual and agrees
+    with the oracle's solveMulti2 (FP64 multishift CG) within 10x the
+    tolerance; 4 rhs x 5 shifts = 20 pairs, two batches in the mixed mode"""
+    L, S, u, u3 = _native()
+    L.qllg_stag_solve_multishift.argtypes = [ctypes.c_void_p, c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p, c_double, c_int, ctypes.c_void_p,
+                                             c_double, c_int, c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p]
+    nrhs, mass = 4, 0.05
+    shifts = [1e-2, 1e-4, 1.0, 1e-3, 0.1]       # unsorted, none zero
+    ns = len(shifts)
+    bs = [qll.gen_source(DIMS, 6100 + r, 6, "even") for r in range(nrhs)]
+    xs = [np.zeros_like(bs[0]) for _ in range(nrhs*ns)]
+    its = (c_int*(nrhs*ns))()
+    tr = (c_double*(nrhs*ns))()
+    rc = L.qllg_stag_solve_multishift(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), mass, ns,
+                                      (c_double*ns)(*shifts), 1e-16, 5000, mode, its, tr)
+    assert rc > 0, qll.last_error()
+    Vh = bs[0].shape[0]//2
+    srt = sorted(range(ns), key=lambda k: shifts[k])   # the oracle's base is its first mass
+    for r in range(nrhs):
+        its_o, xo = orc.solve_multi2(DIMS, u, u3, [np.sqrt(mass**2 + shifts[k]) for k in srt],
+                                     bs[r], 1e-16, 5000, noscale=1)
+        for j, k in enumerate(srt):
+            assert tr[r*ns + k] < (1e-16*1.0001 if mode == qll.SOLVE_MIXED_SINGLE else 1e-15), \
+                (r, k, tr[r*ns + k])
+            assert relerr(xs[r*ns + k][:Vh], xo[j][:Vh]) < 1e-7, (r, k)
+            assert np.all(xs[r*ns + k][Vh:] == 0)
+    L.qllg_stag_destroy(S)
+
+
 def test_unknown_parameter_is_refused():
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
