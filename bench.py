@@ -54,6 +54,14 @@ FP64_ITERS_MEASURED = 454
 TRAFFIC_PER_SITE_BYTES = (537.198592e6 + 113.220096e6)/331776
 
 
+def autotune_report(L):
+    """the Dslash variant the autotuner chose per launch shape, with times"""
+    buf = ctypes.create_string_buffer(16384)
+    L.qllg_autotune_report.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.qllg_autotune_report(buf, len(buf))
+    return [ln for ln in buf.value.decode().splitlines() if ln]
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -286,6 +294,7 @@ def run_gpu(args):
                      # 24^3x48 (650 MB), scaled by sites to this lattice
                      "traffic": TRAFFIC_PER_SITE_BYTES*Vh,
                      "traffic_source": "ncu dram__bytes_read+write at 24^3x48, scaled by sites"},
+        "autotune": autotune_report(L),
         "gpu_launches": nlaunch,
         "clocks": clk.summary(local),
         "device_bytes": int(L.qllg_stag_device_bytes(S)),
@@ -299,6 +308,7 @@ def run_gpu(args):
     L.qllg_stag_destroy(S)
     if rank == 0 and not args.no_serve:
         ts = time.time()
+        out["wilson"] = run_wilson(args)
         out["multishift"] = run_multishift(args)
         out["serving"] = run_serving(args)
         log("multishift and serving %.1fs" % (time.time() - ts))
@@ -306,6 +316,91 @@ def run_gpu(args):
         print(json.dumps(out), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------- Wilson
+def site_index(dims, x):
+    """QLL's one-lane site index (layoutIndex): even sites first, each parity
+    lexicographic with x0 fastest, halved"""
+    L0, L1, L2, _ = dims
+    lex = x[0] + L0*(x[1] + L1*(x[2] + L2*x[3]))
+    par = (x[0] + x[1] + x[2] + x[3]) % 2
+    return lex//2 + par*(int(np.prod(dims))//2)
+
+
+def wilson_links_host(dims, seed, eps, c=0.5):
+    """u[2mu] = c U_mu(x), u[2mu+1] = c U_mu(x-mu)^dagger (host [V][18],
+    entry 3*column + row)"""
+    from qll_gb300 import qll
+    V = int(np.prod(dims))
+    th = qll.gen_gauge(tuple(dims), seed, eps, ks=False)
+    x = np.array(np.meshgrid(*[np.arange(n) for n in dims], indexing="ij")).reshape(4, -1)
+    here = site_index(dims, x)
+    u = []
+    for mu in range(4):
+        y = x.copy()
+        y[mu] = (y[mu] - 1) % dims[mu]
+        nb = np.empty(V, dtype=np.int64)
+        nb[here] = site_index(dims, y)
+        m = th[mu].reshape(V, 3, 3, 2)[nb]            # [site, col, row, re/im] at x-mu
+        adj = np.stack([m[..., 0].transpose(0, 2, 1), -m[..., 1].transpose(0, 2, 1)], axis=-1)
+        u += [np.ascontiguousarray(c*th[mu]), np.ascontiguousarray(c*adj.reshape(V, 18))]
+    return u
+
+
+def run_wilson(args):
+    """C2: Wilson even-odd CGNR at 16^3x32, eps=0.3, kappa=0.12 (QLL mass
+    1/(2 kappa) - 4), Gaussian 4x3 source, tolerance 1e-8: FP32 iterations
+    with FP64 reliable updates against the plain FP64 CG"""
+    from qll_gb300 import qll
+    L = qll.load()
+    L.qllg_wilson_create.restype = ctypes.c_void_p
+    L.qllg_wilson_create.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]
+    L.qllg_wilson_solve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p]
+    L.qllg_wilson_destroy.argtypes = [ctypes.c_void_p]
+    dims, kappa = (16, 16, 16, 32), 0.12
+    mass = 1/(2*kappa) - 4
+    u = wilson_links_host(dims, 1002, 0.3)
+    W = ctypes.c_void_p(L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(u)))
+    if not W.value:
+        raise RuntimeError(qll.last_error())
+    b = qll.gen_source(dims, 2200, 24, "even")
+    Vh = b.shape[0]//2
+    out = {"workload": "C2: Wilson e/o CGNR 16^3x32, eps=0.3, kappa=0.12, true residual 1e-8 "
+                       "(normal-equation rsq 1e-17)"}
+    for name, mode in (("mixed", qll.SOLVE_MIXED_SINGLE), ("fp64", qll.SOLVE_DOUBLE)):
+        best = None
+        for rep in range(2):
+            x = np.zeros_like(b)
+            info = qll.SolveInfo()
+            L.qllg_timing_enable(1)
+            L.qllg_timing_reset()
+            t = time.time()
+            # CGNR stops on the normal-equation residual |S^+ r|^2 < rsq |S^+ b|^2;
+            # 1e-17 there puts the true residual |b - S x|/|b| below 1e-8
+            its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, 1e-17, MAXITS, mode,
+                                      ctypes.byref(info))
+            dt = time.time() - t
+            cnt, tot = ctypes.c_int(), ctypes.c_double()
+            L.qllg_timing_read(b"wilson_dslash", ctypes.byref(cnt), ctypes.byref(tot))
+            L.qllg_timing_enable(0)
+            if its < 0:
+                raise RuntimeError(qll.last_error())
+            if best is None or dt < best["seconds"]:
+                best = {"seconds": dt, "solves_per_s": 1/dt, "iters": its,
+                        "true_rsq": info.true_rsq[0], "dslash_launches": cnt.value,
+                        "dslash_avg_ms": tot.value/max(cnt.value, 1)}
+        out[name] = best
+    # Wilson half-Dslash algorithmic bytes per output site (SURVEY 8d): 8 links
+    # + 8 neighbour spinors + 1 store; the mixed solve's launches are mostly FP32
+    f = out["mixed"]
+    f["dslash_note"] = "avg over the solve's FP32 and FP64 half-Dslash launches"
+    out["fp64"]["dslash_gbs"] = (8*18*8 + 9*24*8)*Vh/(out["fp64"]["dslash_avg_ms"]*1e-3)/1e9
+    out["speedup_mixed_over_fp64"] = out["fp64"]["seconds"]/out["mixed"]["seconds"]
+    L.qllg_wilson_destroy(W)
+    return out
 
 
 # ------------------------------------------------------------- multishift
@@ -573,7 +668,7 @@ def run_dslash_only(args):
     ns = 4 if prec == 2 else 0
     per = (8*18*bs + 8*18*bs)/args.nrhs + 17*(6*bs + ns)
     print(json.dumps({"dslash_only": {"dims": dims, "nrhs": args.nrhs, "prec": args.prec,
-                                      "params": args.param,
+                                      "params": args.param, "autotune": autotune_report(L),
                                       "ms": ms, "algorithmic_gbs": per*Vh*args.nrhs/(ms*1e-3)/1e9,
                                       "error": qll.last_error()}}), flush=True)
     L.qllg_stag_destroy(S)
@@ -644,8 +739,10 @@ def main():
                     choices=["double", "single", "mixed_half", "mixed_single"])
     ap.add_argument("--param", action="append", default=[])
     ap.add_argument("--serve", action="store_true", help="only the serving benchmark")
-    ap.add_argument("--no-serve", action="store_true", help="skip multishift and serving")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the Wilson, multishift and serving legs")
     ap.add_argument("--multishift", action="store_true", help="only the multishift benchmark")
+    ap.add_argument("--wilson", action="store_true", help="only the Wilson benchmark")
     ap.add_argument("--serve-requests", type=int, default=36)
     ap.add_argument("--serve-budget", type=float, default=48.0, help="GiB")
     ap.add_argument("--serve-chunk", type=int, default=20)
@@ -658,6 +755,8 @@ def main():
         print(json.dumps({"serving": run_serving(args)}), flush=True)
     elif args.multishift:
         print(json.dumps({"multishift": run_multishift(args)}), flush=True)
+    elif args.wilson:
+        print(json.dumps({"wilson": run_wilson(args)}), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -221,9 +221,15 @@ void qllg_server_destroy(qllg_server *V);
  * "reliable_delta_single" (0.01, FP32 mixed mode), "reortho" (1), "graph" (1),
  * "poll" (8), "dslash_mr" (1: multi-rhs Dslash with 4 rhs per thread),
  * "ru_compact" (1: the FP64 reliable update runs over the flagged rhs
- * only); returns -1 for an unknown name */
+ * only), "dslash_vec4" (1: 16-byte loads of rhs pairs), "autotune" (1:
+ * time the Dslash variants of each new launch shape and keep the fastest);
+ * returns -1 for an unknown name */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);
+
+/* the autotuner's choices so far, one line per launch shape ("key: chosen
+ * | variant time, ..."); returns the number of shapes */
+int qllg_autotune_report(char *buf, size_t len);
 
 /* kernel timing: when enabled, launches of the named kernel family are
  * bracketed by CUDA events on the library stream; read returns the count

@@ -1,436 +1,15 @@
-// k_stag.cu -- asqtad staggered half-Dslash kernels (sm_103a).
-//
-// One thread per (output site, right-hand side), rhs fastest, so the nrhs
-// threads of a site share every link load (a broadcast from L1) while the
-// spinor loads stay coalesced.  Neighbours are computed in-kernel from the
-// even-odd lexicographic site order (periodic in every direction), which
-// replaces the reference's gather tables (lib/shifts.c:516-736) and halo
-// exchange.  The slot order and the per-slot arithmetic follow dslash2T
-// (lib/stagDslash.c:316-328) and PeqM3AtimesV3o (lib/vla0.c.lua:193-213):
-// slot s = 4*mu + 2*backward + naik, acc += U_s(x) psi(x + d_s).
+// k_stag.cu -- dispatch of the asqtad half-Dslash to the per-precision
+// translation units, and the neighbour table the kernels' index arithmetic
+// gives (for the bit-exactness test against the reference's tables).
 #include "kcommon.cuh"
 
 using namespace qk;
 
+extern "C" int qllg_k_stag_dslash_f64(const qllg_stag_args *a);
+extern "C" int qllg_k_stag_dslash_f32(const qllg_stag_args *a);
+extern "C" int qllg_k_stag_dslash_i16(const qllg_stag_args *a);
+
 namespace {
-
-constexpr int kThreads = 256;
-
-int qllg_mr_disabled() { return qllg_get_param("dslash_mr") == 0; }
-
-template <int PS, int PL, int NS, int NR>
-__global__ void __launch_bounds__(kThreads)
-stag_dslash(qllg_stag_args a)
-{
-  typedef typename Calc<PS, PL>::T T;
-  __shared__ double shm[2*kThreads];
-  const Geo G = make_geo(a.g);
-  const size_t V = (size_t)a.g.V;
-  const size_t total = (size_t)G.Vh * NR;
-  const int p = a.out_parity;
-  const size_t loff = p ? (size_t)G.Vh : 0;
-  const bool skip = a.done && *(volatile const int *)a.done;
-  Acc<T> acc0, acc1;
-  const int rhs = threadIdx.x % NR;
-  const bool act = !a.active || a.active[rhs];
-  const T ca = (T)(a.a ? a.a[rhs] : a.a0);
-  const T cb = (T)a.b;
-  constexpr int PX = VecPrec<PS>::value;   // x and r of the fused CG epilogue
-  T alpha = 0;
-  if(a.mode == 3 && act)
-    alpha = (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs]));
-  if(!skip && act) {
-    for(size_t t = (size_t)blockIdx.x*blockDim.x + threadIdx.x; t < total;
-        t += (size_t)gridDim.x*blockDim.x) {
-      const int site = (int)(t / NR);
-      int x[4];
-      site_coords(G, p, site, x);
-      Cx<T> acc[3], self[3];
-      if(a.self && a.mode == 1) SpinorIO<PS,3>::load(a.self, total, t, self);
-      if(a.mode == 1) {
-#pragma unroll
-        for(int c=0; c<3; c++) { acc[c].r = ca*self[c].r; acc[c].i = ca*self[c].i; }
-      } else {
-#pragma unroll
-        for(int c=0; c<3; c++) { acc[c].r = 0; acc[c].i = 0; }
-      }
-#pragma unroll
-      for(int mu=0; mu<4; mu++) {
-#pragma unroll
-        for(int back=0; back<2; back++) {
-#pragma unroll
-          for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
-            const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
-            const int d = (nk ? 3 : 1)*(back ? -1 : 1);
-            const int k = nbr_index(G, x, mu, d);
-            Cx<T> U[9], v[3];
-            LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
-            SpinorIO<PS,3>::load(a.in, total, (size_t)k*NR + rhs, v);
-#pragma unroll
-            for(int l=0; l<3; l++) {
-#pragma unroll
-              for(int j=0; j<3; j++) cmac(acc[j], U[3*l + j], v[l]);
-            }
-          }
-        }
-      }
-      if(a.self && a.mode != 1) SpinorIO<PS,3>::load(a.self, total, t, self);
-      Cx<T> out[3];
-      if(a.mode == 3) {
-        // Ap = m^2 p - D v; x += alpha p; r -= alpha Ap (cgSolveT, lib/cg.c:101-105)
-        Cx<T> xv[3], rv[3];
-        SpinorIO<PX,3>::load(a.x, total, t, xv);
-        SpinorIO<PX,3>::load(a.r, total, t, rv);
-#pragma unroll
-        for(int c=0; c<3; c++) {
-          T apr = fma(cb, acc[c].r, ca*self[c].r), api = fma(cb, acc[c].i, ca*self[c].i);
-          xv[c].r = fma(alpha, self[c].r, xv[c].r); xv[c].i = fma(alpha, self[c].i, xv[c].i);
-          rv[c].r = fma(-alpha, apr, rv[c].r); rv[c].i = fma(-alpha, api, rv[c].i);
-        }
-        acc0.norm(rv);
-        SpinorIO<PX,3>::store(a.x, total, t, xv);
-        SpinorIO<PX,3>::store(a.r, total, t, rv);
-        continue;
-      }
-      if(a.mode == 2) {
-#pragma unroll
-        for(int c=0; c<3; c++) {
-          T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
-          out[c].r = fma(cb, acc[c].r, sr);
-          out[c].i = fma(cb, acc[c].i, si);
-        }
-      } else {
-#pragma unroll
-        for(int c=0; c<3; c++) out[c] = acc[c];
-      }
-      SpinorIO<PS,3>::store(a.out, total, t, out);
-      if(a.norm_out) acc0.norm(out);
-      if(a.norm_self && a.self) acc1.norm(self);
-    }
-  }
-  double red[2] = {acc0.get(), acc1.get()};
-  if(a.mode == 3) {
-    if(skip) return;   // uniform: the flag was set before this launch
-    double *res[2] = {a.sc->tmp, NULL};
-    if(grid_reduce<2>(red, NR, rhs, a.partial, a.counter, shm, res)) {
-      __syncthreads();
-      if(threadIdx.x == 0) {
-        if(a.mixed) cg_finish_mixed(a.sc, NR);
-        else cg_finish_plain(a.sc, NR);
-      }
-    }
-  } else if(a.norm_out || a.norm_self) {
-    double *res[2] = {a.norm_out, a.norm_self};
-    grid_reduce<2>(red, NR, rhs, a.partial, a.counter, shm, res);
-  }
-}
-
-
-// Multi-rhs variant: a thread owns one site and R consecutive right-hand
-// sides, so each link is loaded and converted once per R rhs and the R
-// accumulator sets give independent FMA chains.  Same epilogues as above.
-template <int PS, int PL, int NS, int NR, int R, bool V4>
-__global__ void __launch_bounds__(kThreads)
-stag_dslash_mr(qllg_stag_args a)
-{
-  typedef typename Calc<PS, PL>::T T;
-  constexpr int Q = NR/R;                       // threads per site
-  constexpr int PX = VecPrec<PS>::value;
-  __shared__ double shm[2*R*kThreads];
-  const Geo G = make_geo(a.g);
-  const size_t V = (size_t)a.g.V;
-  const size_t total = (size_t)G.Vh * NR;
-  const size_t nwork = (size_t)G.Vh * Q;
-  const int p = a.out_parity;
-  const size_t loff = p ? (size_t)G.Vh : 0;
-  const bool skip = a.done && *(volatile const int *)a.done;
-  const int q = threadIdx.x % Q;
-  bool act[R];
-  T ca[R], alpha[R];
-  bool anyact = false, allact = true;
-  constexpr bool v4 = (R == 4) && V4 && PS == QLLG_F32;
-  const T cb = (T)a.b;
-#pragma unroll
-  for(int j=0; j<R; j++) {
-    const int rhs = q*R + j;
-    act[j] = !a.active || a.active[rhs];
-    anyact |= act[j];
-    allact &= act[j];
-    ca[j] = (T)(a.a ? a.a[rhs] : a.a0);
-    alpha[j] = (a.mode == 3 && act[j])
-      ? (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs])) : (T)0;
-  }
-  Acc<T> acc0[R], acc1[R];
-  if(!skip && anyact) {
-    for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < nwork;
-        w += (size_t)gridDim.x*blockDim.x) {
-      const int site = (int)(w / Q);
-      const size_t t0 = (size_t)site*NR + q*R;
-      int x[4];
-      site_coords(G, p, site, x);
-      Cx<T> acc[R][3];
-#pragma unroll
-      for(int j=0; j<R; j++) {
-        if(a.mode == 1 && a.self) {
-          Cx<T> s[3];
-          SpinorIO<PS,3>::load(a.self, total, t0 + j, s);
-#pragma unroll
-          for(int c=0; c<3; c++) { acc[j][c].r = ca[j]*s[c].r; acc[j][c].i = ca[j]*s[c].i; }
-        } else {
-#pragma unroll
-          for(int c=0; c<3; c++) { acc[j][c].r = 0; acc[j][c].i = 0; }
-        }
-      }
-#pragma unroll
-      for(int mu=0; mu<4; mu++) {
-#pragma unroll
-        for(int back=0; back<2; back++) {
-#pragma unroll
-          for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
-            const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
-            const int d = (nk ? 3 : 1)*(back ? -1 : 1);
-            const size_t kb = (size_t)nbr_index(G, x, mu, d)*NR + q*R;
-            Cx<T> U[9];
-            LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
-            if constexpr (v4) {
-              // two rhs per 16-byte load and colour
-#pragma unroll
-              for(int h=0; h<R/2; h++) {
-                if(!act[2*h] && !act[2*h + 1]) continue;
-                Cx<T> v[2][3];
-                Spinor4<PS>::load_half(a.in, total, kb, h, v);
-#pragma unroll
-                for(int jj=0; jj<2; jj++) {
-#pragma unroll
-                  for(int l=0; l<3; l++) {
-#pragma unroll
-                    for(int c=0; c<3; c++) cmac(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
-                  }
-                }
-              }
-            } else {
-#pragma unroll
-              for(int j=0; j<R; j++) {
-                if(!act[j]) continue;
-                Cx<T> v[3];
-                SpinorIO<PS,3>::load(a.in, total, kb + j, v);
-#pragma unroll
-                for(int l=0; l<3; l++) {
-#pragma unroll
-                  for(int c=0; c<3; c++) cmac(acc[j][c], U[3*l + c], v[l]);
-                }
-              }
-            }
-          }
-        }
-      }
-      // epilogue.  With v4 and all R rhs active, the R rhs of the site move
-      // as 16-byte vectors (inactive rhs must keep their old values, so a
-      // partly active group takes the per-rhs path)
-      if constexpr (v4) {
-        if(allact) {
-          // per pair of rhs (one 16-byte vector per colour) to keep few
-          // values live
-#pragma unroll
-          for(int h=0; h<R/2; h++) {
-            Cx<T> sv[2][3];
-            if(a.self) Spinor4<PS>::load_half(a.self, total, t0, h, sv);
-            if(a.mode == 3) {
-              Cx<T> xv[2][3], rv[2][3];
-              Spinor4<PX>::load_half(a.x, total, t0, h, xv);
-              Spinor4<PX>::load_half(a.r, total, t0, h, rv);
-#pragma unroll
-              for(int jj=0; jj<2; jj++) {
-                const int j = 2*h + jj;
-#pragma unroll
-                for(int c=0; c<3; c++) {
-                  T apr = fma(cb, acc[j][c].r, ca[j]*sv[jj][c].r);
-                  T api = fma(cb, acc[j][c].i, ca[j]*sv[jj][c].i);
-                  xv[jj][c].r = fma(alpha[j], sv[jj][c].r, xv[jj][c].r);
-                  xv[jj][c].i = fma(alpha[j], sv[jj][c].i, xv[jj][c].i);
-                  rv[jj][c].r = fma(-alpha[j], apr, rv[jj][c].r);
-                  rv[jj][c].i = fma(-alpha[j], api, rv[jj][c].i);
-                }
-                acc0[j].norm(rv[jj]);
-              }
-              Spinor4<PX>::store_half(a.x, total, t0, h, xv);
-              Spinor4<PX>::store_half(a.r, total, t0, h, rv);
-              continue;
-            }
-            Cx<T> ov[2][3];
-#pragma unroll
-            for(int jj=0; jj<2; jj++) {
-              const int j = 2*h + jj;
-#pragma unroll
-              for(int c=0; c<3; c++) {
-                if(a.mode == 2) {
-                  T sr = a.self ? ca[j]*sv[jj][c].r : (T)0, si = a.self ? ca[j]*sv[jj][c].i : (T)0;
-                  ov[jj][c].r = fma(cb, acc[j][c].r, sr);
-                  ov[jj][c].i = fma(cb, acc[j][c].i, si);
-                } else {
-                  ov[jj][c] = acc[j][c];
-                }
-              }
-              if(a.norm_out) acc0[j].norm(ov[jj]);
-              if(a.norm_self && a.self) acc1[j].norm(sv[jj]);
-            }
-            Spinor4<PS>::store_half(a.out, total, t0, h, ov);
-          }
-          continue;
-        }
-      }
-#pragma unroll
-      for(int j=0; j<R; j++) {
-        if(!act[j]) continue;
-        const size_t t = t0 + j;
-        Cx<T> self[3];
-        if(a.self && a.mode != 1) SpinorIO<PS,3>::load(a.self, total, t, self);
-        if(a.mode == 3) {
-          Cx<T> xv[3], rv[3];
-          SpinorIO<PX,3>::load(a.x, total, t, xv);
-          SpinorIO<PX,3>::load(a.r, total, t, rv);
-#pragma unroll
-          for(int c=0; c<3; c++) {
-            T apr = fma(cb, acc[j][c].r, ca[j]*self[c].r), api = fma(cb, acc[j][c].i, ca[j]*self[c].i);
-            xv[c].r = fma(alpha[j], self[c].r, xv[c].r); xv[c].i = fma(alpha[j], self[c].i, xv[c].i);
-            rv[c].r = fma(-alpha[j], apr, rv[c].r); rv[c].i = fma(-alpha[j], api, rv[c].i);
-          }
-          acc0[j].norm(rv);
-          SpinorIO<PX,3>::store(a.x, total, t, xv);
-          SpinorIO<PX,3>::store(a.r, total, t, rv);
-          continue;
-        }
-        Cx<T> out[3];
-        if(a.mode == 2) {
-#pragma unroll
-          for(int c=0; c<3; c++) {
-            T sr = a.self ? ca[j]*self[c].r : (T)0, si = a.self ? ca[j]*self[c].i : (T)0;
-            out[c].r = fma(cb, acc[j][c].r, sr);
-            out[c].i = fma(cb, acc[j][c].i, si);
-          }
-        } else {
-#pragma unroll
-          for(int c=0; c<3; c++) out[c] = acc[j][c];
-        }
-        SpinorIO<PS,3>::store(a.out, total, t, out);
-        if(a.norm_out) acc0[j].norm(out);
-        if(a.norm_self && a.self) acc1[j].norm(self);
-      }
-    }
-  }
-  double red[2][R];
-#pragma unroll
-  for(int j=0; j<R; j++) { red[0][j] = acc0[j].get(); red[1][j] = acc1[j].get(); }
-  if(a.mode == 3) {
-    if(skip) return;
-    double *res[2] = {a.sc->tmp, NULL};
-    if(grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res)) {
-      __syncthreads();
-      if(threadIdx.x == 0) {
-        if(a.mixed) cg_finish_mixed(a.sc, NR);
-        else cg_finish_plain(a.sc, NR);
-      }
-    }
-  } else if(a.norm_out || a.norm_self) {
-    double *res[2] = {a.norm_out, a.norm_self};
-    grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res);
-  }
-}
-
-// Compacted variant for sparse masks (the FP64 reliable update of the
-// mixed solver, where one or a few rhs of the batch are flagged at a time):
-// work item w maps to (site, k-th flagged rhs), so the cost follows the
-// number of flagged rhs instead of running whole warps at the FP64 rate for
-// one of their lanes.  Modes 0 and 2 without norms.
-template <int PS, int PL, int NS, int NR>
-__global__ void __launch_bounds__(kThreads)
-stag_dslash_compact(qllg_stag_args a)
-{
-  typedef typename Calc<PS, PL>::T T;
-  __shared__ int list[NR];
-  __shared__ int nact_s;
-  if(a.done && *(volatile const int *)a.done) return;      // uniform
-  if(threadIdx.x == 0) {
-    int n = 0;
-    for(int r=0; r<NR; r++) if(a.active[r]) list[n++] = r;
-    nact_s = n;
-  }
-  __syncthreads();
-  const int nact = nact_s;
-  if(!nact) return;
-  const Geo G = make_geo(a.g);
-  const size_t V = (size_t)a.g.V;
-  const size_t total = (size_t)G.Vh * NR;
-  const size_t nwork = (size_t)G.Vh * nact;
-  const int p = a.out_parity;
-  const size_t loff = p ? (size_t)G.Vh : 0;
-  const T cb = (T)a.b;
-  for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < nwork;
-      w += (size_t)gridDim.x*blockDim.x) {
-    const int site = (int)(w / nact);
-    const int rhs = list[w % nact];
-    const size_t t = (size_t)site*NR + rhs;
-    int x[4];
-    site_coords(G, p, site, x);
-    Cx<T> acc[3];
-#pragma unroll
-    for(int c=0; c<3; c++) { acc[c].r = 0; acc[c].i = 0; }
-#pragma unroll
-    for(int mu=0; mu<4; mu++) {
-#pragma unroll
-      for(int back=0; back<2; back++) {
-#pragma unroll
-        for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
-          const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
-          const int d = (nk ? 3 : 1)*(back ? -1 : 1);
-          const int k = nbr_index(G, x, mu, d);
-          Cx<T> U[9], v[3];
-          LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
-          SpinorIO<PS,3>::load(a.in, total, (size_t)k*NR + rhs, v);
-#pragma unroll
-          for(int l=0; l<3; l++) {
-#pragma unroll
-            for(int j=0; j<3; j++) cmac(acc[j], U[3*l + j], v[l]);
-          }
-        }
-      }
-    }
-    Cx<T> out[3];
-    if(a.mode == 2) {
-      const T ca = (T)(a.a ? a.a[rhs] : a.a0);
-      Cx<T> self[3];
-      if(a.self) SpinorIO<PS,3>::load(a.self, total, t, self);
-#pragma unroll
-      for(int c=0; c<3; c++) {
-        T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
-        out[c].r = fma(cb, acc[c].r, sr);
-        out[c].i = fma(cb, acc[c].i, si);
-      }
-    } else {
-#pragma unroll
-      for(int c=0; c<3; c++) out[c] = acc[c];
-    }
-    SpinorIO<PS,3>::store(a.out, total, t, out);
-  }
-}
-
-template <int PS, int PL, int NS, int NR>
-int launch_compact(const qllg_stag_args *a)
-{
-  static int blocks_per_sm = 0;
-  if(!blocks_per_sm) {
-    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm, stag_dslash_compact<PS,PL,NS,NR>, kThreads, 0), "occupancy")) return -1;
-    if(blocks_per_sm < 1) blocks_per_sm = 1;
-  }
-  // sized for one flagged rhs: with more, the grid-stride loop takes them
-  size_t need = ((size_t)a->g.Vh + kThreads - 1)/kThreads;
-  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
-  int grid = (int)(need < maxg ? need : maxg);
-  if(grid < 1) grid = 1;
-  stag_dslash_compact<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
-  return qllg_launched("stag_dslash_compact launch");
-}
 
 __global__ void
 nbr_table(qllg_geom g, int p, int slot, int *out)
@@ -443,89 +22,6 @@ nbr_table(qllg_geom g, int p, int slot, int *out)
   int mu = slot/4, back = (slot/2) & 1, nk = slot & 1;
   int d = (nk ? 3 : 1)*(back ? -1 : 1);
   out[i] = (1 - p)*G.Vh + nbr_index(G, x, mu, d);
-}
-
-// 16-byte vector access to the spinor buffers is allowed when every base
-// pointer the kernel touches is 16-byte aligned (per-colour strides and the
-// 4-rhs offsets keep that alignment)
-bool vec4_ok(const qllg_stag_args *a)
-{
-  const void *ptrs[5] = {a->in, a->self, a->out, a->x, a->r};
-  for(int i=0; i<5; i++) if(((uintptr_t)ptrs[i] & 15u) != 0) return false;
-  return true;
-}
-
-template <int PS, int PL, int NS, int NR, int R>
-int launch_mr(const qllg_stag_args *a)
-{
-  const bool v4 = (R == 4) && PS == QLLG_F32 && qllg_get_param("dslash_vec4") != 0 &&
-                  vec4_ok(a);
-  static int blocks_per_sm[2] = {0, 0};
-  if(!blocks_per_sm[v4]) {
-    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm[v4], v4 ? stag_dslash_mr<PS,PL,NS,NR,R,true> : stag_dslash_mr<PS,PL,NS,NR,R,false>,
-         kThreads, 0), "occupancy")) return -1;
-    if(blocks_per_sm[v4] < 1) blocks_per_sm[v4] = 1;
-  }
-  size_t work = (size_t)a->g.Vh * (NR/R);
-  size_t need = (work + kThreads - 1)/kThreads;
-  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm[v4];
-  if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
-  int grid = (int)(need < maxg ? need : maxg);
-  if(grid < 1) grid = 1;
-  qllg_stag_args A = *a;
-  A.partial = a->rb ? a->rb->partial : NULL;
-  A.counter = a->rb ? a->rb->counter : NULL;
-  if(v4) stag_dslash_mr<PS,PL,NS,NR,R,true><<<grid, kThreads, 0, qllg_stream()>>>(A);
-  else stag_dslash_mr<PS,PL,NS,NR,R,false><<<grid, kThreads, 0, qllg_stream()>>>(A);
-  return qllg_launched("stag_dslash_mr launch");
-}
-
-template <int PS, int PL, int NS, int NR>
-int launch_t(const qllg_stag_args *a)
-{
-  if(a->compact) return launch_compact<PS,PL,NS,NR>(a);
-  if(NR >= 4 && !qllg_mr_disabled()) return launch_mr<PS,PL,NS,NR,(NR >= 4 ? 4 : 1)>(a);
-  static int blocks_per_sm = 0;
-  if(!blocks_per_sm) {
-    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm, stag_dslash<PS,PL,NS,NR>, kThreads, 0), "occupancy")) return -1;
-    if(blocks_per_sm < 1) blocks_per_sm = 1;
-  }
-  size_t total = (size_t)a->g.Vh * NR;
-  size_t need = (total + kThreads - 1)/kThreads;
-  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
-  if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
-  int grid = (int)(need < maxg ? need : maxg);
-  if(grid < 1) grid = 1;
-  qllg_stag_args A = *a;
-  A.partial = a->rb ? a->rb->partial : NULL;
-  A.counter = a->rb ? a->rb->counter : NULL;
-  stag_dslash<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(A);
-  return qllg_launched("stag_dslash launch");
-}
-
-template <int PS, int PL, int NS>
-int launch_nr(const qllg_stag_args *a)
-{
-  switch(a->nrhs) {
-  case 1: return launch_t<PS,PL,NS,1>(a);
-  case 2: return launch_t<PS,PL,NS,2>(a);
-  case 4: return launch_t<PS,PL,NS,4>(a);
-  case 8: return launch_t<PS,PL,NS,8>(a);
-  case 16: return launch_t<PS,PL,NS,16>(a);
-  }
-  qllg_set_error("stag_dslash: nrhs %d not in {1,2,4,8,16}", a->nrhs);
-  return -1;
-}
-
-template <int PS, int PL>
-int launch_ns(const qllg_stag_args *a)
-{
-  if(a->nslots == 16) return launch_nr<PS,PL,16>(a);
-  if(a->nslots == 8) return launch_nr<PS,PL,8>(a);
-  qllg_set_error("stag_dslash: nslots %d not 8 or 16", a->nslots);
-  return -1;
 }
 
 } // namespace
@@ -541,10 +37,9 @@ qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
     qllg_set_error("stag_dslash: reduction requested without workspace");
     return -1;
   }
-  if(ps == QLLG_F64 && pl == QLLG_F64) return launch_ns<QLLG_F64, QLLG_F64>(a);
-  if(ps == QLLG_F32 && pl == QLLG_F32) return launch_ns<QLLG_F32, QLLG_F32>(a);
-  if(ps == QLLG_I16 && pl == QLLG_I16) return launch_ns<QLLG_I16, QLLG_I16>(a);
-
+  if(ps == QLLG_F64 && pl == QLLG_F64) return qllg_k_stag_dslash_f64(a);
+  if(ps == QLLG_F32 && pl == QLLG_F32) return qllg_k_stag_dslash_f32(a);
+  if(ps == QLLG_I16 && pl == QLLG_I16) return qllg_k_stag_dslash_i16(a);
   qllg_set_error("stag_dslash: unsupported precision pair %d/%d", ps, pl);
   return -1;
 }

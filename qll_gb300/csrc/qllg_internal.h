@@ -60,6 +60,10 @@ int   qllg_runtime_init(void);                 /* 0 ok */
 cudaStream_t qllg_stream(void);                /* current library stream */
 void  qllg_set_error(const char *fmt, ...);
 cudaStream_t qllg_stream_swap(cudaStream_t s);
+/* autotuner registry (tune.c): the variant chosen for a launch shape */
+int  qllg_tune_lookup(const char *key);
+void qllg_tune_store(const char *key, int choice, int ncand, const float *ms,
+                     const char *const *names);
 int   qllg_check_cuda(cudaError_t e, const char *what);   /* 0 ok */
 void *qllg_dmalloc(size_t bytes);              /* NULL + error on failure */
 void  qllg_dfree(void *p);
@@ -137,6 +141,7 @@ typedef struct {
   unsigned *counter;      /* device last-block counter (from rb) */
   int compact;           /* threads over (site, flagged rhs of active) only;
                             modes 0 and 2, no norms */
+  int no_tune;           /* caller must not allocate: no autotuning */
   int dag;               /* Wilson only: gamma5 D gamma5 (projector signs flipped) */
   /* mode 3 (staggered CG, fused): Ap = a[rhs]*self - acc stays in registers,
    * then x += alpha self, r -= alpha Ap with alpha = 1/(a pnorm + vnorm) and

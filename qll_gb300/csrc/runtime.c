@@ -270,7 +270,8 @@ static struct { const char *name; double value; } g_params[] = {
   {"poll", 8},               /* first batch of iterations between host checks */
   {"dslash_mr", 1},          /* multi-rhs Dslash: one thread per site and 4 rhs */
   {"ru_compact", 1},         /* reliable-update Dslash over the flagged rhs only */
-  {"dslash_vec4", 1},        /* 16-byte loads of the 4 rhs of a thread (FP32) */
+  {"dslash_vec4", 1},        /* 16-byte loads of rhs pairs (FP32) */
+  {"autotune", 1},           /* time the Dslash variants of a new launch shape */
 };
 
 int

@@ -1067,6 +1067,7 @@ qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
   A.b = 1;
   A.norm_out = norm2_dev;
   A.rb = &rb;
+  A.no_tune = 1;              /* tuning would allocate a side buffer */
   return qllg_k_stag_dslash(prec, prec, &A);
 }
 
