@@ -222,8 +222,10 @@ void qllg_server_destroy(qllg_server *V);
  * "poll" (8), "dslash_mr" (1: multi-rhs Dslash with 4 rhs per thread),
  * "ru_compact" (1: the FP64 reliable update runs over the flagged rhs
  * only), "dslash_vec4" (1: 16-byte loads of rhs pairs), "autotune" (1:
- * time the Dslash variants of each new launch shape and keep the fastest);
- * returns -1 for an unknown name */
+ * time the Dslash variants of each new launch shape and keep the fastest),
+ * "dslash_tile" (1: the shared-memory-staged variant may be chosen),
+ * "dslash_variant" (-1: autotuned; 0-3 forces 4, 2 or 1 rhs per thread or
+ * the staged variant where it applies); returns -1 for an unknown name */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);
 

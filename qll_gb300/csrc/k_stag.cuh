@@ -494,14 +494,327 @@ int launch_plain(const qllg_stag_args *a)
   return qllg_launched("stag_dslash launch");
 }
 
+// ------------------------------------------------ shared-memory staging
+// FP32, 16 slots, 16 rhs: a block takes tiles of 64 consecutive output sites
+// (4 threads per site, 4 rhs each) and walks the 16 slots with a 3-stage
+// pipeline of asynchronous copies (cp.async.cg, 16 bytes, L1 bypassed): while
+// slot n is computed from shared memory, the links and neighbour spinors of
+// slots n+1 and n+2 are in flight, without holding registers.  The copies
+// are fully coalesced (a site's 16 rhs of one colour are 128 contiguous
+// bytes; a tile's link row is 512 contiguous bytes).  In shared memory a
+// (colour, site) segment is padded to 144 bytes so that the 16-byte reads of
+// 8 lanes hit distinct banks.  Needs Vh a multiple of 64 and 16-byte aligned
+// spinor buffers (the launcher checks).
+constexpr int kTileSites = 64;
+constexpr int kTileStages = 3;
+constexpr int kSpSeg = 144;                                  // bytes per (colour, site)
+constexpr int kSpStage = 3*kTileSites*kSpSeg;                // 27648
+constexpr int kLkStage = 9*kTileSites*8;                     // 4608
+constexpr int kStageBytes = kSpStage + kLkStage;             // 32256
+constexpr int kTileSmem = kTileStages*kStageBytes;           // 96768
+
+__device__ __forceinline__ void cp16(void *smem, const void *gmem)
+{
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait()
+{
+  asm volatile("cp.async.wait_group %0;\n" :: "n"(N) : "memory");
+}
+
+template <int NR_>
+__global__ void __launch_bounds__(kThreads, 2)
+stag_dslash_tile(qllg_stag_args a)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  typedef float T;
+  constexpr int NR = 16, R = 4, PX = QLLG_F32;
+  const Geo G = make_geo(a.g);
+  const size_t V = (size_t)a.g.V;
+  const size_t total = (size_t)G.Vh*NR;
+  const int p = a.out_parity;
+  const size_t loff = p ? (size_t)G.Vh : 0;
+  const int tid = threadIdx.x;
+  const int q = tid & 3, i = tid >> 2;            // compute role: site i of the tile, rhs 4q..4q+3
+  bool act[R], allact = true, anyact = false, blockact = !a.active;
+  T ca[R], alpha[R];
+  const T cb = (T)a.b;
+#pragma unroll
+  for(int j=0; j<R; j++) {
+    const int rhs = q*R + j;
+    act[j] = !a.active || a.active[rhs];
+    allact &= act[j];
+    anyact |= act[j];
+    ca[j] = (T)(a.a ? a.a[rhs] : a.a0);
+    alpha[j] = (a.mode == 3 && act[j])
+      ? (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs])) : (T)0;
+  }
+  if(a.active) for(int r=0; r<NR; r++) blockact |= a.active[r] != 0;
+  const bool skip = (a.done && *(volatile const int *)a.done) || !blockact;   // uniform
+  Acc<T> acc0[R], acc1[R];
+  if(!skip) {
+    const int ntiles = G.Vh/kTileSites;
+    const int mytiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x)/(int)gridDim.x + 1 : 0;
+    const size_t cstride = total*8;                 // bytes between colours of a spinor
+    // copy role: sites tid/8 and tid/8 + 32 of the tile, 16-byte part tid%8
+    const int csite = tid >> 3, cpart = tid & 7;
+    int xc[2][4], xn[2][4];                         // copy-site coordinates, this and next tile
+    // the links and neighbour spinors of one slot of one tile, into stage st
+    // (called with compile-time slots from the unrolled loop below)
+    auto issue_slot = [&](int slot, int tile, const int (&xs)[2][4], int st) {
+      const int mu = slot >> 2, back = (slot >> 1) & 1, nk = slot & 1;
+      const int d = (nk ? 3 : 1)*(back ? -1 : 1);
+      unsigned char *base = smem + st*kStageBytes;
+#pragma unroll
+      for(int hh=0; hh<2; hh++) {
+        const char *src = (const char *)a.in + (size_t)nbr_index(G, xs[hh], mu, d)*(NR*8) + cpart*16;
+        unsigned char *dst = base + (csite + 32*hh)*kSpSeg + cpart*16;
+#pragma unroll
+        for(int c=0; c<3; c++) cp16(dst + c*kTileSites*kSpSeg, src + c*cstride);
+      }
+      const char *lk = (const char *)a.links + (((size_t)slot*9)*V + loff + (size_t)tile*kTileSites)*8;
+      for(int ch=tid; ch<9*32; ch+=kThreads) {
+        const int k = ch >> 5, part = ch & 31;
+        cp16(base + kSpStage + k*512 + part*16, lk + (size_t)k*V*8 + part*16);
+      }
+    };
+    if(mytiles > 0) {
+      site_coords(G, p, (int)blockIdx.x*kTileSites + csite, xc[0]);
+      site_coords(G, p, (int)blockIdx.x*kTileSites + csite + 32, xc[1]);
+      issue_slot(0, blockIdx.x, xc, 0);
+      cp_commit();
+      issue_slot(1, blockIdx.x, xc, 1);
+      cp_commit();
+    }
+    Cx<T> acc[R][3];
+    int st = 0, st2 = 2;                            // stages of the current step and of step + 2
+    for(int lt=0; lt<mytiles; lt++) {
+      const int tile = (int)blockIdx.x + lt*(int)gridDim.x;
+      const bool more = lt + 1 < mytiles;
+      const size_t t0 = ((size_t)tile*kTileSites + i)*NR + q*R;
+#pragma unroll
+      for(int slot=0; slot<16; slot++) {
+        if(slot < 14) {
+          issue_slot(slot + 2, tile, xc, st2);
+        } else if(more) {
+          if(slot == 14) {
+            site_coords(G, p, (tile + (int)gridDim.x)*kTileSites + csite, xn[0]);
+            site_coords(G, p, (tile + (int)gridDim.x)*kTileSites + csite + 32, xn[1]);
+          }
+          issue_slot(slot - 14, tile + (int)gridDim.x, xn, st2);
+        }
+        cp_commit();
+        st2 = st2 == kTileStages - 1 ? 0 : st2 + 1;
+        cp_wait<2>();
+        __syncthreads();
+        if(slot == 0) {
+#pragma unroll
+          for(int j=0; j<R; j++) {
+            if(a.mode == 1 && a.self) {
+              Cx<T> sv[3];
+              SpinorIO<QLLG_F32,3>::load(a.self, total, t0 + j, sv);
+#pragma unroll
+              for(int c=0; c<3; c++) { acc[j][c].r = ca[j]*sv[c].r; acc[j][c].i = ca[j]*sv[c].i; }
+            } else {
+#pragma unroll
+              for(int c=0; c<3; c++) { acc[j][c].r = 0; acc[j][c].i = 0; }
+            }
+          }
+        }
+        if(anyact) {
+          const unsigned char *base = smem + st*kStageBytes;
+          Cx<T> U[9];
+          const float2 *lk = (const float2 *)(base + kSpStage);
+#pragma unroll
+          for(int k=0; k<9; k++) { float2 u = lk[k*kTileSites + i]; U[k].r = u.x; U[k].i = u.y; }
+#pragma unroll
+          for(int h=0; h<R/2; h++) {
+            if(!act[2*h] && !act[2*h + 1]) continue;
+            Cx<T> v[2][3];
+#pragma unroll
+            for(int c=0; c<3; c++) {
+              float4 w = *(const float4 *)(base + (c*kTileSites + i)*kSpSeg + q*32 + h*16);
+              v[0][c].r = w.x; v[0][c].i = w.y; v[1][c].r = w.z; v[1][c].i = w.w;
+            }
+#pragma unroll
+            for(int jj=0; jj<2; jj++)
+#pragma unroll
+              for(int l=0; l<3; l++)
+#pragma unroll
+                for(int c=0; c<3; c++) cmac(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
+          }
+        }
+        if(slot == 15 && anyact) {
+          // epilogue of the tile's site (as the 16-byte path of stag_dslash_mr)
+          if(allact) {
+#pragma unroll
+            for(int h=0; h<R/2; h++) {
+              Cx<T> sv[2][3];
+              if(a.self) Spinor4<QLLG_F32>::load_half(a.self, total, t0, h, sv);
+              if(a.mode == 3) {
+                Cx<T> xv[2][3], rv[2][3];
+                Spinor4<PX>::load_half(a.x, total, t0, h, xv);
+                Spinor4<PX>::load_half(a.r, total, t0, h, rv);
+#pragma unroll
+                for(int jj=0; jj<2; jj++) {
+                  const int j = 2*h + jj;
+#pragma unroll
+                  for(int c=0; c<3; c++) {
+                    T apr = fma(cb, acc[j][c].r, ca[j]*sv[jj][c].r);
+                    T api = fma(cb, acc[j][c].i, ca[j]*sv[jj][c].i);
+                    xv[jj][c].r = fma(alpha[j], sv[jj][c].r, xv[jj][c].r);
+                    xv[jj][c].i = fma(alpha[j], sv[jj][c].i, xv[jj][c].i);
+                    rv[jj][c].r = fma(-alpha[j], apr, rv[jj][c].r);
+                    rv[jj][c].i = fma(-alpha[j], api, rv[jj][c].i);
+                  }
+                  acc0[j].norm(rv[jj]);
+                }
+                Spinor4<PX>::store_half(a.x, total, t0, h, xv);
+                Spinor4<PX>::store_half(a.r, total, t0, h, rv);
+                continue;
+              }
+              Cx<T> ov[2][3];
+#pragma unroll
+              for(int jj=0; jj<2; jj++) {
+                const int j = 2*h + jj;
+#pragma unroll
+                for(int c=0; c<3; c++) {
+                  if(a.mode == 2) {
+                    T sr = a.self ? ca[j]*sv[jj][c].r : (T)0, si = a.self ? ca[j]*sv[jj][c].i : (T)0;
+                    ov[jj][c].r = fma(cb, acc[j][c].r, sr);
+                    ov[jj][c].i = fma(cb, acc[j][c].i, si);
+                  } else {
+                    ov[jj][c] = acc[j][c];
+                  }
+                }
+                if(a.norm_out) acc0[j].norm(ov[jj]);
+                if(a.norm_self && a.self) acc1[j].norm(sv[jj]);
+              }
+              Spinor4<QLLG_F32>::store_half(a.out, total, t0, h, ov);
+            }
+          } else {
+#pragma unroll
+            for(int j=0; j<R; j++) {
+              if(!act[j]) continue;
+              const size_t t = t0 + j;
+              Cx<T> self[3];
+              if(a.self && a.mode != 1) SpinorIO<QLLG_F32,3>::load(a.self, total, t, self);
+              if(a.mode == 3) {
+                Cx<T> xv[3], rv[3];
+                SpinorIO<PX,3>::load(a.x, total, t, xv);
+                SpinorIO<PX,3>::load(a.r, total, t, rv);
+#pragma unroll
+                for(int c=0; c<3; c++) {
+                  T apr = fma(cb, acc[j][c].r, ca[j]*self[c].r), api = fma(cb, acc[j][c].i, ca[j]*self[c].i);
+                  xv[c].r = fma(alpha[j], self[c].r, xv[c].r); xv[c].i = fma(alpha[j], self[c].i, xv[c].i);
+                  rv[c].r = fma(-alpha[j], apr, rv[c].r); rv[c].i = fma(-alpha[j], api, rv[c].i);
+                }
+                acc0[j].norm(rv);
+                SpinorIO<PX,3>::store(a.x, total, t, xv);
+                SpinorIO<PX,3>::store(a.r, total, t, rv);
+                continue;
+              }
+              Cx<T> out[3];
+              if(a.mode == 2) {
+#pragma unroll
+                for(int c=0; c<3; c++) {
+                  T sr = a.self ? ca[j]*self[c].r : (T)0, si = a.self ? ca[j]*self[c].i : (T)0;
+                  out[c].r = fma(cb, acc[j][c].r, sr);
+                  out[c].i = fma(cb, acc[j][c].i, si);
+                }
+              } else {
+#pragma unroll
+                for(int c=0; c<3; c++) out[c] = acc[j][c];
+              }
+              SpinorIO<QLLG_F32,3>::store(a.out, total, t, out);
+              if(a.norm_out) acc0[j].norm(out);
+              if(a.norm_self && a.self) acc1[j].norm(self);
+            }
+          }
+        }
+        __syncthreads();
+        st = st == kTileStages - 1 ? 0 : st + 1;
+      }
+      if(more) {
+#pragma unroll
+        for(int hh=0; hh<2; hh++)
+#pragma unroll
+          for(int k=0; k<4; k++) xc[hh][k] = xn[hh][k];
+      }
+    }
+    cp_wait<0>();
+    __syncthreads();
+  }
+  double red[2][R];
+#pragma unroll
+  for(int j=0; j<R; j++) { red[0][j] = acc0[j].get(); red[1][j] = acc1[j].get(); }
+  double *shm = (double *)smem;                   // the pipeline is drained: reuse its buffer
+  if(a.mode == 3) {
+    if(skip) return;
+    double *res[2] = {a.sc->tmp, NULL};
+    if(grid_reduce_mr<2,R>(red, NR, 4, a.partial, a.counter, shm, res)) {
+      __syncthreads();
+      if(threadIdx.x == 0) {
+        if(a.mixed) cg_finish_mixed(a.sc, NR);
+        else cg_finish_plain(a.sc, NR);
+      }
+    }
+  } else if(a.norm_out || a.norm_self) {
+    double *res[2] = {a.norm_out, a.norm_self};
+    grid_reduce_mr<2,R>(red, NR, 4, a.partial, a.counter, shm, res);
+  }
+}
+
+template <int NR_>
+int launch_tile(const qllg_stag_args *a)
+{
+  static int blocks_per_sm = 0;
+  if(!blocks_per_sm) {
+    if(qllg_check_cuda(cudaFuncSetAttribute(stag_dslash_tile<NR_>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            kTileSmem), "tile smem") ||
+       qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &blocks_per_sm, stag_dslash_tile<NR_>, kThreads, kTileSmem), "occupancy")) return -1;
+    if(blocks_per_sm < 1) blocks_per_sm = 1;
+  }
+  size_t ntiles = (size_t)a->g.Vh/kTileSites;
+  size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
+  if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
+  int grid = (int)(ntiles < maxg ? ntiles : maxg);
+  if(grid < 1) grid = 1;
+  qllg_stag_args A = *a;
+  A.partial = a->rb ? a->rb->partial : NULL;
+  A.counter = a->rb ? a->rb->counter : NULL;
+  stag_dslash_tile<NR_><<<grid, kThreads, kTileSmem, qllg_stream()>>>(A);
+  return qllg_launched("stag_dslash_tile launch");
+}
+
 // variants of one launch shape, in the order the autotuner tries them:
-// 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site, rhs)
-constexpr int kNumVariants = 3;
-const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread"};
+// 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
+// rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only)
+constexpr int kNumVariants = 4;
+const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
+                                                "smem-staged 4 rhs/thread"};
+
+template <int PS, int PL, int NS, int NR>
+bool variant_ok(const qllg_stag_args *a, int v)
+{
+  if(v == 0) return NR >= 4;
+  if(v == 1) return NR >= 2;
+  if(v == 2) return true;
+  return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 &&
+         a->g.Vh % kTileSites == 0 && vec4_ok(a) && qllg_get_param("dslash_tile") != 0;
+}
 
 template <int PS, int PL, int NS, int NR>
 int launch_variant(const qllg_stag_args *a, int v)
 {
+  if(!variant_ok<PS,PL,NS,NR>(a, v)) v = NR >= 4 ? 0 : (NR >= 2 ? 1 : 2);
+  if constexpr (PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16) {
+    if(v == 3) return launch_tile<NR>(a);
+  }
   if constexpr (NR >= 4) { if(v == 0) return launch_mr<PS,PL,NS,NR,4>(a); }
   if constexpr (NR >= 2) { if(v == 1) return launch_mr<PS,PL,NS,NR,2>(a); }
   return launch_plain<PS,PL,NS,NR>(a);
@@ -519,6 +832,8 @@ template <int PS, int PL, int NS, int NR>
 int tuned_variant(const qllg_stag_args *a)
 {
   if(NR < 2 || qllg_mr_disabled()) return 2;
+  const int force = (int)qllg_get_param("dslash_variant");
+  if(force >= 0 && force < kNumVariants && variant_ok<PS,PL,NS,NR>(a, force)) return force;
   char key[96];
   snprintf(key, sizeof(key), "stag_dslash p%d/%d s%d n%d V%d (%d %d %d %d)", PS, PL, NS, NR,
            a->g.V, a->g.L[0], a->g.L[1], a->g.L[2], a->g.L[3]);
@@ -545,6 +860,7 @@ int tuned_variant(const qllg_stag_args *a)
   for(int c=0; c<kNumVariants; c++) ms[c] = -1;
   int best = first, rc = 0;
   for(int c=first; c<kNumVariants && !rc; c++) {
+    if(!variant_ok<PS,PL,NS,NR>(&T, c)) continue;
     rc |= launch_variant<PS,PL,NS,NR>(&T, c);                 // warm
     cudaEventRecord(e0, qllg_stream());
     for(int k=0; k<3; k++) rc |= launch_variant<PS,PL,NS,NR>(&T, c);

@@ -272,6 +272,8 @@ static struct { const char *name; double value; } g_params[] = {
   {"ru_compact", 1},         /* reliable-update Dslash over the flagged rhs only */
   {"dslash_vec4", 1},        /* 16-byte loads of rhs pairs (FP32) */
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
+  {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
+  {"dslash_variant", -1},    /* force a Dslash variant (0-3); -1: autotuned */
 };
 
 int

@@ -283,6 +283,60 @@ def test_multishift_multi_rhs_matches_oracle(mode):
     L.qllg_stag_destroy(S)
 
 
+@pytest.mark.parametrize("nrhs", [4, 16])
+def test_dslash_variants_agree(nrhs):
+    """the autotuner's candidates (4, 2, 1 rhs per thread, shared-memory
+    staging) compute bitwise the same FP32 Dslash"""
+    torch = pytest.importorskip("torch")
+    L, S, u, u3 = _native()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_stag_vec_bytes.restype = ctypes.c_size_t
+    L.qllg_stag_vec_bytes.argtypes = [ctypes.c_void_p, c_int, c_int]
+    L.qllg_stag_dslash_device.argtypes = [ctypes.c_void_p, c_int, c_int, c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    n = L.qllg_stag_vec_bytes(S, 1, nrhs)//4
+    g = torch.Generator(device="cuda").manual_seed(91 + nrhs)
+    src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
+    outs = []
+    for v in (0, 1, 2, 3):
+        L.qllg_set_param(b"dslash_variant", v)
+        for parity in (0, 1):
+            dst = torch.full_like(src, float("nan"))
+            torch.cuda.synchronize()
+            assert L.qllg_stag_dslash_device(S, 1, nrhs, parity, ctypes.c_void_p(dst.data_ptr()),
+                                             ctypes.c_void_p(src.data_ptr())) == 0, qll.last_error()
+            torch.cuda.synchronize()
+            outs.append(dst)
+    L.qllg_set_param(b"dslash_variant", -1)
+    for k in range(2, len(outs)):
+        assert torch.equal(outs[k], outs[k % 2]), k
+    L.qllg_stag_destroy(S)
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_mixed_solve_with_each_dslash_variant(variant):
+    """the fused CG epilogue and the norms of every variant: the 16-rhs
+    mixed solve reaches the FP64 true residual and matches the oracle"""
+    L, S, u, u3 = _native()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_set_param(b"dslash_variant", variant)
+    nrhs = 16
+    masses = [0.05 + 0.01*k for k in range(nrhs)]
+    bs = [qll.gen_source(DIMS, 8000 + k, 6, "even") for k in range(nrhs)]
+    xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+    info = qll.SolveInfo()
+    its = L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), (c_double*nrhs)(*masses),
+                            1e-16, 5000, qll.SOLVE_MIXED_SINGLE, byref(info))
+    L.qllg_set_param(b"dslash_variant", -1)
+    assert its > 0, qll.last_error()
+    Vh = bs[0].shape[0]//2
+    for k in (0, 7, 15):
+        assert info.true_rsq[k] < 1e-16*1.0001
+        its_o, xo, _ = orc.solve2(DIMS, u, u3, masses[k], bs[k], 1e-16, 5000, noscale=1)
+        assert relerr(xs[k][:Vh], xo[:Vh]) < 1e-7
+    L.qllg_stag_destroy(S)
+
+
 def test_unknown_parameter_is_refused():
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
