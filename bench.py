@@ -191,8 +191,10 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
-    L.qllg_timing_enable(1)
-    L.qllg_timing_reset()
+    # the timed region runs the production path: each solve's iterations are
+    # one CUDA-graph launch (per-kernel event timing is off, it would force
+    # the host-polled loop); the kernel counter includes the kernels the
+    # graph trips ran
     n0 = L.qllg_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     iters, truer = [], []
@@ -208,6 +210,12 @@ def run_gpu(args):
         torch.cuda.synchronize()
     nlaunch = int(L.qllg_launch_count() - n0)
     ms = ev0.elapsed_time(ev1)
+    # one more solve, untimed, with per-kernel CUDA events on the library
+    # stream: the average launch times of the roofline
+    L.qllg_timing_enable(1)
+    L.qllg_timing_reset()
+    solve()
+    torch.cuda.synchronize()
     cnt, tot = ctypes.c_int(), ctypes.c_double()
     L.qllg_timing_read(b"stag_dslash_f32_n16", ctypes.byref(cnt), ctypes.byref(tot))
     fcnt, ftot = ctypes.c_int(), ctypes.c_double()
@@ -288,7 +296,8 @@ def run_gpu(args):
                      "frac": achieved/peak if peak else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else None,
                      "algorithmic_bytes_per_launch": launch_bytes,
-                     "avg_launch_ms": avg_ms, "launches_timed": cnt.value,
+                     "avg_launch_ms": avg_ms, "launches_event_timed": cnt.value,
+                     "timing_note": "avg launch time from CUDA events over one extra 16-rhs solve after the timed region",
                      "compulsory_frac": compulsory*Vh*NRHS/(avg_ms*1e-3)/1e9/peak if peak else None,
                      # dram read+write of one launch from an ncu capture at
                      # 24^3x48 (650 MB), scaled by sites to this lattice

@@ -596,6 +596,11 @@ stag_dslash_tile(qllg_stag_args a)
       const size_t t0 = ((size_t)tile*kTileSites + i)*NR + q*R;
 #pragma unroll
       for(int slot=0; slot<16; slot++) {
+        // one barrier per step: after it, step n's copies are visible and
+        // every thread is done with step n-1, whose stage is the one step
+        // n+2 fills
+        cp_wait<1>();
+        __syncthreads();
         if(slot < 14) {
           issue_slot(slot + 2, tile, xc, st2);
         } else if(more) {
@@ -607,8 +612,6 @@ stag_dslash_tile(qllg_stag_args a)
         }
         cp_commit();
         st2 = st2 == kTileStages - 1 ? 0 : st2 + 1;
-        cp_wait<2>();
-        __syncthreads();
         if(slot == 0) {
 #pragma unroll
           for(int j=0; j<R; j++) {
@@ -734,7 +737,6 @@ stag_dslash_tile(qllg_stag_args a)
             }
           }
         }
-        __syncthreads();
         st = st == kTileStages - 1 ? 0 : st + 1;
       }
       if(more) {

@@ -60,6 +60,7 @@ int   qllg_runtime_init(void);                 /* 0 ok */
 cudaStream_t qllg_stream(void);                /* current library stream */
 void  qllg_set_error(const char *fmt, ...);
 cudaStream_t qllg_stream_swap(cudaStream_t s);
+void qllg_launch_adjust(long long n);
 /* autotuner registry (tune.c): the variant chosen for a launch shape */
 int  qllg_tune_lookup(const char *key);
 void qllg_tune_store(const char *key, int choice, int ncand, const float *ms,

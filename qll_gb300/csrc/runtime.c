@@ -67,6 +67,14 @@ qllg_launch_count(void)
   return g_launches;
 }
 
+/* kernels launched through a CUDA graph: the capture counted the body once
+ * without running it (-body), each executed trip runs it (+body per trip) */
+void
+qllg_launch_adjust(long long n)
+{
+  g_launches += (unsigned long long)n;
+}
+
 int
 qllg_runtime_init(void)
 {

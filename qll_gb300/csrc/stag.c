@@ -55,8 +55,10 @@ struct qllg_stag {
   struct {                 /* graph-captured solver loops */
     long key[10];
     cudaGraphExec_t exec;
+    int body;              /* kernels in one trip of the loop body */
   } graphs[6];
   int ngraph_next;
+  int graph_body;          /* body of the graph the current solve launched, 0: none */
   unsigned char shared[3]; /* links[p] belong to another operator */
   /* continuous batching (qllg_batch_*): a fixed-width mixed CG whose
    * columns are admitted and retired independently */
@@ -496,7 +498,11 @@ loop_graph(qllg_stag *S, const iter_ctx *c)
   long key[10] = {c->mixed, c->ps, c->pl, c->nrhs, c->reortho, (long)c->x, (long)c->b,
                   (long)c->x64, (long)S->ws_gen, 1};
   for(int i=0; i<6; i++)
-    if(S->graphs[i].exec && !memcmp(S->graphs[i].key, key, sizeof(key))) return S->graphs[i].exec;
+    if(S->graphs[i].exec && !memcmp(S->graphs[i].key, key, sizeof(key))) {
+      S->graph_body = S->graphs[i].body;
+      return S->graphs[i].exec;
+    }
+  unsigned long long n0 = qllg_launch_count();
   cudaGraph_t g = NULL;
   cudaGraphExec_t exec = NULL;
   cudaGraphConditionalHandle h;
@@ -522,11 +528,16 @@ loop_graph(qllg_stag *S, const iter_ctx *c)
   if(qllg_check_cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate")) goto fail;
   cudaGraphDestroy(g);
   {
+    /* the capture counted the body's launches without running them */
+    int body = (int)(qllg_launch_count() - n0);
+    qllg_launch_adjust(-(long long)body);
     int i = S->ngraph_next;
     S->ngraph_next = (i + 1) % 6;
     if(S->graphs[i].exec) cudaGraphExecDestroy(S->graphs[i].exec);
     memcpy(S->graphs[i].key, key, sizeof(key));
     S->graphs[i].exec = exec;
+    S->graphs[i].body = body;
+    S->graph_body = body;
   }
   return exec;
 fail:
@@ -540,9 +551,18 @@ fail:
  * the done flag after each batch */
 int qllg_timing_on(void);
 
+/* after a graph-launched solve: the kernels its trips ran (sc->loops) */
+static void
+count_graph_trips(qllg_stag *S)
+{
+  if(S->graph_body) qllg_launch_adjust((long long)S->graph_body*S->hsc->loops);
+  S->graph_body = 0;
+}
+
 static int
 run_loop(qllg_stag *S, const iter_ctx *c, int maxits)
 {
+  S->graph_body = 0;
   if(qllg_get_param("graph") != 0 && !qllg_timing_on()) {
     /* one iteration launched directly first: every kernel of the body is
      * then loaded before the capture starts */
@@ -594,6 +614,7 @@ cg_plain(qllg_stag *S, int prec, int nrhs, void *x, const void *b, const double 
   c.b = b;
   if(run_loop(S, &c, maxits)) return -1;
   if(pull_scalars(S)) return -1;
+  count_graph_trips(S);
   int its = 0;
   for(int i=0; i<nrhs; i++) if(S->hsc->iters[i] > its) its = S->hsc->iters[i];
   return its;
@@ -659,6 +680,7 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
   c.b = b;
   if(run_loop(S, &c, maxits)) return -1;
   if(pull_scalars(S)) return -1;
+  count_graph_trips(S);
   int its = 0;
   for(int i=0; i<nrhs; i++) if(S->hsc->iters[i] > its) its = S->hsc->iters[i];
   return its;
