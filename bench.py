@@ -469,7 +469,9 @@ def run_serving(args):
     requests solved one shift at a time by the plain FP64 single-rhs CG"""
     from qll_gb300 import qll, serve
     L = serve._lib()
-    ops = [serve.asqtad_operator(d, s, e) for d, s, e in zip(SERVE_LATTICES, SERVE_SEEDS, SERVE_EPS)]
+    # single-stored links: half the resident link bytes per lattice
+    ops = [serve.asqtad_operator(d, s, e, single_store=True)
+           for d, s, e in zip(SERVE_LATTICES, SERVE_SEEDS, SERVE_EPS)]
 
     def server():
         V = serve.Server(int(args.serve_budget*(1 << 30)), chunk=args.serve_chunk, max_batches=2)
@@ -515,7 +517,8 @@ def run_serving(args):
     for S in ops:
         L.qllg_stag_destroy(S)
     return {
-        "workload": "C5: 16^4 + 24^3x48 + 32^3x64 resident; Poisson arrivals (seed 7) at 70% "
+        "workload": "C5: 16^4 + 24^3x48 + 32^3x64 resident (single-stored links); Poisson "
+                    "arrivals (seed 7) at 70% "
                     "of the measured capacity; per request m~U[0.005,0.1], 1-16 shifts "
                     "log-spaced in [1e-4,1], tolerance 1e-8 or 1e-10",
         "requests": len(recs), "shift_solves": cols, "seconds": t_run,

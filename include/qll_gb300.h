@@ -149,6 +149,11 @@ int qllg_smear_fat7(const int dims[4], double *const fl[4], double *const ll[4],
  * backward links) of a resident FP64 operator, built on the GPU */
 qllg_stag *qllg_stag_create_asqtad(const int dims[4], double *const thin[4],
                                    const Fat7Coeffs *coef);
+/* the same with the links single-stored: the 8 forward slots only (half
+ * the memory); the Dslash kernels make the backward links -F^dagger(x-mu),
+ * -L^dagger(x-3mu) on the fly, with bitwise the same products */
+qllg_stag *qllg_stag_create_asqtad_fb(const int dims[4], double *const thin[4],
+                                      const Fat7Coeffs *coef);
 /* the six plaquettes of gaugePlaq (normalised by 3V) */
 int qllg_plaq(const int dims[4], double *const u[4], double plaqs[6]);
 

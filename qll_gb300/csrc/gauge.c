@@ -18,6 +18,8 @@
 #include "qll_gb300.h"
 #include "qllg_internal.h"
 
+void qllg_stag_set_single_store(qllg_stag *S);
+
 int qllg_geom_from_layout(qllg_geom *g, const Layout *l);
 int qllg_stag_attach_links(qllg_stag *S, int prec, void *links);
 qllg_stag *qllg_stag_alloc(const int dims[4], int nslots, int prec);
@@ -203,32 +205,36 @@ qllg_smear_fat7(const int dims[4], double *const fl[4], double *const ll[4],
                     (void *const *)u, (void *const *)(ulong_ ? ulong_ : u));
 }
 
-/* thin links -> fat7 -> 16 slots (forward and negative-adjoint backward)
- * of a resident operator, all on the GPU */
-qllg_stag *
-qllg_stag_create_asqtad(const int dims[4], double *const thin[4], const Fat7Coeffs *coef)
+/* thin links -> fat7 -> the links of a resident operator, all on the GPU:
+ * 16 slots (forward and negative-adjoint backward), or with single_store
+ * the 8 forward slots [fat mu, long mu] whose backward links the kernels
+ * make on the fly */
+static qllg_stag *
+create_asqtad(const int dims[4], double *const thin[4], const Fat7Coeffs *coef, int single_store)
 {
   qllg_geom g;
   if(qllg_runtime_init() || qllg_geom_from_dims(&g, dims)) return NULL;
   size_t fb = 144*(size_t)g.V;
+  const int stored = single_store ? 8 : 16, per_mu = stored/4;
   void *u[4] = {0}, *fl[4] = {0}, *ll[4] = {0};
   qllg_stag *S = NULL;
-  char *links = qllg_dmalloc(fb*16);
+  char *links = qllg_dmalloc(fb*stored);
   if(!links) return NULL;
   for(int d=0; d<4; d++) {
     if(!(u[d] = qllg_dmalloc(fb))) goto out;
     if(mfield_up(QLLG_F64, u[d], thin[d], g.V)) goto out;
-    fl[d] = links + fb*(4*d + 0);
-    ll[d] = links + fb*(4*d + 1);
+    fl[d] = links + fb*(per_mu*d + 0);
+    ll[d] = links + fb*(per_mu*d + 1);
   }
   if(qllg_fat7_device(QLLG_F64, &g, fl, ll, coef, u, u)) goto out;
-  for(int d=0; d<4; d++) {
+  for(int d=0; d<4 && !single_store; d++) {
     /* slot 4mu+2: -F_mu(x-mu)^dagger; slot 4mu+3: -L_mu(x-3mu)^dagger */
     if(qllg_k_mat_shift(QLLG_F64, links + fb*(4*d + 2), fl[d], &g, d, -1, 1, -1.0)) goto out;
     if(qllg_k_mat_shift(QLLG_F64, links + fb*(4*d + 3), ll[d], &g, d, -3, 1, -1.0)) goto out;
   }
   if(qllg_sync()) goto out;
   S = qllg_stag_alloc(dims, 16, QLLG_F64);
+  if(S && single_store) qllg_stag_set_single_store(S);
   if(S && qllg_stag_attach_links(S, QLLG_F64, links)) { qllg_stag_destroy(S); S = NULL; }
   if(S) links = NULL;
 out:
@@ -236,6 +242,18 @@ out:
   for(int d=0; d<4; d++) qllg_dfree(u[d]);
   qllg_dfree(links);
   return S;
+}
+
+qllg_stag *
+qllg_stag_create_asqtad(const int dims[4], double *const thin[4], const Fat7Coeffs *coef)
+{
+  return create_asqtad(dims, thin, coef, 0);
+}
+
+qllg_stag *
+qllg_stag_create_asqtad_fb(const int dims[4], double *const thin[4], const Fat7Coeffs *coef)
+{
+  return create_asqtad(dims, thin, coef, 1);
 }
 
 int

@@ -22,6 +22,37 @@ constexpr int kThreads = 256;
 
 int qllg_mr_disabled() { return qllg_get_param("dslash_mr") == 0; }
 
+// The link of one slot for output site `site` (parity p).  Double-stored
+// operators keep all slots.  Single-stored ones (a.fb, createStaggeredLinksFb)
+// keep the forward slots only, [NS/2][9][V], and a backward slot's link
+// -U(y)^dagger is made here from the forward link at y = x - mu (or x - 3mu),
+// the site whose spinor the slot reads (nb, of the other parity):
+// entry 3l+c of -U^dagger is (-re, im) of entry 3c+l of U, so the products
+// are bitwise those of the double-stored links (dslashFb2T and
+// V_vmeq_xMap_times_xVp, lib/stagDslash.c:110-257, lib/vla.c:1368-1393).
+template <int PL, int NS, typename T>
+__device__ __forceinline__ void slot_link(const qllg_stag_args &a, int mu, int back, int nk,
+                                          size_t V, size_t Vh, size_t loff, size_t site, size_t nb,
+                                          Cx<T> U[9])
+{
+  const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
+  if(!a.fb) {
+    LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+    return;
+  }
+  const int fslot = (NS == 16) ? (2*mu + nk) : mu;
+  if(!back) {
+    LinkIO<PL>::load(a.links, fslot, V, loff + site, a.lscale, U);
+    return;
+  }
+  Cx<T> F[9];
+  LinkIO<PL>::load(a.links, fslot, V, (Vh - loff) + nb, a.lscale, F);
+#pragma unroll
+  for(int l=0; l<3; l++)
+#pragma unroll
+    for(int c=0; c<3; c++) { U[3*l + c].r = -F[3*c + l].r; U[3*l + c].i = F[3*c + l].i; }
+}
+
 template <int PS, int PL, int NS, int NR>
 __global__ void __launch_bounds__(kThreads)
 stag_dslash(qllg_stag_args a)
@@ -64,11 +95,10 @@ stag_dslash(qllg_stag_args a)
         for(int back=0; back<2; back++) {
 #pragma unroll
           for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
-            const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
             const int d = (nk ? 3 : 1)*(back ? -1 : 1);
             const int k = nbr_index(G, x, mu, d);
             Cx<T> U[9], v[3];
-            LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+            slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, (size_t)k, U);
             SpinorIO<PS,3>::load(a.in, total, (size_t)k*NR + rhs, v);
 #pragma unroll
             for(int l=0; l<3; l++) {
@@ -191,11 +221,11 @@ stag_dslash_mr(qllg_stag_args a)
         for(int back=0; back<2; back++) {
 #pragma unroll
           for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
-            const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
             const int d = (nk ? 3 : 1)*(back ? -1 : 1);
-            const size_t kb = (size_t)nbr_index(G, x, mu, d)*NR + q*R;
+            const size_t nb = (size_t)nbr_index(G, x, mu, d);
+            const size_t kb = nb*NR + q*R;
             Cx<T> U[9];
-            LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+            slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
             if constexpr (v4) {
               // two rhs per 16-byte load and colour
 #pragma unroll
@@ -385,11 +415,10 @@ stag_dslash_compact(qllg_stag_args a)
       for(int back=0; back<2; back++) {
 #pragma unroll
         for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
-          const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
           const int d = (nk ? 3 : 1)*(back ? -1 : 1);
           const int k = nbr_index(G, x, mu, d);
           Cx<T> U[9], v[3];
-          LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+          slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, (size_t)k, U);
           SpinorIO<PS,3>::load(a.in, total, (size_t)k*NR + rhs, v);
 #pragma unroll
           for(int l=0; l<3; l++) {
@@ -806,7 +835,7 @@ bool variant_ok(const qllg_stag_args *a, int v)
   if(v == 0) return NR >= 4;
   if(v == 1) return NR >= 2;
   if(v == 2) return true;
-  return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 &&
+  return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
          a->g.Vh % kTileSites == 0 && vec4_ok(a) && qllg_get_param("dslash_tile") != 0;
 }
 
@@ -837,8 +866,8 @@ int tuned_variant(const qllg_stag_args *a)
   const int force = (int)qllg_get_param("dslash_variant");
   if(force >= 0 && force < kNumVariants && variant_ok<PS,PL,NS,NR>(a, force)) return force;
   char key[96];
-  snprintf(key, sizeof(key), "stag_dslash p%d/%d s%d n%d V%d (%d %d %d %d)", PS, PL, NS, NR,
-           a->g.V, a->g.L[0], a->g.L[1], a->g.L[2], a->g.L[3]);
+  snprintf(key, sizeof(key), "stag_dslash p%d/%d s%d%s n%d V%d (%d %d %d %d)", PS, PL, NS,
+           a->fb ? "fb" : "", NR, a->g.V, a->g.L[0], a->g.L[1], a->g.L[2], a->g.L[3]);
   int v = qllg_tune_lookup(key);
   if(v >= 0) return v;
   const int first = NR >= 4 ? 0 : 1;

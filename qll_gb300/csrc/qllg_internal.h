@@ -143,6 +143,8 @@ typedef struct {
   int compact;           /* threads over (site, flagged rhs of active) only;
                             modes 0 and 2, no norms */
   int no_tune;           /* caller must not allocate: no autotuning */
+  int fb;                /* single-stored links: forward slots only, [nslots/2][9][V];
+                            backward links made from them in the kernel */
   int dag;               /* Wilson only: gamma5 D gamma5 (projector signs flipped) */
   /* mode 3 (staggered CG, fused): Ap = a[rhs]*self - acc stays in registers,
    * then x += alpha self, r -= alpha Ap with alpha = 1/(a pnorm + vnorm) and

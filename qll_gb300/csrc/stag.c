@@ -60,6 +60,7 @@ struct qllg_stag {
   int ngraph_next;
   int graph_body;          /* body of the graph the current solve launched, 0: none */
   unsigned char shared[3]; /* links[p] belong to another operator */
+  int fb;                  /* single-stored: the nslots/2 forward slots only */
   /* continuous batching (qllg_batch_*): a fixed-width mixed CG whose
    * columns are admitted and retired independently */
   int batch_on;
@@ -87,6 +88,19 @@ vec_bytes(const qllg_stag *S, int prec, int nrhs)
   return qllg_spinor_bytes(prec, 3)*(size_t)S->g.Vh*nrhs;
 }
 
+/* link slots held in memory: all of them, or the forward half */
+static int
+stored_slots(const qllg_stag *S)
+{
+  return S->fb ? S->nslots/2 : S->nslots;
+}
+
+void
+qllg_stag_set_single_store(qllg_stag *S)
+{
+  S->fb = 1;
+}
+
 static int
 ensure_links(qllg_stag *S, int prec)
 {
@@ -97,10 +111,10 @@ ensure_links(qllg_stag *S, int prec)
     return -1;
   }
   size_t per = qllg_link_bytes(prec)*(size_t)S->g.V;
-  S->links[prec] = qllg_dmalloc(per*S->nslots);
+  S->links[prec] = qllg_dmalloc(per*stored_slots(S));
   if(!S->links[prec]) return -1;
   const double *src = S->links[QLLG_F64];
-  for(int s=0; s<S->nslots; s++) {
+  for(int s=0; s<stored_slots(S); s++) {
     if(qllg_k_link_convert(prec, (char *)S->links[prec] + per*s, S->lscale + s,
                            src + (size_t)s*18*S->g.V, S->g.V)) return -1;
   }
@@ -207,6 +221,7 @@ qllg_stag_share(qllg_stag *S)
   int dims[4] = {S->g.L[0], S->g.L[1], S->g.L[2], S->g.L[3]};
   qllg_stag *T = qllg_stag_alloc(dims, S->nslots, S->master);
   if(!T) return NULL;
+  T->fb = S->fb;
   for(int p=0; p<3; p++) {
     T->links[p] = S->links[p];
     T->shared[p] = S->links[p] != NULL;
@@ -240,7 +255,11 @@ qllg_stag_destroy(qllg_stag *S)
   free(S);
 }
 
-/* copy the operator's FP64 link slots to host arrays [V][18] */
+int qllg_k_mat_shift(int prec, void *out, const void *in, const qllg_geom *g, int mu, int len,
+                     int adj, double sgn);
+
+/* copy the operator's FP64 link slots to host arrays [V][18] (backward
+ * slots of a single-stored operator are made from its forward ones) */
 int
 qllg_stag_get_links(qllg_stag *S, double *const out[16])
 {
@@ -249,8 +268,25 @@ qllg_stag_get_links(qllg_stag *S, double *const out[16])
   void *st = qllg_stage(hb);
   if(!st) return -1;
   for(int s=0; s<S->nslots; s++) {
-    if(qllg_k_link_to_aos(QLLG_F64, (char *)S->links[QLLG_F64] + per*s, st, 1, S->g.V)) return -1;
-    if(qllg_d2h(out[s], st, hb)) return -1;
+    const char *src = (const char *)S->links[QLLG_F64] + per*s;
+    void *tmp = NULL;
+    if(S->fb) {
+      /* single-stored: forward slots as held, backward ones made here */
+      const int n16 = S->nslots == 16;
+      const int mu = n16 ? s/4 : s/2, back = n16 ? (s/2) & 1 : s & 1, nk = n16 ? s & 1 : 0;
+      src = (const char *)S->links[QLLG_F64] + per*(n16 ? 2*mu + nk : mu);
+      if(back) {
+        if(!(tmp = qllg_dmalloc(per)) ||
+           qllg_k_mat_shift(QLLG_F64, tmp, src, &S->g, mu, nk ? -3 : -1, 1, -1.0)) {
+          qllg_dfree(tmp);
+          return -1;
+        }
+        src = tmp;
+      }
+    }
+    int rc = qllg_k_link_to_aos(QLLG_F64, src, st, 1, S->g.V) || qllg_d2h(out[s], st, hb);
+    if(tmp) { qllg_sync(); qllg_dfree(tmp); }
+    if(rc) return -1;
   }
   return 0;
 }
@@ -266,7 +302,7 @@ qllg_stag_device_bytes(const qllg_stag *S)
 {
   size_t b = 0;
   for(int p=0; p<3; p++)
-    if(S->links[p] && !S->shared[p]) b += qllg_link_bytes(p)*(size_t)S->g.V*S->nslots;
+    if(S->links[p] && !S->shared[p]) b += qllg_link_bytes(p)*(size_t)S->g.V*stored_slots(S);
   for(int i=0; i<WS_N; i++) b += S->ws_bytes[i];
   if(S->bstage) b += 48*(size_t)S->g.Vh;
   return b;
@@ -287,6 +323,7 @@ dslash_half_x(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void
   A.out_parity = out_parity;
   A.nrhs = nrhs;
   A.nslots = S->nslots;
+  A.fb = S->fb;
   A.links = S->links[pl];
   A.lscale = S->lscale;
   A.in = in;
@@ -418,6 +455,7 @@ cg_iteration(qllg_stag *S, int ps, int pl, int nrhs, void *x, void *r, void *p, 
   A.out_parity = 0;
   A.nrhs = nrhs;
   A.nslots = S->nslots;
+  A.fb = S->fb;
   A.links = S->links[pl];
   A.lscale = S->lscale;
   A.in = v;
@@ -1081,6 +1119,7 @@ qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
   A.out_parity = out_parity;
   A.nrhs = nrhs;
   A.nslots = S->nslots;
+  A.fb = S->fb;
   A.links = S->links[prec];
   A.lscale = S->lscale;
   A.in = in_dev;
@@ -1300,30 +1339,29 @@ qllg_stag_solve_multishift(qllg_stag *S, int nrhs, void *const x[], void *const 
 }
 
 /* createStaggeredLinksFb (lib/stagDslash.c:464-519): only the forward
- * links u[2mu] (and u3[2mu]) are read; the backward slots -U^dagger(x-mu)
- * and -U3^dagger(x-3mu) that dslashFb2T applies on the fly
- * (V_vmeq_xMap_times_xVp, lib/vla.c:1368-1393) are built once on the GPU */
-int qllg_k_mat_shift(int prec, void *out, const void *in, const qllg_geom *g, int mu, int len,
-                     int adj, double sgn);
+ * links u[2mu] (and u3[2mu]) are read and held; the backward links
+ * -U^dagger(x-mu) and -U3^dagger(x-3mu) are applied on the fly as
+ * dslashFb2T does (V_vmeq_xMap_times_xVp, lib/vla.c:1368-1393), so the
+ * resident links take half the memory of the double-stored form */
 
 static qllg_stag *
 stag_create_fb(const int dims[4], void *const u[8], void *const u3[8], int dbl)
 {
   qllg_geom g;
   if(qllg_runtime_init() || qllg_geom_from_dims(&g, dims)) return NULL;
-  int nslots = u3 ? 16 : 8, prec = dbl ? QLLG_F64 : QLLG_F32;
+  /* single-stored: the forward slots [fat mu, long mu] (or [fat mu]) only;
+   * the kernels make the backward links from them */
+  int nslots = u3 ? 16 : 8, stored = nslots/2, prec = dbl ? QLLG_F64 : QLLG_F32;
   size_t per = qllg_link_bytes(prec)*(size_t)g.V, hb = (dbl ? 8 : 4)*18*(size_t)g.V;
-  char *links = qllg_dmalloc(per*nslots);
+  char *links = qllg_dmalloc(per*stored);
   void *stage = qllg_stage(hb);
   if(!links || !stage) { qllg_dfree(links); return NULL; }
   for(int mu=0; mu<4; mu++) {
     for(int nk=0; nk<(u3 ? 2 : 1); nk++) {
-      int fs = u3 ? 4*mu + nk : 2*mu;              /* forward slot */
-      int bs = u3 ? 4*mu + 2 + nk : 2*mu + 1;      /* backward slot */
+      const int fs = u3 ? 2*mu + nk : mu;
       const void *h = nk ? u3[2*mu] : u[2*mu];
       if(!h || qllg_h2d(stage, h, hb) ||
-         qllg_k_link_from_aos(prec, links + per*fs, NULL, stage, dbl, g.V) ||
-         qllg_k_mat_shift(prec, links + per*bs, links + per*fs, &g, mu, nk ? -3 : -1, 1, -1.0)) {
+         qllg_k_link_from_aos(prec, links + per*fs, NULL, stage, dbl, g.V)) {
         qllg_sync();
         qllg_dfree(links);
         return NULL;
@@ -1333,6 +1371,7 @@ stag_create_fb(const int dims[4], void *const u[8], void *const u3[8], int dbl)
   if(qllg_sync()) { qllg_dfree(links); return NULL; }
   qllg_stag *S = qllg_stag_alloc(dims, nslots, prec);
   if(!S) { qllg_dfree(links); return NULL; }
+  S->fb = 1;
   qllg_stag_attach_links(S, prec, links);
   return S;
 }

@@ -44,21 +44,23 @@ def _lib():
         L.qllg_server_stats.argtypes = [c_void_p, POINTER(ServerInfo)]
         L.qllg_server_destroy.argtypes = [c_void_p]
         L.qllg_server_destroy.restype = None
-        L.qllg_stag_create_asqtad.restype = c_void_p
-        L.qllg_stag_create_asqtad.argtypes = [POINTER(c_int), POINTER(c_void_p),
-                                              POINTER(qll.Fat7Coeffs)]
+        for fn in (L.qllg_stag_create_asqtad, L.qllg_stag_create_asqtad_fb):
+            fn.restype = c_void_p
+            fn.argtypes = [POINTER(c_int), POINTER(c_void_p), POINTER(qll.Fat7Coeffs)]
         L.qllg_stag_destroy.argtypes = [c_void_p]
         L.qllg_stag_destroy.restype = None
         _declared = True
     return L
 
 
-def asqtad_operator(dims, seed, eps):
-    """resident asqtad operator from seeded thin links (fat7 on the GPU)"""
+def asqtad_operator(dims, seed, eps, single_store=False):
+    """resident asqtad operator from seeded thin links (fat7 on the GPU);
+    single_store keeps the forward links only (half the link memory)"""
     L = _lib()
     thin = qll.gen_gauge(tuple(dims), seed, eps, ks=True)
     coef = qll.asqtad_coeffs()
-    S = L.qllg_stag_create_asqtad(qll.dims_c(tuple(dims)), qll.vp_array(thin), ctypes.byref(coef))
+    create = L.qllg_stag_create_asqtad_fb if single_store else L.qllg_stag_create_asqtad
+    S = create(qll.dims_c(tuple(dims)), qll.vp_array(thin), ctypes.byref(coef))
     if not S:
         raise RuntimeError(qll.last_error())
     return c_void_p(S)

@@ -293,3 +293,74 @@ def test_wilson_cgnr_matches_oracle(mode):
     else:
         assert info.reliable_updates > 0
     L.qllg_wilson_destroy(ctypes.c_void_p(W))
+
+
+def test_single_stored_operator_matches_double_stored():
+    """qllg_stag_create_asqtad_fb holds the 8 forward slots only and makes
+    the backward links in the kernels: the Dslash (every precision and rhs
+    count), the links it reports and a mixed solve are bitwise those of the
+    double-stored operator, at about half the resident link bytes"""
+    torch = pytest.importorskip("torch")
+    L = qll.load()
+    vp = ctypes.c_void_p
+    for fn in ("qllg_stag_create_asqtad", "qllg_stag_create_asqtad_fb"):
+        getattr(L, fn).restype = vp
+        getattr(L, fn).argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(vp),
+                                   ctypes.POINTER(qll.Fat7Coeffs)]
+    L.qllg_stag_vec_bytes.restype = ctypes.c_size_t
+    L.qllg_stag_vec_bytes.argtypes = [vp, c_int, c_int]
+    L.qllg_stag_dslash_device.argtypes = [vp, c_int, c_int, c_int, vp, vp]
+    L.qllg_stag_device_bytes.restype = ctypes.c_size_t
+    L.qllg_stag_device_bytes.argtypes = [vp]
+    L.qllg_stag_get_links.argtypes = [vp, ctypes.POINTER(vp)]
+    dims = (8, 8, 8, 8)
+    th = qll.gen_gauge(dims, 1005, 0.3, ks=True)
+    c = qll.asqtad_coeffs()
+    S2 = vp(L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(th), byref(c)))
+    S1 = vp(L.qllg_stag_create_asqtad_fb(qll.dims_c(dims), qll.vp_array(th), byref(c)))
+    assert S2.value and S1.value, qll.last_error()
+    assert L.qllg_stag_device_bytes(S1)*2 == L.qllg_stag_device_bytes(S2)
+    V = int(np.prod(dims))
+    l2 = [np.zeros((V, 18)) for _ in range(16)]
+    l1 = [np.zeros((V, 18)) for _ in range(16)]
+    assert L.qllg_stag_get_links(S2, qll.vp_array(l2)) == 0
+    assert L.qllg_stag_get_links(S1, qll.vp_array(l1)) == 0
+    for k in range(16):
+        assert np.array_equal(l1[k], l2[k]), k
+    g = torch.Generator(device="cuda").manual_seed(5)
+    for prec in (0, 1, 2):
+        for nrhs in (1, 4, 16):
+            n = L.qllg_stag_vec_bytes(S2, prec, nrhs)
+            if prec == 0:
+                src = torch.randn(n//8, dtype=torch.float64, device="cuda", generator=g)
+            else:
+                src = torch.randn(n//4, dtype=torch.float32, device="cuda", generator=g)
+                if prec == 2:
+                    src = src.view(-1, 4)
+                    src[:, 3] = 1.0
+                    src = src.reshape(-1)
+            for parity in (0, 1):
+                o2, o1 = torch.zeros_like(src), torch.zeros_like(src)
+                torch.cuda.synchronize()
+                assert L.qllg_stag_dslash_device(S2, prec, nrhs, parity, vp(o2.data_ptr()),
+                                                 vp(src.data_ptr())) == 0, qll.last_error()
+                assert L.qllg_stag_dslash_device(S1, prec, nrhs, parity, vp(o1.data_ptr()),
+                                                 vp(src.data_ptr())) == 0, qll.last_error()
+                torch.cuda.synchronize()
+                assert torch.equal(o1.view(torch.uint8), o2.view(torch.uint8)), (prec, nrhs, parity)
+    nrhs = 8
+    masses = (c_double*nrhs)(*[0.05 + 0.01*k for k in range(nrhs)])
+    bs = [qll.gen_source(dims, 9000 + k, 6, "even") for k in range(nrhs)]
+    sol = []
+    for S in (S2, S1):
+        xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+        info = qll.SolveInfo()
+        its = L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), masses, 1e-16, 5000,
+                                qll.SOLVE_MIXED_SINGLE, byref(info))
+        assert its > 0, qll.last_error()
+        sol.append((list(info.iters[:nrhs]), xs))
+    assert sol[0][0] == sol[1][0]
+    for k in range(nrhs):
+        assert np.array_equal(sol[0][1][k], sol[1][1][k])
+    L.qllg_stag_destroy(S1)
+    L.qllg_stag_destroy(S2)
