@@ -92,6 +92,22 @@ int qllg_stag_solve(qllg_stag *S, int nrhs, void *const x[], void *const b[],
 int qllg_stag_solve_device(qllg_stag *S, int nrhs, void *x_dev, const void *b_dev,
                            const double mass[], double rsq, int maxits, int mode,
                            qllg_solve_info *info);
+/* embedding codes' layouts (the QDP/QOP pattern of embedqop.c:193-258,
+ * whose packM/packV repack on the host, qopstag.c:123-196): the caller's
+ * arrays as they are, reordered and transposed on the GPU.  Foreign site s
+ * is QLL site perm[s] (perm NULL: the same order, as MILC's even-first
+ * order is for one rank); links [V][18] row-major (entry 3*row + col) when
+ * row_major, else column-major; fat[8]/lng[8] double-stored slots in
+ * createStaggeredLinks order.  Vectors: FP64 [V][6] host arrays in the
+ * foreign order, of which upload reads the even sites and download writes
+ * all sites (zero at the odd ones); the device side is the even-site
+ * multi-rhs layout of qllg_stag_vec_alloc. */
+qllg_stag *qllg_stag_create_foreign(const int dims[4], double *const fat[8], double *const lng[8],
+                                    const int *perm, int row_major);
+int qllg_stag_vec_upload_foreign(qllg_stag *S, void *v_dev, int nrhs, void *const h[],
+                                 const int *perm);
+int qllg_stag_vec_download_foreign(qllg_stag *S, const void *v_dev, int nrhs, void *const h[],
+                                   const int *perm);
 /* multi-rhs multishift solve (solveMulti2 of lib/stagDslash.c:625-657 for
  * many rhs): for every rhs r and shift k, (m^2 + shift_k - D_eo D_oe)
  * x[r*nshift + k] = b[r] on the even sites, each to |r|^2 < rsq |b|^2.

@@ -57,6 +57,42 @@ __global__ void to_aos(const void *dev, S *stage, int nsites, int nrhs, size_t r
   }
 }
 
+// site order and matrix convention of an embedding code (QDP/QLA or MILC)
+// <-> the reference's one-lane order: foreign site s is QLL site perm[s]
+// (identity when perm is NULL); with transpose, n = 18 reals are a 3x3
+// complex matrix stored row-major (entry 3*row + col), the reference's
+// being column-major (packM/unpackM's transpose, qopstag.c:123-196)
+__global__ void aos_from_foreign_k(double *out, const double *in, const int *perm, int V, int n,
+                                   int transpose)
+{
+  for(size_t s = (size_t)blockIdx.x*blockDim.x + threadIdx.x; s < (size_t)V;
+      s += (size_t)gridDim.x*blockDim.x) {
+    const size_t q = perm ? (size_t)perm[s] : s;
+    const double *src = in + s*n;
+    double *dst = out + q*n;
+    if(transpose) {
+#pragma unroll
+      for(int r=0; r<3; r++)
+#pragma unroll
+        for(int c=0; c<3; c++) {
+          dst[2*(3*c + r)] = src[2*(3*r + c)];
+          dst[2*(3*c + r) + 1] = src[2*(3*r + c) + 1];
+        }
+    } else {
+      for(int e=0; e<n; e++) dst[e] = src[e];
+    }
+  }
+}
+
+__global__ void aos_to_foreign_k(double *out, const double *in, const int *perm, int V, int n)
+{
+  for(size_t s = (size_t)blockIdx.x*blockDim.x + threadIdx.x; s < (size_t)V;
+      s += (size_t)gridDim.x*blockDim.x) {
+    const size_t q = perm ? (size_t)perm[s] : s;
+    for(int e=0; e<n; e++) out[s*n + e] = in[q*n + e];
+  }
+}
+
 // one column (rhs col of nrhs) of an FP64 device vector <-> a contiguous
 // [nsites][6] double array (the continuous-batching solver moves requests
 // in and out of single columns while the others keep running)
@@ -438,6 +474,22 @@ qllg_k_spinor_to_aos(int prec, const void *dev, void *stage, int dbl, int nsites
     else to_aos<P,NC,float><<<g,kT,0,st>>>(dev, (float *)stage, nsites, nrhs, rs);
   });
   return done("to_aos");
+}
+
+extern "C" int
+qllg_k_aos_from_foreign(double *out, const double *in, const int *perm, int V, int n, int transpose)
+{
+  if(transpose && n != 18) { qllg_set_error("aos_from_foreign: transpose needs 18 reals"); return -1; }
+  aos_from_foreign_k<<<grid_for((size_t)V, 0, 0), kT, 0, qllg_stream()>>>(out, in, perm, V, n,
+                                                                          transpose);
+  return done("aos_from_foreign");
+}
+
+extern "C" int
+qllg_k_aos_to_foreign(double *out, const double *in, const int *perm, int V, int n)
+{
+  aos_to_foreign_k<<<grid_for((size_t)V, 0, 0), kT, 0, qllg_stream()>>>(out, in, perm, V, n);
+  return done("aos_to_foreign");
 }
 
 extern "C" int

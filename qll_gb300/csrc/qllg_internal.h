@@ -220,6 +220,11 @@ typedef struct {
 int qllg_k_mcg_admit(int ps, void *x64, void *r64, void *xs, void *rs, void *p, const void *b,
                      int nsites, int nrhs, qllg_cg_scalars *s, const qllg_admit_args *ad,
                      qllg_redbuf *rb);
+/* foreign site order / row-major matrices <-> the reference's order, FP64
+ * [V][n] device arrays (foreign site s is QLL site perm[s]) */
+int qllg_k_aos_from_foreign(double *out, const double *in, const int *perm, int V, int n,
+                            int transpose);
+int qllg_k_aos_to_foreign(double *out, const double *in, const int *perm, int V, int n);
 /* one column of an FP64 [3][nsites][nrhs] device vector <-> a contiguous
  * [nsites][6] device array */
 int qllg_k_column_from_aos(void *dev, const double *stage, int nsites, int nrhs, int col);

@@ -1241,6 +1241,106 @@ cgms_host(qllg_stag *S, void *const x[], const void *y, const double shifts[], i
   return its;
 }
 
+/* ------------------------------------------- foreign layouts (QDP, MILC) */
+/* The embedding pattern of the reference (embedqop.c:193-258) repacks a
+ * QOP/QDP code's double-stored links and vectors on the host (packM/packV,
+ * qopstag.c:123-196: a site reordering and a matrix transpose) before
+ * createStaggeredSolver.  Here the caller hands its arrays as they are:
+ * foreign site s is QLL site perm[s] (NULL: the same order, as MILC's
+ * even-first order is for one rank), matrices row-major when row_major;
+ * the reordering and transpose run on the GPU.  fat[8]/lng[8] are the
+ * double-stored slots in createStaggeredLinks order. */
+static int *
+perm_upload(const int *perm, int V)
+{
+  if(!perm) return NULL;
+  int *d = qllg_dmalloc(sizeof(int)*(size_t)V);
+  if(d && qllg_h2d(d, perm, sizeof(int)*(size_t)V)) { qllg_dfree(d); return NULL; }
+  return d;
+}
+
+qllg_stag *
+qllg_stag_create_foreign(const int dims[4], double *const fat[8], double *const lng[8],
+                         const int *perm, int row_major)
+{
+  qllg_geom g;
+  if(qllg_runtime_init() || qllg_geom_from_dims(&g, dims)) return NULL;
+  const int nslots = lng ? 16 : 8;
+  const size_t hb = 8*18*(size_t)g.V, per = qllg_link_bytes(QLLG_F64)*(size_t)g.V;
+  int *dperm = perm_upload(perm, g.V);
+  double *in = qllg_dmalloc(hb), *qll = qllg_dmalloc(hb);
+  char *links = qllg_dmalloc(per*nslots);
+  qllg_stag *S = NULL;
+  if((perm && !dperm) || !in || !qll || !links) goto out;
+  for(int s=0; s<nslots; s++) {
+    const double *h = (nslots == 16) ? ((s & 1) ? lng[s/2] : fat[s/2]) : fat[s];
+    if(!h) { qllg_set_error("foreign links: slot %d is NULL", s); goto out; }
+    if(qllg_h2d(in, h, hb) || qllg_k_aos_from_foreign(qll, in, dperm, g.V, 18, row_major) ||
+       qllg_k_link_from_aos(QLLG_F64, links + per*s, NULL, qll, 1, g.V)) goto out;
+  }
+  if(qllg_sync()) goto out;
+  S = qllg_stag_alloc(dims, nslots, QLLG_F64);
+  if(S) { qllg_stag_attach_links(S, QLLG_F64, links); links = NULL; }
+out:
+  qllg_sync();
+  qllg_dfree(dperm);
+  qllg_dfree(in);
+  qllg_dfree(qll);
+  qllg_dfree(links);
+  return S;
+}
+
+/* device FP64 vector of nrhs rhs (even sites) <-> host arrays [V][6] in the
+ * foreign site order (upload reads their even sites, download writes all
+ * sites, zero at the odd ones) */
+int
+qllg_stag_vec_upload_foreign(qllg_stag *S, void *v_dev, int nrhs, void *const h[],
+                             const int *perm)
+{
+  const int V = S->g.V;
+  const size_t hb = 48*(size_t)V;
+  int *dperm = perm_upload(perm, V);
+  double *in = qllg_dmalloc(hb), *qll = qllg_dmalloc(hb*nrhs);
+  int rc = -1;
+  if((perm && !dperm) || !in || !qll) goto out;
+  for(int r=0; r<nrhs; r++)
+    if(qllg_h2d(in, h[r], hb) || qllg_k_aos_from_foreign(qll + 6*(size_t)V*r, in, dperm, V, 6, 0))
+      goto out;
+  /* the even half of each reordered block, rhs blocks 6V reals apart */
+  rc = qllg_k_spinor_from_aos(QLLG_F64, v_dev, qll, 1, S->g.Vh, 3, nrhs, 6*(size_t)V);
+out:
+  qllg_sync();
+  qllg_dfree(dperm);
+  qllg_dfree(in);
+  qllg_dfree(qll);
+  return rc;
+}
+
+int
+qllg_stag_vec_download_foreign(qllg_stag *S, const void *v_dev, int nrhs, void *const h[],
+                               const int *perm)
+{
+  const int V = S->g.V;
+  const size_t hb = 48*(size_t)V;
+  int *dperm = perm_upload(perm, V);
+  double *out = qllg_dmalloc(hb), *qll = qllg_dmalloc(hb*nrhs);
+  int rc = -1;
+  if((perm && !dperm) || !out || !qll) goto out;
+  /* odd sites of the reordered blocks are zero, as the solvers leave them */
+  if(qllg_check_cuda(cudaMemsetAsync(qll, 0, hb*nrhs, qllg_stream()), "clear")) goto out;
+  if(qllg_k_spinor_to_aos(QLLG_F64, v_dev, qll, 1, S->g.Vh, 3, nrhs, 6*(size_t)V)) goto out;
+  for(int r=0; r<nrhs; r++)
+    if(qllg_k_aos_to_foreign(out, qll + 6*(size_t)V*r, dperm, V, 6) || qllg_d2h(h[r], out, hb))
+      goto out;
+  rc = 0;
+out:
+  qllg_sync();
+  qllg_dfree(dperm);
+  qllg_dfree(out);
+  qllg_dfree(qll);
+  return rc;
+}
+
 /* ------------------------------------------------ multi-rhs multishift */
 /* For every rhs r and shift k: (m^2 + shift_k - D_eo D_oe) x[r*nshift + k]
  * = b[r] on the even sites, stopping at |r_k|^2 < rsq |b_r|^2.

@@ -337,6 +337,63 @@ def test_mixed_solve_with_each_dslash_variant(variant):
     L.qllg_stag_destroy(S)
 
 
+def test_foreign_layout_adapters():
+    """links and vectors in an embedding code's layout (a shuffled site
+    order, row-major matrices) reordered on the GPU give bitwise the
+    operator and the solution of the reference-ordered arrays"""
+    L, S, u, u3 = _native()
+    vp = ctypes.c_void_p
+    L.qllg_stag_create_foreign.restype = vp
+    L.qllg_stag_create_foreign.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(vp),
+                                           ctypes.POINTER(vp), ctypes.POINTER(c_int), c_int]
+    for fn in ("qllg_stag_vec_upload_foreign", "qllg_stag_vec_download_foreign"):
+        getattr(L, fn).argtypes = [vp, vp, c_int, ctypes.POINTER(vp), ctypes.POINTER(c_int)]
+    V = int(np.prod(DIMS))
+    rng = np.random.default_rng(12)
+    perm = rng.permutation(V).astype(np.int32)          # foreign site s is QLL site perm[s]
+
+    def foreign(a, n):
+        f = np.empty_like(a)
+        f[np.arange(V)] = a[perm]
+        if n == 18:                                       # column-major -> row-major
+            f = f.reshape(V, 3, 3, 2).transpose(0, 2, 1, 3).reshape(V, 18)
+        return np.ascontiguousarray(f)
+
+    fu = [foreign(a, 18) for a in u]
+    fu3 = [foreign(a, 18) for a in u3]
+    pp = perm.ctypes.data_as(ctypes.POINTER(c_int))
+    F = vp(L.qllg_stag_create_foreign(qll.dims_c(DIMS), qll.vp_array(fu), qll.vp_array(fu3), pp, 1))
+    assert F.value, qll.last_error()
+    nrhs = 4
+    masses = (c_double*nrhs)(0.05, 0.1, 0.2, 0.5)
+    bs = [qll.gen_source(DIMS, 9100 + k, 6, "even") for k in range(nrhs)]
+    # reference-ordered solve on the reference-ordered operator
+    xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+    info = qll.SolveInfo()
+    assert L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), masses, 1e-16, 5000,
+                             qll.SOLVE_DOUBLE, byref(info)) > 0, qll.last_error()
+    # foreign-ordered arrays through the adapters
+    fb = [foreign(b, 6) for b in bs]
+    bd, xd = vp(L.qllg_stag_vec_alloc(F, nrhs)), vp(L.qllg_stag_vec_alloc(F, nrhs))
+    assert L.qllg_stag_vec_upload_foreign(F, bd, nrhs, qll.vp_array(fb), pp) == 0, qll.last_error()
+    info2 = qll.SolveInfo()
+    assert L.qllg_stag_solve_device(F, nrhs, xd, bd, masses, 1e-16, 5000, qll.SOLVE_DOUBLE,
+                                    byref(info2)) > 0, qll.last_error()
+    fx = [np.full_like(bs[0], np.nan) for _ in range(nrhs)]
+    assert L.qllg_stag_vec_download_foreign(F, xd, nrhs, qll.vp_array(fx), pp) == 0
+    assert list(info.iters[:nrhs]) == list(info2.iters[:nrhs])
+    Vh = V//2
+    for k in range(nrhs):
+        back = np.empty_like(fx[k])
+        back[perm] = fx[k]                                # to the reference order
+        assert np.array_equal(back[:Vh], xs[k][:Vh]), k
+        assert np.all(back[Vh:] == 0)
+    L.qllg_stag_vec_free(bd)
+    L.qllg_stag_vec_free(xd)
+    L.qllg_stag_destroy(F)
+    L.qllg_stag_destroy(S)
+
+
 def test_unknown_parameter_is_refused():
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
