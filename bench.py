@@ -73,6 +73,23 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws, device="cuda"):
+    """the largest x over the ranks of the job (the slowest rank's time)"""
+    if ws == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seeds(rank):
+    """gauge and source seeds of one replica: every rank solves its own
+    configuration and sources (replicas, no collective in the data path)"""
+    return SEED_GAUGE + 17*rank, SEED_SRC + 100*rank
+
+
 class Clocks:
     """nvidia-smi sampling of SM clock and throttle reasons during a region"""
 
@@ -147,14 +164,15 @@ def run_gpu(args):
     L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
 
     t0 = time.time()
-    thin = qll.gen_gauge(DIMS, SEED_GAUGE + 17*rank, EPS, ks=True)
+    seed_gauge, seed_src = replica_seeds(rank)
+    thin = qll.gen_gauge(DIMS, seed_gauge, EPS, ks=True)
     coef = qll.asqtad_coeffs()
     S = L.qllg_stag_create_asqtad(qll.dims_c(DIMS), qll.vp_array(thin), ctypes.byref(coef))
     if not S:
         raise RuntimeError(qll.last_error())
     S = ctypes.c_void_p(S)
     del thin
-    srcs = [qll.gen_source(DIMS, SEED_SRC + 100*rank + r, 6, "even") for r in range(NRHS)]
+    srcs = [qll.gen_source(DIMS, seed_src + r, 6, "even") for r in range(NRHS)]
     xs = [np.zeros_like(srcs[0]) for _ in range(NRHS)]
     masses = (ctypes.c_double*NRHS)(*([MASS]*NRHS))
     b_dev = L.qllg_stag_vec_alloc(S, NRHS)
@@ -221,12 +239,7 @@ def run_gpu(args):
     fcnt, ftot = ctypes.c_int(), ctypes.c_double()
     L.qllg_timing_read(b"stag_cg_fused_f32_n16", ctypes.byref(fcnt), ctypes.byref(ftot))
     L.qllg_timing_enable(0)
-    t_max = ms
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(ms, ws)
     value = ws*NRHS*args.steps/(t_max*1e-3)
 
     # end to end through the host-array API: H2D of the sources and D2H of
@@ -242,11 +255,7 @@ def run_gpu(args):
         if its < 0:
             raise RuntimeError(qll.last_error())
     torch.cuda.synchronize()
-    te = time.time() - te
-    if ws > 1:
-        t = torch.tensor([te], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        te = float(t.item())
+    te = max_over_ranks(time.time() - te, ws)
     e2e = ws*NRHS*e2e_steps/te
     Vh = srcs[0].shape[0]//2
     bytes_io = NRHS*Vh*6*8
