@@ -216,8 +216,8 @@ def run_gpu(args):
     n0 = L.qllg_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     iters, truer = [], []
-    with Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                             else "/tmp", "bench_clocks_r%d.csv" % rank)) as clk:
+    with Clocks(os.path.join(os.environ.get("QLLG_CLOCKS_DIR", "/tmp"),
+                             "bench_clocks_r%d.csv" % rank)) as clk:
         torch.cuda.nvtx.range_push("timed")
         ev0.record(stream)
         for _ in range(args.steps):
@@ -261,8 +261,9 @@ def run_gpu(args):
     bytes_io = NRHS*Vh*6*8
 
     # roofline of the dominant kernel: the 16-rhs FP32 asqtad half-Dslash
-    # (D_oe p).  Algorithmic bytes per output site and rhs, SURVEY.md 8(d):
-    # 16 neighbour spinors + 1 store, links shared by the 16 rhs:
+    # (D_oe p).  Algorithmic bytes per output site and rhs (the lattice
+    # convention: 16 neighbour spinor loads + 1 store, links shared by the
+    # 16 rhs):
     # (8*18*4 + 8*18*4)/16 + 17*(6*4) = 480 B
     per_site_rhs = (8*18*4 + 8*18*4)/16 + 17*(6*4)
     launch_bytes = per_site_rhs*Vh*NRHS

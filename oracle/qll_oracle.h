@@ -104,8 +104,8 @@ void or_gamma(int d, double g[32]);
                            real mass, int sign, const real *y,               \
                            const char *sub);                                 \
   /* wilsonSolve (lib/wilsonDslash.c:287-364) with the norms over all 24     \
-   * reals of a site (the reference sums a 6-real window, which reads        \
-   * memory that was never written: see the design doc) */                        \
+   * reals of a site (the reference sums a 6-real window, :308,310, which    \
+   * reads memory that was never written) */                                 \
   int or_wilson_solve##S(const int dims[4], real *x, real *const u[8],       \
                          real mass, const real *y, double rsq, int maxits,   \
                          int noscale);                                       \
