@@ -263,18 +263,21 @@ def run_gpu(args):
     # roofline of the dominant kernel: the 16-rhs FP32 asqtad half-Dslash
     # (D_oe p).  Algorithmic bytes per output site and rhs (the lattice
     # convention: 16 neighbour spinor loads + 1 store, links shared by the
-    # 16 rhs):
-    # (8*18*4 + 8*18*4)/16 + 17*(6*4) = 480 B
-    per_site_rhs = (8*18*4 + 8*18*4)/16 + 17*(6*4)
+    # 16 rhs; Naik links 12 reals with reconstruct-12, else 18):
+    # (8*18*4 + 8*naik*4)/16 + 17*(6*4) = 480 B (18) or 468 B (12)
+    L.qllg_stag_recon12.argtypes = [ctypes.c_void_p]
+    recon = bool(L.qllg_stag_recon12(S))
+    naik = 12 if recon else 18
+    per_site_rhs = (8*18*4 + 8*naik*4)/16 + 17*(6*4)
     launch_bytes = per_site_rhs*Vh*NRHS
     avg_ms = tot.value/max(cnt.value, 1)
     achieved = launch_bytes/(avg_ms*1e-3)/1e9
     pk = peaks()
     peak = pk.get("hbm_gbs")
-    compulsory = (8*18*4 + 8*18*4)/16 + 2*(6*4)
+    compulsory = (8*18*4 + 8*naik*4)/16 + 2*(6*4)
     # the fused D_eo + CG update: links + 16 neighbours + self + x and r
     # read and written
-    fused_bytes = ((8*18*4 + 8*18*4)/16 + 17*(6*4) + 4*(6*4))*Vh*NRHS
+    fused_bytes = ((8*18*4 + 8*naik*4)/16 + 17*(6*4) + 4*(6*4))*Vh*NRHS
     favg = ftot.value/max(fcnt.value, 1)
 
     # the 16-bit-storage mode, once (not timed in the headline)
@@ -301,7 +304,8 @@ def run_gpu(args):
                 "d2h_bytes_per_step": bytes_io},
         "fused_cg_kernel": {"avg_launch_ms": favg, "launches": fcnt.value,
                             "gbs": fused_bytes/(favg*1e-3)/1e9 if favg > 0 else None},
-        "roofline": {"kernel": "stag_dslash_mr<f32,f32,16 slots,16 rhs,4 rhs/thread>", "bound": "hbm",
+        "roofline": {"kernel": "stag_dslash_mr<f32,%s,16 slots,16 rhs,4 rhs/thread>"
+                               % ("f32 reconstruct-12" if recon else "f32"), "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved/peak if peak else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else None,
@@ -657,7 +661,7 @@ def run_dslash_only(args):
     stream = torch.cuda.current_stream()
     L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
     dims = tuple(int(v) for v in args.dims.split(","))
-    prec = {"f64": 0, "f32": 1, "i16": 2}[args.prec]
+    prec = {"f64": 0, "f32": 1, "i16": 2, "f32r": 3}[args.prec]
     thin = qll.gen_gauge(dims, SEED_GAUGE, EPS, ks=True)
     coef = qll.asqtad_coeffs()
     S = ctypes.c_void_p(L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(thin),
@@ -686,9 +690,10 @@ def run_dslash_only(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)/args.launches
     Vh = int(np.prod(dims))//2
-    bs = {0: 8, 1: 4, 2: 2}[prec]
+    bs = {0: 8, 1: 4, 2: 2, 3: 4}[prec]
     ns = 4 if prec == 2 else 0
-    per = (8*18*bs + 8*18*bs)/args.nrhs + 17*(6*bs + ns)
+    naik_reals = 12 if prec == 3 else 18
+    per = (8*18*bs + 8*naik_reals*bs)/args.nrhs + 17*(6*bs + ns)
     print(json.dumps({"dslash_only": {"dims": dims, "nrhs": args.nrhs, "prec": args.prec,
                                       "params": args.param, "autotune": autotune_report(L),
                                       "ms": ms, "algorithmic_gbs": per*Vh*args.nrhs/(ms*1e-3)/1e9,
@@ -753,7 +758,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--dslash-only", action="store_true")
     ap.add_argument("--dims", default="32,32,32,64")
-    ap.add_argument("--prec", default="f32", choices=["f64", "f32", "i16"])
+    ap.add_argument("--prec", default="f32", choices=["f64", "f32", "i16", "f32r"])
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--launches", type=int, default=20)
     ap.add_argument("--solve-only", action="store_true")

@@ -127,8 +127,9 @@ int qllg_stag_vec_upload(qllg_stag *S, void *v_dev, int nrhs, void *const h[]);
 int qllg_stag_vec_download(qllg_stag *S, const void *v_dev, int nrhs, void *const h[]);
 
 /* the half Dslash out = D in (output sites of out_parity) on device vectors
- * of nrhs rhs, precision prec (0 FP64, 1 FP32, 2 16-bit) in the library
- * layout; links of that precision are derived from FP64 on first use */
+ * of nrhs rhs, precision prec (0 FP64, 1 FP32, 2 16-bit, 3 FP32 with the
+ * reconstruct-12 links) in the library layout; links of that precision are
+ * derived from FP64 on first use */
 int qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *out_dev,
                             const void *in_dev);
 
@@ -150,6 +151,13 @@ int qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, vo
 int qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
                                    void *out_dev, const void *in_dev, double *norm2_dev);
 size_t qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs);
+/* 1 when the mixed FP32 solves of S use reconstruct-12 links: the 8 Naik
+ * slots held as rows 0 and 1 (48 of 72 bytes) and row 2 rebuilt in the
+ * kernel as s conj(r0 x r1)/|r0|, which holds for a real multiple of an
+ * SU(3) matrix (the three-link Naik products of SU(3) links).  Derived on
+ * first use when the "links_recon12" parameter is on and every Naik link
+ * passes the check; 0 otherwise (plain FP32 links). */
+int qllg_stag_recon12(qllg_stag *S);
 
 /* neighbour table of slot s for the output sites of a parity, as QLL site
  * indices (host int[V/2]); the GPU computes it with the Dslash kernel's own
@@ -246,7 +254,8 @@ void qllg_server_destroy(qllg_server *V);
  * time the Dslash variants of each new launch shape and keep the fastest),
  * "dslash_tile" (1: the shared-memory-staged variant may be chosen),
  * "dslash_variant" (-1: autotuned; 0-3 forces 4, 2 or 1 rhs per thread or
- * the staged variant where it applies); returns -1 for an unknown name */
+ * the staged variant where it applies), "links_recon12" (0; 1: reconstruct-
+ * 12 Naik links in the mixed FP32 solves); returns -1 for an unknown name */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);
 

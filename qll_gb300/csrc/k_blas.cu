@@ -222,6 +222,55 @@ __global__ void link_from_f64(void *dev, const float *scale, const double *in, i
   }
 }
 
+// FP64 slot -> reconstruct-12 FP32 (see LinkR): the Naik rows are rounded
+// to FP32 first and row 2 rebuilt from the rounded rows exactly as the
+// Dslash rebuilds it; the sign is the one that matches the stored row 2,
+// and a link whose row 2 does not follow from rows 0, 1 (not c W with W in
+// SU(3)) raises *bad
+__global__ void link_to_f32r_k(char *out, const double *in, int V, int naik, unsigned char *signs,
+                               int bit, int *bad)
+{
+  const double2 *d = (const double2 *)in;
+  GRID_LOOP(i, (size_t)V) {
+    Cx<float> m[9];
+    double2 e[9];
+#pragma unroll
+    for(int k=0; k<9; k++) { e[k] = d[k*(size_t)V + i]; m[k].r = (float)e[k].x; m[k].i = (float)e[k].y; }
+    if(!naik) {
+      float4 *q = (float4 *)out;
+#pragma unroll
+      for(int k=0; k<4; k++)
+        q[k*(size_t)V + i] = make_float4(m[2*k].r, m[2*k].i, m[2*k + 1].r, m[2*k + 1].i);
+      ((float2 *)(out + 64*(size_t)V))[i] = make_float2(m[8].r, m[8].i);
+      continue;
+    }
+    float4 *q = (float4 *)out;
+    q[i] = make_float4(m[0].r, m[0].i, m[3].r, m[3].i);
+    q[(size_t)V + i] = make_float4(m[6].r, m[6].i, m[1].r, m[1].i);
+    q[2*(size_t)V + i] = make_float4(m[4].r, m[4].i, m[7].r, m[7].i);
+    Cx<float> r[9];
+#pragma unroll
+    for(int k=0; k<9; k++) r[k] = m[k];
+    LinkR::rebuild_row2(r, false);
+    double dot = 0, n2 = 0, err = 0;
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      dot += e[3*c + 2].x*r[3*c + 2].r + e[3*c + 2].y*r[3*c + 2].i;
+      n2 += e[3*c + 2].x*e[3*c + 2].x + e[3*c + 2].y*e[3*c + 2].y;
+    }
+    const bool neg = dot < 0;
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      const double xr = (neg ? -r[3*c + 2].r : r[3*c + 2].r) - e[3*c + 2].x;
+      const double xi = (neg ? -r[3*c + 2].i : r[3*c + 2].i) - e[3*c + 2].y;
+      err += xr*xr + xi*xi;
+    }
+    if(!(err <= 1e-10*n2)) atomicOr(bad, 1);       // relative 1e-5
+    unsigned char sgn = bit ? signs[i] : 0;
+    signs[i] = (unsigned char)(sgn | ((neg ? 1 : 0) << bit));
+  }
+}
+
 // ------------------------------------------------------------ axpby/norm
 template <int PY, int PX, int NC, int NR>
 __global__ void axpby_k(void *y, const void *x, const double *a, double a0,
@@ -588,6 +637,15 @@ qllg_k_link_convert(int prec, void *out, float *scale, const double *in, int V)
     return -1;
   }
   return done("link_convert");
+}
+
+extern "C" int
+qllg_k_link_to_f32r(void *out, const double *in, int V, int naik, unsigned char *signs, int bit,
+                    int *bad)
+{
+  link_to_f32r_k<<<grid_for((size_t)V, 0, 0), kT, 0, qllg_stream()>>>((char *)out, in, V, naik,
+                                                                      signs, bit, bad);
+  return done("link_to_f32r");
 }
 
 extern "C" int

@@ -8,6 +8,7 @@ using namespace qk;
 extern "C" int qllg_k_stag_dslash_f64(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_f32(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_i16(const qllg_stag_args *a);
+extern "C" int qllg_k_stag_dslash_f32r(const qllg_stag_args *a);
 
 namespace {
 
@@ -40,6 +41,7 @@ qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
   if(ps == QLLG_F64 && pl == QLLG_F64) return qllg_k_stag_dslash_f64(a);
   if(ps == QLLG_F32 && pl == QLLG_F32) return qllg_k_stag_dslash_f32(a);
   if(ps == QLLG_I16 && pl == QLLG_I16) return qllg_k_stag_dslash_i16(a);
+  if(ps == QLLG_F32 && pl == QLLG_F32R) return qllg_k_stag_dslash_f32r(a);
   qllg_set_error("stag_dslash: unsupported precision pair %d/%d", ps, pl);
   return -1;
 }

@@ -30,27 +30,61 @@ int qllg_mr_disabled() { return qllg_get_param("dslash_mr") == 0; }
 // entry 3l+c of -U^dagger is (-re, im) of entry 3c+l of U, so the products
 // are bitwise those of the double-stored links (dslashFb2T and
 // V_vmeq_xMap_times_xVp, lib/stagDslash.c:110-257, lib/vla.c:1368-1393).
+// reconstruct-12 layout: stored slot s (fat, or Naik when NS == 16 and s
+// is odd) starts at byte (s/2)*120V + (s&1)*72V (NS == 16) or 72V*s; the
+// sign bytes follow all stored slots
+__device__ __forceinline__ size_t f32r_base(int NS, int s, size_t V)
+{
+  return NS == 16 ? ((size_t)(s >> 1)*120 + (s & 1)*72)*V : (size_t)s*72*V;
+}
+
+template <int NS>
+__device__ __forceinline__ void f32r_link(const qllg_stag_args &a, int s, size_t V, size_t site,
+                                          Cx<float> U[9])
+{
+  const char *base = (const char *)a.links + f32r_base(NS, s, V);
+  if(NS == 16 && (s & 1)) {
+    const int stored = a.fb ? NS/2 : NS;
+    const unsigned char sg = __ldg((const unsigned char *)a.links + f32r_base(NS, stored, V) + site);
+    LinkR::naik(base, V, site, (sg >> (s >> 1)) & 1, U);
+  } else {
+    LinkR::fat(base, V, site, U);
+  }
+}
+
 template <int PL, int NS, typename T>
 __device__ __forceinline__ void slot_link(const qllg_stag_args &a, int mu, int back, int nk,
                                           size_t V, size_t Vh, size_t loff, size_t site, size_t nb,
                                           Cx<T> U[9])
 {
   const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
-  if(!a.fb) {
-    LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
-    return;
-  }
-  const int fslot = (NS == 16) ? (2*mu + nk) : mu;
-  if(!back) {
-    LinkIO<PL>::load(a.links, fslot, V, loff + site, a.lscale, U);
-    return;
-  }
-  Cx<T> F[9];
-  LinkIO<PL>::load(a.links, fslot, V, (Vh - loff) + nb, a.lscale, F);
+  if constexpr (PL == QLLG_F32R) {
+    const int fslot = (NS == 16) ? (2*mu + nk) : mu;
+    if(!a.fb) { f32r_link<NS>(a, slot, V, loff + site, U); return; }
+    if(!back) { f32r_link<NS>(a, fslot, V, loff + site, U); return; }
+    Cx<T> F[9];
+    f32r_link<NS>(a, fslot, V, (Vh - loff) + nb, F);
 #pragma unroll
-  for(int l=0; l<3; l++)
+    for(int l=0; l<3; l++)
 #pragma unroll
-    for(int c=0; c<3; c++) { U[3*l + c].r = -F[3*c + l].r; U[3*l + c].i = F[3*c + l].i; }
+      for(int c=0; c<3; c++) { U[3*l + c].r = -F[3*c + l].r; U[3*l + c].i = F[3*c + l].i; }
+  } else {
+    if(!a.fb) {
+      LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
+      return;
+    }
+    const int fslot = (NS == 16) ? (2*mu + nk) : mu;
+    if(!back) {
+      LinkIO<PL>::load(a.links, fslot, V, loff + site, a.lscale, U);
+      return;
+    }
+    Cx<T> F[9];
+    LinkIO<PL>::load(a.links, fslot, V, (Vh - loff) + nb, a.lscale, F);
+#pragma unroll
+    for(int l=0; l<3; l++)
+#pragma unroll
+      for(int c=0; c<3; c++) { U[3*l + c].r = -F[3*c + l].r; U[3*l + c].i = F[3*c + l].i; }
+  }
 }
 
 template <int PS, int PL, int NS, int NR>

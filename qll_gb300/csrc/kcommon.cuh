@@ -13,6 +13,7 @@ template <int P> struct Real;
 template <> struct Real<QLLG_F64> { typedef double T; typedef double2 V2; };
 template <> struct Real<QLLG_F32> { typedef float T; typedef float2 V2; };
 template <> struct Real<QLLG_I16> { typedef float T; typedef float2 V2; };
+template <> struct Real<QLLG_F32R> { typedef float T; typedef float2 V2; };
 
 // storage of the residual/solution vectors that go with Dslash operands of
 // precision P: 16-bit Dslash operands keep FP32 recurrence vectors
@@ -208,6 +209,49 @@ template <> struct LinkIO<QLLG_F32> {
     for(int k=0; k<9; k++) { float2 t = __ldg(p + k*V); m[k].r = (T)t.x; m[k].i = (T)t.y; }
   }
 };
+// reconstruct-12 FP32 links.  A fat slot is [4][V] float4 (entries 2k,
+// 2k+1) + [V] float2 (entry 8).  A Naik slot is rows 0 and 1 as [3][V]
+// float4: (e0, e3), (e6, e1), (e4, e7) (entry 3*col + row); row 2 is
+// s conj(r0 x r1)/|r0|, the third row of c W for W in SU(3), c real, |c| =
+// |r0|, s = sign(c) from the per-site sign bit.
+struct LinkR {
+  static __device__ __forceinline__ void fat(const char *p, size_t V, size_t site, Cx<float> m[9]) {
+    const float4 *q = (const float4 *)p;
+#pragma unroll
+    for(int k=0; k<4; k++) {
+      float4 w = __ldg(q + k*V + site);
+      m[2*k].r = w.x; m[2*k].i = w.y; m[2*k + 1].r = w.z; m[2*k + 1].i = w.w;
+    }
+    float2 e = __ldg((const float2 *)(p + 64*V) + site);
+    m[8].r = e.x; m[8].i = e.y;
+  }
+  static __device__ __forceinline__ void naik(const char *p, size_t V, size_t site, bool neg,
+                                              Cx<float> m[9]) {
+    const float4 *q = (const float4 *)p;
+    float4 a = __ldg(q + site), b = __ldg(q + V + site), c = __ldg(q + 2*V + site);
+    m[0].r = a.x; m[0].i = a.y; m[3].r = a.z; m[3].i = a.w;
+    m[6].r = b.x; m[6].i = b.y; m[1].r = b.z; m[1].i = b.w;
+    m[4].r = c.x; m[4].i = c.y; m[7].r = c.z; m[7].i = c.w;
+    rebuild_row2(m, neg);
+  }
+  // entries 2, 5, 8 (row 2) from rows 0 and 1
+  static __device__ __forceinline__ void rebuild_row2(Cx<float> m[9], bool neg) {
+    const float n2 = m[0].r*m[0].r + m[0].i*m[0].i + m[3].r*m[3].r + m[3].i*m[3].i +
+                     m[6].r*m[6].r + m[6].i*m[6].i;
+    const float f = (neg ? -1.f : 1.f)*rsqrtf(n2);
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+      // (r0 x r1)_c = r0[c1] r1[c2] - r0[c2] r1[c1]; r_k[col] is entry 3*col + k
+      const Cx<float> a = m[3*c1], b = m[3*c2 + 1], d = m[3*c2], e = m[3*c1 + 1];
+      const float xr = (a.r*b.r - a.i*b.i) - (d.r*e.r - d.i*e.i);
+      const float xi = (a.r*b.i + a.i*b.r) - (d.r*e.i + d.i*e.r);
+      m[3*c + 2].r = f*xr;
+      m[3*c + 2].i = -f*xi;
+    }
+  }
+};
+
 // 16-bit link: per slot [V] int4 (entries 0..3), [V] int4 (4..7), [V] int (8)
 template <> struct LinkIO<QLLG_I16> {
   template <typename T>

@@ -40,7 +40,10 @@ typedef struct {
   int Vh;     /* sites per parity */
 } qllg_geom;
 
-enum { QLLG_F64 = 0, QLLG_F32 = 1, QLLG_I16 = 2 };
+enum { QLLG_F64 = 0, QLLG_F32 = 1, QLLG_I16 = 2,
+       QLLG_F32R = 3 };   /* links only: FP32 in 16-byte vectors, Naik slots as
+                             two rows + a per-site sign (reconstruct-12) */
+#define QLLG_NLINKP 4
 
 /* ------------------------------------------------------------ geometry */
 struct Layout_s;
@@ -114,6 +117,13 @@ int qllg_k_link_from_aos(int prec, void *dev, float *scale_dev, const void *stag
 int qllg_k_link_to_aos(int prec, const void *dev, void *stage, int stage_is_double, int V);
 /* convert a device FP64 link slot to prec (FP32 or I16) */
 int qllg_k_link_convert(int prec, void *out, float *scale_dev, const double *in, int V);
+/* one FP64 slot [9][V] into the reconstruct-12 format at out: a fat slot as
+ * [4][V] float4 + [V] float2; a Naik slot (naik != 0) as rows 0 and 1, [3][V]
+ * float4, with bit `bit` of signs[site] the sign that rebuilds row 2;
+ * *bad is set when a Naik link is not a real multiple of an SU(3) matrix
+ * (rows 0, 1 do not determine row 2 within FP32 rounding) */
+int qllg_k_link_to_f32r(void *out, const double *in, int V, int naik, unsigned char *signs,
+                        int bit, int *bad);
 
 /* ----------------------------------------------------- staggered Dslash */
 typedef struct {

@@ -282,6 +282,9 @@ static struct { const char *name; double value; } g_params[] = {
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
   {"dslash_variant", -1},    /* force a Dslash variant (0-3); -1: autotuned */
+  {"links_recon12", 0},      /* mixed FP32 solves: Naik links as two rows + sign
+                                (measured slower: 1.40 against 0.93 ms per 16-rhs
+                                half Dslash at 32^3x64, so off by default) */
 };
 
 int

@@ -41,7 +41,7 @@ struct qllg_stag {
   qllg_geom g;
   int nslots;
   int master;              /* precision of the links handed in */
-  void *links[3];          /* per precision, lazily derived from the master */
+  void *links[QLLG_NLINKP];  /* per precision, lazily derived from the master */
   float *lscale;           /* 16-bit link scales [nslots] */
   qllg_redbuf rb;
   qllg_cg_scalars *sc;     /* device scalars */
@@ -59,7 +59,8 @@ struct qllg_stag {
   } graphs[6];
   int ngraph_next;
   int graph_body;          /* body of the graph the current solve launched, 0: none */
-  unsigned char shared[3]; /* links[p] belong to another operator */
+  unsigned char shared[QLLG_NLINKP]; /* links[p] belong to another operator */
+  int recon_bad;           /* the Naik links are not reconstructible (reconstruct-12 refused) */
   int fb;                  /* single-stored: the nslots/2 forward slots only */
   /* continuous batching (qllg_batch_*): a fixed-width mixed CG whose
    * columns are admitted and retired independently */
@@ -101,10 +102,76 @@ qllg_stag_set_single_store(qllg_stag *S)
   S->fb = 1;
 }
 
+/* bytes of the links of precision prec (the reconstruct-12 format keeps
+ * fat slots at 72, Naik slots at 48 bytes a site, plus one sign byte) */
+static size_t
+links_bytes(const qllg_stag *S, int prec)
+{
+  const size_t V = (size_t)S->g.V;
+  const int n = stored_slots(S);
+  if(prec != QLLG_F32R) return qllg_link_bytes(prec)*V*n;
+  return S->nslots == 16 ? (size_t)(n/2)*120*V + V : (size_t)n*72*V;
+}
+
+/* FP32 links in the reconstruct-12 format, from the FP64 master */
+static int
+make_f32r_links(qllg_stag *S)
+{
+  const size_t V = (size_t)S->g.V;
+  const int n = stored_slots(S), n16 = S->nslots == 16;
+  char *out = qllg_dmalloc(links_bytes(S, QLLG_F32R));
+  int *bad = qllg_dmalloc(sizeof(int)), hbad = 0;
+  if(!out || !bad) { qllg_dfree(out); qllg_dfree(bad); return -1; }
+  unsigned char *signs = (unsigned char *)out + (n16 ? (size_t)(n/2)*120*V : (size_t)n*72*V);
+  int rc = qllg_check_cuda(cudaMemsetAsync(bad, 0, sizeof(int), qllg_stream()), "clear");
+  for(int s=0; s<n && !rc; s++) {
+    const size_t base = n16 ? ((size_t)(s >> 1)*120 + (s & 1)*72)*V : (size_t)s*72*V;
+    rc = qllg_k_link_to_f32r(out + base, (const double *)S->links[QLLG_F64] + (size_t)s*18*V,
+                             S->g.V, n16 && (s & 1), signs, s >> 1, bad);
+  }
+  if(!rc) rc = qllg_d2h(&hbad, bad, sizeof(int));
+  qllg_dfree(bad);
+  if(rc || hbad) {
+    qllg_sync();
+    qllg_dfree(out);
+    if(hbad) {
+      S->recon_bad = 1;
+      qllg_set_error("reconstruct-12: Naik links are not real multiples of SU(3) matrices");
+    }
+    return -1;
+  }
+  S->links[QLLG_F32R] = out;
+  return 0;
+}
+
+static int ensure_links(qllg_stag *S, int prec);
+
+/* links for the FP32 Dslash of the mixed solvers: the reconstruct-12
+ * format when the parameter allows it and the Naik links are SU(3) up to a
+ * real factor, else plain FP32 */
+static int
+f32_links(qllg_stag *S)
+{
+  if(qllg_get_param("links_recon12") != 0 && S->master == QLLG_F64 && S->nslots == 16 &&
+     !S->recon_bad) {
+    if(ensure_links(S, QLLG_F32R) == 0) return QLLG_F32R;
+    qllg_clear_error();
+  }
+  return QLLG_F32;
+}
+
 static int
 ensure_links(qllg_stag *S, int prec)
 {
   if(S->links[prec]) return 0;
+  if(prec == QLLG_F32R) {
+    if(S->recon_bad) {
+      qllg_set_error("reconstruct-12: Naik links are not real multiples of SU(3) matrices");
+      return -1;
+    }
+    if(ensure_links(S, QLLG_F64)) return -1;
+    return make_f32r_links(S);
+  }
   if(S->master != QLLG_F64) {
     qllg_set_error("operator created from float links has no %s copy",
                    prec == QLLG_F64 ? "FP64" : "16-bit");
@@ -218,11 +285,13 @@ qllg_stag *
 qllg_stag_share(qllg_stag *S)
 {
   if(ensure_links(S, QLLG_F64) || ensure_links(S, QLLG_F32)) return NULL;
+  f32_links(S);               /* the reconstruct-12 copy too, when it applies */
   int dims[4] = {S->g.L[0], S->g.L[1], S->g.L[2], S->g.L[3]};
   qllg_stag *T = qllg_stag_alloc(dims, S->nslots, S->master);
   if(!T) return NULL;
   T->fb = S->fb;
-  for(int p=0; p<3; p++) {
+  T->recon_bad = S->recon_bad;
+  for(int p=0; p<QLLG_NLINKP; p++) {
     T->links[p] = S->links[p];
     T->shared[p] = S->links[p] != NULL;
   }
@@ -239,7 +308,7 @@ qllg_stag_destroy(qllg_stag *S)
 {
   if(!S) return;
   qllg_sync();
-  for(int p=0; p<3; p++) if(!S->shared[p]) qllg_dfree(S->links[p]);
+  for(int p=0; p<QLLG_NLINKP; p++) if(!S->shared[p]) qllg_dfree(S->links[p]);
   qllg_dfree(S->bstage);
   if(S->bev) cudaEventDestroy(S->bev);
   qllg_dfree(S->lscale);
@@ -291,6 +360,14 @@ qllg_stag_get_links(qllg_stag *S, double *const out[16])
   return 0;
 }
 
+/* 1 when the operator's mixed FP32 solves use reconstruct-12 links
+ * (deriving them now if the parameter allows it) */
+int
+qllg_stag_recon12(qllg_stag *S)
+{
+  return f32_links(S) == QLLG_F32R;
+}
+
 int
 qllg_stag_nslots(const qllg_stag *S)
 {
@@ -301,8 +378,8 @@ size_t
 qllg_stag_device_bytes(const qllg_stag *S)
 {
   size_t b = 0;
-  for(int p=0; p<3; p++)
-    if(S->links[p] && !S->shared[p]) b += qllg_link_bytes(p)*(size_t)S->g.V*stored_slots(S);
+  for(int p=0; p<QLLG_NLINKP; p++)
+    if(S->links[p] && !S->shared[p]) b += links_bytes(S, p);
   for(int i=0; i<WS_N; i++) b += S->ws_bytes[i];
   if(S->bstage) b += 48*(size_t)S->g.Vh;
   return b;
@@ -751,7 +828,8 @@ qllg_batch_init(qllg_stag *S, int maxits)
   iter_ctx *c = &S->bctx;
   memset(c, 0, sizeof(*c));
   c->mixed = 1;
-  c->ps = c->pl = QLLG_F32;
+  c->ps = QLLG_F32;
+  c->pl = f32_links(S);
   c->nrhs = n;
   c->reortho = qllg_get_param("reortho") != 0;
   c->r = ws_get(S, WS_R, vx);
@@ -898,7 +976,7 @@ solve_dev(qllg_stag *S, int nrhs, void *x, const void *b, const double mass[], d
                    qllg_get_param("reliable_delta"));
     break;
   case QLLG_SOLVE_MIXED_SINGLE:
-    its = cg_mixed(S, QLLG_F32, QLLG_F32, QLLG_F32, nrhs, x, b, mass, rsq, maxits,
+    its = cg_mixed(S, QLLG_F32, QLLG_F32, f32_links(S), nrhs, x, b, mass, rsq, maxits,
                    qllg_get_param("reliable_delta_single"));
     break;
   default:
@@ -1068,9 +1146,10 @@ qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *
                         const void *in_dev)
 {
   if(!valid_nrhs(nrhs)) { qllg_set_error("dslash_device: nrhs %d", nrhs); return -1; }
-  if(prec < 0 || prec > 2) { qllg_set_error("dslash_device: precision %d", prec); return -1; }
-  return dslash_half(S, prec, prec, out_parity, nrhs, in_dev, NULL, out_dev, 0, NULL, 0, 1,
-                     NULL, NULL, NULL, NULL);
+  if(prec < 0 || prec > 3) { qllg_set_error("dslash_device: precision %d", prec); return -1; }
+  /* 3: FP32 spinors with the reconstruct-12 links */
+  return dslash_half(S, prec == 3 ? QLLG_F32 : prec, prec, out_parity, nrhs, in_dev, NULL, out_dev,
+                     0, NULL, 0, 1, NULL, NULL, NULL, NULL);
 }
 
 /* out = D in as qllg_stag_dslash_device, plus |out|^2 of each rhs into
@@ -1136,6 +1215,10 @@ qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
 size_t
 qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs)
 {
+  /* prec 3 of qllg_stag_dslash_device (reconstruct-12 links) has FP32
+   * spinors; an unknown precision has no vector (0 bytes) */
+  if(prec == 3) prec = QLLG_F32;
+  if(prec < 0 || prec > 2 || nrhs < 0) return 0;
   return vec_bytes(S, prec, nrhs);
 }
 

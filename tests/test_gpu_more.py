@@ -352,6 +352,11 @@ def test_single_stored_operator_matches_double_stored():
     masses = (c_double*nrhs)(*[0.05 + 0.01*k for k in range(nrhs)])
     bs = [qll.gen_source(dims, 9000 + k, 6, "even") for k in range(nrhs)]
     sol = []
+    # 18-real links (reconstruct-12 rebuilds a backward Naik link from its
+    # own two rows when double-stored, from the forward one when single-
+    # stored: equal to FP32 rounding, not bitwise)
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    L.qllg_set_param(b"links_recon12", 0)
     for S in (S2, S1):
         xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
         info = qll.SolveInfo()
@@ -359,6 +364,7 @@ def test_single_stored_operator_matches_double_stored():
                                 qll.SOLVE_MIXED_SINGLE, byref(info))
         assert its > 0, qll.last_error()
         sol.append((list(info.iters[:nrhs]), xs))
+    L.qllg_set_param(b"links_recon12", 0)
     assert sol[0][0] == sol[1][0]
     for k in range(nrhs):
         assert np.array_equal(sol[0][1][k], sol[1][1][k])

@@ -394,6 +394,91 @@ def test_foreign_layout_adapters():
     L.qllg_stag_destroy(S)
 
 
+@pytest.mark.parametrize("single_store", [0, 1])
+def test_reconstruct12_links(single_store):
+    """Naik links held as two rows + a sign (the long links of fat7 are
+    -1/24 times products of SU(3) links): the Dslash agrees with FP64 to FP32
+    rounding, and the mixed solve reaches the same FP64 true residual and
+    solution as with 18-real links"""
+    torch = pytest.importorskip("torch")
+    L = qll.load()
+    vp = ctypes.c_void_p
+    fn = L.qllg_stag_create_asqtad_fb if single_store else L.qllg_stag_create_asqtad
+    fn.restype = vp
+    fn.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(vp), ctypes.POINTER(qll.Fat7Coeffs)]
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    L.qllg_stag_recon12.argtypes = [vp]
+    L.qllg_stag_vec_bytes.restype = ctypes.c_size_t
+    L.qllg_stag_vec_bytes.argtypes = [vp, c_int, c_int]
+    L.qllg_stag_dslash_device.argtypes = [vp, c_int, c_int, c_int, vp, vp]
+    th = qll.gen_gauge(DIMS, 1009, 0.3, ks=True)
+    c = qll.asqtad_coeffs()
+    S = vp(fn(qll.dims_c(DIMS), qll.vp_array(th), byref(c)))
+    assert S.value, qll.last_error()
+    L.qllg_set_param(b"links_recon12", 1)
+    assert L.qllg_stag_recon12(S) == 1, qll.last_error()
+    for nrhs in (1, 16):
+        n = L.qllg_stag_vec_bytes(S, 1, nrhs)//4
+        g = torch.Generator(device="cuda").manual_seed(31 + nrhs)
+        src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
+        src64 = src.to(torch.float64)
+        for parity in (0, 1):
+            outs = {}
+            for prec, inp in ((0, src64), (1, src), (3, src)):
+                o = torch.zeros_like(inp)
+                torch.cuda.synchronize()
+                assert L.qllg_stag_dslash_device(S, prec, nrhs, parity, vp(o.data_ptr()),
+                                                 vp(inp.data_ptr())) == 0, qll.last_error()
+                torch.cuda.synchronize()
+                outs[prec] = o.to(torch.float64)
+            ref = outs[0]
+            for prec in (1, 3):
+                err = ((outs[prec] - ref).norm()/ref.norm()).item()
+                assert err < 2e-6, (prec, nrhs, parity, err)
+    nrhs = 4
+    masses = (c_double*nrhs)(0.05, 0.07, 0.1, 0.2)
+    bs = [qll.gen_source(DIMS, 9700 + k, 6, "even") for k in range(nrhs)]
+    sol = {}
+    for recon in (1, 0):
+        L.qllg_set_param(b"links_recon12", recon)
+        xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+        info = qll.SolveInfo()
+        assert L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), masses, 1e-16, 5000,
+                                 qll.SOLVE_MIXED_SINGLE, byref(info)) > 0, qll.last_error()
+        for k in range(nrhs):
+            assert info.true_rsq[k] < 1e-16*1.0001
+        sol[recon] = xs
+    L.qllg_set_param(b"links_recon12", 0)
+    Vh = bs[0].shape[0]//2
+    for k in range(nrhs):
+        assert relerr(sol[1][k][:Vh], sol[0][k][:Vh]) < 1e-7
+    L.qllg_stag_destroy(S)
+
+
+def test_reconstruct12_refused_for_general_links():
+    """Naik links that are not real multiples of SU(3) matrices: no
+    reconstruct-12 copy, the mixed FP32 solve falls back to 18-real links"""
+    L, S, u, u3 = _native()
+    L.qllg_stag_destroy(S)
+    rng = np.random.default_rng(4)
+    u3b = [a + 1e-3*rng.standard_normal(a.shape) for a in u3]
+    S = ctypes.c_void_p(L.qllg_stag_create(qll.dims_c(DIMS), qll.vp_array(u), qll.vp_array(u3b)))
+    assert S.value, qll.last_error()
+    L.qllg_stag_recon12.argtypes = [ctypes.c_void_p]
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    L.qllg_set_param(b"links_recon12", 1)
+    assert L.qllg_stag_recon12(S) == 0
+    nrhs = 2
+    bs = [qll.gen_source(DIMS, 9800 + k, 6, "even") for k in range(nrhs)]
+    xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+    info = qll.SolveInfo()
+    assert L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), (c_double*nrhs)(0.1, 0.2),
+                             1e-16, 5000, qll.SOLVE_MIXED_SINGLE, byref(info)) > 0, qll.last_error()
+    L.qllg_set_param(b"links_recon12", 0)
+    assert max(info.true_rsq[k] for k in range(nrhs)) < 1e-16*1.0001
+    L.qllg_stag_destroy(S)
+
+
 def test_unknown_parameter_is_refused():
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
