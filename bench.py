@@ -54,6 +54,16 @@ FP64_ITERS_MEASURED = 454
 TRAFFIC_PER_SITE_BYTES = (537.198592e6 + 113.220096e6)/331776
 
 
+def apply_params(L, args):
+    """library parameters given as --param name=value"""
+    from qll_gb300 import qll
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    for kv in args.param:
+        k, v = kv.split("=")
+        if L.qllg_set_param(k.encode(), float(v)) != 0:
+            raise SystemExit(qll.last_error())
+
+
 def autotune_report(L):
     """the Dslash variant the autotuner chose per launch shape, with times"""
     buf = ctypes.create_string_buffer(16384)
@@ -162,6 +172,7 @@ def run_gpu(args):
     L.qllg_stag_device_bytes.restype = ctypes.c_size_t
     stream = torch.cuda.current_stream()
     L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
+    apply_params(L, args)
 
     t0 = time.time()
     seed_gauge, seed_src = replica_seeds(rank)
@@ -429,8 +440,9 @@ def run_wilson(args):
 # ------------------------------------------------------------- multishift
 def run_multishift(args):
     """C3: 24^3x48, m=0.02, 12 shifts log-spaced over 1e-4..1, 8 Gaussian
-    rhs, tolerance 1e-8 on every shift: the mixed multi-rhs solve (every
-    (rhs, shift) pair a column of the 16-wide FP32 mixed CG) against the
+    rhs, tolerance 1e-8 on every shift: the mixed multi-rhs solve (FP32
+    multishift CG for the 8 rhs at once, then every (rhs, shift) pair
+    refined by the FP32 mixed CG with FP64 reliable updates) against the
     reference's FP64 multishift CG run rhs after rhs"""
     from qll_gb300 import qll, serve
     L = serve._lib()
@@ -438,6 +450,7 @@ def run_multishift(args):
                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    apply_params(L, args)
     dims, nrhs, mass = (24, 24, 24, 48), 8, 0.02
     shifts = [10**(-4 + 4*k/11) for k in range(12)]
     ns = len(shifts)
@@ -462,7 +475,8 @@ def run_multishift(args):
             best = dt if best is None else min(best, dt)
         out[name] = {"seconds": best, "rhs_per_s": nrhs/best, "shift_solves_per_s": nrhs*ns/best,
                      "max_iters": max(its), "max_true_rsq": max(tr[:]),
-                     "note": ("pairs packed 16 per launch, FP64 reliable updates"
+                     "note": ("FP32 multishift CG of the 8 rhs at once, then the pairs refined "
+                              "16 per launch with FP64 reliable updates"
                               if mode == qll.SOLVE_MIXED_SINGLE else
                               "reference algorithm (cgmsSolveT) in FP64, one rhs per call")}
     out["speedup_mixed_over_fp64"] = out["fp64_cgms"]["seconds"]/out["mixed"]["seconds"]

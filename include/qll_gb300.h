@@ -112,10 +112,13 @@ int qllg_stag_vec_download_foreign(qllg_stag *S, const void *v_dev, int nrhs, vo
  * many rhs): for every rhs r and shift k, (m^2 + shift_k - D_eo D_oe)
  * x[r*nshift + k] = b[r] on the even sites, each to |r|^2 < rsq |b|^2.
  * QLLG_SOLVE_DOUBLE runs the reference's FP64 multishift CG per rhs;
- * QLLG_SOLVE_MIXED_SINGLE runs every (rhs, shift) pair as a column of the
- * 16-wide FP32 mixed CG with FP64 reliable updates.  Host arrays [V][6]
- * FP64; iters and true_rsq (FP64 |b - A_k x|^2/|b|^2) per pair, may be
- * NULL.  Returns the largest iteration count. */
+ * QLLG_SOLVE_MIXED_SINGLE runs the multishift recurrence for up to 16 rhs
+ * at once in FP32 vectors (FP64 recurrences) to |r|^2 < max(rsq,
+ * "multishift_guess_rsq") |b|^2, then takes every (rhs, shift) pair from
+ * there to rsq with the FP32 mixed CG and FP64 reliable updates, 16 pairs a
+ * launch.  Host arrays [V][6] FP64; iters (both stages) and true_rsq (FP64
+ * |b - A_k x|^2/|b|^2) per pair, may be NULL.  Returns the largest
+ * iteration count. */
 int qllg_stag_solve_multishift(qllg_stag *S, int nrhs, void *const x[], void *const b[],
                                double mass, int nshift, const double shifts[], double rsq,
                                int maxits, int mode, int iters[], double true_rsq[]);

@@ -120,6 +120,20 @@ __global__ void column_to_aos_k(const void *dev, double *stage, int nsites, int 
   }
 }
 
+// column jd of an [3][nsites][nd] field (precision PD) = column js of an
+// [3][nsites][ns] field (precision PS)
+template <int PD, int PSRC>
+__global__ void column_copy_k(void *dst, int nd, int jd, const void *src, int ns, int js, int nsites)
+{
+  typedef typename Calc<PD,PSRC>::T T;
+  for(size_t s = (size_t)blockIdx.x*blockDim.x + threadIdx.x; s < (size_t)nsites;
+      s += (size_t)gridDim.x*blockDim.x) {
+    Cx<T> v[3];
+    SpinorIO<PSRC,3>::load(src, (size_t)nsites*ns, s*ns + js, v);
+    SpinorIO<PD,3>::store(dst, (size_t)nsites*nd, s*nd + jd, v);
+  }
+}
+
 // a chunk of a graph-captured solver loop: at most n more trips
 __global__ void chunk_limit_k(int *loops, int *limit, int n)
 {
@@ -555,6 +569,21 @@ qllg_k_column_to_aos(const void *dev, double *stage, int nsites, int nrhs, int c
   column_to_aos_k<<<grid_for((size_t)nsites, 0, 0), kT, 0, qllg_stream()>>>(dev, stage, nsites,
                                                                             nrhs, col);
   return done("column_to_aos");
+}
+
+extern "C" int
+qllg_k_column_copy(int pd, void *dst, int nd, int jd, int psrc, const void *src, int ns, int js,
+                   int nsites)
+{
+  const int g = grid_for((size_t)nsites, 0, 0);
+  cudaStream_t st = qllg_stream();
+#define CC(A,B) if(pd == A && psrc == B) { \
+    column_copy_k<A,B><<<g,kT,0,st>>>(dst, nd, jd, src, ns, js, nsites); \
+    return done("column_copy"); }
+  CC(QLLG_F64, QLLG_F64) CC(QLLG_F64, QLLG_F32) CC(QLLG_F32, QLLG_F64) CC(QLLG_F32, QLLG_F32)
+#undef CC
+  qllg_set_error("column_copy: precisions %d/%d", pd, psrc);
+  return -1;
 }
 
 extern "C" int

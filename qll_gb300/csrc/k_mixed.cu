@@ -26,6 +26,55 @@ int grid_for(size_t total, qllg_redbuf *rb)
   return g < 1 ? 1 : (int)g;
 }
 
+// start from an initial guess: x64 holds it and t64 = A x64 (computed by
+// the caller in FP64); r64 = b - t64, rs = r64 rounded, xs = p = 0, and
+// the scalars of a fresh solve with |r|^2 = |b - A x0|^2 (rsq_stop holds
+// the relative target on entry and becomes absolute, as in mcg_init)
+template <int PS, int NR>
+__global__ void __launch_bounds__(kT)
+mcg_init_guess_k(void *r64, void *xs, void *rs, void *p, const void *b, const void *t64,
+                 int nsites, qllg_cg_scalars *s, double *partial, unsigned *counter)
+{
+  __shared__ double shm[2*kT];
+  size_t total = (size_t)nsites*NR;
+  double red[2] = {0, 0};
+  GRID_LOOP(t, total) {
+    Cx<double> bv[3], tv[3];
+    SpinorIO<QLLG_F64,3>::load(b, total, t, bv);
+    SpinorIO<QLLG_F64,3>::load(t64, total, t, tv);
+    Cx<float> rf[3], zf[3];
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      red[1] += bv[c].r*bv[c].r + bv[c].i*bv[c].i;
+      tv[c].r = bv[c].r - tv[c].r; tv[c].i = bv[c].i - tv[c].i;
+      red[0] += tv[c].r*tv[c].r + tv[c].i*tv[c].i;
+      rf[c].r = (float)tv[c].r; rf[c].i = (float)tv[c].i; zf[c].r = 0; zf[c].i = 0;
+    }
+    SpinorIO<QLLG_F64,3>::store(r64, total, t, tv);
+    SpinorIO<VecPrec<PS>::value,3>::store(rs, total, t, rf);
+    SpinorIO<QLLG_F32,3>::store(xs, total, t, zf);
+    SpinorIO<PS,3>::store(p, total, t, zf);
+  }
+  double *res[2] = {s->tmp, s->prev};
+  if(grid_reduce<2>(red, NR, threadIdx.x % NR, partial, counter, shm, res)) {
+    __syncthreads();
+    if(threadIdx.x == 0) {
+      int any = 0;
+      for(int q=0; q<NR; q++) {
+        const double r2 = s->tmp[q], bs = s->prev[q];
+        s->bsq[q] = bs; s->rsq[q] = r2; s->maxr2[q] = r2;
+        s->rsq_stop[q] *= bs;
+        s->iters[q] = 0; s->ru[q] = 0; s->nru[q] = 0;
+        s->active[q] = (bs > 0 && s->maxits > 0 && r2 >= s->rsq_stop[q]) ? 1 : 0;
+        any |= s->active[q];
+      }
+      s->done = !any;
+      s->no_ru = 1;
+      s->count = 0;
+    }
+  }
+}
+
 template <int PX, int PS, int NR>
 __global__ void __launch_bounds__(kT)
 mcg_init_k(void *x64, void *r64, void *xs, void *rs, void *p, const void *b, int nsites,
@@ -363,6 +412,22 @@ qllg_k_mcg_init(int px, int ps, void *x64, void *r64, void *xs, void *rs, void *
   PXS_SWITCH(px, ps, NR_SWITCH(nrhs, (mcg_init_k<PX,PS,NR><<<g,kT,0,st>>>(x64, r64, xs, rs, p, b,
                                       nsites, s, rb->partial, rb->counter))));
   return done("mcg_init");
+}
+
+extern "C" int
+qllg_k_mcg_init_guess(int ps, void *r64, void *xs, void *rs, void *p, const void *b,
+                      const void *t64, int nsites, int nrhs, qllg_cg_scalars *s, qllg_redbuf *rb)
+{
+  int g = grid_for((size_t)nsites*nrhs, rb);
+  cudaStream_t st = qllg_stream();
+  if(ps == QLLG_F32) {
+    NR_SWITCH(nrhs, (mcg_init_guess_k<QLLG_F32,NR><<<g,kT,0,st>>>(r64, xs, rs, p, b, t64, nsites, s,
+                                                                 rb->partial, rb->counter)));
+  } else if(ps == QLLG_I16) {
+    NR_SWITCH(nrhs, (mcg_init_guess_k<QLLG_I16,NR><<<g,kT,0,st>>>(r64, xs, rs, p, b, t64, nsites, s,
+                                                                 rb->partial, rb->counter)));
+  } else { qllg_set_error("mcg_init_guess: precision %d", ps); return -1; }
+  return done("mcg_init_guess");
 }
 
 extern "C" int

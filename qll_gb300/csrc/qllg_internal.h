@@ -221,6 +221,12 @@ int qllg_batch_launch(struct qllg_stag *S, int iters);
 int qllg_batch_poll(struct qllg_stag *S);
 int qllg_batch_retire(struct qllg_stag *S, int col, double *out);
 const qllg_cg_scalars *qllg_batch_scalars(const struct qllg_stag *S);
+/* mixed CG from an initial guess: x64 holds it, t64 = A x64 (FP64);
+ * r64 = b - t64, rs = r64, xs = p = 0, fresh scalars with rsq_stop scaled
+ * by |b|^2 */
+int qllg_k_mcg_init_guess(int ps, void *r64, void *xs, void *rs, void *p, const void *b,
+                          const void *t64, int nsites, int nrhs, qllg_cg_scalars *s,
+                          qllg_redbuf *rb);
 /* admission of right-hand sides into columns of a running mixed batch */
 typedef struct {
   int mask[QLLG_MAXRHS];        /* columns admitted now */
@@ -239,6 +245,10 @@ int qllg_k_aos_to_foreign(double *out, const double *in, const int *perm, int V,
  * [nsites][6] device array */
 int qllg_k_column_from_aos(void *dev, const double *stage, int nsites, int nrhs, int col);
 int qllg_k_column_to_aos(const void *dev, double *stage, int nsites, int nrhs, int col);
+/* column jd of a [3][nsites][nd] field of precision pd = column js of a
+ * [3][nsites][ns] field of precision ps (FP64/FP32) */
+int qllg_k_column_copy(int pd, void *dst, int nd, int jd, int ps, const void *src, int ns, int js,
+                       int nsites);
 /* *limit = *loops + n on the stream (the next graph launch runs at most n
  * more trips) */
 int qllg_k_chunk_limit(int *loops, int *limit, int n);
@@ -354,6 +364,27 @@ typedef struct {
   int n, iteration, itnlim, done;
 } qllg_cgms_scalars;
 
+/* multishift CG for up to QLLG_MAXRHS right-hand sides at once (the same
+ * shifts for all): cgmsSolveT's recurrences per rhs column, FP64 */
+typedef struct {
+  double a[QLLG_MAXRHS][QLLG_MAXSHIFT], b[QLLG_MAXRHS][QLLG_MAXSHIFT];
+  double bo[QLLG_MAXRHS][QLLG_MAXSHIFT], z[QLLG_MAXRHS][QLLG_MAXSHIFT];
+  double zo[QLLG_MAXRHS][QLLG_MAXSHIFT], zn[QLLG_MAXRHS][QLLG_MAXSHIFT];
+  double shifts[QLLG_MAXSHIFT];
+  double mass2[QLLG_MAXRHS];    /* m_0^2 per column (the Dslash epilogue's a[]) */
+  double rsq[QLLG_MAXRHS], oldrsq[QLLG_MAXRHS], rsqstop[QLLG_MAXRHS];
+  double pnorm[QLLG_MAXRHS], vnorm[QLLG_MAXRHS], tmp[QLLG_MAXRHS];
+  int active[QLLG_MAXRHS], iteration[QLLG_MAXRHS];
+  int n, nr, itnlim, done;
+} qllg_mcgms_scalars;
+int qllg_k_mcgms_pre(qllg_mcgms_scalars *s);
+int qllg_k_mcgms_coef(qllg_mcgms_scalars *s);
+/* FP32 fields of nr rhs, the n shift fields back to back (stride fs bytes):
+ * out_i += b_i p_i, r -= b_0 Ap, |r|^2 per rhs, stop test, a_i */
+int qllg_k_mcgms_update_xr(void *out, void *r, const void *ps, const void *Ap, int nsites, int nr,
+                           size_t fs, qllg_mcgms_scalars *s, qllg_redbuf *rb);
+int qllg_k_mcgms_update_p(void *ps, const void *r, int nsites, int nr, size_t fs,
+                          qllg_mcgms_scalars *s);
 /* start of an iteration: shift (bo,zo,z) <- (b,z,zn) after the first one;
  * oldrsq = rsq */
 int qllg_k_cgms_pre(qllg_cgms_scalars *s);

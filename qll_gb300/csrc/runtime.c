@@ -282,6 +282,11 @@ static struct { const char *name; double value; } g_params[] = {
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
   {"dslash_variant", -1},    /* force a Dslash variant (0-3); -1: autotuned */
+  {"multishift_guess_rsq", 1e-10}, /* mixed multishift: the FP32 multishift CG
+                                       goes to |r|^2 < this |b|^2 before the
+                                       pairs are refined in FP64 (C3 at
+                                       24^3x48: 0.73 s at 1e-9 and 1e-10,
+                                       0.81 s at 1e-11, 0.85 s at 1e-12) */
   {"links_recon12", 0},      /* mixed FP32 solves: Naik links as two rows + sign
                                 (measured slower: 1.40 against 0.93 ms per 16-rhs
                                 half Dslash at 32^3x64, so off by default) */

@@ -48,6 +48,7 @@ struct qllg_stag {
   qllg_cg_scalars *hsc;    /* pinned host copy */
   qllg_cgms_scalars *cs;   /* multishift scalars, device */
   qllg_cgms_scalars *hcs;  /* pinned host copy */
+  qllg_mcgms_scalars *mcs; /* multi-rhs multishift scalars, device (on first use) */
   void *ws[WS_N];
   size_t ws_bytes[WS_N];
   unsigned ws_gen;         /* bumped when a workspace buffer moves */
@@ -315,6 +316,7 @@ qllg_stag_destroy(qllg_stag *S)
   qllg_dfree(S->sc);
   if(S->hsc) cudaFreeHost(S->hsc);
   qllg_dfree(S->cs);
+  qllg_dfree(S->mcs);
   if(S->hcs) cudaFreeHost(S->hcs);
   qllg_redbuf_free(&S->rb);
   for(int i=0; i<WS_N; i++) qllg_dfree(S->ws[i]);
@@ -762,7 +764,7 @@ true_residual(qllg_stag *S, int nrhs, const void *x, const void *b, double *out)
  * (solution increment), links in pl */
 static int
 cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *b,
-         const double mass[], double rsq, int maxits, double delta)
+         const double mass[], double rsq, int maxits, double delta, int guess)
 {
   if(ensure_links(S, pl) || ensure_links(S, QLLG_F64)) return -1;
   /* p, v: Dslash operands in ps; r and the solution increment in FP32 */
@@ -784,7 +786,13 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
   if(push_scalars(S)) return -1;
   int Vh = S->g.Vh;
   qllg_cg_scalars *sc = S->sc;
-  if(qllg_k_mcg_init(QLLG_F32, ps, x64, r64, xs, rs, p, b, Vh, nrhs, sc, &S->rb)) return -1;
+  if(guess) {
+    /* x64 holds an initial guess: start from r = b - A x64 (FP64) */
+    if(apply_normal(S, QLLG_F64, QLLG_F64, nrhs, x64, w64, t64, NULL, NULL, NULL, NULL) ||
+       qllg_k_mcg_init_guess(ps, r64, xs, rs, p, b, t64, Vh, nrhs, sc, &S->rb)) return -1;
+  } else if(qllg_k_mcg_init(QLLG_F32, ps, x64, r64, xs, rs, p, b, Vh, nrhs, sc, &S->rb)) {
+    return -1;
+  }
   iter_ctx c;
   memset(&c, 0, sizeof(c));
   c.mixed = 1;
@@ -973,11 +981,11 @@ solve_dev(qllg_stag *S, int nrhs, void *x, const void *b, const double mass[], d
     break;
   case QLLG_SOLVE_MIXED_HALF:
     its = cg_mixed(S, QLLG_I16, QLLG_F32, QLLG_I16, nrhs, x, b, mass, rsq, maxits,
-                   qllg_get_param("reliable_delta"));
+                   qllg_get_param("reliable_delta"), 0);
     break;
   case QLLG_SOLVE_MIXED_SINGLE:
     its = cg_mixed(S, QLLG_F32, QLLG_F32, f32_links(S), nrhs, x, b, mass, rsq, maxits,
-                   qllg_get_param("reliable_delta_single"));
+                   qllg_get_param("reliable_delta_single"), 0);
     break;
   default:
     qllg_set_error("solve: unknown mode %d", mode);
@@ -1425,16 +1433,86 @@ out:
 }
 
 /* ------------------------------------------------ multi-rhs multishift */
+/* cgmsSolveT (lib/cgms.c:6-179) for nr rhs at once in FP32 (vectors) with
+ * FP64 recurrences per rhs column: bf the sources [3][Vh][nr] FP32, out n
+ * solution fields of the same shape back to back, shifts relative to the
+ * base m0^2 (shifts[0] = 0 for the base system itself); stops each column
+ * at |r|^2 < rsq |b|^2.  Returns the largest iteration count. */
+static int
+mcgms_run(qllg_stag *S, int pl, int nr, void *out, const void *bf, const double shifts[], int n,
+          double mass0, double rsq, int itnlim)
+{
+  const int Vh = S->g.Vh;
+  const size_t vb = vec_bytes(S, QLLG_F32, nr);
+  if(ensure_links(S, pl)) return -1;
+  void *r = ws_get(S, WS_R, vb), *Ap = ws_get(S, WS_AP, vb), *v = ws_get(S, WS_V, vb);
+  if(!r || !Ap || !v) return -1;
+  if(!S->mcs && !(S->mcs = qllg_dmalloc(sizeof(qllg_mcgms_scalars)))) return -1;
+  qllg_mcgms_scalars *h = malloc(sizeof(qllg_mcgms_scalars));
+  void *ps = qllg_dmalloc(vb*n);
+  double bn[QLLG_MAXRHS];
+  int rc = -1;
+  if(!h || !ps) goto out;
+  if(qllg_k_norm2(QLLG_F32, bf, Vh, 3, nr, S->sc->tmp, &S->rb) ||
+     qllg_d2h(bn, S->sc->tmp, sizeof(double)*nr)) goto out;
+  memset(h, 0, sizeof(*h));
+  h->n = n;
+  h->nr = nr;
+  h->itnlim = itnlim;
+  for(int i=0; i<n; i++) h->shifts[i] = shifts[i];
+  int any = 0;
+  for(int q=0; q<nr; q++) {
+    h->mass2[q] = mass0*mass0;
+    h->rsq[q] = bn[q];
+    h->rsqstop[q] = rsq*bn[q];
+    h->active[q] = bn[q] > 0;
+    any |= h->active[q];
+    for(int i=0; i<n; i++) { h->zo[q][i] = h->z[q][i] = 1; h->bo[q][i] = -1; h->a[q][i] = 0; }
+  }
+  h->done = !any;
+  if(qllg_check_cuda(cudaMemcpyAsync(S->mcs, h, sizeof(*h), cudaMemcpyHostToDevice, qllg_stream()),
+                     "push multishift scalars")) goto out;
+  if(qllg_check_cuda(cudaMemsetAsync(out, 0, vb*n, qllg_stream()), "clear") ||
+     qllg_k_copy(QLLG_F32, r, bf, Vh, 3, nr)) goto out;
+  for(int i=0; i<n; i++) if(qllg_k_copy(QLLG_F32, (char *)ps + vb*i, bf, Vh, 3, nr)) goto out;
+  for(int batch=8;;) {
+    for(int it=0; it<batch; it++) {
+      qllg_mcgms_scalars *m = S->mcs;
+      if(qllg_k_mcgms_pre(m) ||
+         dslash_half(S, QLLG_F32, pl, 1, nr, ps, NULL, v, 0, NULL, 0, 1, m->vnorm, NULL, m->active,
+                     &m->done) ||
+         dslash_half(S, QLLG_F32, pl, 0, nr, v, ps, Ap, 2, m->mass2, 0, -1, NULL, m->pnorm,
+                     m->active, &m->done) ||
+         qllg_k_mcgms_coef(m) ||
+         qllg_k_mcgms_update_xr(out, r, ps, Ap, Vh, nr, vb, m, &S->rb) ||
+         qllg_k_mcgms_update_p(ps, r, Vh, nr, vb, m)) goto out;
+    }
+    if(qllg_d2h(&h->done, &S->mcs->done, sizeof(int))) goto out;
+    if(h->done) break;
+    if(batch < 64) batch *= 2;
+  }
+  if(qllg_d2h(h, S->mcs, sizeof(*h))) goto out;
+  rc = 0;
+  for(int q=0; q<nr; q++) if(h->iteration[q] > rc) rc = h->iteration[q];
+out:
+  qllg_sync();
+  qllg_dfree(ps);
+  free(h);
+  return rc;
+}
+
 /* For every rhs r and shift k: (m^2 + shift_k - D_eo D_oe) x[r*nshift + k]
  * = b[r] on the even sites, stopping at |r_k|^2 < rsq |b_r|^2.
  *  - QLLG_SOLVE_DOUBLE: the reference's multishift CG (cgmsSolveT,
  *    lib/cgms.c:6-179) in FP64, all shifts of one rhs from one Krylov
  *    space, one rhs after the other (solveMulti2 per rhs);
- *  - QLLG_SOLVE_MIXED_SINGLE: every (rhs, shift) pair is a column of the
- *    16-wide FP32 mixed CG with FP64 reliable updates (one multi-rhs Dslash
- *    launch per half iteration serves 16 pairs, each link loaded once for
- *    all of them); pairs go in order of shift, so a batch holds pairs of
- *    similar iteration counts.
+ *  - QLLG_SOLVE_MIXED_SINGLE: first the same recurrence for up to 16 rhs
+ *    at once in FP32 vectors (one multi-rhs Dslash per half iteration for
+ *    all of them, FP64 recurrences per rhs), to about FP32 accuracy; then
+ *    every (rhs, shift) pair from that first solution to the requested
+ *    FP64 true residual, as a column of the 16-wide FP32 mixed CG with FP64
+ *    reliable updates (pairs in order of shift, so a launch holds pairs of
+ *    similar iteration counts).
  * Host arrays [V][6] FP64 (the even half is read and written).  iters and
  * true_rsq (|b - A_k x|^2/|b|^2 in FP64) are per pair, optional. */
 int
@@ -1487,38 +1565,98 @@ qllg_stag_solve_multishift(qllg_stag *S, int nrhs, void *const x[], void *const 
     qllg_set_error("multishift: mode %d (QLLG_SOLVE_DOUBLE or QLLG_SOLVE_MIXED_SINGLE)", mode);
     return -1;
   }
-  const int npair = nrhs*nshift;
-  size_t vb = vec_bytes(S, QLLG_F64, QLLG_MAXRHS);
-  void *bd = ws_get(S, WS_B, vb), *xd = ws_get(S, WS_OUT, vb);
-  void *stage = qllg_stage(48*(size_t)Vh);
-  if(!bd || !xd || !stage) return -1;
-  for(int p0=0; p0<npair; p0+=QLLG_MAXRHS) {
-    int n = npair - p0 < QLLG_MAXRHS ? npair - p0 : QLLG_MAXRHS;
-    int nc = pad_nrhs(n);
-    double m[QLLG_MAXRHS], tr[QLLG_MAXRHS];
-    if(qllg_check_cuda(cudaMemsetAsync(bd, 0, vec_bytes(S, QLLG_F64, nc), qllg_stream()),
-                       "multishift clear")) return -1;
-    for(int j=0; j<nc; j++) {
-      int pr = p0 + (j < n ? j : 0), k = pr / nrhs, r = pr % nrhs;
-      m[j] = sqrt(mass*mass + shifts[k]);
-      if(j >= n) continue;            /* padding: b = 0, starts inactive */
-      if(qllg_h2d(stage, b[r], 48*(size_t)Vh) ||
-         qllg_k_column_from_aos(bd, stage, Vh, nc, j)) return -1;
-    }
-    qllg_solve_info info;
-    int its = solve_dev(S, nc, xd, bd, m, rsq, maxits, QLLG_SOLVE_MIXED_SINGLE, &info);
-    if(its < 0) return -1;
-    if(its > maxit_seen) maxit_seen = its;
-    if(true_rsq && true_residual(S, nc, xd, bd, tr)) return -1;
-    for(int j=0; j<n; j++) {
-      int pr = p0 + j, k = pr / nrhs, r = pr % nrhs;
-      if(qllg_k_column_to_aos(xd, stage, Vh, nc, j) ||
-         qllg_d2h(x[r*nshift + k], stage, 48*(size_t)Vh)) return -1;
-      if(iters) iters[r*nshift + k] = info.iters[j];
-      if(true_rsq) true_rsq[r*nshift + k] = tr[j];
+  /* 1. the reference's multishift recurrence for up to 16 rhs at once, in
+   *    FP32 vectors (FP64 recurrences): a first solution of every pair,
+   *    good to about FP32 accuracy, from one Krylov space per rhs.  The
+   *    base system is the smallest shift (cgmsSolveT takes the others as
+   *    offsets from its first). */
+  int order[QLLG_MAXSHIFT], pos[QLLG_MAXSHIFT], kmin = 0;
+  for(int k=1; k<nshift; k++) if(shifts[k] < shifts[kmin]) kmin = k;
+  double rel[QLLG_MAXSHIFT];
+  order[0] = kmin;
+  for(int k=0, j=1; k<nshift; k++) if(k != kmin) order[j++] = k;
+  for(int j=0; j<nshift; j++) { rel[j] = shifts[order[j]] - shifts[kmin]; pos[order[j]] = j; }
+  const double mass0 = sqrt(mass*mass + shifts[kmin]);
+  const int pl = f32_links(S);
+  const double rsq_guess = rsq > qllg_get_param("multishift_guess_rsq") ? rsq
+                                                                       : qllg_get_param("multishift_guess_rsq");
+  const int ngroup = (nrhs + QLLG_MAXRHS - 1)/QLLG_MAXRHS;
+  void **gb = calloc(ngroup, sizeof(void *)), **gx = calloc(ngroup, sizeof(void *));
+  int *gits = calloc(ngroup, sizeof(int));
+  void *stage = qllg_stage(48*(size_t)Vh), *bf = NULL;
+  int rc = -1;
+  if(!gb || !gx || !gits || !stage) goto done;
+  for(int g=0; g<ngroup; g++) {
+    const int g0 = g*QLLG_MAXRHS, nreal = nrhs - g0 < QLLG_MAXRHS ? nrhs - g0 : QLLG_MAXRHS;
+    const int nr = pad_nrhs(nreal);
+    gb[g] = qllg_dmalloc(vec_bytes(S, QLLG_F64, nr));
+    gx[g] = qllg_dmalloc(vec_bytes(S, QLLG_F32, nr)*nshift);
+    bf = qllg_dmalloc(vec_bytes(S, QLLG_F32, nr));
+    if(!gb[g] || !gx[g] || !bf) goto done;
+    if(qllg_check_cuda(cudaMemsetAsync(gb[g], 0, vec_bytes(S, QLLG_F64, nr), qllg_stream()), "clear"))
+      goto done;
+    for(int j=0; j<nreal; j++)
+      if(qllg_h2d(stage, b[g0 + j], 48*(size_t)Vh) ||
+         qllg_k_column_from_aos(gb[g], stage, Vh, nr, j)) goto done;
+    if(qllg_k_spinor_convert(QLLG_F32, bf, QLLG_F64, gb[g], Vh, 3, nr, NULL)) goto done;
+    gits[g] = mcgms_run(S, pl, nr, gx[g], bf, rel, nshift, mass0, rsq_guess, maxits);
+    qllg_sync();
+    qllg_dfree(bf);
+    bf = NULL;
+    if(gits[g] < 0) goto done;
+  }
+  /* 2. every pair to the requested FP64 true residual: the FP32 mixed CG
+   *    with reliable updates, started from its first solution, 16 pairs per
+   *    launch in order of shift */
+  {
+    const int npair = nrhs*nshift;
+    size_t vb = vec_bytes(S, QLLG_F64, QLLG_MAXRHS);
+    void *bd = ws_get(S, WS_B, vb), *xd = ws_get(S, WS_OUT, vb);
+    if(!bd || !xd) goto done;
+    const double delta = qllg_get_param("reliable_delta_single");
+    for(int p0=0; p0<npair; p0+=QLLG_MAXRHS) {
+      int n = npair - p0 < QLLG_MAXRHS ? npair - p0 : QLLG_MAXRHS;
+      int nc = pad_nrhs(n);
+      double m[QLLG_MAXRHS], tr[QLLG_MAXRHS];
+      if(qllg_check_cuda(cudaMemsetAsync(bd, 0, vec_bytes(S, QLLG_F64, nc), qllg_stream()), "clear") ||
+         qllg_check_cuda(cudaMemsetAsync(xd, 0, vec_bytes(S, QLLG_F64, nc), qllg_stream()), "clear"))
+        goto done;
+      for(int j=0; j<nc; j++) {
+        int pr = p0 + (j < n ? j : 0), k = pr / nrhs, r = pr % nrhs;
+        m[j] = sqrt(mass*mass + shifts[k]);
+        if(j >= n) continue;            /* padding: b = 0, starts inactive */
+        const int g = r/QLLG_MAXRHS, jr = r % QLLG_MAXRHS;
+        const int nr = pad_nrhs(nrhs - g*QLLG_MAXRHS < QLLG_MAXRHS ? nrhs - g*QLLG_MAXRHS : QLLG_MAXRHS);
+        const char *guess = (const char *)gx[g] + vec_bytes(S, QLLG_F32, nr)*pos[k];
+        if(qllg_k_column_copy(QLLG_F64, bd, nc, j, QLLG_F64, gb[g], nr, jr, Vh) ||
+           qllg_k_column_copy(QLLG_F64, xd, nc, j, QLLG_F32, guess, nr, jr, Vh)) goto done;
+      }
+      int its = cg_mixed(S, QLLG_F32, QLLG_F32, pl, nc, xd, bd, m, rsq, maxits, delta, 1);
+      if(its < 0) goto done;
+      int rits[QLLG_MAXRHS];
+      for(int j=0; j<nc; j++) rits[j] = S->hsc->iters[j];
+      if(true_rsq && true_residual(S, nc, xd, bd, tr)) goto done;
+      for(int j=0; j<n; j++) {
+        int pr = p0 + j, k = pr / nrhs, r = pr % nrhs;
+        if(qllg_k_column_to_aos(xd, stage, Vh, nc, j) ||
+           qllg_d2h(x[r*nshift + k], stage, 48*(size_t)Vh)) goto done;
+        const int total = gits[r/QLLG_MAXRHS] + rits[j];
+        if(iters) iters[r*nshift + k] = total;
+        if(total > maxit_seen) maxit_seen = total;
+        if(true_rsq) true_rsq[r*nshift + k] = tr[j];
+      }
     }
   }
-  return maxit_seen;
+  rc = maxit_seen;
+done:
+  qllg_sync();
+  if(bf) qllg_dfree(bf);
+  for(int g=0; gb && g<ngroup; g++) qllg_dfree(gb[g]);
+  for(int g=0; gx && g<ngroup; g++) qllg_dfree(gx[g]);
+  free(gb);
+  free(gx);
+  free(gits);
+  return rc;
 }
 
 /* createStaggeredLinksFb (lib/stagDslash.c:464-519): only the forward
