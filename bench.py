@@ -194,8 +194,8 @@ def run_gpu(args):
 
     info = qll.SolveInfo()
 
-    def solve(mode=qll.SOLVE_MIXED_SINGLE, nrhs=NRHS, x=x_dev, b=b_dev):
-        its = L.qllg_stag_solve_device(S, nrhs, x, b, masses, RSQ, MAXITS, mode,
+    def solve(mode=qll.SOLVE_MIXED_SINGLE, nrhs=NRHS, x=x_dev, b=b_dev, rsq=RSQ):
+        its = L.qllg_stag_solve_device(S, nrhs, x, b, masses, rsq, MAXITS, mode,
                                        ctypes.byref(info))
         if its < 0:
             raise RuntimeError(qll.last_error())
@@ -254,14 +254,21 @@ def run_gpu(args):
     value = ws*NRHS*args.steps/(t_max*1e-3)
 
     # end to end through the host-array API: H2D of the sources and D2H of
-    # the solutions are inside the timed region
+    # the solutions are inside the timed region; the host arrays are in
+    # pinned (page-locked) memory
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy()
+        t[:] = a.reshape(-1)
+        return t
+    srcs_p = [pinned(s) for s in srcs]
+    xs_p = [pinned(x) for x in xs]
     e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
     te = time.time()
     for _ in range(e2e_steps):
-        its = L.qllg_stag_solve(S, NRHS, qll.vp_array(xs), qll.vp_array(srcs), masses, RSQ,
+        its = L.qllg_stag_solve(S, NRHS, qll.vp_array(xs_p), qll.vp_array(srcs_p), masses, RSQ,
                                 MAXITS, qll.SOLVE_MIXED_SINGLE, ctypes.byref(info))
         if its < 0:
             raise RuntimeError(qll.last_error())
@@ -297,6 +304,14 @@ def run_gpu(args):
     torch.cuda.synchronize()
     t_h = time.time() - t_h
 
+    # the same 16-rhs mixed solve to true residual 1e-10 (|r|^2 < 1e-20 |b|^2),
+    # the tighter tolerance of the same workload, once
+    t_t = time.time()
+    its_tight = solve(rsq=1e-20)
+    torch.cuda.synchronize()
+    t_t = time.time() - t_t
+    tight_true = max(info.true_rsq[r] for r in range(NRHS))
+
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max/args.steps,
@@ -309,10 +324,13 @@ def run_gpu(args):
         "iters_per_solve": iters, "max_true_rsq": max(truer),
         "mixed_16bit_storage": {"solves_per_s": ws*NRHS/t_h, "iters": its_half,
                                 "note": "16-bit Krylov vectors with per-site scale; slower at m=0.01"},
+        "tol_1e-10": {"solves_per_s": ws*NRHS/t_t, "iters": its_tight, "max_true_rsq": tight_true,
+                      "note": "the same mixed 16-rhs solve to true residual 1e-10, once, untimed by events"},
         "fp64_single_rhs": {"solves_per_s": 1/fp64_s, "iters": its64, "true_rsq": fp64_true,
                             "speedup_of_value": value/ws*fp64_s},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": bytes_io,
-                "d2h_bytes_per_step": bytes_io},
+                "d2h_bytes_per_step": bytes_io, "host_memory": "pinned",
+                "api": "qllg_stag_solve (host arrays)"},
         "fused_cg_kernel": {"avg_launch_ms": favg, "launches": fcnt.value,
                             "gbs": fused_bytes/(favg*1e-3)/1e9 if favg > 0 else None},
         "roofline": {"kernel": "stag_dslash_mr<f32,%s,16 slots,16 rhs,4 rhs/thread>"

@@ -12,6 +12,7 @@
 // slot s = 4*mu + 2*backward + naik, acc += U_s(x) psi(x + d_s).
 #pragma once
 #include <stdio.h>
+#include <type_traits>
 #include "kcommon.cuh"
 
 using namespace qk;
@@ -39,12 +40,12 @@ __device__ __forceinline__ size_t f32r_base(int NS, int s, size_t V)
 }
 
 template <int NS>
-__device__ __forceinline__ void f32r_link(const qllg_stag_args &a, int s, size_t V, size_t site,
+__device__ __forceinline__ void f32r_link(const qllg_stag_args &a, bool fb, int s, size_t V, size_t site,
                                           Cx<float> U[9])
 {
   const char *base = (const char *)a.links + f32r_base(NS, s, V);
   if(NS == 16 && (s & 1)) {
-    const int stored = a.fb ? NS/2 : NS;
+    const int stored = fb ? NS/2 : NS;
     const unsigned char sg = __ldg((const unsigned char *)a.links + f32r_base(NS, stored, V) + site);
     LinkR::naik(base, V, site, (sg >> (s >> 1)) & 1, U);
   } else {
@@ -52,24 +53,27 @@ __device__ __forceinline__ void f32r_link(const qllg_stag_args &a, int s, size_t
   }
 }
 
-template <int PL, int NS, typename T>
+// FB: 0 or 1 when the caller knows a.fb at compile time (no branch on it),
+// -1 to read it at run time
+template <int PL, int NS, int FB = -1, typename T>
 __device__ __forceinline__ void slot_link(const qllg_stag_args &a, int mu, int back, int nk,
                                           size_t V, size_t Vh, size_t loff, size_t site, size_t nb,
                                           Cx<T> U[9])
 {
   const int slot = (NS == 16) ? (4*mu + 2*back + nk) : (2*mu + back);
+  const bool fb = FB < 0 ? a.fb != 0 : FB != 0;
   if constexpr (PL == QLLG_F32R) {
     const int fslot = (NS == 16) ? (2*mu + nk) : mu;
-    if(!a.fb) { f32r_link<NS>(a, slot, V, loff + site, U); return; }
-    if(!back) { f32r_link<NS>(a, fslot, V, loff + site, U); return; }
+    if(!fb) { f32r_link<NS>(a, fb, slot, V, loff + site, U); return; }
+    if(!back) { f32r_link<NS>(a, fb, fslot, V, loff + site, U); return; }
     Cx<T> F[9];
-    f32r_link<NS>(a, fslot, V, (Vh - loff) + nb, F);
+    f32r_link<NS>(a, fb, fslot, V, (Vh - loff) + nb, F);
 #pragma unroll
     for(int l=0; l<3; l++)
 #pragma unroll
       for(int c=0; c<3; c++) { U[3*l + c].r = -F[3*c + l].r; U[3*l + c].i = F[3*c + l].i; }
   } else {
-    if(!a.fb) {
+    if(!fb) {
       LinkIO<PL>::load(a.links, slot, V, loff + site, a.lscale, U);
       return;
     }
@@ -194,17 +198,38 @@ stag_dslash(qllg_stag_args a)
 }
 
 
+// Launch shapes of the multi-rhs kernel.  CFG 0: 256 threads, 2 blocks/SM
+// (FP64: 1; 2 rhs/thread: 3) and the register cap that gives; 1: CFG 0 with
+// the complex FMAs on packed FP32 pairs (cmac_f2).  2-4 are "lean": the
+// per-rhs scalars and the norm sums in shared memory, for more resident
+// warps at fewer registers: 2: 3 blocks/SM (80 registers); 3: 4 blocks/SM
+// (64); 4: 128 threads, 9 blocks/SM (56).  5 and 6: CFG 0 and lean CFG 0
+// with the slot loop software-pipelined one slot ahead
+template <int PS, int R, int CFG> struct MrCfg {
+  static constexpr int threads = CFG == 4 ? 128 : 256;
+  static constexpr int minb = CFG == 2 ? 3 : CFG == 3 ? 4 : CFG == 4 ? 9 :
+                              (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
+  static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
+  static constexpr bool lean = (CFG >= 2 && CFG <= 4) || CFG == 6;
+  static constexpr bool pf = CFG >= 5;
+};
+
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
 // sides, so each link is loaded and converted once per R rhs and the R
 // accumulator sets give independent FMA chains.  Same epilogues as above.
-template <int PS, int PL, int NS, int NR, int R, bool V4>
-__global__ void __launch_bounds__(kThreads, PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2))
+template <int PS, int PL, int NS, int NR, int R, bool V4, int CFG>
+__global__ void __launch_bounds__(MrCfg<PS,R,CFG>::threads, MrCfg<PS,R,CFG>::minb)
 stag_dslash_mr(qllg_stag_args a)
 {
   typedef typename Calc<PS, PL>::T T;
   constexpr int Q = NR/R;                       // threads per site
   constexpr int PX = VecPrec<PS>::value;
-  __shared__ double shm[2*R*kThreads];
+  constexpr bool F2 = MrCfg<PS,R,CFG>::f2;
+  constexpr bool PF = MrCfg<PS,R,CFG>::pf;
+  constexpr int TB = MrCfg<PS,R,CFG>::threads;
+  constexpr bool LEAN = MrCfg<PS,R,CFG>::lean;
+  __shared__ double shm[2*R*TB];
+  __shared__ T s_ca[LEAN ? NR : 1], s_alpha[LEAN ? NR : 1];
   const Geo G = make_geo(a.g);
   const size_t V = (size_t)a.g.V;
   const size_t total = (size_t)G.Vh * NR;
@@ -224,11 +249,41 @@ stag_dslash_mr(qllg_stag_args a)
     act[j] = !a.active || a.active[rhs];
     anyact |= act[j];
     allact &= act[j];
-    ca[j] = (T)(a.a ? a.a[rhs] : a.a0);
-    alpha[j] = (a.mode == 3 && act[j])
-      ? (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs])) : (T)0;
+    if constexpr (!LEAN) {
+      ca[j] = (T)(a.a ? a.a[rhs] : a.a0);
+      alpha[j] = (a.mode == 3 && act[j])
+        ? (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs])) : (T)0;
+    }
   }
-  Acc<T> acc0[R], acc1[R];
+  // LEAN: the per-rhs scalars and the compensated norm sums live in shared
+  // memory instead of registers (the sums in shm, [2][R][TB], until the
+  // grid reduction takes it over)
+  if constexpr (LEAN) {
+    if(threadIdx.x < NR) {
+      const int rhs = threadIdx.x;
+      s_ca[rhs] = (T)(a.a ? a.a[rhs] : a.a0);
+      s_alpha[rhs] = (a.mode == 3 && (!a.active || a.active[rhs]))
+        ? (T)(1.0/(a.sc->mass2[rhs]*a.sc->pnorm[rhs] + a.sc->vnorm[rhs])) : (T)0;
+    }
+    __syncthreads();
+  }
+  auto cav = [&](int j) -> T { if constexpr (LEAN) return s_ca[q*R + j]; else return ca[j]; };
+  auto alv = [&](int j) -> T { if constexpr (LEAN) return s_alpha[q*R + j]; else return alpha[j]; };
+  Acc<T> acc0r[LEAN ? 1 : R], acc1r[LEAN ? 1 : R];
+  Acc<T> *accs = reinterpret_cast<Acc<T> *>(shm);
+  static_assert(sizeof(Acc<T>) <= sizeof(double), "norm sums in shm");
+  if constexpr (LEAN) {
+#pragma unroll
+    for(int j=0; j<2*R; j++) accs[j*TB + threadIdx.x] = Acc<T>();
+  }
+  auto norm0 = [&](int j, const Cx<T> (&v)[3]) {
+    if constexpr (LEAN) { Acc<T> t = accs[j*TB + threadIdx.x]; t.norm(v); accs[j*TB + threadIdx.x] = t; }
+    else acc0r[j].norm(v);
+  };
+  auto norm1 = [&](int j, const Cx<T> (&v)[3]) {
+    if constexpr (LEAN) { Acc<T> t = accs[(R + j)*TB + threadIdx.x]; t.norm(v); accs[(R + j)*TB + threadIdx.x] = t; }
+    else acc1r[j].norm(v);
+  };
   if(!skip && anyact) {
     for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < nwork;
         w += (size_t)gridDim.x*blockDim.x) {
@@ -243,54 +298,114 @@ stag_dslash_mr(qllg_stag_args a)
           Cx<T> s[3];
           SpinorIO<PS,3>::load(a.self, total, t0 + j, s);
 #pragma unroll
-          for(int c=0; c<3; c++) { acc[j][c].r = ca[j]*s[c].r; acc[j][c].i = ca[j]*s[c].i; }
+          for(int c=0; c<3; c++) { acc[j][c].r = cav(j)*s[c].r; acc[j][c].i = cav(j)*s[c].i; }
         } else {
 #pragma unroll
           for(int c=0; c<3; c++) { acc[j][c].r = 0; acc[j][c].i = 0; }
         }
       }
+      // the 16 (or 8) slots.  With every rhs of the thread active (the
+      // usual case) the unrolled slot loop has no branches, so the compiler
+      // can move the loads of later slots ahead of the FMAs of earlier ones
+      auto slots = [&](auto ck) {
+        constexpr bool CK = decltype(ck)::value;     // check the active flags
 #pragma unroll
-      for(int mu=0; mu<4; mu++) {
+        for(int mu=0; mu<4; mu++) {
 #pragma unroll
-        for(int back=0; back<2; back++) {
+          for(int back=0; back<2; back++) {
 #pragma unroll
-          for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
-            const int d = (nk ? 3 : 1)*(back ? -1 : 1);
-            const size_t nb = (size_t)nbr_index(G, x, mu, d);
-            const size_t kb = nb*NR + q*R;
-            Cx<T> U[9];
-            slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
-            if constexpr (v4) {
-              // two rhs per 16-byte load and colour
+            for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
+              const int d = (nk ? 3 : 1)*(back ? -1 : 1);
+              const size_t nb = (size_t)nbr_index(G, x, mu, d);
+              const size_t kb = nb*NR + q*R;
+              Cx<T> U[9];
+              slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
+              if constexpr (v4) {
+                // two rhs per 16-byte load and colour
 #pragma unroll
-              for(int h=0; h<R/2; h++) {
-                if(!act[2*h] && !act[2*h + 1]) continue;
-                Cx<T> v[2][3];
-                Spinor4<PS>::load_half(a.in, total, kb, h, v);
+                for(int h=0; h<R/2; h++) {
+                  if constexpr (CK) { if(!act[2*h] && !act[2*h + 1]) continue; }
+                  Cx<T> v[2][3];
+                  Spinor4<PS>::load_half(a.in, total, kb, h, v);
 #pragma unroll
-                for(int jj=0; jj<2; jj++) {
+                  for(int jj=0; jj<2; jj++) {
+#pragma unroll
+                    for(int l=0; l<3; l++) {
+#pragma unroll
+                      for(int c=0; c<3; c++) {
+                        if constexpr (F2) cmac_f2(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
+                        else cmac(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
+                      }
+                    }
+                  }
+                }
+              } else {
+#pragma unroll
+                for(int j=0; j<R; j++) {
+                  if constexpr (CK) { if(!act[j]) continue; }
+                  Cx<T> v[3];
+                  SpinorIO<PS,3>::load(a.in, total, kb + j, v);
 #pragma unroll
                   for(int l=0; l<3; l++) {
 #pragma unroll
-                    for(int c=0; c<3; c++) cmac(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
+                    for(int c=0; c<3; c++) cmac(acc[j][c], U[3*l + c], v[l]);
                   }
-                }
-              }
-            } else {
-#pragma unroll
-              for(int j=0; j<R; j++) {
-                if(!act[j]) continue;
-                Cx<T> v[3];
-                SpinorIO<PS,3>::load(a.in, total, kb + j, v);
-#pragma unroll
-                for(int l=0; l<3; l++) {
-#pragma unroll
-                  for(int c=0; c<3; c++) cmac(acc[j][c], U[3*l + c], v[l]);
                 }
               }
             }
           }
         }
+      };
+      if constexpr (PF && v4) {
+        // software pipeline, one slot ahead: the links and neighbour
+        // spinors of slot s+1 are loaded before the FMAs of slot s.  The
+        // run-time branch on a.fb in slot_link keeps the compiler from
+        // hoisting loads further ahead than that
+        constexpr int NSL = NS;
+        auto load_slot = [&](int sl, Cx<T> (&U)[9], Cx<T> (&v)[R][3]) {
+          const int mu = NS == 16 ? sl >> 2 : sl >> 1;
+          const int back = NS == 16 ? (sl >> 1) & 1 : sl & 1;
+          const int nk = NS == 16 ? sl & 1 : 0;
+          const int d = (nk ? 3 : 1)*(back ? -1 : 1);
+          const size_t nb = (size_t)nbr_index(G, x, mu, d);
+          slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
+#pragma unroll
+          for(int h=0; h<R/2; h++) {
+            Cx<T> w[2][3];
+            Spinor4<PS>::load_half(a.in, total, nb*NR + q*R, h, w);
+#pragma unroll
+            for(int c=0; c<3; c++) { v[2*h][c] = w[0][c]; v[2*h + 1][c] = w[1][c]; }
+          }
+        };
+        auto fma_slot = [&](const Cx<T> (&U)[9], const Cx<T> (&v)[R][3]) {
+#pragma unroll
+          for(int j=0; j<R; j++) {
+#pragma unroll
+            for(int l=0; l<3; l++) {
+#pragma unroll
+              for(int c=0; c<3; c++) {
+                if constexpr (F2) cmac_f2(acc[j][c], U[3*l + c], v[j][l]);
+                else cmac(acc[j][c], U[3*l + c], v[j][l]);
+              }
+            }
+          }
+        };
+        if(allact) {
+          Cx<T> U0[9], U1[9], v0[R][3], v1[R][3];
+          load_slot(0, U0, v0);
+#pragma unroll
+          for(int sl=0; sl<NSL; sl+=2) {
+            load_slot(sl + 1, U1, v1);
+            fma_slot(U0, v0);
+            if(sl + 2 < NSL) load_slot(sl + 2, U0, v0);
+            fma_slot(U1, v1);
+          }
+        } else {
+          slots(std::integral_constant<bool, true>());
+        }
+      } else {
+        if(allact) slots(std::integral_constant<bool, false>());
+        else slots(std::integral_constant<bool, true>());
       }
       // epilogue.  With v4 and all R rhs active, the R rhs of the site move
       // as 16-byte vectors (inactive rhs must keep their old values, so a
@@ -312,14 +427,14 @@ stag_dslash_mr(qllg_stag_args a)
                 const int j = 2*h + jj;
 #pragma unroll
                 for(int c=0; c<3; c++) {
-                  T apr = fma(cb, acc[j][c].r, ca[j]*sv[jj][c].r);
-                  T api = fma(cb, acc[j][c].i, ca[j]*sv[jj][c].i);
-                  xv[jj][c].r = fma(alpha[j], sv[jj][c].r, xv[jj][c].r);
-                  xv[jj][c].i = fma(alpha[j], sv[jj][c].i, xv[jj][c].i);
-                  rv[jj][c].r = fma(-alpha[j], apr, rv[jj][c].r);
-                  rv[jj][c].i = fma(-alpha[j], api, rv[jj][c].i);
+                  T apr = fma(cb, acc[j][c].r, cav(j)*sv[jj][c].r);
+                  T api = fma(cb, acc[j][c].i, cav(j)*sv[jj][c].i);
+                  xv[jj][c].r = fma(alv(j), sv[jj][c].r, xv[jj][c].r);
+                  xv[jj][c].i = fma(alv(j), sv[jj][c].i, xv[jj][c].i);
+                  rv[jj][c].r = fma(-alv(j), apr, rv[jj][c].r);
+                  rv[jj][c].i = fma(-alv(j), api, rv[jj][c].i);
                 }
-                acc0[j].norm(rv[jj]);
+                norm0(j, rv[jj]);
               }
               Spinor4<PX>::store_half(a.x, total, t0, h, xv);
               Spinor4<PX>::store_half(a.r, total, t0, h, rv);
@@ -332,15 +447,15 @@ stag_dslash_mr(qllg_stag_args a)
 #pragma unroll
               for(int c=0; c<3; c++) {
                 if(a.mode == 2) {
-                  T sr = a.self ? ca[j]*sv[jj][c].r : (T)0, si = a.self ? ca[j]*sv[jj][c].i : (T)0;
+                  T sr = a.self ? cav(j)*sv[jj][c].r : (T)0, si = a.self ? cav(j)*sv[jj][c].i : (T)0;
                   ov[jj][c].r = fma(cb, acc[j][c].r, sr);
                   ov[jj][c].i = fma(cb, acc[j][c].i, si);
                 } else {
                   ov[jj][c] = acc[j][c];
                 }
               }
-              if(a.norm_out) acc0[j].norm(ov[jj]);
-              if(a.norm_self && a.self) acc1[j].norm(sv[jj]);
+              if(a.norm_out) norm0(j, ov[jj]);
+              if(a.norm_self && a.self) norm1(j, sv[jj]);
             }
             Spinor4<PS>::store_half(a.out, total, t0, h, ov);
           }
@@ -359,11 +474,11 @@ stag_dslash_mr(qllg_stag_args a)
           SpinorIO<PX,3>::load(a.r, total, t, rv);
 #pragma unroll
           for(int c=0; c<3; c++) {
-            T apr = fma(cb, acc[j][c].r, ca[j]*self[c].r), api = fma(cb, acc[j][c].i, ca[j]*self[c].i);
-            xv[c].r = fma(alpha[j], self[c].r, xv[c].r); xv[c].i = fma(alpha[j], self[c].i, xv[c].i);
-            rv[c].r = fma(-alpha[j], apr, rv[c].r); rv[c].i = fma(-alpha[j], api, rv[c].i);
+            T apr = fma(cb, acc[j][c].r, cav(j)*self[c].r), api = fma(cb, acc[j][c].i, cav(j)*self[c].i);
+            xv[c].r = fma(alv(j), self[c].r, xv[c].r); xv[c].i = fma(alv(j), self[c].i, xv[c].i);
+            rv[c].r = fma(-alv(j), apr, rv[c].r); rv[c].i = fma(-alv(j), api, rv[c].i);
           }
-          acc0[j].norm(rv);
+          norm0(j, rv);
           SpinorIO<PX,3>::store(a.x, total, t, xv);
           SpinorIO<PX,3>::store(a.r, total, t, rv);
           continue;
@@ -372,7 +487,7 @@ stag_dslash_mr(qllg_stag_args a)
         if(a.mode == 2) {
 #pragma unroll
           for(int c=0; c<3; c++) {
-            T sr = a.self ? ca[j]*self[c].r : (T)0, si = a.self ? ca[j]*self[c].i : (T)0;
+            T sr = a.self ? cav(j)*self[c].r : (T)0, si = a.self ? cav(j)*self[c].i : (T)0;
             out[c].r = fma(cb, acc[j][c].r, sr);
             out[c].i = fma(cb, acc[j][c].i, si);
           }
@@ -381,14 +496,23 @@ stag_dslash_mr(qllg_stag_args a)
           for(int c=0; c<3; c++) out[c] = acc[j][c];
         }
         SpinorIO<PS,3>::store(a.out, total, t, out);
-        if(a.norm_out) acc0[j].norm(out);
-        if(a.norm_self && a.self) acc1[j].norm(self);
+        if(a.norm_out) norm0(j, out);
+        if(a.norm_self && a.self) norm1(j, self);
       }
     }
   }
   double red[2][R];
+  if constexpr (LEAN) {
 #pragma unroll
-  for(int j=0; j<R; j++) { red[0][j] = acc0[j].get(); red[1][j] = acc1[j].get(); }
+    for(int j=0; j<R; j++) {
+      red[0][j] = accs[j*TB + threadIdx.x].get();
+      red[1][j] = accs[(R + j)*TB + threadIdx.x].get();
+    }
+    __syncthreads();                 // the grid reduction reuses shm
+  } else {
+#pragma unroll
+    for(int j=0; j<R; j++) { red[0][j] = acc0r[j].get(); red[1][j] = acc1r[j].get(); }
+  }
   if(a.mode == 3) {
     if(skip) return;
     double *res[2] = {a.sc->tmp, NULL};
@@ -509,20 +633,26 @@ bool vec4_ok(const qllg_stag_args *a)
   return true;
 }
 
-template <int PS, int PL, int NS, int NR, int R>
+// CFG 0 falls back to per-rhs loads when the buffers are not 16-byte
+// aligned; the other launch shapes are 16-byte only (variant_ok checks)
+template <int PS, int PL, int NS, int NR, int R, int CFG = 0>
 int launch_mr(const qllg_stag_args *a)
 {
-  const bool v4 = (R % 2 == 0) && PS == QLLG_F32 && qllg_get_param("dslash_vec4") != 0 &&
-                  vec4_ok(a);
+  constexpr int TB = MrCfg<PS,R,CFG>::threads;
+  const bool v4 = CFG != 0 ||
+                  ((R % 2 == 0) && PS == QLLG_F32 && qllg_get_param("dslash_vec4") != 0 && vec4_ok(a));
+  auto kern = [](bool vec) {
+    if constexpr (CFG == 0) return vec ? stag_dslash_mr<PS,PL,NS,NR,R,true,0> : stag_dslash_mr<PS,PL,NS,NR,R,false,0>;
+    else { (void)vec; return stag_dslash_mr<PS,PL,NS,NR,R,true,CFG>; }
+  };
   static int blocks_per_sm[2] = {0, 0};
   if(!blocks_per_sm[v4]) {
     if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm[v4], v4 ? stag_dslash_mr<PS,PL,NS,NR,R,true> : stag_dslash_mr<PS,PL,NS,NR,R,false>,
-         kThreads, 0), "occupancy")) return -1;
+         &blocks_per_sm[v4], kern(v4), TB, 0), "occupancy")) return -1;
     if(blocks_per_sm[v4] < 1) blocks_per_sm[v4] = 1;
   }
   size_t work = (size_t)a->g.Vh * (NR/R);
-  size_t need = (work + kThreads - 1)/kThreads;
+  size_t need = (work + TB - 1)/TB;
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm[v4];
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
   int grid = (int)(need < maxg ? need : maxg);
@@ -530,8 +660,7 @@ int launch_mr(const qllg_stag_args *a)
   qllg_stag_args A = *a;
   A.partial = a->rb ? a->rb->partial : NULL;
   A.counter = a->rb ? a->rb->counter : NULL;
-  if(v4) stag_dslash_mr<PS,PL,NS,NR,R,true><<<grid, kThreads, 0, qllg_stream()>>>(A);
-  else stag_dslash_mr<PS,PL,NS,NR,R,false><<<grid, kThreads, 0, qllg_stream()>>>(A);
+  kern(v4)<<<grid, TB, 0, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash_mr launch");
 }
 
@@ -858,10 +987,15 @@ int launch_tile(const qllg_stag_args *a)
 
 // variants of one launch shape, in the order the autotuner tries them:
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
-// rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only)
-constexpr int kNumVariants = 4;
+// rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
+// spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
+// launch shapes, MrCfg 1-6 as variants 4-9
+constexpr int kNumVariants = 10;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
-                                                "smem-staged 4 rhs/thread"};
+                                                "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
+                                                "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
+                                                "4 rhs/thread lean 56 regs", "4 rhs/thread prefetch",
+                                                "4 rhs/thread lean prefetch"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -869,6 +1003,8 @@ bool variant_ok(const qllg_stag_args *a, int v)
   if(v == 0) return NR >= 4;
   if(v == 1) return NR >= 2;
   if(v == 2) return true;
+  if(v >= 4)
+    return PS == QLLG_F32 && NR == 16 && vec4_ok(a) && qllg_get_param("dslash_vec4") != 0;
   return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
          a->g.Vh % kTileSites == 0 && vec4_ok(a) && qllg_get_param("dslash_tile") != 0;
 }
@@ -880,6 +1016,18 @@ int launch_variant(const qllg_stag_args *a, int v)
   if constexpr (PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16) {
     if(v == 3) return launch_tile<NR>(a);
   }
+  if constexpr (PS == QLLG_F32 && NR == 16) {
+    if(v >= 4) {
+      switch(v) {
+      case 4: return launch_mr<PS,PL,NS,NR,4,1>(a);
+      case 5: return launch_mr<PS,PL,NS,NR,4,2>(a);
+      case 6: return launch_mr<PS,PL,NS,NR,4,3>(a);
+      case 7: return launch_mr<PS,PL,NS,NR,4,4>(a);
+      case 8: return launch_mr<PS,PL,NS,NR,4,5>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,6>(a);
+      }
+    }
+  }
   if constexpr (NR >= 4) { if(v == 0) return launch_mr<PS,PL,NS,NR,4>(a); }
   if constexpr (NR >= 2) { if(v == 1) return launch_mr<PS,PL,NS,NR,2>(a); }
   return launch_plain<PS,PL,NS,NR>(a);
@@ -888,7 +1036,9 @@ int launch_variant(const qllg_stag_args *a, int v)
 // Autotuner: the first launch of a shape (precisions, slots, rhs, lattice)
 // times each variant on a side output buffer (mode 0, no reductions, every
 // rhs active: the same Dslash work the solvers do) and keeps the fastest
-// in the registry; later launches of that shape, in every mode, use it.
+// in the registry; later launches of that shape use it, in every mode but
+// the fused CG update (mode 3), which is timed the same way on copies of
+// its x, r and scalars under a key of its own.
 // All variants give bitwise the same Dslash output; only the order of the
 // per-rhs reductions differs between them.  No tuning during a stream
 // capture or for callers that must not allocate: they use a tuned choice
@@ -899,25 +1049,50 @@ int tuned_variant(const qllg_stag_args *a)
   if(NR < 2 || qllg_mr_disabled()) return 2;
   const int force = (int)qllg_get_param("dslash_variant");
   if(force >= 0 && force < kNumVariants && variant_ok<PS,PL,NS,NR>(a, force)) return force;
+  // the fused CG launch (mode 3: its epilogue reads and writes x and r) is
+  // tuned on its own: its best launch shape differs from the plain one's
+  const bool fused = a->mode == 3;
   char key[96];
-  snprintf(key, sizeof(key), "stag_dslash p%d/%d s%d%s n%d V%d (%d %d %d %d)", PS, PL, NS,
-           a->fb ? "fb" : "", NR, a->g.V, a->g.L[0], a->g.L[1], a->g.L[2], a->g.L[3]);
+  snprintf(key, sizeof(key), "stag_dslash%s p%d/%d s%d%s n%d V%d (%d %d %d %d)", fused ? " fused" : "",
+           PS, PL, NS, a->fb ? "fb" : "", NR, a->g.V, a->g.L[0], a->g.L[1], a->g.L[2], a->g.L[3]);
   int v = qllg_tune_lookup(key);
   if(v >= 0) return v;
   const int first = NR >= 4 ? 0 : 1;
   if(a->no_tune || qllg_capturing() || qllg_get_param("autotune") == 0) return first;
   qllg_stag_args T = *a;
-  T.mode = 0;
-  T.self = NULL;
-  T.norm_out = T.norm_self = NULL;
-  T.active = NULL;
-  T.done = NULL;
-  T.x = T.r = NULL;
-  T.sc = NULL;
-  T.rb = NULL;
-  T.compact = 0;
-  T.out = qllg_dmalloc(qllg_spinor_bytes(PS, 3)*(size_t)a->g.Vh*NR);
-  if(!T.out) return -1;
+  void *scratch[3] = {NULL, NULL, NULL};
+  if(fused) {
+    // the same launch on copies of x, r and the CG scalars
+    const size_t xb = qllg_spinor_bytes(VecPrec<PS>::value, 3)*(size_t)a->g.Vh*NR;
+    const size_t rbytes = qllg_spinor_bytes(PS, 3)*(size_t)a->g.Vh*NR;
+    const size_t sizes[3] = {xb, rbytes, sizeof(qllg_cg_scalars)};
+    const void *src[3] = {a->x, a->r, a->sc};
+    for(int i=0; i<3; i++) {
+      scratch[i] = qllg_dmalloc(sizes[i]);
+      if(!scratch[i] || qllg_check_cuda(cudaMemcpyAsync(scratch[i], src[i], sizes[i],
+                                                         cudaMemcpyDeviceToDevice, qllg_stream()),
+                                        "tune copy")) {
+        for(int k=0; k<=i; k++) qllg_dfree(scratch[k]);
+        return -1;
+      }
+    }
+    T.x = scratch[0];
+    T.r = scratch[1];
+    T.sc = (qllg_cg_scalars *)scratch[2];
+    T.done = NULL;
+  } else {
+    T.mode = 0;
+    T.self = NULL;
+    T.norm_out = T.norm_self = NULL;
+    T.active = NULL;
+    T.done = NULL;
+    T.x = T.r = NULL;
+    T.sc = NULL;
+    T.rb = NULL;
+    T.compact = 0;
+    T.out = scratch[0] = qllg_dmalloc(qllg_spinor_bytes(PS, 3)*(size_t)a->g.Vh*NR);
+    if(!T.out) return -1;
+  }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -939,7 +1114,7 @@ int tuned_variant(const qllg_stag_args *a)
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   qllg_sync();
-  qllg_dfree(T.out);
+  for(int i=0; i<3; i++) qllg_dfree(scratch[i]);
   if(rc) return -1;
   qllg_tune_store(key, best, kNumVariants, ms, kVariantName);
   return best;
@@ -965,6 +1140,16 @@ int launch_nr(const qllg_stag_args *a)
   case 16: return launch_t<PS,PL,NS,16>(a);
   }
   qllg_set_error("stag_dslash: nrhs %d not in {1,2,4,8,16}", a->nrhs);
+  return -1;
+}
+
+// one slot count only (the FP32 instantiations are split by slot count
+// over two translation units, which compile in parallel)
+template <int PS, int PL, int NS>
+int launch_ns_only(const qllg_stag_args *a)
+{
+  if(a->nslots == NS) return launch_nr<PS,PL,NS>(a);
+  qllg_set_error("stag_dslash: nslots %d not 8 or 16", a->nslots);
   return -1;
 }
 

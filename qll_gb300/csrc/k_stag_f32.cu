@@ -1,9 +1,13 @@
 // k_stag_f32.cu -- the FP32 instantiations of the asqtad half-Dslash
-// (kernels and launchers in k_stag.cuh).
+// (kernels and launchers in k_stag.cuh): 16 slots here, 8 slots (fat links
+// only) in k_stag_f32_ns8.cu.
 #include "k_stag.cuh"
+
+extern "C" int qllg_k_stag_dslash_f32_ns8(const qllg_stag_args *a);
 
 extern "C" int
 qllg_k_stag_dslash_f32(const qllg_stag_args *a)
 {
-  return launch_ns<QLLG_F32, QLLG_F32>(a);
+  if(a->nslots == 8) return qllg_k_stag_dslash_f32_ns8(a);
+  return launch_ns_only<QLLG_F32, QLLG_F32, 16>(a);
 }

@@ -1,9 +1,13 @@
 // k_stag_f32r.cu -- the FP32-spinor, reconstruct-12-link instantiations of
-// the asqtad half-Dslash (kernels and launchers in k_stag.cuh).
+// the asqtad half-Dslash (kernels and launchers in k_stag.cuh): 16 slots
+// here, 8 slots in k_stag_f32r_ns8.cu (the two compile in parallel).
 #include "k_stag.cuh"
+
+extern "C" int qllg_k_stag_dslash_f32r_ns8(const qllg_stag_args *a);
 
 extern "C" int
 qllg_k_stag_dslash_f32r(const qllg_stag_args *a)
 {
-  return launch_ns<QLLG_F32, QLLG_F32R>(a);
+  if(a->nslots == 8) return qllg_k_stag_dslash_f32r_ns8(a);
+  return launch_ns_only<QLLG_F32, QLLG_F32R, 16>(a);
 }

@@ -12,7 +12,7 @@
 #include "qllg_internal.h"
 
 #define NTUNE 256
-#define NCAND 8
+#define NCAND 16
 
 static struct {
   char key[96];

@@ -348,6 +348,20 @@ def test_single_stored_operator_matches_double_stored():
                                                  vp(src.data_ptr())) == 0, qll.last_error()
                 torch.cuda.synchronize()
                 assert torch.equal(o1.view(torch.uint8), o2.view(torch.uint8)), (prec, nrhs, parity)
+    # every autotuner candidate of the 16-rhs FP32 kernel, single-stored
+    # against double-stored
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    n = L.qllg_stag_vec_bytes(S2, 1, 16)
+    src = torch.randn(n//4, dtype=torch.float32, device="cuda", generator=g)
+    for v in range(10):
+        L.qllg_set_param(b"dslash_variant", v)
+        o2, o1 = torch.zeros_like(src), torch.zeros_like(src)
+        torch.cuda.synchronize()
+        assert L.qllg_stag_dslash_device(S2, 1, 16, 1, vp(o2.data_ptr()), vp(src.data_ptr())) == 0
+        assert L.qllg_stag_dslash_device(S1, 1, 16, 1, vp(o1.data_ptr()), vp(src.data_ptr())) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(o1.view(torch.uint8), o2.view(torch.uint8)), v
+    L.qllg_set_param(b"dslash_variant", -1)
     nrhs = 8
     masses = (c_double*nrhs)(*[0.05 + 0.01*k for k in range(nrhs)])
     bs = [qll.gen_source(dims, 9000 + k, 6, "even") for k in range(nrhs)]
