@@ -693,7 +693,7 @@ def run_dslash_only(args):
     stream = torch.cuda.current_stream()
     L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
     dims = tuple(int(v) for v in args.dims.split(","))
-    prec = {"f64": 0, "f32": 1, "i16": 2, "f32r": 3}[args.prec]
+    prec = {"f64": 0, "f32": 1, "i16": 2, "f32r": 3, "df": 4}[args.prec]
     thin = qll.gen_gauge(dims, SEED_GAUGE, EPS, ks=True)
     coef = qll.asqtad_coeffs()
     S = ctypes.c_void_p(L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(thin),
@@ -764,10 +764,25 @@ def run_solve_only(args):
     L.qllg_stag_vec_upload(S, b, nrhs, qll.vp_array(srcs))
     masses = (ctypes.c_double*nrhs)(*([MASS]*nrhs))
     info = qll.SolveInfo()
+    fams = ["stag_dslash_f32_n%d" % nrhs, "stag_cg_fused_f32_n%d" % nrhs,
+            "stag_dslash_f64_n%d" % nrhs, "stag_dslash_df_n%d" % nrhs]
     for k in range(args.launches):
+        timed = args.timing and k == args.launches - 1
+        if timed:
+            # per-kernel-family CUDA events (the host-polled loop, no graph)
+            L.qllg_timing_enable(1)
+            L.qllg_timing_reset()
         t = time.time()
         its = L.qllg_stag_solve_device(S, nrhs, x, b, masses, RSQ, MAXITS, mode, ctypes.byref(info))
         dt = time.time() - t
+        if timed:
+            L.qllg_timing_enable(0)
+            tm = {}
+            for f in fams:
+                cnt, tot = ctypes.c_int(), ctypes.c_double()
+                L.qllg_timing_read(f.encode(), ctypes.byref(cnt), ctypes.byref(tot))
+                tm[f] = {"launches": cnt.value, "ms": tot.value}
+            print(json.dumps({"timing": tm}), flush=True)
         print(json.dumps({"solve_only": {"dims": dims, "nrhs": nrhs, "mode": args.mode,
                                          "params": args.param, "iters": its,
                                          "reliable_updates": info.reliable_updates,
@@ -798,6 +813,8 @@ def main():
                     choices=["double", "single", "mixed_half", "mixed_single"])
     ap.add_argument("--param", action="append", default=[])
     ap.add_argument("--serve", action="store_true", help="only the serving benchmark")
+    ap.add_argument("--timing", action="store_true",
+                    help="--solve-only: per-kernel-family event times of the last solve")
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the Wilson, multishift and serving legs")
     ap.add_argument("--multishift", action="store_true", help="only the multishift benchmark")

@@ -59,7 +59,10 @@ enum {
 typedef struct {
   int iters[16];          /* iterations per right-hand side */
   double rsq[16];         /* final |r|^2/|b|^2 of the solver's recurrence */
-  double true_rsq[16];    /* |b - A x|^2/|b|^2 recomputed in FP64 */
+  double true_rsq[16];    /* |b - A x|^2/|b|^2 in FP64 for the returned x:
+                             recomputed after an FP64 solve; for the mixed
+                             modes the residual of the final reliable update,
+                             which every rhs ends on (r = b - A x in FP64) */
   int reliable_updates;
   int total_iters;        /* iterations of the batch (max over rhs) */
   double seconds;         /* device time of the solve */
@@ -131,8 +134,10 @@ int qllg_stag_vec_download(qllg_stag *S, const void *v_dev, int nrhs, void *cons
 
 /* the half Dslash out = D in (output sites of out_parity) on device vectors
  * of nrhs rhs, precision prec (0 FP64, 1 FP32, 2 16-bit, 3 FP32 with the
- * reconstruct-12 links) in the library layout; links of that precision are
- * derived from FP64 on first use */
+ * reconstruct-12 links, 4 double-float: each real a (hi, lo) pair of floats
+ * in the FP64 layout, the arithmetic of the mixed solver's reliable
+ * updates) in the library layout; links of that precision are derived from
+ * FP64 on first use */
 int qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *out_dev,
                             const void *in_dev);
 

@@ -236,6 +236,43 @@ __global__ void link_from_f64(void *dev, const float *scale, const double *in, i
   }
 }
 
+// FP64 values -> double-float (hi, lo) pairs, value by value (links: a slot
+// is 9 V complex entries, laid out as in FP64)
+__global__ void to_df_k(float2 *out, const double *in, size_t n)
+{
+  GRID_LOOP(i, n) {
+    const dfl d(in[i]);
+    out[i] = make_float2(d.h, d.l);
+  }
+}
+
+// FP64 spinor columns <-> double-float, for the rhs whose active[] entry is
+// eq (any nonzero one when eq is 0, every rhs when active is NULL);
+// nothing when *skip is set.  The conversion back may run in place.
+template <int NR, bool TO>
+__global__ void __launch_bounds__(kT)
+spinor_df_k(void *out, const void *in, int nsites, int ncomp, const int *active, int eq,
+            const int *skip)
+{
+  if(skip && *(volatile const int *)skip) return;
+  bool any = !active;
+  if(active) for(int r=0; r<NR; r++) any |= active[r] != 0 && (!eq || active[r] == eq);
+  if(!any) return;
+  const size_t total = (size_t)nsites*NR*ncomp;
+  GRID_LOOP(t, total) {
+    const int rhs = (int)(t % NR);
+    if(active && (!active[rhs] || (eq && active[rhs] != eq))) continue;
+    if(TO) {
+      const double2 d = ((const double2 *)in)[t];
+      const dfl re(d.x), im(d.y);
+      ((float4 *)out)[t] = make_float4(re.h, re.l, im.h, im.l);
+    } else {
+      const float4 q = ((const float4 *)in)[t];
+      ((double2 *)out)[t] = make_double2((double)q.x + (double)q.y, (double)q.z + (double)q.w);
+    }
+  }
+}
+
 // FP64 slot -> reconstruct-12 FP32 (see LinkR): the Naik rows are rounded
 // to FP32 first and row 2 rebuilt from the rounded rows exactly as the
 // Dslash rebuilds it; the sign is the one that matches the stored row 2,
@@ -661,11 +698,24 @@ qllg_k_link_convert(int prec, void *out, float *scale, const double *in, int V)
     if(qllg_check_cuda(cudaMemsetAsync(scale, 0, sizeof(float), st), "memset")) return -1;
     link_f64_maxabs<<<grid_for((size_t)V*18, 0, 0),kT,0,st>>>(in, V, (unsigned *)scale);
     link_from_f64<QLLG_I16><<<g,kT,0,st>>>(out, scale, in, V);
+  } else if(prec == QLLG_DF) {
+    to_df_k<<<grid_for((size_t)V*18, 0, 0),kT,0,st>>>((float2 *)out, in, (size_t)V*18);
   } else {
     qllg_set_error("link_convert: precision %d", prec);
     return -1;
   }
   return done("link_convert");
+}
+
+extern "C" int
+qllg_k_spinor_df(int to_df, void *out, const void *in, int nsites, int ncomp, int nrhs,
+                 const int *active, int eq, const int *skip)
+{
+  const int g = grid_for((size_t)nsites*nrhs*ncomp, 0, 0);
+  cudaStream_t st = qllg_stream();
+  if(to_df) { NR_SWITCH(nrhs, (spinor_df_k<NR,true><<<g,kT,0,st>>>(out, in, nsites, ncomp, active, eq, skip))); }
+  else { NR_SWITCH(nrhs, (spinor_df_k<NR,false><<<g,kT,0,st>>>(out, in, nsites, ncomp, active, eq, skip))); }
+  return done("spinor_df");
 }
 
 extern "C" int

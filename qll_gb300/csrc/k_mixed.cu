@@ -226,11 +226,8 @@ mcg_update_k(void *xs, void *rs, const void *p, const void *Ap, int nsites,
         double r2 = s->tmp[q];
         s->iters[q]++;
         s->rsq[q] = r2;
-        if(r2 < s->delta2*s->maxr2[q] || r2 < s->rsq_stop[q] || s->iters[q] >= s->maxits ||
-           !(r2 == r2)) {
-          s->ru[q] = 1;
-          anyru = 1;
-        }
+        s->ru[q] = ru_kind(s, q, r2);
+        anyru |= s->ru[q] != 0;
       }
       s->no_ru = !anyru;
       s->count++;
@@ -587,8 +584,8 @@ scg_xr_k(void *x, void *r, const void *p, const void *Ap, int nsites, qllg_cg_sc
           s->rsq[q] = r2;
           s->alpha[q] = r2/s->prev[q];
           if(mixed) {
-            if(r2 < s->delta2*s->maxr2[q] || r2 < s->rsq_stop[q] || s->iters[q] >= s->maxits ||
-               !(r2 == r2)) { s->ru[q] = 1; anyru = 1; }
+            s->ru[q] = ru_kind(s, q, r2);
+            anyru |= s->ru[q] != 0;
           } else if(!(r2 >= s->rsq_stop[q] && s->iters[q] < s->maxits)) {
             s->active[q] = 0;
           }

@@ -9,6 +9,7 @@ extern "C" int qllg_k_stag_dslash_f64(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_f32(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_i16(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_f32r(const qllg_stag_args *a);
+extern "C" int qllg_k_stag_dslash_df(const qllg_stag_args *a);
 
 namespace {
 
@@ -30,8 +31,8 @@ nbr_table(qllg_geom g, int p, int slot, int *out)
 extern "C" int
 qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
 {
-  if(a->compact && (!a->active || a->norm_out || a->norm_self || a->mode == 1 || a->mode == 3)) {
-    qllg_set_error("stag_dslash: compacted launch needs a mask and takes modes 0 and 2 only");
+  if(a->compact && (a->norm_out || a->norm_self || a->mode == 1 || a->mode == 3)) {
+    qllg_set_error("stag_dslash: compacted launch takes modes 0 and 2 only, without norms");
     return -1;
   }
   if((a->norm_out || a->norm_self || a->mode == 3) && !a->rb) {
@@ -42,6 +43,7 @@ qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
   if(ps == QLLG_F32 && pl == QLLG_F32) return qllg_k_stag_dslash_f32(a);
   if(ps == QLLG_I16 && pl == QLLG_I16) return qllg_k_stag_dslash_i16(a);
   if(ps == QLLG_F32 && pl == QLLG_F32R) return qllg_k_stag_dslash_f32r(a);
+  if(ps == QLLG_DF && pl == QLLG_DF) return qllg_k_stag_dslash_df(a);
   qllg_set_error("stag_dslash: unsupported precision pair %d/%d", ps, pl);
   return -1;
 }

@@ -544,7 +544,8 @@ stag_dslash_compact(qllg_stag_args a)
   if(a.done && *(volatile const int *)a.done) return;      // uniform
   if(threadIdx.x == 0) {
     int n = 0;
-    for(int r=0; r<NR; r++) if(a.active[r]) list[n++] = r;
+    for(int r=0; r<NR; r++)
+      if(!a.active || (a.active[r] && (!a.active_eq || a.active[r] == a.active_eq))) list[n++] = r;
     nact_s = n;
   }
   __syncthreads();
@@ -594,8 +595,8 @@ stag_dslash_compact(qllg_stag_args a)
 #pragma unroll
       for(int c=0; c<3; c++) {
         T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
-        out[c].r = fma(cb, acc[c].r, sr);
-        out[c].i = fma(cb, acc[c].i, si);
+        out[c].r = kfma(cb, acc[c].r, sr);
+        out[c].i = kfma(cb, acc[c].i, si);
       }
     } else {
 #pragma unroll
@@ -1062,10 +1063,10 @@ int tuned_variant(const qllg_stag_args *a)
   qllg_stag_args T = *a;
   void *scratch[3] = {NULL, NULL, NULL};
   if(fused) {
-    // the same launch on copies of x, r and the CG scalars
+    // the same launch on copies of x, r and the CG scalars.  The kernel
+    // reads and writes x and r in VecPrec<PS> (FP32 for 16-bit operands)
     const size_t xb = qllg_spinor_bytes(VecPrec<PS>::value, 3)*(size_t)a->g.Vh*NR;
-    const size_t rbytes = qllg_spinor_bytes(PS, 3)*(size_t)a->g.Vh*NR;
-    const size_t sizes[3] = {xb, rbytes, sizeof(qllg_cg_scalars)};
+    const size_t sizes[3] = {xb, xb, sizeof(qllg_cg_scalars)};
     const void *src[3] = {a->x, a->r, a->sc};
     for(int i=0; i<3; i++) {
       scratch[i] = qllg_dmalloc(sizes[i]);

@@ -14,16 +14,65 @@ template <> struct Real<QLLG_F64> { typedef double T; typedef double2 V2; };
 template <> struct Real<QLLG_F32> { typedef float T; typedef float2 V2; };
 template <> struct Real<QLLG_I16> { typedef float T; typedef float2 V2; };
 template <> struct Real<QLLG_F32R> { typedef float T; typedef float2 V2; };
+template <> struct Real<QLLG_DF> { typedef float T; typedef float4 V2; };
 
 // storage of the residual/solution vectors that go with Dslash operands of
 // precision P: 16-bit Dslash operands keep FP32 recurrence vectors
 template <int P> struct VecPrec { static constexpr int value = (P == QLLG_F64) ? QLLG_F64 : QLLG_F32; };
+
+// ----------------------------------------------------------- double-float
+// A real as the unevaluated sum h + l of two floats with |l| <= ulp(h)/2,
+// about 48 significant bits, computed with FP32 instructions only: this
+// part runs FP32 at many times its FP64 rate.  Products use Dekker's exact
+// product through fma (a.h*b.h = p + e exactly), sums Knuth's TwoSum; the
+// cross terms a.h*b.l + a.l*b.h are rounded once more and a.l*b.l is
+// dropped, so a product or a fused multiply-add is good to about 2^-47
+// relative.  __fmul_rn/__fadd_rn/__fsub_rn keep the compiler from
+// contracting the error terms into fmas.
+// a*b + c with one rounding, for every arithmetic type of the Dslash
+// kernels (double-float below)
+__device__ __forceinline__ float kfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double kfma(double a, double b, double c) { return ::fma(a, b, c); }
+
+struct dfl {
+  float h, l;
+  __device__ __forceinline__ dfl() {}
+  __device__ __forceinline__ dfl(float hh, float ll) : h(hh), l(ll) {}
+  __device__ __forceinline__ dfl(double d) {
+    h = __double2float_rn(d);
+    l = __double2float_rn(d - (double)h);
+  }
+  __device__ __forceinline__ explicit operator double() const { return (double)h + (double)l; }
+};
+__device__ __forceinline__ dfl df_fast2sum(float s, float e) {   // needs |s| >= |e| or s = 0
+  const float h = __fadd_rn(s, e);
+  return dfl(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ dfl operator-(const dfl &a) { return dfl(-a.h, -a.l); }
+__device__ __forceinline__ dfl operator*(const dfl &a, const dfl &b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_fast2sum(p, e);
+}
+__device__ __forceinline__ dfl kfma(const dfl &a, const dfl &b, const dfl &c) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = __fadd_rn(c.h, p);                    // TwoSum(c.h, p) = s + err
+  const float bb = __fsub_rn(s, c.h);
+  const float err = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  return df_fast2sum(s, __fadd_rn(err, __fadd_rn(c.l, e)));
+}
 
 // arithmetic type of a kernel that reads precision A and writes B
 template <int A, int B> struct Calc { typedef float T; };
 template <int B> struct Calc<QLLG_F64, B> { typedef double T; };
 template <int A> struct Calc<A, QLLG_F64> { typedef double T; };
 template <> struct Calc<QLLG_F64, QLLG_F64> { typedef double T; };
+template <> struct Calc<QLLG_DF, QLLG_DF> { typedef dfl T; };
 
 // ---------------------------------------------------------------- geometry
 struct Geo {
@@ -57,8 +106,8 @@ template <typename T> struct Cx { T r, i; };
 
 template <typename T>
 __device__ __forceinline__ void cmac(Cx<T> &acc, const Cx<T> &m, const Cx<T> &v) {
-  acc.r = fma(m.r, v.r, acc.r); acc.i = fma(m.i, v.r, acc.i);
-  acc.r = fma(-m.i, v.i, acc.r); acc.i = fma(m.r, v.i, acc.i);
+  acc.r = kfma(m.r, v.r, acc.r); acc.i = kfma(m.i, v.r, acc.i);
+  acc.r = kfma(-m.i, v.i, acc.r); acc.i = kfma(m.r, v.i, acc.i);
 }
 
 // cmac for FP32 on packed pairs (fma.rn.f32x2, sm_100 and later): the same
@@ -109,6 +158,24 @@ template <int NC> struct SpinorIO<QLLG_F32, NC> {
     float2 *p = (float2 *)b;
 #pragma unroll
     for(int c=0; c<NC; c++) p[c*stride + idx] = make_float2((float)v[c].r, (float)v[c].i);
+  }
+};
+
+// double-float spinor: one float4 (re.h, re.l, im.h, im.l) per complex
+// component, laid out as FP64
+template <int NC> struct SpinorIO<QLLG_DF, NC> {
+  static __device__ __forceinline__ void load(const void *b, size_t stride, size_t idx, Cx<dfl> v[NC]) {
+    const float4 *p = (const float4 *)b;
+#pragma unroll
+    for(int c=0; c<NC; c++) {
+      float4 t = __ldg(p + c*stride + idx);
+      v[c].r = dfl(t.x, t.y); v[c].i = dfl(t.z, t.w);
+    }
+  }
+  static __device__ __forceinline__ void store(void *b, size_t stride, size_t idx, const Cx<dfl> v[NC]) {
+    float4 *p = (float4 *)b;
+#pragma unroll
+    for(int c=0; c<NC; c++) p[c*stride + idx] = make_float4(v[c].r.h, v[c].r.l, v[c].i.h, v[c].i.l);
   }
 };
 
@@ -223,6 +290,14 @@ template <> struct LinkIO<QLLG_F32> {
     const float2 *p = (const float2 *)b + (size_t)slot*9*V + site;
 #pragma unroll
     for(int k=0; k<9; k++) { float2 t = __ldg(p + k*V); m[k].r = (T)t.x; m[k].i = (T)t.y; }
+  }
+};
+// double-float links: one float4 per complex entry, laid out as FP64
+template <> struct LinkIO<QLLG_DF> {
+  static __device__ __forceinline__ void load(const void *b, int slot, size_t V, size_t site, const float *, Cx<dfl> m[9]) {
+    const float4 *p = (const float4 *)b + (size_t)slot*9*V + site;
+#pragma unroll
+    for(int k=0; k<9; k++) { float4 t = __ldg(p + k*V); m[k].r = dfl(t.x, t.y); m[k].i = dfl(t.z, t.w); }
   }
 };
 // reconstruct-12 FP32 links.  A fat slot is [4][V] float4 (entries 2k,
@@ -451,6 +526,15 @@ __device__ inline void cg_finish_plain(qllg_cg_scalars *s, int nr) {
 
 // mixed CG: flag a reliable update when the sloppy residual fell by delta
 // since the last one, passed the target, hit maxits or is not a number
+// the reliable update rhs q takes after an iteration with |r|^2 = r2: 0
+// none; 1 an intermediate one (r2 fell by delta^2 since the last); 2 a final
+// candidate (converged, iteration limit, or not a number), on which the
+// solve of that rhs may stop, so its residual b - A x must be FP64
+__device__ __forceinline__ int ru_kind(const qllg_cg_scalars *s, int q, double r2) {
+  if(r2 < s->rsq_stop[q] || s->iters[q] >= s->maxits || !(r2 == r2)) return 2;
+  return r2 < s->delta2*s->maxr2[q] ? 1 : 0;
+}
+
 __device__ inline void cg_finish_mixed(qllg_cg_scalars *s, int nr) {
   int anyru = 0;
   for(int q=0; q<nr; q++) {
@@ -459,11 +543,8 @@ __device__ inline void cg_finish_mixed(qllg_cg_scalars *s, int nr) {
     double r2 = s->tmp[q];
     s->iters[q]++;
     s->rsq[q] = r2;
-    if(r2 < s->delta2*s->maxr2[q] || r2 < s->rsq_stop[q] || s->iters[q] >= s->maxits ||
-       !(r2 == r2)) {
-      s->ru[q] = 1;
-      anyru = 1;
-    }
+    s->ru[q] = ru_kind(s, q, r2);
+    anyru |= s->ru[q] != 0;
   }
   s->no_ru = !anyru;
   s->count++;

@@ -41,9 +41,13 @@ typedef struct {
 } qllg_geom;
 
 enum { QLLG_F64 = 0, QLLG_F32 = 1, QLLG_I16 = 2,
-       QLLG_F32R = 3 };   /* links only: FP32 in 16-byte vectors, Naik slots as
+       QLLG_F32R = 3,     /* links only: FP32 in 16-byte vectors, Naik slots as
                              two rows + a per-site sign (reconstruct-12) */
-#define QLLG_NLINKP 4
+       QLLG_DF = 4 };     /* double-float: each real as the unevaluated sum of
+                             two floats (hi, lo), same bytes as FP64; the
+                             reliable-update Dslash computes in it with FP32
+                             instructions */
+#define QLLG_NLINKP 5
 
 /* ------------------------------------------------------------ geometry */
 struct Layout_s;
@@ -52,10 +56,10 @@ void *qllg_stage(size_t bytes);          /* shared device staging buffer */
 void qllg_stage_release(void);
 /* bytes of one site and rhs of a spinor with ncomp complex components */
 static inline size_t qllg_spinor_bytes(int prec, int ncomp) {
-  return prec == QLLG_F64 ? 16u*ncomp : (prec == QLLG_F32 ? 8u*ncomp : 16u);
+  return (prec == QLLG_F64 || prec == QLLG_DF) ? 16u*ncomp : (prec == QLLG_F32 ? 8u*ncomp : 16u);
 }
 static inline size_t qllg_link_bytes(int prec) {
-  return prec == QLLG_F64 ? 144u : (prec == QLLG_F32 ? 72u : 36u);
+  return (prec == QLLG_F64 || prec == QLLG_DF) ? 144u : (prec == QLLG_F32 ? 72u : 36u);
 }
 
 /* ------------------------------------------------------------ runtime */
@@ -122,6 +126,11 @@ int qllg_k_link_convert(int prec, void *out, float *scale_dev, const double *in,
  * float4, with bit `bit` of signs[site] the sign that rebuilds row 2;
  * *bad is set when a Naik link is not a real multiple of an SU(3) matrix
  * (rows 0, 1 do not determine row 2 within FP32 rounding) */
+/* FP64 spinor columns -> double-float (to_df 1) or back (0, may run in
+ * place), for the rhs whose active[] entry is eq (any nonzero one when eq
+ * is 0, all when active is NULL); nothing when *skip */
+int qllg_k_spinor_df(int to_df, void *out, const void *in, int nsites, int ncomp, int nrhs,
+                     const int *active, int eq, const int *skip);
 int qllg_k_link_to_f32r(void *out, const double *in, int V, int naik, unsigned char *signs,
                         int bit, int *bad);
 
@@ -152,6 +161,8 @@ typedef struct {
   unsigned *counter;      /* device last-block counter (from rb) */
   int compact;           /* threads over (site, flagged rhs of active) only;
                             modes 0 and 2, no norms */
+  int active_eq;         /* compact: flagged means active[r] == active_eq
+                            (any nonzero entry when 0) */
   int no_tune;           /* caller must not allocate: no autotuning */
   int fb;                /* single-stored links: forward slots only, [nslots/2][9][V];
                             backward links made from them in the kernel */
@@ -193,7 +204,8 @@ typedef struct qllg_cg_scalars_s {
   int iters[QLLG_MAXRHS];
   double orth_re[QLLG_MAXRHS];  /* <r,p>/|r|^2 after a reliable update */
   double orth_im[QLLG_MAXRHS];
-  int ru[QLLG_MAXRHS];          /* rhs that take a reliable update now */
+  int ru[QLLG_MAXRHS];          /* rhs that take a reliable update now: 1 an
+                                   intermediate one, 2 a final candidate */
   int nru[QLLG_MAXRHS];         /* reliable updates taken per rhs */
   int maxits;
   int done;                     /* all rhs inactive */

@@ -278,10 +278,13 @@ static struct { const char *name; double value; } g_params[] = {
   {"poll", 8},               /* first batch of iterations between host checks */
   {"dslash_mr", 1},          /* multi-rhs Dslash: one thread per site and 4 rhs */
   {"ru_compact", 1},         /* reliable-update Dslash over the flagged rhs only */
+  {"ru_df", 1},              /* intermediate reliable updates of the mixed CG in
+                                double-float (FP32 pipes, about 48 bits); the
+                                final ones, on which a rhs may stop, in FP64 */
   {"dslash_vec4", 1},        /* 16-byte loads of rhs pairs (FP32) */
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
-  {"dslash_variant", -1},    /* force a Dslash variant (0-3); -1: autotuned */
+  {"dslash_variant", -1},    /* force a Dslash variant (0-9); -1: autotuned */
   {"multishift_guess_rsq", 1e-10}, /* mixed multishift: the FP32 multishift CG
                                        goes to |r|^2 < this |b|^2 before the
                                        pairs are refined in FP64 (C3 at

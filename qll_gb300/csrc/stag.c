@@ -26,7 +26,7 @@ int qllg_geom_from_layout(qllg_geom *g, const Layout *l);
 Layout *qllg_current_layout(void);
 
 enum { WS_X, WS_R, WS_P, WS_AP, WS_V, WS_B, WS_IO, WS_X64, WS_R64, WS_T64, WS_V64,
-       WS_PS, WS_OUT, WS_N };
+       WS_PS, WS_OUT, WS_XDF, WS_N };
 
 /* what one solver iteration launches */
 typedef struct {
@@ -34,6 +34,8 @@ typedef struct {
   int ps, pl, nrhs, reortho;
   void *x, *r, *p, *v;       /* sloppy (or only) vectors */
   void *x64, *r64, *t64, *w64;
+  void *xdf;                 /* double-float copy of x64 for the intermediate
+                                reliable updates, NULL: all in FP64 */
   const void *b;
 } iter_ctx;
 
@@ -54,7 +56,7 @@ struct qllg_stag {
   unsigned ws_gen;         /* bumped when a workspace buffer moves */
   cudaEvent_t ev0, ev1;
   struct {                 /* graph-captured solver loops */
-    long key[10];
+    long key[11];
     cudaGraphExec_t exec;
     int body;              /* kernels in one trip of the loop body */
   } graphs[6];
@@ -393,7 +395,7 @@ static int
 dslash_half_x(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *in,
               const void *self, void *out, int mode, const double *a, double a0, double b,
               double *norm_out, double *norm_self, const int *active, const int *done,
-              int compact)
+              int compact, int active_eq)
 {
   if(ensure_links(S, pl)) return -1;
   qllg_stag_args A;
@@ -418,7 +420,8 @@ dslash_half_x(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void
   A.done = done;
   A.rb = &S->rb;
   A.compact = compact;
-  static const char *pn[3] = {"f64", "f32", "i16"};
+  A.active_eq = active_eq;
+  static const char *pn[5] = {"f64", "f32", "i16", "f32r", "df"};
   char fam[32];
   snprintf(fam, sizeof(fam), "stag_dslash_%s_n%d", pn[ps], nrhs);
   qllg_tm_begin(fam);
@@ -433,7 +436,7 @@ dslash_half(qllg_stag *S, int ps, int pl, int out_parity, int nrhs, const void *
             double *norm_out, double *norm_self, const int *active, const int *done)
 {
   return dslash_half_x(S, ps, pl, out_parity, nrhs, in, self, out, mode, a, a0, b, norm_out,
-                       norm_self, active, done, 0);
+                       norm_self, active, done, 0, 0);
 }
 
 /* host [V][6] parity block(s) <-> device single-rhs block */
@@ -507,12 +510,12 @@ apply_normal(qllg_stag *S, int ps, int pl, int nrhs, const void *p, void *v, voi
  * many are flagged); every launch returns at once when *done is set */
 static int
 apply_normal_flagged(qllg_stag *S, int prec, int nrhs, const void *x, void *w, void *t,
-                     const int *active, const int *done)
+                     const int *active, int eq, const int *done)
 {
   if(dslash_half_x(S, prec, prec, 1, nrhs, x, NULL, w, 0, NULL, 0, 1, NULL, NULL, active, done,
-                   1)) return -1;
+                   1, eq)) return -1;
   return dslash_half_x(S, prec, prec, 0, nrhs, w, x, t, 2, S->sc->mass2, 0, -1, NULL, NULL,
-                       active, done, 1);
+                       active, done, 1, eq);
 }
 
 /* one CG iteration in three launches (cgSolveT, lib/cg.c:77-115):
@@ -597,8 +600,16 @@ issue_iteration(qllg_stag *S, const iter_ctx *c)
    * no rhs is flagged */
   if(qllg_k_mcg_accum(QLLG_F32, c->x64, c->x, Vh, 3, c->nrhs, sc)) return -1;
   if(qllg_get_param("ru_compact") != 0) {
-    if(apply_normal_flagged(S, QLLG_F64, c->nrhs, c->x64, c->w64, c->t64, sc->ru, &sc->no_ru))
-      return -1;
+    if(c->xdf) {
+      /* intermediate updates (ru 1) in double-float: x64 to (hi, lo)
+       * pairs, A x in the FP32 pipes, t back to FP64 in place; the final
+       * candidates (ru 2) below in FP64 */
+      if(qllg_k_spinor_df(1, c->xdf, c->x64, Vh, 3, c->nrhs, sc->ru, 1, &sc->no_ru) ||
+         apply_normal_flagged(S, QLLG_DF, c->nrhs, c->xdf, c->w64, c->t64, sc->ru, 1, &sc->no_ru) ||
+         qllg_k_spinor_df(0, c->t64, c->t64, Vh, 3, c->nrhs, sc->ru, 1, &sc->no_ru)) return -1;
+    }
+    if(apply_normal_flagged(S, QLLG_F64, c->nrhs, c->x64, c->w64, c->t64, sc->ru, c->xdf ? 2 : 0,
+                            &sc->no_ru)) return -1;
   } else if(apply_normal(S, QLLG_F64, QLLG_F64, c->nrhs, c->x64, c->w64, c->t64, NULL, NULL,
                          sc->ru, &sc->no_ru)) return -1;
   if(qllg_k_mcg_residual(QLLG_F32, c->r64, c->r, c->b, c->t64, Vh, 3, c->nrhs, 0, sc, &S->rb))
@@ -612,8 +623,8 @@ issue_iteration(qllg_stag *S, const iter_ctx *c)
 static cudaGraphExec_t
 loop_graph(qllg_stag *S, const iter_ctx *c)
 {
-  long key[10] = {c->mixed, c->ps, c->pl, c->nrhs, c->reortho, (long)c->x, (long)c->b,
-                  (long)c->x64, (long)S->ws_gen, 1};
+  long key[11] = {c->mixed, c->ps, c->pl, c->nrhs, c->reortho, (long)c->x, (long)c->b,
+                  (long)c->x64, (long)S->ws_gen, (long)c->xdf, 1};
   for(int i=0; i<6; i++)
     if(S->graphs[i].exec && !memcmp(S->graphs[i].key, key, sizeof(key))) {
       S->graph_body = S->graphs[i].body;
@@ -759,6 +770,20 @@ true_residual(qllg_stag *S, int nrhs, const void *x, const void *b, double *out)
   return 0;
 }
 
+/* info->true_rsq after a solve on FP64 vectors.  A mixed solve stops every
+ * rhs on a reliable update, whose FP64 residual b - A x64 is that of the
+ * returned x (left in rsq by the residual kernel), so only the FP64 solve
+ * recomputes it */
+static int
+fill_true_rsq(qllg_stag *S, int mode, int nrhs, const void *x, const void *b, qllg_solve_info *info)
+{
+  if(mode == QLLG_SOLVE_MIXED_SINGLE || mode == QLLG_SOLVE_MIXED_HALF) {
+    for(int i=0; i<nrhs; i++) info->true_rsq[i] = info->rsq[i];
+    return 0;
+  }
+  return true_residual(S, nrhs, x, b, info->true_rsq);
+}
+
 /* mixed-precision reliable-update CG on FP64 device vectors x64, b (even
  * sites, nrhs rhs): sloppy vectors in ps storage (p, v, Ap, r) and px
  * (solution increment), links in pl */
@@ -801,6 +826,9 @@ cg_mixed(qllg_stag *S, int ps, int px, int pl, int nrhs, void *x64, const void *
   c.x = xs; c.r = rs; c.p = p; c.v = v;
   c.x64 = x64; c.r64 = r64; c.t64 = t64; c.w64 = w64;
   c.b = b;
+  if(qllg_get_param("ru_df") != 0 && qllg_get_param("ru_compact") != 0) {
+    if(ensure_links(S, QLLG_DF) || !(c.xdf = ws_get(S, WS_XDF, v64))) return -1;
+  }
   if(run_loop(S, &c, maxits)) return -1;
   if(pull_scalars(S)) return -1;
   count_graph_trips(S);
@@ -1031,7 +1059,7 @@ qllg_stag_solve_device(qllg_stag *S, int nrhs, void *x_dev, const void *b_dev,
   }
   int its = solve_dev(S, nrhs, x_dev, b_dev, mass, rsq, maxits, mode, info);
   if(its >= 0 && info && S->master == QLLG_F64) {
-    if(true_residual(S, nrhs, x_dev, b_dev, info->true_rsq)) return -1;
+    if(fill_true_rsq(S, mode, nrhs, x_dev, b_dev, info)) return -1;
   }
   return its;
 }
@@ -1119,7 +1147,7 @@ stag_solve_host(qllg_stag *S, int nrhs, void *const x[], void *const b[], const 
   int its = solve_dev(S, n, xd, bd, m, rsq, maxits, mode, info);
   if(its < 0) return -1;
   if(info && dbl && prec == QLLG_F64) {
-    if(true_residual(S, n, xd, bd, info->true_rsq)) return -1;
+    if(fill_true_rsq(S, mode, n, xd, bd, info)) return -1;
   }
   if(post_scale) {
     double sc[QLLG_MAXRHS];
@@ -1154,7 +1182,12 @@ qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *
                         const void *in_dev)
 {
   if(!valid_nrhs(nrhs)) { qllg_set_error("dslash_device: nrhs %d", nrhs); return -1; }
-  if(prec < 0 || prec > 3) { qllg_set_error("dslash_device: precision %d", prec); return -1; }
+  if(prec < 0 || prec > 4) { qllg_set_error("dslash_device: precision %d", prec); return -1; }
+  /* 4: double-float spinors and links, the reliable-update kernel over
+   * every rhs */
+  if(prec == QLLG_DF)
+    return dslash_half_x(S, QLLG_DF, QLLG_DF, out_parity, nrhs, in_dev, NULL, out_dev, 0, NULL, 0, 1,
+                         NULL, NULL, NULL, NULL, 1, 0);
   /* 3: FP32 spinors with the reconstruct-12 links */
   return dslash_half(S, prec == 3 ? QLLG_F32 : prec, prec, out_parity, nrhs, in_dev, NULL, out_dev,
                      0, NULL, 0, 1, NULL, NULL, NULL, NULL);
@@ -1226,7 +1259,7 @@ qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs)
   /* prec 3 of qllg_stag_dslash_device (reconstruct-12 links) has FP32
    * spinors; an unknown precision has no vector (0 bytes) */
   if(prec == 3) prec = QLLG_F32;
-  if(prec < 0 || prec > 2 || nrhs < 0) return 0;
+  if(prec < 0 || (prec > 2 && prec != QLLG_DF) || nrhs < 0) return 0;
   return vec_bytes(S, prec, nrhs);
 }
 

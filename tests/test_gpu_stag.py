@@ -192,9 +192,11 @@ def test_graph_loop_matches_host_loop(mode):
 def test_compact_reliable_update_matches_masked(mode):
     """the reliable update over the flagged rhs only (threads compacted onto
     them) and the masked multi-rhs launch compute the same FP64 residuals:
-    identical iterations and bitwise identical solutions"""
+    identical iterations and bitwise identical solutions (every update in
+    FP64: ru_df 0)"""
     L, S, u, u3 = _native()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_set_param(b"ru_df", 0)
     nrhs = 8
     masses = (c_double*nrhs)(*[0.05 + 0.02*k for k in range(nrhs)])
     bs = [qll.gen_source(DIMS, 5100 + k, 6, "even") for k in range(nrhs)]
@@ -209,6 +211,7 @@ def test_compact_reliable_update_matches_masked(mode):
         assert info.reliable_updates > 0
         out[compact] = (list(info.iters[:nrhs]), xs)
     L.qllg_set_param(b"ru_compact", 1)
+    L.qllg_set_param(b"ru_df", 1)
     assert out[0][0] == out[1][0]
     for k in range(nrhs):
         assert np.array_equal(out[0][1][k], out[1][1][k])
