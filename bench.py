@@ -722,7 +722,7 @@ def run_dslash_only(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)/args.launches
     Vh = int(np.prod(dims))//2
-    bs = {0: 8, 1: 4, 2: 2, 3: 4}[prec]
+    bs = {0: 8, 1: 4, 2: 2, 3: 4, 4: 8}[prec]
     ns = 4 if prec == 2 else 0
     naik_reals = 12 if prec == 3 else 18
     per = (8*18*bs + 8*naik_reals*bs)/args.nrhs + 17*(6*bs + ns)
@@ -805,7 +805,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--dslash-only", action="store_true")
     ap.add_argument("--dims", default="32,32,32,64")
-    ap.add_argument("--prec", default="f32", choices=["f64", "f32", "i16", "f32r"])
+    ap.add_argument("--prec", default="f32", choices=["f64", "f32", "i16", "f32r", "df"])
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--launches", type=int, default=20)
     ap.add_argument("--solve-only", action="store_true")

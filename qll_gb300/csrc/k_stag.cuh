@@ -534,8 +534,8 @@ stag_dslash_mr(qllg_stag_args a)
 // work item w maps to (site, k-th flagged rhs), so the cost follows the
 // number of flagged rhs instead of running whole warps at the FP64 rate for
 // one of their lanes.  Modes 0 and 2 without norms.
-template <int PS, int PL, int NS, int NR>
-__global__ void __launch_bounds__(kThreads)
+template <int PS, int PL, int NS, int NR, int MINB = 1>
+__global__ void __launch_bounds__(kThreads, MINB)
 stag_dslash_compact(qllg_stag_args a)
 {
   typedef typename Calc<PS, PL>::T T;
@@ -568,11 +568,14 @@ stag_dslash_compact(qllg_stag_args a)
     Cx<T> acc[3];
 #pragma unroll
     for(int c=0; c<3; c++) { acc[c].r = 0; acc[c].i = 0; }
-#pragma unroll
+    // double-float: one slot is about 600 instructions, so the slot loops
+    // stay rolled (16 unrolled slots would not fit the instruction cache)
+    constexpr int UMU = PS == QLLG_DF ? 1 : 4, UB = PS == QLLG_DF ? 1 : 2;
+#pragma unroll UMU
     for(int mu=0; mu<4; mu++) {
-#pragma unroll
+#pragma unroll UB
       for(int back=0; back<2; back++) {
-#pragma unroll
+#pragma unroll UB
         for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
           const int d = (nk ? 3 : 1)*(back ? -1 : 1);
           const int k = nbr_index(G, x, mu, d);
@@ -606,13 +609,14 @@ stag_dslash_compact(qllg_stag_args a)
   }
 }
 
-template <int PS, int PL, int NS, int NR>
+// MINB: resident blocks per SM the compiler must allow (a register cap)
+template <int PS, int PL, int NS, int NR, int MINB = 1>
 int launch_compact(const qllg_stag_args *a)
 {
   static int blocks_per_sm = 0;
   if(!blocks_per_sm) {
     if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm, stag_dslash_compact<PS,PL,NS,NR>, kThreads, 0), "occupancy")) return -1;
+         &blocks_per_sm, stag_dslash_compact<PS,PL,NS,NR,MINB>, kThreads, 0), "occupancy")) return -1;
     if(blocks_per_sm < 1) blocks_per_sm = 1;
   }
   // sized for one flagged rhs: with more, the grid-stride loop takes them
@@ -620,7 +624,7 @@ int launch_compact(const qllg_stag_args *a)
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
   int grid = (int)(need < maxg ? need : maxg);
   if(grid < 1) grid = 1;
-  stag_dslash_compact<PS,PL,NS,NR><<<grid, kThreads, 0, qllg_stream()>>>(*a);
+  stag_dslash_compact<PS,PL,NS,NR,MINB><<<grid, kThreads, 0, qllg_stream()>>>(*a);
   return qllg_launched("stag_dslash_compact launch");
 }
 

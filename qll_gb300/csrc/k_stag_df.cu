@@ -7,15 +7,15 @@
 
 namespace {
 
-template <int NS>
+template <int NS, int MB>
 int launch_df_nr(const qllg_stag_args *a)
 {
   switch(a->nrhs) {
-  case 1: return launch_compact<QLLG_DF,QLLG_DF,NS,1>(a);
-  case 2: return launch_compact<QLLG_DF,QLLG_DF,NS,2>(a);
-  case 4: return launch_compact<QLLG_DF,QLLG_DF,NS,4>(a);
-  case 8: return launch_compact<QLLG_DF,QLLG_DF,NS,8>(a);
-  case 16: return launch_compact<QLLG_DF,QLLG_DF,NS,16>(a);
+  case 1: return launch_compact<QLLG_DF,QLLG_DF,NS,1,MB>(a);
+  case 2: return launch_compact<QLLG_DF,QLLG_DF,NS,2,MB>(a);
+  case 4: return launch_compact<QLLG_DF,QLLG_DF,NS,4,MB>(a);
+  case 8: return launch_compact<QLLG_DF,QLLG_DF,NS,8,MB>(a);
+  case 16: return launch_compact<QLLG_DF,QLLG_DF,NS,16,MB>(a);
   }
   qllg_set_error("stag_dslash: nrhs %d not in {1,2,4,8,16}", a->nrhs);
   return -1;
@@ -30,8 +30,9 @@ qllg_k_stag_dslash_df(const qllg_stag_args *a)
     qllg_set_error("stag_dslash: double-float runs the compacted reliable-update launch only");
     return -1;
   }
-  if(a->nslots == 16) return launch_df_nr<16>(a);
-  if(a->nslots == 8) return launch_df_nr<8>(a);
+  const int mb = (int)qllg_get_param("df_blocks");
+  if(a->nslots == 16) return mb >= 3 ? launch_df_nr<16,3>(a) : launch_df_nr<16,1>(a);
+  if(a->nslots == 8) return mb >= 3 ? launch_df_nr<8,3>(a) : launch_df_nr<8,1>(a);
   qllg_set_error("stag_dslash: nslots %d not 8 or 16", a->nslots);
   return -1;
 }

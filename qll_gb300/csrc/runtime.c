@@ -278,6 +278,10 @@ static struct { const char *name; double value; } g_params[] = {
   {"poll", 8},               /* first batch of iterations between host checks */
   {"dslash_mr", 1},          /* multi-rhs Dslash: one thread per site and 4 rhs */
   {"ru_compact", 1},         /* reliable-update Dslash over the flagged rhs only */
+  {"df_blocks", 3},          /* register cap of the double-float reliable-update
+                                Dslash: resident blocks of 256 it must allow
+                                (1 or 3; 32^3x64, 1 rhs: 0.47 and 0.41 ms,
+                                the FP64 one 1.04 ms) */
   {"ru_df", 1},              /* intermediate reliable updates of the mixed CG in
                                 double-float (FP32 pipes, about 48 bits); the
                                 final ones, on which a rhs may stop, in FP64 */
