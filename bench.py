@@ -729,6 +729,7 @@ def run_dslash_only(args):
     print(json.dumps({"dslash_only": {"dims": dims, "nrhs": args.nrhs, "prec": args.prec,
                                       "params": args.param, "autotune": autotune_report(L),
                                       "ms": ms, "algorithmic_gbs": per*Vh*args.nrhs/(ms*1e-3)/1e9,
+                                      "bulk_error": L.qllg_k_bulk_error(1),
                                       "error": qll.last_error()}}), flush=True)
     L.qllg_stag_destroy(S)
 

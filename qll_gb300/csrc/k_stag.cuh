@@ -204,14 +204,16 @@ stag_dslash(qllg_stag_args a)
 // per-rhs scalars and the norm sums in shared memory, for more resident
 // warps at fewer registers: 2: 3 blocks/SM (80 registers); 3: 4 blocks/SM
 // (64); 4: 128 threads, 9 blocks/SM (56).  5 and 6: CFG 0 and lean CFG 0
-// with the slot loop software-pipelined one slot ahead
+// with the slot loop software-pipelined one slot ahead.  7 and 8: CFG 0
+// and lean CFG 3 with the direction loop rolled (a quarter of the code)
 template <int PS, int R, int CFG> struct MrCfg {
   static constexpr int threads = CFG == 4 ? 128 : 256;
-  static constexpr int minb = CFG == 2 ? 3 : CFG == 3 ? 4 : CFG == 4 ? 9 :
+  static constexpr int minb = (CFG == 2) ? 3 : (CFG == 3 || CFG == 8) ? 4 : CFG == 4 ? 9 :
                               (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
-  static constexpr bool lean = (CFG >= 2 && CFG <= 4) || CFG == 6;
-  static constexpr bool pf = CFG >= 5;
+  static constexpr bool lean = (CFG >= 2 && CFG <= 4) || CFG == 6 || CFG == 8;
+  static constexpr bool pf = CFG == 5 || CFG == 6;
+  static constexpr bool roll = CFG == 7 || CFG == 8;   // the direction loop rolled (4 slots a trip)
 };
 
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
@@ -309,7 +311,8 @@ stag_dslash_mr(qllg_stag_args a)
       // can move the loads of later slots ahead of the FMAs of earlier ones
       auto slots = [&](auto ck) {
         constexpr bool CK = decltype(ck)::value;     // check the active flags
-#pragma unroll
+        constexpr int UMU = MrCfg<PS,R,CFG>::roll ? 1 : 4;
+#pragma unroll UMU
         for(int mu=0; mu<4; mu++) {
 #pragma unroll
           for(int back=0; back<2; back++) {
@@ -990,17 +993,22 @@ int launch_tile(const qllg_stag_args *a)
   return qllg_launched("stag_dslash_tile launch");
 }
 
+#include "k_stag_bulk.cuh"
+
 // variants of one launch shape, in the order the autotuner tries them:
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes, MrCfg 1-6 as variants 4-9
-constexpr int kNumVariants = 10;
+// launch shapes, MrCfg 1-8 as variants 4-11; 12 = the bulk-copy pipeline
+// (FP32 links and spinors, 16 slots, 16 rhs, k_stag_bulk.cuh)
+constexpr int kNumVariants = 13;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
                                                 "4 rhs/thread lean 56 regs", "4 rhs/thread prefetch",
-                                                "4 rhs/thread lean prefetch"};
+                                                "4 rhs/thread lean prefetch", "4 rhs/thread rolled",
+                                                "4 rhs/thread lean 64 regs rolled",
+                                                "bulk-copy pipeline"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1008,6 +1016,9 @@ bool variant_ok(const qllg_stag_args *a, int v)
   if(v == 0) return NR >= 4;
   if(v == 1) return NR >= 2;
   if(v == 2) return true;
+  if(v == 12)
+    return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
+           a->g.Vh % kBkSites == 0 && vec4_ok(a) && qllg_get_param("dslash_bulk") != 0;
   if(v >= 4)
     return PS == QLLG_F32 && NR == 16 && vec4_ok(a) && qllg_get_param("dslash_vec4") != 0;
   return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
@@ -1020,6 +1031,7 @@ int launch_variant(const qllg_stag_args *a, int v)
   if(!variant_ok<PS,PL,NS,NR>(a, v)) v = NR >= 4 ? 0 : (NR >= 2 ? 1 : 2);
   if constexpr (PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16) {
     if(v == 3) return launch_tile<NR>(a);
+    if(v == 12) return launch_bulk<NR>(a);
   }
   if constexpr (PS == QLLG_F32 && NR == 16) {
     if(v >= 4) {
@@ -1029,7 +1041,9 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 6: return launch_mr<PS,PL,NS,NR,4,3>(a);
       case 7: return launch_mr<PS,PL,NS,NR,4,4>(a);
       case 8: return launch_mr<PS,PL,NS,NR,4,5>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,6>(a);
+      case 9: return launch_mr<PS,PL,NS,NR,4,6>(a);
+      case 10: return launch_mr<PS,PL,NS,NR,4,7>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,8>(a);
       }
     }
   }

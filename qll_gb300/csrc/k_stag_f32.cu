@@ -11,3 +11,17 @@ qllg_k_stag_dslash_f32(const qllg_stag_args *a)
   if(a->nslots == 8) return qllg_k_stag_dslash_f32_ns8(a);
   return launch_ns_only<QLLG_F32, QLLG_F32, 16>(a);
 }
+
+// the bulk-copy pipeline's error flag (a bounded wait ran out): returns it
+// and clears it when reset is set
+extern "C" int
+qllg_k_bulk_error(int reset)
+{
+  int v = 0;
+  if(cudaMemcpyFromSymbol(&v, g_bulk_err, sizeof(int)) != cudaSuccess) return -1;
+  if(reset && v) {
+    const int z = 0;
+    if(cudaMemcpyToSymbol(g_bulk_err, &z, sizeof(int)) != cudaSuccess) return -1;
+  }
+  return v;
+}

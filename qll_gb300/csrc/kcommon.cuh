@@ -454,30 +454,35 @@ __device__ __forceinline__ bool grid_reduce(double (&val)[NR], int nrhs, int rhs
 
 // Same reduction when each thread holds R right-hand sides: thread t works
 // on rhs q*R + j (j < R) with q = t % Q and Q = nrhs/R threads per site.
+// ntr: the first ntr threads of the block hold values (0: all); the others
+// (a producer warp) only take part in the barriers
 template <int NRED, int R>
 __device__ __forceinline__ bool grid_reduce_mr(double (&val)[NRED][R], int nrhs, int Q,
                                                double *partial, unsigned *counter,
                                                double *shm /* NRED*R*blockDim */,
-                                               double *result[NRED]) {
-  const int tid = threadIdx.x, nt = blockDim.x;
+                                               double *result[NRED], int ntr = 0) {
+  const int tid = threadIdx.x, nt = ntr ? ntr : blockDim.x;
+  const bool in = tid < nt;
+  if(in) {
 #pragma unroll
-  for(int n=0; n<NRED; n++)
+    for(int n=0; n<NRED; n++)
 #pragma unroll
-    for(int j=0; j<R; j++) shm[(n*R + j)*nt + tid] = val[n][j];
+      for(int j=0; j<R; j++) shm[(n*R + j)*nt + tid] = val[n][j];
+  }
   __syncthreads();
   {
     const int K = NRED*nrhs, J = nt/K, c = tid % K, l = tid / K;
     const int n = c / nrhs, r = c % nrhs, j = r % R, qq = r / R;
     double s = 0;
-    for(int i=l; i<nt/Q; i+=J) s += shm[(n*R + j)*nt + qq + Q*i];
+    if(in) for(int i=l; i<nt/Q; i+=J) s += shm[(n*R + j)*nt + qq + Q*i];
     __syncthreads();
-    shm[tid] = s;
+    if(in) shm[tid] = s;
     __syncthreads();
     for(int w=J/2; w>0; w>>=1) {
-      if(l < w) shm[c + K*l] += shm[c + K*(l + w)];
+      if(in && l < w) shm[c + K*l] += shm[c + K*(l + w)];
       __syncthreads();
     }
-    if(l == 0) partial[(size_t)blockIdx.x*(2*QLLG_MAXRHS) + n*QLLG_MAXRHS + r] = shm[c];
+    if(in && l == 0) partial[(size_t)blockIdx.x*(2*QLLG_MAXRHS) + n*QLLG_MAXRHS + r] = shm[c];
   }
   __threadfence();
   __shared__ bool last;
@@ -491,15 +496,16 @@ __device__ __forceinline__ bool grid_reduce_mr(double (&val)[NRED][R], int nrhs,
   const int c = tid % K, l = tid / K;
   const int q = c / nrhs, r = c % nrhs;
   double s = 0;
-  for(int b=l; b<nb; b+=J)
-    s += ((volatile double *)partial)[(size_t)b*(2*QLLG_MAXRHS) + q*QLLG_MAXRHS + r];
-  shm[tid] = s;
+  if(in)
+    for(int b=l; b<nb; b+=J)
+      s += ((volatile double *)partial)[(size_t)b*(2*QLLG_MAXRHS) + q*QLLG_MAXRHS + r];
+  if(in) shm[tid] = s;
   __syncthreads();
   for(int w=J/2; w>0; w>>=1) {
-    if(l < w) shm[c + K*l] += shm[c + K*(l + w)];
+    if(in && l < w) shm[c + K*l] += shm[c + K*(l + w)];
     __syncthreads();
   }
-  if(l == 0) {
+  if(in && l == 0) {
 #pragma unroll
     for(int qq=0; qq<NRED; qq++) if(qq == q && result[qq]) result[qq][r] = shm[c];
   }

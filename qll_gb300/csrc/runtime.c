@@ -288,7 +288,8 @@ static struct { const char *name; double value; } g_params[] = {
   {"dslash_vec4", 1},        /* 16-byte loads of rhs pairs (FP32) */
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
-  {"dslash_variant", -1},    /* force a Dslash variant (0-9); -1: autotuned */
+  {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
+  {"dslash_variant", -1},    /* force a Dslash variant (0-12); -1: autotuned */
   {"multishift_guess_rsq", 1e-10}, /* mixed multishift: the FP32 multishift CG
                                        goes to |r|^2 < this |b|^2 before the
                                        pairs are refined in FP64 (C3 at

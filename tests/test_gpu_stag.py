@@ -289,8 +289,8 @@ def test_multishift_multi_rhs_matches_oracle(mode):
 @pytest.mark.parametrize("nrhs", [4, 16])
 def test_dslash_variants_agree(nrhs):
     """the autotuner's candidates (4, 2, 1 rhs per thread, shared-memory
-    staging, the launch shapes with more registers, 8 rhs per thread, packed
-    FP32 FMAs) compute bitwise the same FP32 Dslash"""
+    staging, the other launch shapes of the 4-rhs kernel, the bulk-copy
+    pipeline) compute bitwise the same FP32 Dslash"""
     torch = pytest.importorskip("torch")
     L, S, u, u3 = _native()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
@@ -302,7 +302,7 @@ def test_dslash_variants_agree(nrhs):
     g = torch.Generator(device="cuda").manual_seed(91 + nrhs)
     src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
     outs = []
-    for v in range(10):
+    for v in range(13):
         L.qllg_set_param(b"dslash_variant", v)
         for parity in (0, 1):
             dst = torch.full_like(src, float("nan"))
@@ -314,10 +314,12 @@ def test_dslash_variants_agree(nrhs):
     L.qllg_set_param(b"dslash_variant", -1)
     for k in range(2, len(outs)):
         assert torch.equal(outs[k], outs[k % 2]), k
+    # no bounded wait of the bulk-copy pipeline ran out
+    assert L.qllg_k_bulk_error(1) == 0
     L.qllg_stag_destroy(S)
 
 
-@pytest.mark.parametrize("variant", range(10))
+@pytest.mark.parametrize("variant", range(13))
 def test_mixed_solve_with_each_dslash_variant(variant):
     """the fused CG epilogue and the norms of every variant: the 16-rhs
     mixed solve reaches the FP64 true residual and matches the oracle"""
