@@ -205,15 +205,18 @@ stag_dslash(qllg_stag_args a)
 // warps at fewer registers: 2: 3 blocks/SM (80 registers); 3: 4 blocks/SM
 // (64); 4: 128 threads, 9 blocks/SM (56).  5 and 6: CFG 0 and lean CFG 0
 // with the slot loop software-pipelined one slot ahead.  7 and 8: CFG 0
-// and lean CFG 3 with the direction loop rolled (a quarter of the code)
+// and lean CFG 3 with the direction loop rolled (a quarter of the code);
+// 9 and 11: lean CFG 2 and 4 rolled the same way; 10: lean CFG 3 with
+// every slot loop rolled
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int threads = CFG == 4 ? 128 : 256;
-  static constexpr int minb = (CFG == 2) ? 3 : (CFG == 3 || CFG == 8) ? 4 : CFG == 4 ? 9 :
-                              (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
+  static constexpr int threads = (CFG == 4 || CFG == 11) ? 128 : 256;
+  static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8 || CFG == 10) ? 4 :
+                              (CFG == 4 || CFG == 11) ? 9 : (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
-  static constexpr bool lean = (CFG >= 2 && CFG <= 4) || CFG == 6 || CFG == 8;
+  static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
   static constexpr bool pf = CFG == 5 || CFG == 6;
-  static constexpr bool roll = CFG == 7 || CFG == 8;   // the direction loop rolled (4 slots a trip)
+  // 1: the direction loop rolled (4 slots a trip); 2: every slot loop rolled
+  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG == 11) ? 1 : 0;
 };
 
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
@@ -312,11 +315,12 @@ stag_dslash_mr(qllg_stag_args a)
       auto slots = [&](auto ck) {
         constexpr bool CK = decltype(ck)::value;     // check the active flags
         constexpr int UMU = MrCfg<PS,R,CFG>::roll ? 1 : 4;
+        constexpr int UB = MrCfg<PS,R,CFG>::roll == 2 ? 1 : 2;
 #pragma unroll UMU
         for(int mu=0; mu<4; mu++) {
-#pragma unroll
+#pragma unroll UB
           for(int back=0; back<2; back++) {
-#pragma unroll
+#pragma unroll UB
             for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
               const int d = (nk ? 3 : 1)*(back ? -1 : 1);
               const size_t nb = (size_t)nbr_index(G, x, mu, d);
@@ -999,16 +1003,19 @@ int launch_tile(const qllg_stag_args *a)
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes, MrCfg 1-8 as variants 4-11; 12 = the bulk-copy pipeline
-// (FP32 links and spinors, 16 slots, 16 rhs, k_stag_bulk.cuh)
-constexpr int kNumVariants = 13;
+// launch shapes, MrCfg 1-8 as variants 4-11 and 9-11 as 13-15; 12 = the
+// bulk-copy pipeline (FP32 links and spinors, 16 slots, 16 rhs,
+// k_stag_bulk.cuh)
+constexpr int kNumVariants = 16;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
                                                 "4 rhs/thread lean 56 regs", "4 rhs/thread prefetch",
                                                 "4 rhs/thread lean prefetch", "4 rhs/thread rolled",
                                                 "4 rhs/thread lean 64 regs rolled",
-                                                "bulk-copy pipeline"};
+                                                "bulk-copy pipeline", "4 rhs/thread lean 80 regs rolled",
+                                                "4 rhs/thread lean 64 regs all rolled",
+                                                "4 rhs/thread lean 56 regs rolled"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1043,7 +1050,10 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 8: return launch_mr<PS,PL,NS,NR,4,5>(a);
       case 9: return launch_mr<PS,PL,NS,NR,4,6>(a);
       case 10: return launch_mr<PS,PL,NS,NR,4,7>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,8>(a);
+      case 11: return launch_mr<PS,PL,NS,NR,4,8>(a);
+      case 13: return launch_mr<PS,PL,NS,NR,4,9>(a);
+      case 14: return launch_mr<PS,PL,NS,NR,4,10>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,11>(a);
       }
     }
   }
