@@ -49,9 +49,10 @@ METRIC = "mixed-precision multi-RHS asqtad CG solves/s at 1e-8 true residual"
 # iterations of the FP64 CG (cgSolveT) on this workload, measured with the
 # library's FP64 solver on GB300 (same recurrence as the reference)
 FP64_ITERS_MEASURED = 454
-# DRAM bytes (read + write) per even site of one 16-rhs FP32 half Dslash,
-# ncu capture at 24^3x48: 537.2 MB + 113.2 MB over 331,776 sites
-TRAFFIC_PER_SITE_BYTES = (537.198592e6 + 113.220096e6)/331776
+# DRAM bytes (read + write) per even site of one 16-rhs FP32 half Dslash
+# (the autotuned lean 64-register rolled launch shape), ncu capture at
+# 24^3x48: 554.7 MB + 121.5 MB over 331,776 sites
+TRAFFIC_PER_SITE_BYTES = (554.6688e6 + 121.459712e6)/331776
 
 
 def apply_params(L, args):
@@ -62,6 +63,16 @@ def apply_params(L, args):
         k, v = kv.split("=")
         if L.qllg_set_param(k.encode(), float(v)) != 0:
             raise SystemExit(qll.last_error())
+
+
+def tuned_choice(L):
+    """the launch shape the autotuner chose for the 16-rhs FP32 half Dslash
+    of the headline lattice (plain launch)"""
+    key = "stag_dslash p1/1 s16 n16 V%d (%d %d %d %d)" % ((int(np.prod(DIMS)),) + tuple(DIMS))
+    for line in autotune_report(L):
+        if line.startswith(key + ":"):
+            return line[len(key) + 1:].split("|")[0].strip()
+    return "untuned"
 
 
 def autotune_report(L):
@@ -333,8 +344,9 @@ def run_gpu(args):
                 "api": "qllg_stag_solve (host arrays)"},
         "fused_cg_kernel": {"avg_launch_ms": favg, "launches": fcnt.value,
                             "gbs": fused_bytes/(favg*1e-3)/1e9 if favg > 0 else None},
-        "roofline": {"kernel": "stag_dslash_mr<f32,%s,16 slots,16 rhs,4 rhs/thread>"
-                               % ("f32 reconstruct-12" if recon else "f32"), "bound": "hbm",
+        "roofline": {"kernel": "stag_dslash_mr<f32,%s,16 slots,16 rhs>, %s"
+                               % ("f32 reconstruct-12" if recon else "f32", tuned_choice(L)),
+                     "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved/peak if peak else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else None,

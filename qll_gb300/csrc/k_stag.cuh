@@ -91,6 +91,16 @@ __device__ __forceinline__ void slot_link(const qllg_stag_args &a, int mu, int b
   }
 }
 
+// 32-byte load of 8 floats (ld.global.nc.v8.f32, sm_100 and later); p
+// 32-byte aligned
+__device__ __forceinline__ void ldg_v8(float f[8], const void *p)
+{
+  asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]),
+                 "=f"(f[6]), "=f"(f[7])
+               : "l"(p));
+}
+
 template <int PS, int PL, int NS, int NR>
 __global__ void __launch_bounds__(kThreads)
 stag_dslash(qllg_stag_args a)
@@ -207,16 +217,17 @@ stag_dslash(qllg_stag_args a)
 // with the slot loop software-pipelined one slot ahead.  7 and 8: CFG 0
 // and lean CFG 3 with the direction loop rolled (a quarter of the code);
 // 9 and 11: lean CFG 2 and 4 rolled the same way; 10: lean CFG 3 with
-// every slot loop rolled
+// every slot loop rolled; 12: CFG 8 with 32-byte spinor loads
 template <int PS, int R, int CFG> struct MrCfg {
   static constexpr int threads = (CFG == 4 || CFG == 11) ? 128 : 256;
-  static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8 || CFG == 10) ? 4 :
+  static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8 || CFG == 10 || CFG == 12) ? 4 :
                               (CFG == 4 || CFG == 11) ? 9 : (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
   static constexpr bool pf = CFG == 5 || CFG == 6;
   // 1: the direction loop rolled (4 slots a trip); 2: every slot loop rolled
-  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG == 11) ? 1 : 0;
+  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG == 11 || CFG == 12) ? 1 : 0;
+  static constexpr bool v8 = CFG == 12 && PS == QLLG_F32;   // 32-byte spinor loads
 };
 
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
@@ -230,6 +241,7 @@ stag_dslash_mr(qllg_stag_args a)
   constexpr int Q = NR/R;                       // threads per site
   constexpr int PX = VecPrec<PS>::value;
   constexpr bool F2 = MrCfg<PS,R,CFG>::f2;
+  constexpr bool V8 = MrCfg<PS,R,CFG>::v8;
   constexpr bool PF = MrCfg<PS,R,CFG>::pf;
   constexpr int TB = MrCfg<PS,R,CFG>::threads;
   constexpr bool LEAN = MrCfg<PS,R,CFG>::lean;
@@ -327,7 +339,27 @@ stag_dslash_mr(qllg_stag_args a)
               const size_t kb = nb*NR + q*R;
               Cx<T> U[9];
               slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
-              if constexpr (v4) {
+              if constexpr (v4 && V8 && !CK && R == 4) {
+                // the 4 rhs of a colour in one 32-byte load: a warp request
+                // then covers whole 128-byte site blocks of 4 sites instead
+                // of halves of 8 (half the L1 wavefronts)
+                Cx<T> v[4][3];
+#pragma unroll
+                for(int l=0; l<3; l++) {
+                  float f[8];
+                  ldg_v8(f, (const float2 *)a.in + (size_t)l*total + kb);
+#pragma unroll
+                  for(int j=0; j<4; j++) { v[j][l].r = f[2*j]; v[j][l].i = f[2*j + 1]; }
+                }
+#pragma unroll
+                for(int j=0; j<4; j++) {
+#pragma unroll
+                  for(int l=0; l<3; l++) {
+#pragma unroll
+                    for(int c=0; c<3; c++) cmac(acc[j][c], U[3*l + c], v[j][l]);
+                  }
+                }
+              } else if constexpr (v4) {
                 // two rhs per 16-byte load and colour
 #pragma unroll
                 for(int h=0; h<R/2; h++) {
@@ -1003,10 +1035,10 @@ int launch_tile(const qllg_stag_args *a)
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes, MrCfg 1-8 as variants 4-11 and 9-11 as 13-15; 12 = the
+// launch shapes, MrCfg 1-8 as variants 4-11 and 9-12 as 13-16; 12 = the
 // bulk-copy pipeline (FP32 links and spinors, 16 slots, 16 rhs,
 // k_stag_bulk.cuh)
-constexpr int kNumVariants = 16;
+constexpr int kNumVariants = 17;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
@@ -1015,7 +1047,8 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "4 rhs/thread lean 64 regs rolled",
                                                 "bulk-copy pipeline", "4 rhs/thread lean 80 regs rolled",
                                                 "4 rhs/thread lean 64 regs all rolled",
-                                                "4 rhs/thread lean 56 regs rolled"};
+                                                "4 rhs/thread lean 56 regs rolled",
+                                                "4 rhs/thread lean 64 regs rolled 32-byte"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1026,6 +1059,9 @@ bool variant_ok(const qllg_stag_args *a, int v)
   if(v == 12)
     return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
            a->g.Vh % kBkSites == 0 && vec4_ok(a) && qllg_get_param("dslash_bulk") != 0;
+  if(v == 16)
+    return PS == QLLG_F32 && NR == 16 && vec4_ok(a) && ((uintptr_t)a->in & 31u) == 0 &&
+           qllg_get_param("dslash_vec4") != 0;
   if(v >= 4)
     return PS == QLLG_F32 && NR == 16 && vec4_ok(a) && qllg_get_param("dslash_vec4") != 0;
   return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
@@ -1053,7 +1089,8 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 11: return launch_mr<PS,PL,NS,NR,4,8>(a);
       case 13: return launch_mr<PS,PL,NS,NR,4,9>(a);
       case 14: return launch_mr<PS,PL,NS,NR,4,10>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,11>(a);
+      case 15: return launch_mr<PS,PL,NS,NR,4,11>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,12>(a);
       }
     }
   }

@@ -86,7 +86,7 @@ template <int NR_>
 __global__ void __launch_bounds__(kBkThreads, 2)
 stag_dslash_bulk(qllg_stag_args a)
 {
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(16) unsigned char smem[];   // 16-byte copies, 8-byte barriers
   typedef float T;
   constexpr int NR = 16, R = 4, Q = 4, PS = QLLG_F32, PX = QLLG_F32;
   uint64_t *full = (uint64_t *)(smem + kBkStages*kBkStage);

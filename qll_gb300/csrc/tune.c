@@ -12,7 +12,7 @@
 #include "qllg_internal.h"
 
 #define NTUNE 256
-#define NCAND 16
+#define NCAND 24
 
 static struct {
   char key[96];
