@@ -254,14 +254,22 @@ __global__ void __launch_bounds__(kT)
 spinor_df_k(void *out, const void *in, int nsites, int ncomp, const int *active, int eq,
             const int *skip)
 {
-  if(skip && *(volatile const int *)skip) return;
-  bool any = !active;
-  if(active) for(int r=0; r<NR; r++) any |= active[r] != 0 && (!eq || active[r] == eq);
-  if(!any) return;
-  const size_t total = (size_t)nsites*NR*ncomp;
-  GRID_LOOP(t, total) {
-    const int rhs = (int)(t % NR);
-    if(active && (!active[rhs] || (eq && active[rhs] != eq))) continue;
+  // threads over (component, site, k-th flagged rhs) only
+  __shared__ int list[NR];
+  __shared__ int nact_s;
+  if(skip && *(volatile const int *)skip) return;          // uniform
+  if(threadIdx.x == 0) {
+    int n = 0;
+    for(int r=0; r<NR; r++)
+      if(!active || (active[r] && (!eq || active[r] == eq))) list[n++] = r;
+    nact_s = n;
+  }
+  __syncthreads();
+  const int nact = nact_s;
+  if(!nact) return;
+  const size_t work = (size_t)nsites*ncomp*nact;
+  GRID_LOOP(w, work) {
+    const size_t t = (w/nact)*NR + list[w % nact];
     if(TO) {
       const double2 d = ((const double2 *)in)[t];
       const dfl re(d.x), im(d.y);
@@ -711,7 +719,8 @@ extern "C" int
 qllg_k_spinor_df(int to_df, void *out, const void *in, int nsites, int ncomp, int nrhs,
                  const int *active, int eq, const int *skip)
 {
-  const int g = grid_for((size_t)nsites*nrhs*ncomp, 0, 0);
+  // sized for one flagged rhs: with more, the grid-stride loop takes them
+  const int g = grid_for((size_t)nsites*ncomp, 0, 0);
   cudaStream_t st = qllg_stream();
   if(to_df) { NR_SWITCH(nrhs, (spinor_df_k<NR,true><<<g,kT,0,st>>>(out, in, nsites, ncomp, active, eq, skip))); }
   else { NR_SWITCH(nrhs, (spinor_df_k<NR,false><<<g,kT,0,st>>>(out, in, nsites, ncomp, active, eq, skip))); }

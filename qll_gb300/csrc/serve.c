@@ -105,8 +105,8 @@ int
 qllg_server_add_lattice(qllg_server *V, qllg_stag *S)
 {
   if(V->nlat == MAXLAT) { qllg_set_error("server: more than %d lattices", MAXLAT); return -1; }
-  /* the batches run FP32 Dslashes and FP64 reliable updates on these
-   * links: make both resident now and count them */
+  /* the batches run FP32 Dslashes and double-float/FP64 reliable updates
+   * on these links: make them resident now and count them */
   qllg_stag *probe = qllg_stag_share(S);
   if(!probe) return -1;
   qllg_stag_destroy(probe);

@@ -289,6 +289,10 @@ qllg_stag_share(qllg_stag *S)
 {
   if(ensure_links(S, QLLG_F64) || ensure_links(S, QLLG_F32)) return NULL;
   f32_links(S);               /* the reconstruct-12 copy too, when it applies */
+  /* and the double-float copy of the reliable updates, so that the
+   * operators sharing S do not each make their own */
+  if(qllg_get_param("ru_df") != 0 && qllg_get_param("ru_compact") != 0 && S->master == QLLG_F64 &&
+     ensure_links(S, QLLG_DF)) return NULL;
   int dims[4] = {S->g.L[0], S->g.L[1], S->g.L[2], S->g.L[3]};
   qllg_stag *T = qllg_stag_alloc(dims, S->nslots, S->master);
   if(!T) return NULL;
@@ -850,9 +854,11 @@ size_t
 qllg_batch_bytes(const qllg_stag *S)
 {
   const int n = QLLG_MAXRHS;
-  /* rs, p, v, xs in FP32; r64, t64, w64, x64, b in FP64; one column of
-   * staging */
-  return 4*vec_bytes(S, QLLG_F32, n) + 5*vec_bytes(S, QLLG_F64, n) + 48*(size_t)S->g.Vh;
+  /* rs, p, v, xs in FP32; r64, t64, w64, x64, b in FP64 (and the
+   * double-float copy of x64 for the intermediate reliable updates); one
+   * column of staging */
+  const int ndf = qllg_get_param("ru_df") != 0 && qllg_get_param("ru_compact") != 0;
+  return 4*vec_bytes(S, QLLG_F32, n) + (5 + ndf)*vec_bytes(S, QLLG_F64, n) + 48*(size_t)S->g.Vh;
 }
 
 int
@@ -879,6 +885,9 @@ qllg_batch_init(qllg_stag *S, int maxits)
   c->b = ws_get(S, WS_B, v64);
   if(!c->r || !c->p || !c->v || !c->x || !c->r64 || !c->t64 || !c->w64 || !c->x64 || !c->b)
     return -1;
+  if(qllg_get_param("ru_df") != 0 && qllg_get_param("ru_compact") != 0) {
+    if(ensure_links(S, QLLG_DF) || !(c->xdf = ws_get(S, WS_XDF, v64))) return -1;
+  }
   if(!S->bstage && !(S->bstage = qllg_dmalloc(48*(size_t)S->g.Vh))) return -1;
   if(!S->bev && qllg_check_cuda(cudaEventCreateWithFlags(&S->bev, cudaEventDisableTiming),
                                 "batch event")) return -1;
