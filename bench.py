@@ -527,6 +527,7 @@ def run_serving(args):
     requests solved one shift at a time by the plain FP64 single-rhs CG"""
     from qll_gb300 import qll, serve
     L = serve._lib()
+    apply_params(L, args)
     # single-stored links: half the resident link bytes per lattice
     ops = [serve.asqtad_operator(d, s, e, single_store=True)
            for d, s, e in zip(SERVE_LATTICES, SERVE_SEEDS, SERVE_EPS)]
@@ -588,6 +589,7 @@ def run_serving(args):
         "max_true_rsq_over_tol2": worst,
         "hbm_budget_bytes": st.budget_bytes, "hbm_used_bytes_end": st.used_bytes,
         "chunk_iters": args.serve_chunk,
+        "autotune": autotune_report(L),
         "serial_fp64_baseline": {"requests_per_s": n_serial/t_serial, "sample": "%d requests, "
                                  "one per lattice, each shift a separate FP64 single-rhs CG"
                                  % n_serial},

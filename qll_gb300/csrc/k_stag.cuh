@@ -260,6 +260,11 @@ stag_dslash_mr(qllg_stag_args a)
   bool anyact = false, allact = true;
   constexpr bool v4 = (R % 2 == 0) && V4 && PS == QLLG_F32;
   const T cb = (T)a.b;
+  // every rhs of the launch active: the slot loop without the active
+  // checks.  Chosen per launch, not per thread, so that a launch runs one
+  // copy of the unrolled loop (two would compete for the instruction cache)
+  bool allrhs = !a.one_path;
+  if(a.active) for(int r=0; r<NR; r++) allrhs &= a.active[r] != 0;
 #pragma unroll
   for(int j=0; j<R; j++) {
     const int rhs = q*R + j;
@@ -321,7 +326,7 @@ stag_dslash_mr(qllg_stag_args a)
           for(int c=0; c<3; c++) { acc[j][c].r = 0; acc[j][c].i = 0; }
         }
       }
-      // the 16 (or 8) slots.  With every rhs of the thread active (the
+      // the 16 (or 8) slots.  With every rhs of the launch active (the
       // usual case) the unrolled slot loop has no branches, so the compiler
       // can move the loads of later slots ahead of the FMAs of earlier ones
       auto slots = [&](auto ck) {
@@ -429,7 +434,7 @@ stag_dslash_mr(qllg_stag_args a)
             }
           }
         };
-        if(allact) {
+        if(allrhs) {
           Cx<T> U0[9], U1[9], v0[R][3], v1[R][3];
           load_slot(0, U0, v0);
 #pragma unroll
@@ -443,7 +448,7 @@ stag_dslash_mr(qllg_stag_args a)
           slots(std::integral_constant<bool, true>());
         }
       } else {
-        if(allact) slots(std::integral_constant<bool, false>());
+        if(allrhs) slots(std::integral_constant<bool, false>());
         else slots(std::integral_constant<bool, true>());
       }
       // epilogue.  With v4 and all R rhs active, the R rhs of the site move
@@ -704,6 +709,7 @@ int launch_mr(const qllg_stag_args *a)
   qllg_stag_args A = *a;
   A.partial = a->rb ? a->rb->partial : NULL;
   A.counter = a->rb ? a->rb->counter : NULL;
+  A.one_path = qllg_get_param("dslash_split") == 0;
   kern(v4)<<<grid, TB, 0, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash_mr launch");
 }
@@ -1103,8 +1109,8 @@ int launch_variant(const qllg_stag_args *a, int v)
 // times each variant on a side output buffer (mode 0, no reductions, every
 // rhs active: the same Dslash work the solvers do) and keeps the fastest
 // in the registry; later launches of that shape use it, in every mode but
-// the fused CG update (mode 3), which is timed the same way on copies of
-// its x, r and scalars under a key of its own.
+// the fused CG update (mode 3), which is timed the same way (every rhs
+// active) on copies of its x, r and scalars under a key of its own.
 // All variants give bitwise the same Dslash output; only the order of the
 // per-rhs reductions differs between them.  No tuning during a stream
 // capture or for callers that must not allocate: they use a tuned choice
@@ -1146,6 +1152,10 @@ int tuned_variant(const qllg_stag_args *a)
     T.r = scratch[1];
     T.sc = (qllg_cg_scalars *)scratch[2];
     T.done = NULL;
+    // every rhs active, as for the plain launch: a first launch with few
+    // active columns (a serving batch filling up) would favour shapes that
+    // are slow once the batch is full
+    T.active = NULL;
   } else {
     T.mode = 0;
     T.self = NULL;

@@ -163,6 +163,8 @@ typedef struct {
                             modes 0 and 2, no norms */
   int active_eq;         /* compact: flagged means active[r] == active_eq
                             (any nonzero entry when 0) */
+  int one_path;          /* multi-rhs Dslash: always the slot loop with the
+                            active checks (one code path) */
   int no_tune;           /* caller must not allocate: no autotuning */
   int fb;                /* single-stored links: forward slots only, [nslots/2][9][V];
                             backward links made from them in the kernel */

@@ -289,6 +289,8 @@ static struct { const char *name; double value; } g_params[] = {
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
+  {"dslash_split", 1},       /* multi-rhs Dslash: a slot loop without the active
+                                checks for launches with every rhs active */
   {"dslash_variant", -1},    /* force a Dslash variant (0-12); -1: autotuned */
   {"multishift_guess_rsq", 1e-10}, /* mixed multishift: the FP32 multishift CG
                                        goes to |r|^2 < this |b|^2 before the
