@@ -372,6 +372,7 @@ def run_gpu(args):
     L.qllg_stag_destroy(S)
     if rank == 0 and not args.no_serve:
         ts = time.time()
+        out["c1"] = run_c1(args)
         out["wilson"] = run_wilson(args)
         out["multishift"] = run_multishift(args)
         out["serving"] = run_serving(args)
@@ -418,6 +419,7 @@ def run_wilson(args):
     with FP64 reliable updates against the plain FP64 CG"""
     from qll_gb300 import qll
     L = qll.load()
+    apply_params(L, args)
     L.qllg_wilson_create.restype = ctypes.c_void_p
     L.qllg_wilson_create.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]
     L.qllg_wilson_solve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -464,6 +466,65 @@ def run_wilson(args):
     out["fp64"]["dslash_gbs"] = (8*18*8 + 9*24*8)*Vh/(out["fp64"]["dslash_avg_ms"]*1e-3)/1e9
     out["speedup_mixed_over_fp64"] = out["fp64"]["seconds"]/out["mixed"]["seconds"]
     L.qllg_wilson_destroy(W)
+    return out
+
+
+# ---------------------------------------------------------------------- C1
+def run_c1(args):
+    """C1: 8^4, eps=0.3, m=0.1, one source, FP64 CG to true residual 1e-8
+    (rsq 1e-16): the GPU FP64 and mixed solves (time and iterations; no
+    roofline claim, 8^4 fits in L2) beside the oracle's FP64 CG (cgSolveT
+    restated) on the host cores on the same links; equal FP64 iteration
+    counts are the parity check"""
+    from ctypes import POINTER
+    from qll_gb300 import qll
+    L = qll.load()
+    apply_params(L, args)
+    L.qllg_stag_create_asqtad.restype = ctypes.c_void_p
+    L.qllg_stag_create_asqtad.argtypes = [ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_void_p),
+                                          ctypes.POINTER(qll.Fat7Coeffs)]
+    L.qllg_stag_get_links.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+    dims, mass, rsq = (8, 8, 8, 8), 0.1, 1e-16
+    thin = qll.gen_gauge(dims, 1001, 0.3, ks=True)
+    S = ctypes.c_void_p(L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(thin),
+                                                  ctypes.byref(qll.asqtad_coeffs())))
+    if not S.value:
+        raise RuntimeError(qll.last_error())
+    src = qll.gen_source(dims, 2100, 6, "even")
+    out = {"workload": "C1: asqtad CG 8^4, eps=0.3, m=0.1, 1 rhs, true residual 1e-8"}
+    for name, mode in (("fp64", qll.SOLVE_DOUBLE), ("mixed", qll.SOLVE_MIXED_SINGLE)):
+        best = None
+        for _ in range(3):
+            x = np.zeros_like(src)
+            info = qll.SolveInfo()
+            t = time.time()
+            its = L.qllg_stag_solve(S, 1, qll.vp_array([x]), qll.vp_array([src]),
+                                    (ctypes.c_double*1)(mass), rsq, MAXITS, mode, ctypes.byref(info))
+            dt = time.time() - t
+            if its < 0:
+                raise RuntimeError(qll.last_error())
+            if best is None or dt < best["seconds"]:
+                best = {"seconds": dt, "iters": its, "true_rsq": info.true_rsq[0],
+                        "api": "qllg_stag_solve (host arrays)"}
+        out[name] = best
+    V = int(np.prod(dims))
+    links = [np.zeros((V, 18)) for _ in range(16)]
+    if L.qllg_stag_get_links(S, qll.vp_array(links)):
+        raise RuntimeError(qll.last_error())
+    L.qllg_stag_destroy(S)
+    lib, _ = _oracle()
+    PA = (POINTER(ctypes.c_double)*8)
+    u = PA(*[links[2*i].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
+    u3 = PA(*[links[2*i + 1].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
+    x = np.zeros_like(src)
+    fr = ctypes.c_double()
+    t = time.time()
+    its = lib.or_solve2D((ctypes.c_int*4)(*dims), x.ctypes.data_as(POINTER(ctypes.c_double)), u, u3,
+                         ctypes.c_double(mass), src.ctypes.data_as(POINTER(ctypes.c_double)),
+                         ctypes.c_double(rsq), MAXITS, 1, ctypes.byref(fr))
+    out["cpu_oracle_fp64"] = {"seconds": time.time() - t, "iters": its, "cores": lib.or_num_threads(),
+                              "kind": "port"}
     return out
 
 

@@ -132,9 +132,155 @@ wilson_dslash(qllg_stag_args a)
   }
 }
 
+// one component of a spinor, one row of a link (the layouts of SpinorIO and
+// LinkIO: component-major spinors, [slot][9][V] links, entry 3*col + row)
+template <int P, typename T>
+__device__ __forceinline__ Cx<T> comp_load(const void *b, size_t stride, size_t idx, int c)
+{
+  Cx<T> z;
+  if constexpr (P == QLLG_F64) {
+    const double2 t = __ldg((const double2 *)b + c*stride + idx); z.r = (T)t.x; z.i = (T)t.y;
+  } else {
+    const float2 t = __ldg((const float2 *)b + c*stride + idx); z.r = (T)t.x; z.i = (T)t.y;
+  }
+  return z;
+}
+template <int P, typename T>
+__device__ __forceinline__ void comp_store(void *b, size_t stride, size_t idx, int c, const Cx<T> &z)
+{
+  if constexpr (P == QLLG_F64) ((double2 *)b)[c*stride + idx] = make_double2((double)z.r, (double)z.i);
+  else ((float2 *)b)[c*stride + idx] = make_float2((float)z.r, (float)z.i);
+}
+
+// Small launches (one rhs, fewer sites than the GPU holds threads): three
+// threads per site, one per output colour j.  Each loads the neighbour
+// spinor (the three share it through L1), projects it, and applies row j
+// of the link only, so the launch has three times the threads at a third
+// of the registers.  The per-thread arithmetic follows wilson_dslash (the
+// same projector, phase and reconstruction), restricted to colour j.
+template <int PS, int PL>
+__global__ void __launch_bounds__(kThreads)
+wilson_dslash_c3(qllg_stag_args a)
+{
+  typedef typename Calc<PS, PL>::T T;
+  __shared__ double shm[2*kThreads];
+  const Geo G = make_geo(a.g);
+  const size_t V = (size_t)a.g.V;
+  const size_t total = (size_t)G.Vh;                  // one rhs
+  const int p = a.out_parity;
+  const size_t loff = p ? (size_t)G.Vh : 0;
+  const bool skip = a.done && *(volatile const int *)a.done;
+  Acc<T> acc0, acc1;
+  const bool act = !a.active || a.active[0];
+  const T ca = (T)(a.a ? a.a[0] : a.a0);
+  const T cb = (T)a.b;
+  if(!skip && act) {
+    for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < 3*total;
+        w += (size_t)gridDim.x*blockDim.x) {
+      const int site = (int)(w / 3), j = (int)(w % 3);
+      int x[4];
+      site_coords(G, p, site, x);
+      Cx<T> acc[4], self[4];
+#pragma unroll
+      for(int sp=0; sp<4; sp++) {
+        if(a.self && a.mode == 1) {
+          self[sp] = comp_load<PS,T>(a.self, total, site, 3*sp + j);
+          acc[sp].r = ca*self[sp].r; acc[sp].i = ca*self[sp].i;
+        } else {
+          acc[sp].r = 0; acc[sp].i = 0;
+        }
+      }
+#pragma unroll
+      for(int mu=0; mu<4; mu++) {
+#pragma unroll
+        for(int back=0; back<2; back++) {
+          const int sgn = (back ? 1 : -1)*(a.dag ? -1 : 1);
+          const int k = nbr_index(G, x, mu, back ? -1 : 1);
+          const int slot = 2*mu + back;
+          Cx<T> Ur[3], f[12];
+#pragma unroll
+          for(int l=0; l<3; l++)
+            Ur[l] = comp_load<PL,T>(a.links, 0, (size_t)(slot*9 + 3*l + j)*V + loff + site, 0);
+          SpinorIO<PS,12>::load(a.in, total, (size_t)k, f);
+#pragma unroll
+          for(int hk=0; hk<2; hk++) {
+            const int col = gcol(mu, hk);
+            const int ph = gph(mu, hk) + (sgn < 0 ? 2 : 0);
+            Cx<T> h[3], tt;
+#pragma unroll
+            for(int c=0; c<3; c++) {
+              Cx<T> y = phase(f[3*col + c], ph);
+              h[c].r = f[3*hk + c].r + y.r; h[c].i = f[3*hk + c].i + y.i;
+            }
+            tt.r = 0; tt.i = 0;
+#pragma unroll
+            for(int l=0; l<3; l++) cmac(tt, Ur[l], h[l]);
+            acc[hk].r -= tt.r; acc[hk].i -= tt.i;
+#pragma unroll
+            for(int ar=2; ar<4; ar++) {
+              if(gcol(mu, ar) == hk) {
+                const int pa = gph(mu, ar) + (sgn < 0 ? 0 : 2);
+                Cx<T> y = phase(tt, pa);
+                acc[ar].r += y.r; acc[ar].i += y.i;
+              }
+            }
+          }
+        }
+      }
+      if(a.self && a.mode != 1) {
+#pragma unroll
+        for(int sp=0; sp<4; sp++) self[sp] = comp_load<PS,T>(a.self, total, site, 3*sp + j);
+      }
+      Cx<T> out[4];
+#pragma unroll
+      for(int sp=0; sp<4; sp++) {
+        if(a.mode == 2) {
+          T sr = a.self ? ca*self[sp].r : (T)0, si = a.self ? ca*self[sp].i : (T)0;
+          out[sp].r = fma(cb, acc[sp].r, sr); out[sp].i = fma(cb, acc[sp].i, si);
+        } else out[sp] = acc[sp];
+        comp_store<PS,T>(a.out, total, site, 3*sp + j, out[sp]);
+      }
+      if(a.norm_out) acc0.norm(out);
+      if(a.norm_self && a.self) acc1.norm(self);
+    }
+  }
+  double red[2] = {acc0.get(), acc1.get()};
+  if(a.norm_out || a.norm_self) {
+    double *res[2] = {a.norm_out, a.norm_self};
+    grid_reduce<2>(red, 1, 0, a.partial, a.counter, shm, res);
+  }
+}
+
+template <int PS, int PL>
+int launch_c3(const qllg_stag_args *a)
+{
+  static int bps = 0;
+  if(!bps) {
+    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &bps, wilson_dslash_c3<PS,PL>, kThreads, 0), "occupancy")) return -1;
+    if(bps < 1) bps = 1;
+  }
+  size_t need = (3*(size_t)a->g.Vh + kThreads - 1)/kThreads;
+  size_t maxg = (size_t)qllg_num_sms()*bps;
+  if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
+  int grid = (int)(need < maxg ? need : maxg);
+  if(grid < 1) grid = 1;
+  qllg_stag_args A = *a;
+  A.partial = a->rb ? a->rb->partial : NULL;
+  A.counter = a->rb ? a->rb->counter : NULL;
+  wilson_dslash_c3<PS,PL><<<grid, kThreads, 0, qllg_stream()>>>(A);
+  return qllg_launched("wilson_dslash_c3 launch");
+}
+
 template <int PS, int PL, int NR>
 int launch_t(const qllg_stag_args *a)
 {
+  // FP32, one rhs, fewer sites than half the GPU's resident threads: three
+  // threads per site
+  if constexpr (NR == 1 && PS == QLLG_F32) {
+    if(qllg_get_param("wilson_c3") != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
+      return launch_c3<PS,PL>(a);
+  }
   static int bps = 0;
   if(!bps) {
     if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(

@@ -289,6 +289,10 @@ static struct { const char *name; double value; } g_params[] = {
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
+  {"wilson_c3", 0},          /* small one-rhs FP32 Wilson launches: three threads
+                                per site, one per output colour (C2 at 16^3x32:
+                                17.8 ms per mixed solve against 14.7 ms with one
+                                thread per site, so off) */
   {"dslash_split", 1},       /* multi-rhs Dslash: a slot loop without the active
                                 checks for launches with every rhs active */
   {"dslash_variant", -1},    /* force a Dslash variant (0-12); -1: autotuned */
