@@ -459,8 +459,9 @@ def run_wilson(args):
                         "true_rsq": info.true_rsq[0], "dslash_launches": cnt.value,
                         "dslash_avg_ms": tot.value/max(cnt.value, 1)}
         out[name] = best
-    # Wilson half-Dslash algorithmic bytes per output site: 8 links
-    # + 8 neighbour spinors + 1 store; the mixed solve's launches are mostly FP32
+    # Wilson half-Dslash algorithmic bytes per output site (the lattice
+    # convention, no neighbour reuse): 8 links + 8 neighbour spinors + 1
+    # store; the mixed solve's launches are mostly FP32
     f = out["mixed"]
     f["dslash_note"] = "avg over the solve's FP32 and FP64 half-Dslash launches"
     out["fp64"]["dslash_gbs"] = (8*18*8 + 9*24*8)*Vh/(out["fp64"]["dslash_avg_ms"]*1e-3)/1e9

@@ -254,16 +254,27 @@ int qllg_server_request(const qllg_server *V, int id, qllg_request_info *info);
 int qllg_server_stats(const qllg_server *V, qllg_server_info *info);
 void qllg_server_destroy(qllg_server *V);
 
-/* solver parameters: "reliable_delta" (0.1, 16-bit mixed mode),
- * "reliable_delta_single" (0.01, FP32 mixed mode), "reortho" (1), "graph" (1),
- * "poll" (8), "dslash_mr" (1: multi-rhs Dslash with 4 rhs per thread),
- * "ru_compact" (1: the FP64 reliable update runs over the flagged rhs
- * only), "dslash_vec4" (1: 16-byte loads of rhs pairs), "autotune" (1:
- * time the Dslash variants of each new launch shape and keep the fastest),
- * "dslash_tile" (1: the shared-memory-staged variant may be chosen),
- * "dslash_variant" (-1: autotuned; 0-3 forces 4, 2 or 1 rhs per thread or
- * the staged variant where it applies), "links_recon12" (0; 1: reconstruct-
- * 12 Naik links in the mixed FP32 solves); returns -1 for an unknown name */
+/* solver parameters (name, default):
+ *  "reliable_delta" (0.1, 16-bit mixed mode) and "reliable_delta_single"
+ *    (0.01, FP32 mixed mode): a reliable update when |r| falls by this factor;
+ *  "reortho" (1), "graph" (1: the solver loop as one CUDA-graph launch),
+ *    "poll" (8: first batch of host-polled iterations);
+ *  "ru_compact" (1: reliable updates over the flagged rhs only), "ru_df" (1:
+ *    intermediate reliable updates in double-float, final ones in FP64),
+ *    "df_blocks" (3: register cap of the double-float kernel);
+ *  "dslash_mr" (1: multi-rhs Dslash kernels), "dslash_vec4" (1: 16-byte
+ *    loads of rhs pairs), "dslash_split" (1: a slot loop without the active
+ *    checks when every rhs of a launch is active);
+ *  "autotune" (1: time the Dslash launch shapes of each new shape and keep
+ *    the fastest), "dslash_tile" and "dslash_bulk" (1: the staged and the
+ *    bulk-copy candidates may be chosen), "dslash_variant" (-1: autotuned;
+ *    0-16 forces a candidate where it applies, qllg_autotune_report names
+ *    them);
+ *  "links_recon12" (0; 1: reconstruct-12 Naik links in the FP32 solves),
+ *  "multishift_guess_rsq" (1e-10: the mixed multishift's first stage
+ *    stops at |r|^2 < this |b|^2), "wilson_c3" (0; 1: three threads per site
+ *    in small one-rhs FP32 Wilson launches).
+ * Returns -1 for an unknown name. */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);
 
