@@ -217,16 +217,18 @@ stag_dslash(qllg_stag_args a)
 // with the slot loop software-pipelined one slot ahead.  7 and 8: CFG 0
 // and lean CFG 3 with the direction loop rolled (a quarter of the code);
 // 9 and 11: lean CFG 2 and 4 rolled the same way; 10: lean CFG 3 with
-// every slot loop rolled; 12: CFG 8 with 32-byte spinor loads
+// every slot loop rolled; 12: CFG 8 with 32-byte spinor loads; 13: lean,
+// rolled, 5 blocks/SM (48 registers)
 template <int PS, int R, int CFG> struct MrCfg {
   static constexpr int threads = (CFG == 4 || CFG == 11) ? 128 : 256;
   static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8 || CFG == 10 || CFG == 12) ? 4 :
-                              (CFG == 4 || CFG == 11) ? 9 : (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
+                              (CFG == 4 || CFG == 11) ? 9 : CFG == 13 ? 5 :
+                              (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
   static constexpr bool pf = CFG == 5 || CFG == 6;
   // 1: the direction loop rolled (4 slots a trip); 2: every slot loop rolled
-  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG == 11 || CFG == 12) ? 1 : 0;
+  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG == 11 || CFG == 12 || CFG == 13) ? 1 : 0;
   static constexpr bool v8 = CFG == 12 && PS == QLLG_F32;   // 32-byte spinor loads
 };
 
@@ -1041,10 +1043,11 @@ int launch_tile(const qllg_stag_args *a)
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes, MrCfg 1-8 as variants 4-11 and 9-12 as 13-16; 12 = the
+// launch shapes, MrCfg 1-8 as variants 4-11 and 9-12 as 13-16, and the
+// 2-rhs kernel lean and rolled at 64 and 48 registers as 17, 18; 12 = the
 // bulk-copy pipeline (FP32 links and spinors, 16 slots, 16 rhs,
 // k_stag_bulk.cuh)
-constexpr int kNumVariants = 17;
+constexpr int kNumVariants = 19;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
@@ -1054,7 +1057,9 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "bulk-copy pipeline", "4 rhs/thread lean 80 regs rolled",
                                                 "4 rhs/thread lean 64 regs all rolled",
                                                 "4 rhs/thread lean 56 regs rolled",
-                                                "4 rhs/thread lean 64 regs rolled 32-byte"};
+                                                "4 rhs/thread lean 64 regs rolled 32-byte",
+                                                "2 rhs/thread lean 64 regs rolled",
+                                                "2 rhs/thread lean 48 regs rolled"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1096,7 +1101,9 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 13: return launch_mr<PS,PL,NS,NR,4,9>(a);
       case 14: return launch_mr<PS,PL,NS,NR,4,10>(a);
       case 15: return launch_mr<PS,PL,NS,NR,4,11>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,12>(a);
+      case 16: return launch_mr<PS,PL,NS,NR,4,12>(a);
+      case 17: return launch_mr<PS,PL,NS,NR,2,8>(a);
+      default: return launch_mr<PS,PL,NS,NR,2,13>(a);
       }
     }
   }
