@@ -218,17 +218,18 @@ stag_dslash(qllg_stag_args a)
 // and lean CFG 3 with the direction loop rolled (a quarter of the code);
 // 9 and 11: lean CFG 2 and 4 rolled the same way; 10: lean CFG 3 with
 // every slot loop rolled; 12: CFG 8 with 32-byte spinor loads; 13: lean,
-// rolled, 5 blocks/SM (48 registers)
+// rolled, 5 blocks/SM (48 registers); 14 and 15: lean, rolled, 128 threads,
+// 7 and 8 blocks/SM (72 and 64 registers)
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int threads = (CFG == 4 || CFG == 11) ? 128 : 256;
+  static constexpr int threads = (CFG == 4 || CFG == 11 || CFG == 14 || CFG == 15) ? 128 : 256;
   static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8 || CFG == 10 || CFG == 12) ? 4 :
-                              (CFG == 4 || CFG == 11) ? 9 : CFG == 13 ? 5 :
+                              (CFG == 4 || CFG == 11) ? 9 : CFG == 13 ? 5 : CFG == 14 ? 7 : CFG == 15 ? 8 :
                               (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
   static constexpr bool pf = CFG == 5 || CFG == 6;
   // 1: the direction loop rolled (4 slots a trip); 2: every slot loop rolled
-  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG == 11 || CFG == 12 || CFG == 13) ? 1 : 0;
+  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG >= 11) ? 1 : 0;
   static constexpr bool v8 = CFG == 12 && PS == QLLG_F32;   // 32-byte spinor loads
 };
 
@@ -1044,10 +1045,11 @@ int launch_tile(const qllg_stag_args *a)
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
 // launch shapes, MrCfg 1-8 as variants 4-11 and 9-12 as 13-16, and the
-// 2-rhs kernel lean and rolled at 64 and 48 registers as 17, 18; 12 = the
+// 2-rhs kernel lean and rolled at 64 and 48 registers as 17, 18, MrCfg 14
+// and 15 as 19 and 20; 12 = the
 // bulk-copy pipeline (FP32 links and spinors, 16 slots, 16 rhs,
 // k_stag_bulk.cuh)
-constexpr int kNumVariants = 19;
+constexpr int kNumVariants = 21;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
@@ -1059,7 +1061,9 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "4 rhs/thread lean 56 regs rolled",
                                                 "4 rhs/thread lean 64 regs rolled 32-byte",
                                                 "2 rhs/thread lean 64 regs rolled",
-                                                "2 rhs/thread lean 48 regs rolled"};
+                                                "2 rhs/thread lean 48 regs rolled",
+                                                "4 rhs/thread lean 72 regs rolled (128 threads)",
+                                                "4 rhs/thread lean 64 regs rolled (128 threads)"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1103,7 +1107,9 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 15: return launch_mr<PS,PL,NS,NR,4,11>(a);
       case 16: return launch_mr<PS,PL,NS,NR,4,12>(a);
       case 17: return launch_mr<PS,PL,NS,NR,2,8>(a);
-      default: return launch_mr<PS,PL,NS,NR,2,13>(a);
+      case 18: return launch_mr<PS,PL,NS,NR,2,13>(a);
+      case 19: return launch_mr<PS,PL,NS,NR,4,14>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,15>(a);
       }
     }
   }
