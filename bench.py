@@ -274,6 +274,11 @@ def run_gpu(args):
     srcs_p = [pinned(s) for s in srcs]
     xs_p = [pinned(x) for x in xs]
     e2e_steps = max(1, min(args.steps, 3))
+    # one untimed warm-up through the same call (its device buffers differ
+    # from the device-API solves above, so it captures its own solver graph)
+    if L.qllg_stag_solve(S, NRHS, qll.vp_array(xs_p), qll.vp_array(srcs_p), masses, RSQ,
+                         MAXITS, qll.SOLVE_MIXED_SINGLE, ctypes.byref(info)) < 0:
+        raise RuntimeError(qll.last_error())
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
