@@ -1190,15 +1190,20 @@ int tuned_variant(const qllg_stag_args *a)
   int best = first, rc = 0;
   for(int c=first; c<kNumVariants && !rc; c++) {
     if(!variant_ok<PS,PL,NS,NR>(&T, c)) continue;
+    // the fastest of five timed launches after a warm one: candidates are
+    // often within a few percent, and the minimum is steadier than a mean
     rc |= launch_variant<PS,PL,NS,NR>(&T, c);                 // warm
-    cudaEventRecord(e0, qllg_stream());
-    for(int k=0; k<3; k++) rc |= launch_variant<PS,PL,NS,NR>(&T, c);
-    cudaEventRecord(e1, qllg_stream());
-    cudaEventSynchronize(e1);
-    ms[c] = 0;
-    cudaEventElapsedTime(&ms[c], e0, e1);
-    ms[c] /= 3;
-    if(ms[c] < ms[best]) best = c;
+    ms[c] = -1;
+    for(int k=0; k<5 && !rc; k++) {
+      cudaEventRecord(e0, qllg_stream());
+      rc |= launch_variant<PS,PL,NS,NR>(&T, c);
+      cudaEventRecord(e1, qllg_stream());
+      cudaEventSynchronize(e1);
+      float t = 0;
+      cudaEventElapsedTime(&t, e0, e1);
+      if(ms[c] < 0 || t < ms[c]) ms[c] = t;
+    }
+    if(ms[c] >= 0 && (ms[best] < 0 || ms[c] < ms[best])) best = c;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
