@@ -91,16 +91,6 @@ __device__ __forceinline__ void slot_link(const qllg_stag_args &a, int mu, int b
   }
 }
 
-// 32-byte load of 8 floats (ld.global.nc.v8.f32, sm_100 and later); p
-// 32-byte aligned
-__device__ __forceinline__ void ldg_v8(float f[8], const void *p)
-{
-  asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-               : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]),
-                 "=f"(f[6]), "=f"(f[7])
-               : "l"(p));
-}
-
 template <int PS, int PL, int NS, int NR>
 __global__ void __launch_bounds__(kThreads)
 stag_dslash(qllg_stag_args a)
@@ -210,27 +200,24 @@ stag_dslash(qllg_stag_args a)
 
 // Launch shapes of the multi-rhs kernel.  CFG 0: 256 threads, 2 blocks/SM
 // (FP64: 1; 2 rhs/thread: 3) and the register cap that gives; 1: CFG 0 with
-// the complex FMAs on packed FP32 pairs (cmac_f2).  2-4 are "lean": the
-// per-rhs scalars and the norm sums in shared memory, for more resident
-// warps at fewer registers: 2: 3 blocks/SM (80 registers); 3: 4 blocks/SM
-// (64); 4: 128 threads, 9 blocks/SM (56).  5 and 6: CFG 0 and lean CFG 0
-// with the slot loop software-pipelined one slot ahead.  7 and 8: CFG 0
-// and lean CFG 3 with the direction loop rolled (a quarter of the code);
-// 9 and 11: lean CFG 2 and 4 rolled the same way; 10: lean CFG 3 with
-// every slot loop rolled; 12: CFG 8 with 32-byte spinor loads; 13: lean,
-// rolled, 5 blocks/SM (48 registers); 14 and 15: lean, rolled, 128 threads,
-// 7 and 8 blocks/SM (72 and 64 registers)
+// the complex FMAs on packed FP32 pairs (cmac_f2).  The others are "lean":
+// the per-rhs scalars and the norm sums in shared memory, for more resident
+// warps at fewer registers.  2 and 3: 3 and 4 blocks/SM (80 and 64
+// registers); 5 and 6: CFG 0 and lean CFG 0 with the slot loop software-
+// pipelined one slot ahead; 7, 8 and 9: CFG 0 and lean CFG 3 and 2 with the
+// direction loop rolled (a quarter of the code, and fewer loads hoisted);
+// 14 and 15: lean and rolled in 128-thread blocks, 7 and 8 blocks/SM (72 and
+// 64 registers).  (Candidates measured slower and dropped: 56 and 48
+// registers, every slot loop rolled, 32-byte spinor loads, lean 2 rhs per
+// thread.)
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int threads = (CFG == 4 || CFG == 11 || CFG == 14 || CFG == 15) ? 128 : 256;
-  static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8 || CFG == 10 || CFG == 12) ? 4 :
-                              (CFG == 4 || CFG == 11) ? 9 : CFG == 13 ? 5 : CFG == 14 ? 7 : CFG == 15 ? 8 :
-                              (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
+  static constexpr int threads = (CFG == 14 || CFG == 15) ? 128 : 256;
+  static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8) ? 4 :
+                              CFG == 14 ? 7 : CFG == 15 ? 8 : (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
   static constexpr bool pf = CFG == 5 || CFG == 6;
-  // 1: the direction loop rolled (4 slots a trip); 2: every slot loop rolled
-  static constexpr int roll = CFG == 10 ? 2 : (CFG == 7 || CFG == 8 || CFG == 9 || CFG >= 11) ? 1 : 0;
-  static constexpr bool v8 = CFG == 12 && PS == QLLG_F32;   // 32-byte spinor loads
+  static constexpr bool roll = CFG == 7 || CFG == 8 || CFG == 9 || CFG >= 14;   // direction loop rolled
 };
 
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
@@ -244,7 +231,6 @@ stag_dslash_mr(qllg_stag_args a)
   constexpr int Q = NR/R;                       // threads per site
   constexpr int PX = VecPrec<PS>::value;
   constexpr bool F2 = MrCfg<PS,R,CFG>::f2;
-  constexpr bool V8 = MrCfg<PS,R,CFG>::v8;
   constexpr bool PF = MrCfg<PS,R,CFG>::pf;
   constexpr int TB = MrCfg<PS,R,CFG>::threads;
   constexpr bool LEAN = MrCfg<PS,R,CFG>::lean;
@@ -335,39 +321,18 @@ stag_dslash_mr(qllg_stag_args a)
       auto slots = [&](auto ck) {
         constexpr bool CK = decltype(ck)::value;     // check the active flags
         constexpr int UMU = MrCfg<PS,R,CFG>::roll ? 1 : 4;
-        constexpr int UB = MrCfg<PS,R,CFG>::roll == 2 ? 1 : 2;
 #pragma unroll UMU
         for(int mu=0; mu<4; mu++) {
-#pragma unroll UB
+#pragma unroll
           for(int back=0; back<2; back++) {
-#pragma unroll UB
+#pragma unroll
             for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
               const int d = (nk ? 3 : 1)*(back ? -1 : 1);
               const size_t nb = (size_t)nbr_index(G, x, mu, d);
               const size_t kb = nb*NR + q*R;
               Cx<T> U[9];
               slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
-              if constexpr (v4 && V8 && !CK && R == 4) {
-                // the 4 rhs of a colour in one 32-byte load: a warp request
-                // then covers whole 128-byte site blocks of 4 sites instead
-                // of halves of 8 (half the L1 wavefronts)
-                Cx<T> v[4][3];
-#pragma unroll
-                for(int l=0; l<3; l++) {
-                  float f[8];
-                  ldg_v8(f, (const float2 *)a.in + (size_t)l*total + kb);
-#pragma unroll
-                  for(int j=0; j<4; j++) { v[j][l].r = f[2*j]; v[j][l].i = f[2*j + 1]; }
-                }
-#pragma unroll
-                for(int j=0; j<4; j++) {
-#pragma unroll
-                  for(int l=0; l<3; l++) {
-#pragma unroll
-                    for(int c=0; c<3; c++) cmac(acc[j][c], U[3*l + c], v[j][l]);
-                  }
-                }
-              } else if constexpr (v4) {
+              if constexpr (v4) {
                 // two rhs per 16-byte load and colour
 #pragma unroll
                 for(int h=0; h<R/2; h++) {
@@ -1044,24 +1009,16 @@ int launch_tile(const qllg_stag_args *a)
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes, MrCfg 1-8 as variants 4-11 and 9-12 as 13-16, and the
-// 2-rhs kernel lean and rolled at 64 and 48 registers as 17, 18, MrCfg 14
-// and 15 as 19 and 20; 12 = the
-// bulk-copy pipeline (FP32 links and spinors, 16 slots, 16 rhs,
-// k_stag_bulk.cuh)
-constexpr int kNumVariants = 21;
+// launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15 as variants 4-10 and
+// 12-14) and 11 = the bulk-copy pipeline (FP32 links and spinors, 16 slots,
+// 16 rhs, k_stag_bulk.cuh)
+constexpr int kNumVariants = 15;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
-                                                "4 rhs/thread lean 56 regs", "4 rhs/thread prefetch",
-                                                "4 rhs/thread lean prefetch", "4 rhs/thread rolled",
-                                                "4 rhs/thread lean 64 regs rolled",
+                                                "4 rhs/thread prefetch", "4 rhs/thread lean prefetch",
+                                                "4 rhs/thread rolled", "4 rhs/thread lean 64 regs rolled",
                                                 "bulk-copy pipeline", "4 rhs/thread lean 80 regs rolled",
-                                                "4 rhs/thread lean 64 regs all rolled",
-                                                "4 rhs/thread lean 56 regs rolled",
-                                                "4 rhs/thread lean 64 regs rolled 32-byte",
-                                                "2 rhs/thread lean 64 regs rolled",
-                                                "2 rhs/thread lean 48 regs rolled",
                                                 "4 rhs/thread lean 72 regs rolled (128 threads)",
                                                 "4 rhs/thread lean 64 regs rolled (128 threads)"};
 
@@ -1071,12 +1028,9 @@ bool variant_ok(const qllg_stag_args *a, int v)
   if(v == 0) return NR >= 4;
   if(v == 1) return NR >= 2;
   if(v == 2) return true;
-  if(v == 12)
+  if(v == 11)
     return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
            a->g.Vh % kBkSites == 0 && vec4_ok(a) && qllg_get_param("dslash_bulk") != 0;
-  if(v == 16)
-    return PS == QLLG_F32 && NR == 16 && vec4_ok(a) && ((uintptr_t)a->in & 31u) == 0 &&
-           qllg_get_param("dslash_vec4") != 0;
   if(v >= 4)
     return PS == QLLG_F32 && NR == 16 && vec4_ok(a) && qllg_get_param("dslash_vec4") != 0;
   return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
@@ -1089,7 +1043,7 @@ int launch_variant(const qllg_stag_args *a, int v)
   if(!variant_ok<PS,PL,NS,NR>(a, v)) v = NR >= 4 ? 0 : (NR >= 2 ? 1 : 2);
   if constexpr (PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16) {
     if(v == 3) return launch_tile<NR>(a);
-    if(v == 12) return launch_bulk<NR>(a);
+    if(v == 11) return launch_bulk<NR>(a);
   }
   if constexpr (PS == QLLG_F32 && NR == 16) {
     if(v >= 4) {
@@ -1097,18 +1051,12 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 4: return launch_mr<PS,PL,NS,NR,4,1>(a);
       case 5: return launch_mr<PS,PL,NS,NR,4,2>(a);
       case 6: return launch_mr<PS,PL,NS,NR,4,3>(a);
-      case 7: return launch_mr<PS,PL,NS,NR,4,4>(a);
-      case 8: return launch_mr<PS,PL,NS,NR,4,5>(a);
-      case 9: return launch_mr<PS,PL,NS,NR,4,6>(a);
-      case 10: return launch_mr<PS,PL,NS,NR,4,7>(a);
-      case 11: return launch_mr<PS,PL,NS,NR,4,8>(a);
-      case 13: return launch_mr<PS,PL,NS,NR,4,9>(a);
-      case 14: return launch_mr<PS,PL,NS,NR,4,10>(a);
-      case 15: return launch_mr<PS,PL,NS,NR,4,11>(a);
-      case 16: return launch_mr<PS,PL,NS,NR,4,12>(a);
-      case 17: return launch_mr<PS,PL,NS,NR,2,8>(a);
-      case 18: return launch_mr<PS,PL,NS,NR,2,13>(a);
-      case 19: return launch_mr<PS,PL,NS,NR,4,14>(a);
+      case 7: return launch_mr<PS,PL,NS,NR,4,5>(a);
+      case 8: return launch_mr<PS,PL,NS,NR,4,6>(a);
+      case 9: return launch_mr<PS,PL,NS,NR,4,7>(a);
+      case 10: return launch_mr<PS,PL,NS,NR,4,8>(a);
+      case 12: return launch_mr<PS,PL,NS,NR,4,9>(a);
+      case 13: return launch_mr<PS,PL,NS,NR,4,14>(a);
       default: return launch_mr<PS,PL,NS,NR,4,15>(a);
       }
     }
