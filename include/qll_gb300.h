@@ -271,6 +271,9 @@ void qllg_server_destroy(qllg_server *V);
  *    0-14 forces a candidate where it applies, qllg_autotune_report names
  *    them);
  *  "links_recon12" (0; 1: reconstruct-12 Naik links in the FP32 solves),
+ *  "solve2_mixed" (0; 1: the drop-in solve2D runs FP32 iterations with FP64
+ *    reliable updates, to the same true residual, instead of the reference's
+ *    FP64 CG);
  *  "multishift_guess_rsq" (1e-10: the mixed multishift's first stage
  *    stops at |r|^2 < this |b|^2), "wilson_c3" (0; 1: three threads per site
  *    in small one-rhs FP32 Wilson launches).

@@ -289,6 +289,8 @@ static struct { const char *name; double value; } g_params[] = {
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
+  {"solve2_mixed", 0},       /* solve2D (drop-in): FP32 iterations with FP64 reliable
+                                updates instead of the reference's FP64 CG */
   {"wilson_c3", 0},          /* small one-rhs FP32 Wilson launches: three threads
                                 per site, one per output colour (C2 at 16^3x32:
                                 17.8 ms per mixed solve against 14.7 ms with one

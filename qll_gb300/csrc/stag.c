@@ -1876,8 +1876,11 @@ solve2##S_(StaggeredSolver##S_ *ss, real *x, real mass, real *y, double rsq,    
   if(rsq < 0) { ss->cgls.verbose = 3; rsq = -rsq; }                               \
   double m = ss->mass, sc = (double)mass;                                         \
   void *xa[1] = {x}, *ya[1] = {y};                                                \
-  int its = stag_solve_host(S, 1, xa, ya, &m, rsq, maxits,                        \
-                            DBL ? QLLG_SOLVE_DOUBLE : QLLG_SOLVE_SINGLE, NULL,    \
+  /* the reference's precision, or (solve2_mixed, D only) FP32 iterations      \
+   * with FP64 reliable updates to the same true residual */                      \
+  int mode = DBL ? QLLG_SOLVE_DOUBLE : QLLG_SOLVE_SINGLE;                         \
+  if(DBL && qllg_get_param("solve2_mixed") != 0) mode = QLLG_SOLVE_MIXED_SINGLE;  \
+  int its = stag_solve_host(S, 1, xa, ya, &m, rsq, maxits, mode, NULL,            \
                             !ss->noscale, &sc);                                   \
   ss->its = its;                                                                  \
   return its;                                                                     \

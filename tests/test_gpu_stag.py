@@ -100,6 +100,26 @@ def test_solve2_matches_oracle(prec):
     getattr(L, "freeStaggeredSolver" + prec)(byref(ss))
 
 
+def test_solve2_mixed_switch():
+    """solve2_mixed 1: the drop-in solve2D runs the FP32 mixed solver; the
+    solution reaches the same tolerance as the oracle's FP64 CG, with the
+    reference's mass scaling"""
+    L, lay, ss, u, u3 = _make_solver("D")
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    b = qll.gen_source(DIMS, 2003, 6, "even")
+    x = np.zeros_like(b)
+    L.qllg_set_param(b"solve2_mixed", 1)
+    its = L.solve2D(byref(ss), qll.ptr(x), c_double(0.1), qll.ptr(b), 1e-16, 2000, b"even")
+    L.qllg_set_param(b"solve2_mixed", 0)
+    assert its > 0, qll.last_error()
+    its_o, xo, _ = orc.solve2(DIMS, u, u3, 0.1, b, 1e-16, 2000)
+    Vh = b.shape[0]//2
+    # both are within the tolerance of the exact solution: |x - x*| <= cond |r|/|b|
+    assert relerr(x[:Vh], xo[:Vh]) < 1e-5
+    assert np.all(x[Vh:] == 0)
+    L.freeStaggeredSolverD(byref(ss))
+
+
 def test_solve2_noscale_and_mass_zero_scaling():
     L, lay, ss, u, u3 = _make_solver("D")
     b = qll.gen_source(DIMS, 2002, 6, "even")
