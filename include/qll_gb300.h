@@ -255,8 +255,9 @@ int qllg_server_stats(const qllg_server *V, qllg_server_info *info);
 void qllg_server_destroy(qllg_server *V);
 
 /* solver parameters (name, default):
- *  "reliable_delta" (0.1, 16-bit mixed mode) and "reliable_delta_single"
- *    (0.01, FP32 mixed mode): a reliable update when |r| falls by this factor;
+ *  "reliable_delta" (0.1, 16-bit mixed mode),
+ *  "reliable_delta_single" (0.01, FP32 mixed mode): a reliable update when
+ *    |r| falls by this factor;
  *  "reortho" (1), "graph" (1: the solver loop as one CUDA-graph launch),
  *    "poll" (8: first batch of host-polled iterations);
  *  "ru_compact" (1: reliable updates over the flagged rhs only), "ru_df" (1:
@@ -266,8 +267,8 @@ void qllg_server_destroy(qllg_server *V);
  *    loads of rhs pairs), "dslash_split" (1: a slot loop without the active
  *    checks when every rhs of a launch is active);
  *  "autotune" (1: time the Dslash launch shapes of each new shape and keep
- *    the fastest), "dslash_tile" and "dslash_bulk" (1: the staged and the
- *    bulk-copy candidates may be chosen), "dslash_variant" (-1: autotuned;
+ *    the fastest), "dslash_tile" (1) and "dslash_bulk" (1): the staged and
+ *    the bulk-copy candidates may be chosen; "dslash_variant" (-1: autotuned;
  *    0-14 forces a candidate where it applies, qllg_autotune_report names
  *    them);
  *  "links_recon12" (0; 1: reconstruct-12 Naik links in the FP32 solves),

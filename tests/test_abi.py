@@ -54,3 +54,27 @@ def test_library_loads_without_gpu_and_reports_errors():
     rc = L.qllg_stag_nbr_table(qll.dims_c((3, 4, 4, 4)), 0, 0, out)
     assert rc < 0
     assert qll.last_error()
+
+
+def test_documented_parameters_exist_with_their_defaults():
+    """every solver parameter the header documents is known to the library,
+    with the default the header states (no GPU needed: the table is host
+    state)"""
+    import ctypes
+    text = open(os.path.join(INC, "qll_gb300.h")).read()
+    block = text[text.index("/* solver parameters (name, default):"):]
+    block = block[:block.index("*/")]
+    documented = re.findall(r'"(\w+)" \(([-0-9.e]+)', block)
+    assert len(documented) >= 15
+    L = qll.load()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_set_param.restype = ctypes.c_int
+    L.qllg_get_param.argtypes = [ctypes.c_char_p]
+    L.qllg_get_param.restype = ctypes.c_double
+    for name, default in documented:
+        assert L.qllg_get_param(name.encode()) == float(default), name
+        assert L.qllg_set_param(name.encode(), float(default)) == 0, name
+    assert L.qllg_set_param(b"no_such_parameter", 1.0) == -1
+    # and the header documents every parameter of the library's table
+    table = re.findall(r'\{"(\w+)",', open(os.path.join(ROOT, "qll_gb300", "csrc", "runtime.c")).read())
+    assert set(table) == {n for n, _ in documented}
