@@ -52,7 +52,7 @@ wilson_dslash(qllg_stag_args a)
   const bool skip = a.done && *(volatile const int *)a.done;
   Acc<T> acc0, acc1;
   const int rhs = threadIdx.x % NR;
-  const bool act = !a.active || a.active[rhs];
+  const bool act = !a.active || (a.active[rhs] && (!a.active_eq || a.active[rhs] == a.active_eq));
   const T ca = (T)(a.a ? a.a[rhs] : a.a0);
   const T cb = (T)a.b;
   if(!skip && act) {
@@ -117,7 +117,7 @@ wilson_dslash(qllg_stag_args a)
       for(int c=0; c<12; c++) {
         if(a.mode == 2) {
           T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
-          out[c].r = fma(cb, acc[c].r, sr); out[c].i = fma(cb, acc[c].i, si);
+          out[c].r = kfma(cb, acc[c].r, sr); out[c].i = kfma(cb, acc[c].i, si);
         } else out[c] = acc[c];
       }
       SpinorIO<PS,12>::store(a.out, total, t, out);
@@ -323,6 +323,8 @@ qllg_k_wilson_dslash(int ps, int pl, const qllg_stag_args *a)
   }
   if(ps == QLLG_F64 && pl == QLLG_F64) return launch_nr<QLLG_F64, QLLG_F64>(a);
   if(ps == QLLG_F32 && pl == QLLG_F32) return launch_nr<QLLG_F32, QLLG_F32>(a);
-  qllg_set_error("wilson_dslash: unsupported precision pair %d/%d", ps, pl);
+  // double-float (the reliable updates of the mixed CGNR): one rhs
+  if(ps == QLLG_DF && pl == QLLG_DF && a->nrhs == 1) return launch_t<QLLG_DF, QLLG_DF, 1>(a);
+  qllg_set_error("wilson_dslash: unsupported precision pair %d/%d (%d rhs)", ps, pl, a->nrhs);
   return -1;
 }

@@ -49,6 +49,15 @@ __device__ __forceinline__ dfl df_fast2sum(float s, float e) {   // needs |s| >=
   return dfl(h, __fsub_rn(e, __fsub_rn(h, s)));
 }
 __device__ __forceinline__ dfl operator-(const dfl &a) { return dfl(-a.h, -a.l); }
+__device__ __forceinline__ dfl operator+(const dfl &a, const dfl &b) {
+  const float s = __fadd_rn(a.h, b.h);                  // TwoSum(a.h, b.h) = s + err
+  const float bb = __fsub_rn(s, a.h);
+  const float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+  return df_fast2sum(s, __fadd_rn(err, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dfl operator-(const dfl &a, const dfl &b) { return a + (-b); }
+__device__ __forceinline__ dfl &operator+=(dfl &a, const dfl &b) { a = a + b; return a; }
+__device__ __forceinline__ dfl &operator-=(dfl &a, const dfl &b) { a = a - b; return a; }
 __device__ __forceinline__ dfl operator*(const dfl &a, const dfl &b) {
   const float p = __fmul_rn(a.h, b.h);
   float e = fmaf(a.h, b.h, -p);
@@ -379,6 +388,18 @@ template <> struct Acc<double> {
   template <int N> __device__ __forceinline__ void norm(const Cx<double> (&v)[N]) {
 #pragma unroll
     for(int c=0; c<N; c++) s += v[c].r*v[c].r + v[c].i*v[c].i;
+  }
+  __device__ __forceinline__ double get() const { return s; }
+};
+// double-float data: the norm in FP64 (only diagnostics use it)
+template <> struct Acc<dfl> {
+  double s = 0;
+  template <int N> __device__ __forceinline__ void norm(const Cx<dfl> (&v)[N]) {
+#pragma unroll
+    for(int c=0; c<N; c++) {
+      const double r = (double)v[c].r, i = (double)v[c].i;
+      s += r*r + i*i;
+    }
   }
   __device__ __forceinline__ double get() const { return s; }
 };

@@ -29,12 +29,12 @@ int qllg_geom_from_layout(qllg_geom *g, const Layout *l);
 Layout *qllg_current_layout(void);
 
 enum { WW_X, WW_R, WW_P, WW_AP, WW_S, WW_V, WW_B, WW_X64, WW_R64, WW_T64, WW_S64, WW_V64,
-       WW_IO, WW_N };
+       WW_XDF, WW_IO, WW_N };
 
 struct qllg_wilson {
   qllg_geom g;
   int master;
-  void *links[2];          /* FP64, FP32: [8][9][V] */
+  void *links[QLLG_NLINKP];  /* by precision (FP64, FP32, double-float): [8][9][V] */
   qllg_redbuf rb;
   qllg_cg_scalars *sc, *hsc;
   void *ws[WW_N];
@@ -77,7 +77,7 @@ qllg_wilson_destroy(qllg_wilson *W)
 {
   if(!W) return;
   qllg_sync();
-  for(int p=0; p<2; p++) qllg_dfree(W->links[p]);
+  for(int p=0; p<QLLG_NLINKP; p++) qllg_dfree(W->links[p]);
   qllg_dfree(W->sc);
   if(W->hsc) cudaFreeHost(W->hsc);
   qllg_redbuf_free(&W->rb);
@@ -132,10 +132,11 @@ qllg_wilson_create_f(const int dims[4], float *const u[8])
   return wilson_create(dims, (void *const *)u, 0);
 }
 
+/* one half-Dslash; with active_eq, only the rhs whose flag equals it */
 static int
-whalf(qllg_wilson *W, int prec, int out_parity, const void *in, const void *self, void *out,
-      int mode, double a0, double b, double *norm_out, double *norm_self, const int *active,
-      const int *done, int dag)
+whalf_eq(qllg_wilson *W, int prec, int out_parity, const void *in, const void *self, void *out,
+         int mode, double a0, double b, double *norm_out, double *norm_self, const int *active,
+         int active_eq, const int *done, int dag)
 {
   if(wlinks(W, prec)) return -1;
   qllg_stag_args A;
@@ -154,6 +155,7 @@ whalf(qllg_wilson *W, int prec, int out_parity, const void *in, const void *self
   A.norm_out = norm_out;
   A.norm_self = norm_self;
   A.active = active;
+  A.active_eq = active_eq;
   A.done = done;
   A.rb = &W->rb;
   A.dag = dag;
@@ -161,6 +163,15 @@ whalf(qllg_wilson *W, int prec, int out_parity, const void *in, const void *self
   int rc = qllg_k_wilson_dslash(prec, prec, &A);
   qllg_tm_end();
   return rc;
+}
+
+static int
+whalf(qllg_wilson *W, int prec, int out_parity, const void *in, const void *self, void *out,
+      int mode, double a0, double b, double *norm_out, double *norm_self, const int *active,
+      const int *done, int dag)
+{
+  return whalf_eq(W, prec, out_parity, in, self, out, mode, a0, b, norm_out, norm_self, active, 0,
+                  done, dag);
 }
 
 static int
@@ -268,11 +279,18 @@ wilson_ref_cg(qllg_wilson *W, void *x, const void *b, double mass, double rsq, i
 
 /* out = S in (dag: S^dagger); tmp: odd scratch; |out|^2 into norm */
 static int
+apply_schur_eq(qllg_wilson *W, int prec, const void *in, void *out, void *tmp, double a, int dag,
+               double *norm, const int *active, int eq, const int *done)
+{
+  if(whalf_eq(W, prec, 1, in, NULL, tmp, 0, 0, 1, NULL, NULL, active, eq, done, dag)) return -1;
+  return whalf_eq(W, prec, 0, tmp, in, out, 2, a, -1.0/a, norm, NULL, active, eq, done, dag);
+}
+
+static int
 apply_schur(qllg_wilson *W, int prec, const void *in, void *out, void *tmp, double a, int dag,
             double *norm, const int *active, const int *done)
 {
-  if(whalf(W, prec, 1, in, NULL, tmp, 0, 0, 1, NULL, NULL, active, done, dag)) return -1;
-  return whalf(W, prec, 0, tmp, in, out, 2, a, -1.0/a, norm, NULL, active, done, dag);
+  return apply_schur_eq(W, prec, in, out, tmp, a, dag, norm, active, 0, done);
 }
 
 static int
@@ -293,6 +311,12 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   void *r = wws(W, WW_R, vs), *p = wws(W, WW_P, vs), *Ap = wws(W, WW_AP, vs);
   void *Sp = wws(W, WW_S, vs), *v = wws(W, WW_V, vs);
   if(!xs || !r || !p || !Ap || !Sp || !v) return -1;
+  /* intermediate reliable updates (ru 1) in double-float: S^+ S x in the
+   * FP32 pipes at about 44-bit precision; the final one (ru 2), whose
+   * residual may end the solve, in FP64 */
+  void *xdf = NULL;
+  if(ps != QLLG_F64 && qllg_get_param("ru_df") != 0 &&
+     (wlinks(W, QLLG_DF) || !(xdf = wws(W, WW_XDF, wvec(W, QLLG_DF))))) return -1;
   memset(W->hsc, 0, sizeof(qllg_cg_scalars));
   W->hsc->rsq_stop[0] = rsq;
   W->hsc->maxits = maxits;
@@ -310,8 +334,15 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
       if(qllg_k_scg_update_xr(ps, ps, xs, r, p, Ap, Vh, 12, 1, sc, &W->rb)) return -1;
       if(ps != QLLG_F64) {
         if(qllg_k_mcg_accum(ps, x64, xs, Vh, 12, 1, sc)) return -1;
-        if(apply_schur(W, QLLG_F64, x64, s64, vv64, a, 0, NULL, sc->ru, &sc->no_ru)) return -1;
-        if(apply_schur(W, QLLG_F64, s64, t64, vv64, a, 1, NULL, sc->ru, &sc->no_ru)) return -1;
+        /* the double-float pass reuses s64, vv64 and t64 (same size); t
+         * goes back to FP64 in place */
+        if(xdf && (qllg_k_spinor_df(1, xdf, x64, Vh, 12, 1, sc->ru, 1, &sc->no_ru) ||
+                   apply_schur_eq(W, QLLG_DF, xdf, s64, vv64, a, 0, NULL, sc->ru, 1, &sc->no_ru) ||
+                   apply_schur_eq(W, QLLG_DF, s64, t64, vv64, a, 1, NULL, sc->ru, 1, &sc->no_ru) ||
+                   qllg_k_spinor_df(0, t64, t64, Vh, 12, 1, sc->ru, 1, &sc->no_ru))) return -1;
+        const int eq = xdf ? 2 : 0;
+        if(apply_schur_eq(W, QLLG_F64, x64, s64, vv64, a, 0, NULL, sc->ru, eq, &sc->no_ru) ||
+           apply_schur_eq(W, QLLG_F64, s64, t64, vv64, a, 1, NULL, sc->ru, eq, &sc->no_ru)) return -1;
         if(qllg_k_mcg_residual(ps, r64, r, bp, t64, Vh, 12, 1, 1, sc, &W->rb)) return -1;
       }
       if(qllg_k_scg_update_p(ps, p, r, Vh, 12, 1, sc)) return -1;

@@ -319,6 +319,45 @@ def test_wilson_cgnr_matches_oracle(mode):
     L.qllg_wilson_destroy(ctypes.c_void_p(W))
 
 
+def test_wilson_double_float_reliable_updates():
+    """the mixed CGNR with its intermediate reliable updates in double-float
+    (ru_df 1, the Wilson kernel on (hi, lo) float pairs) and in FP64 (0):
+    both reach the FP64 true residual in about the same iterations, with
+    solutions that agree with each other and with the oracle's CGNR"""
+    L = qll.load()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    L.qllg_wilson_create.restype = ctypes.c_void_p
+    L.qllg_wilson_create.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_void_p)]
+    L.qllg_wilson_solve.restype = c_int
+    L.qllg_wilson_solve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double,
+                                    c_double, c_int, c_int, ctypes.POINTER(qll.SolveInfo)]
+    u = list(wilson_links(DIMS))
+    W = L.qllg_wilson_create(qll.dims_c(DIMS), qll.vp_array(u))
+    assert W, qll.last_error()
+    b = qll.gen_source(DIMS, 29, 24, "even")
+    Vh = b.shape[0]//2
+    mass = 1/(2*0.12) - 4
+    res = {}
+    for ru_df in (1, 0):
+        L.qllg_set_param(b"ru_df", ru_df)
+        x = np.zeros_like(b)
+        info = qll.SolveInfo()
+        its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, 1e-20, 5000,
+                                  qll.SOLVE_MIXED_SINGLE, byref(info))
+        assert its > 0, qll.last_error()
+        assert info.reliable_updates > 1
+        res[ru_df] = (x, its, info.true_rsq[0])
+    L.qllg_set_param(b"ru_df", 1)
+    its_o, xo, _ = orc.wilson_cgnr(DIMS, u, mass, b, 1e-20, 5000)
+    for ru_df in (1, 0):
+        x, its, tr = res[ru_df]
+        assert tr < 1e-16, (ru_df, tr)
+        assert relerr(x[:Vh], xo[:Vh]) < 1e-7, ru_df
+    assert abs(res[1][1] - res[0][1]) <= 2, (res[1][1], res[0][1])
+    assert relerr(res[1][0][:Vh], res[0][0][:Vh]) < 1e-7
+    L.qllg_wilson_destroy(ctypes.c_void_p(W))
+
+
 def test_single_stored_operator_matches_double_stored():
     """qllg_stag_create_asqtad_fb holds the 8 forward slots only and makes
     the backward links in the kernels: the Dslash (every precision and rhs
