@@ -140,6 +140,8 @@ __device__ __forceinline__ Cx<T> comp_load(const void *b, size_t stride, size_t 
   Cx<T> z;
   if constexpr (P == QLLG_F64) {
     const double2 t = __ldg((const double2 *)b + c*stride + idx); z.r = (T)t.x; z.i = (T)t.y;
+  } else if constexpr (P == QLLG_DF) {
+    const float4 t = __ldg((const float4 *)b + c*stride + idx); z.r = dfl(t.x, t.y); z.i = dfl(t.z, t.w);
   } else {
     const float2 t = __ldg((const float2 *)b + c*stride + idx); z.r = (T)t.x; z.i = (T)t.y;
   }
@@ -149,6 +151,7 @@ template <int P, typename T>
 __device__ __forceinline__ void comp_store(void *b, size_t stride, size_t idx, int c, const Cx<T> &z)
 {
   if constexpr (P == QLLG_F64) ((double2 *)b)[c*stride + idx] = make_double2((double)z.r, (double)z.i);
+  else if constexpr (P == QLLG_DF) ((float4 *)b)[c*stride + idx] = make_float4(z.r.h, z.r.l, z.i.h, z.i.l);
   else ((float2 *)b)[c*stride + idx] = make_float2((float)z.r, (float)z.i);
 }
 
@@ -171,7 +174,7 @@ wilson_dslash_c3(qllg_stag_args a)
   const size_t loff = p ? (size_t)G.Vh : 0;
   const bool skip = a.done && *(volatile const int *)a.done;
   Acc<T> acc0, acc1;
-  const bool act = !a.active || a.active[0];
+  const bool act = !a.active || (a.active[0] && (!a.active_eq || a.active[0] == a.active_eq));
   const T ca = (T)(a.a ? a.a[0] : a.a0);
   const T cb = (T)a.b;
   if(!skip && act) {
@@ -236,7 +239,7 @@ wilson_dslash_c3(qllg_stag_args a)
       for(int sp=0; sp<4; sp++) {
         if(a.mode == 2) {
           T sr = a.self ? ca*self[sp].r : (T)0, si = a.self ? ca*self[sp].i : (T)0;
-          out[sp].r = fma(cb, acc[sp].r, sr); out[sp].i = fma(cb, acc[sp].i, si);
+          out[sp].r = kfma(cb, acc[sp].r, sr); out[sp].i = kfma(cb, acc[sp].i, si);
         } else out[sp] = acc[sp];
         comp_store<PS,T>(a.out, total, site, 3*sp + j, out[sp]);
       }
@@ -275,10 +278,12 @@ int launch_c3(const qllg_stag_args *a)
 template <int PS, int PL, int NR>
 int launch_t(const qllg_stag_args *a)
 {
-  // FP32, one rhs, fewer sites than half the GPU's resident threads: three
-  // threads per site
-  if constexpr (NR == 1 && PS == QLLG_F32) {
-    if(qllg_get_param("wilson_c3") != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
+  // one rhs, fewer sites than half the GPU's resident threads: three
+  // threads per site (FP32 on request; double-float by default, whose
+  // one-thread kernel holds one block of 256 threads per SM)
+  if constexpr (NR == 1 && (PS == QLLG_F32 || PS == QLLG_DF)) {
+    const char *knob = PS == QLLG_DF ? "wilson_df_c3" : "wilson_c3";
+    if(qllg_get_param(knob) != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
       return launch_c3<PS,PL>(a);
   }
   static int bps = 0;

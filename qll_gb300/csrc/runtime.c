@@ -295,6 +295,9 @@ static struct { const char *name; double value; } g_params[] = {
                                 per site, one per output colour (C2 at 16^3x32:
                                 17.8 ms per mixed solve against 14.7 ms with one
                                 thread per site, so off) */
+  {"wilson_df_c3", 1},       /* the same for the double-float Wilson launches of
+                                the CGNR's reliable updates, whose one-thread
+                                kernel holds one block of 256 threads per SM */
   {"dslash_split", 1},       /* multi-rhs Dslash: a slot loop without the active
                                 checks for launches with every rhs active */
   {"dslash_variant", -1},    /* force a Dslash variant (0-14, qllg_autotune_report names

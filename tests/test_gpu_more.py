@@ -321,9 +321,10 @@ def test_wilson_cgnr_matches_oracle(mode):
 
 def test_wilson_double_float_reliable_updates():
     """the mixed CGNR with its intermediate reliable updates in double-float
-    (ru_df 1, the Wilson kernel on (hi, lo) float pairs) and in FP64 (0):
-    both reach the FP64 true residual in about the same iterations, with
-    solutions that agree with each other and with the oracle's CGNR"""
+    (ru_df 1, the Wilson kernel on (hi, lo) float pairs, with three threads
+    or one thread per site) and in FP64 (ru_df 0): each reaches the FP64
+    true residual in about the same iterations, with solutions that agree
+    with each other and with the oracle's CGNR"""
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
     L.qllg_wilson_create.restype = ctypes.c_void_p
@@ -338,23 +339,24 @@ def test_wilson_double_float_reliable_updates():
     Vh = b.shape[0]//2
     mass = 1/(2*0.12) - 4
     res = {}
-    for ru_df in (1, 0):
+    for ru_df, c3 in ((1, 1), (1, 0), (0, 1)):
         L.qllg_set_param(b"ru_df", ru_df)
+        L.qllg_set_param(b"wilson_df_c3", c3)
         x = np.zeros_like(b)
         info = qll.SolveInfo()
         its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, 1e-20, 5000,
                                   qll.SOLVE_MIXED_SINGLE, byref(info))
         assert its > 0, qll.last_error()
         assert info.reliable_updates > 1
-        res[ru_df] = (x, its, info.true_rsq[0])
+        res[ru_df, c3] = (x, its, info.true_rsq[0])
     L.qllg_set_param(b"ru_df", 1)
+    L.qllg_set_param(b"wilson_df_c3", 1)
     its_o, xo, _ = orc.wilson_cgnr(DIMS, u, mass, b, 1e-20, 5000)
-    for ru_df in (1, 0):
-        x, its, tr = res[ru_df]
-        assert tr < 1e-16, (ru_df, tr)
-        assert relerr(x[:Vh], xo[:Vh]) < 1e-7, ru_df
-    assert abs(res[1][1] - res[0][1]) <= 2, (res[1][1], res[0][1])
-    assert relerr(res[1][0][:Vh], res[0][0][:Vh]) < 1e-7
+    for key, (x, its, tr) in res.items():
+        assert tr < 1e-16, (key, tr)
+        assert relerr(x[:Vh], xo[:Vh]) < 1e-7, key
+        assert abs(its - res[0, 1][1]) <= 2, (key, its, res[0, 1][1])
+        assert relerr(x[:Vh], res[0, 1][0][:Vh]) < 1e-7, key
     L.qllg_wilson_destroy(ctypes.c_void_p(W))
 
 
