@@ -419,7 +419,7 @@ def wilson_links_host(dims, seed, eps, c=0.5):
 
 
 def run_wilson(args):
-    """C2: Wilson even-odd CGNR at 16^3x32, eps=0.3, kappa=0.12 (QLL mass
+    """C2: Wilson even-odd CGNR at 16^3x32 (--wilson-dims for another lattice), eps=0.3, kappa=0.12 (QLL mass
     1/(2 kappa) - 4), Gaussian 4x3 source, tolerance 1e-8: FP32 iterations
     with FP64 reliable updates against the plain FP64 CG"""
     from qll_gb300 import qll
@@ -431,7 +431,7 @@ def run_wilson(args):
                                     ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_void_p]
     L.qllg_wilson_destroy.argtypes = [ctypes.c_void_p]
-    dims, kappa = (16, 16, 16, 32), 0.12
+    dims, kappa = tuple(int(v) for v in args.wilson_dims.split(",")), 0.12
     mass = 1/(2*kappa) - 4
     u = wilson_links_host(dims, 1002, 0.3)
     W = ctypes.c_void_p(L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(u)))
@@ -439,8 +439,8 @@ def run_wilson(args):
         raise RuntimeError(qll.last_error())
     b = qll.gen_source(dims, 2200, 24, "even")
     Vh = b.shape[0]//2
-    out = {"workload": "C2: Wilson e/o CGNR 16^3x32, eps=0.3, kappa=0.12, true residual 1e-8 "
-                       "(normal-equation rsq 1e-17)"}
+    out = {"workload": "C2: Wilson e/o CGNR %s, eps=0.3, kappa=0.12, true residual 1e-8 "
+                       "(normal-equation rsq 1e-17)" % "x".join(map(str, dims))}
     for name, mode in (("mixed", qll.SOLVE_MIXED_SINGLE), ("fp64", qll.SOLVE_DOUBLE)):
         best = None
         for rep in range(2):
@@ -901,6 +901,7 @@ def main():
                     help="skip the Wilson, multishift and serving legs")
     ap.add_argument("--multishift", action="store_true", help="only the multishift benchmark")
     ap.add_argument("--wilson", action="store_true", help="only the Wilson benchmark")
+    ap.add_argument("--wilson-dims", default="16,16,16,32", help="lattice of the Wilson benchmark")
     ap.add_argument("--serve-requests", type=int, default=36)
     ap.add_argument("--serve-budget", type=float, default=48.0, help="GiB")
     ap.add_argument("--serve-chunk", type=int, default=20)
