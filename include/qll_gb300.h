@@ -261,8 +261,7 @@ void qllg_server_destroy(qllg_server *V);
  *  "reortho" (1), "graph" (1: the solver loop as one CUDA-graph launch),
  *    "poll" (8: first batch of host-polled iterations);
  *  "ru_compact" (1: reliable updates over the flagged rhs only), "ru_df" (1:
- *    intermediate reliable updates in double-float, final ones in FP64; the
- *    staggered mixed CG and the Wilson mixed CGNR),
+ *    intermediate reliable updates in double-float, final ones in FP64),
  *    "df_blocks" (3: register cap of the double-float kernel);
  *  "dslash_mr" (1: multi-rhs Dslash kernels), "dslash_vec4" (1: 16-byte
  *    loads of rhs pairs), "dslash_split" (1: a slot loop without the active
@@ -278,8 +277,10 @@ void qllg_server_destroy(qllg_server *V);
  *    FP64 CG);
  *  "multishift_guess_rsq" (1e-10: the mixed multishift's first stage
  *    stops at |r|^2 < this |b|^2), "wilson_c3" (0; 1: three threads per site
- *    in small one-rhs FP32 Wilson launches), "wilson_df_c3" (1: the same in
- *    the double-float Wilson launches of the CGNR's reliable updates).
+ *    in small one-rhs FP32 Wilson launches), "wilson_ru_df" (0; 1: the
+ *    Wilson mixed CGNR's intermediate reliable updates in double-float),
+ *    "wilson_df_c3" (1: three threads per site in the small double-float
+ *    Wilson launches).
  * Returns -1 for an unknown name. */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);

@@ -295,9 +295,14 @@ static struct { const char *name; double value; } g_params[] = {
                                 per site, one per output colour (C2 at 16^3x32:
                                 17.8 ms per mixed solve against 14.7 ms with one
                                 thread per site, so off) */
-  {"wilson_df_c3", 1},       /* the same for the double-float Wilson launches of
-                                the CGNR's reliable updates, whose one-thread
-                                kernel holds one block of 256 threads per SM */
+  {"wilson_ru_df", 0},       /* intermediate reliable updates of the Wilson mixed
+                                CGNR in double-float.  Off: the double-float
+                                Wilson kernel is about as slow as the FP64 one,
+                                and its extra launches cost more (C2 15.1 against
+                                14.8 ms per solve, 32^3x64 139 against 128 ms) */
+  {"wilson_df_c3", 1},       /* three threads per site in the small double-float
+                                Wilson launches, whose one-thread kernel holds one
+                                block of 256 threads per SM */
   {"dslash_split", 1},       /* multi-rhs Dslash: a slot loop without the active
                                 checks for launches with every rhs active */
   {"dslash_variant", -1},    /* force a Dslash variant (0-14, qllg_autotune_report names

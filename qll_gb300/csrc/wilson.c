@@ -311,11 +311,11 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   void *r = wws(W, WW_R, vs), *p = wws(W, WW_P, vs), *Ap = wws(W, WW_AP, vs);
   void *Sp = wws(W, WW_S, vs), *v = wws(W, WW_V, vs);
   if(!xs || !r || !p || !Ap || !Sp || !v) return -1;
-  /* intermediate reliable updates (ru 1) in double-float: S^+ S x in the
-   * FP32 pipes at about 44-bit precision; the final one (ru 2), whose
-   * residual may end the solve, in FP64 */
+  /* on request, intermediate reliable updates (ru 1) in double-float:
+   * S^+ S x in the FP32 pipes at about 44-bit precision; the final one
+   * (ru 2), whose residual may end the solve, in FP64 */
   void *xdf = NULL;
-  if(ps != QLLG_F64 && qllg_get_param("ru_df") != 0 &&
+  if(ps != QLLG_F64 && qllg_get_param("wilson_ru_df") != 0 &&
      (wlinks(W, QLLG_DF) || !(xdf = wws(W, WW_XDF, wvec(W, QLLG_DF))))) return -1;
   memset(W->hsc, 0, sizeof(qllg_cg_scalars));
   W->hsc->rsq_stop[0] = rsq;

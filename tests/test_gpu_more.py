@@ -321,8 +321,8 @@ def test_wilson_cgnr_matches_oracle(mode):
 
 def test_wilson_double_float_reliable_updates():
     """the mixed CGNR with its intermediate reliable updates in double-float
-    (ru_df 1, the Wilson kernel on (hi, lo) float pairs, with three threads
-    or one thread per site) and in FP64 (ru_df 0): each reaches the FP64
+    (wilson_ru_df 1, the Wilson kernel on (hi, lo) float pairs, with three
+    threads or one thread per site) and in FP64 (0): each reaches the FP64
     true residual in about the same iterations, with solutions that agree
     with each other and with the oracle's CGNR"""
     L = qll.load()
@@ -340,7 +340,7 @@ def test_wilson_double_float_reliable_updates():
     mass = 1/(2*0.12) - 4
     res = {}
     for ru_df, c3 in ((1, 1), (1, 0), (0, 1)):
-        L.qllg_set_param(b"ru_df", ru_df)
+        L.qllg_set_param(b"wilson_ru_df", ru_df)
         L.qllg_set_param(b"wilson_df_c3", c3)
         x = np.zeros_like(b)
         info = qll.SolveInfo()
@@ -349,7 +349,7 @@ def test_wilson_double_float_reliable_updates():
         assert its > 0, qll.last_error()
         assert info.reliable_updates > 1
         res[ru_df, c3] = (x, its, info.true_rsq[0])
-    L.qllg_set_param(b"ru_df", 1)
+    L.qllg_set_param(b"wilson_ru_df", 0)
     L.qllg_set_param(b"wilson_df_c3", 1)
     its_o, xo, _ = orc.wilson_cgnr(DIMS, u, mass, b, 1e-20, 5000)
     for key, (x, its, tr) in res.items():
