@@ -256,8 +256,8 @@ void qllg_server_destroy(qllg_server *V);
 
 /* solver parameters (name, default):
  *  "reliable_delta" (0.1, 16-bit mixed mode),
- *  "reliable_delta_single" (0.01, FP32 mixed mode): a reliable update when
- *    |r| falls by this factor;
+ *  "reliable_delta_single" (0.01, FP32 mixed mode, staggered CG and Wilson
+ *    CGNR): a reliable update when |r| falls by this factor;
  *  "reortho" (1), "graph" (1: the solver loop as one CUDA-graph launch),
  *    "poll" (8: first batch of host-polled iterations);
  *  "ru_compact" (1: reliable updates over the flagged rhs only), "ru_df" (1:

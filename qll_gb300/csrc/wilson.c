@@ -320,7 +320,8 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   memset(W->hsc, 0, sizeof(qllg_cg_scalars));
   W->hsc->rsq_stop[0] = rsq;
   W->hsc->maxits = maxits;
-  W->hsc->delta2 = (ps == QLLG_F64) ? 0 : 0.01;
+  const double delta = qllg_get_param("reliable_delta_single");
+  W->hsc->delta2 = (ps == QLLG_F64) ? 0 : delta*delta;
   if(wpush(W)) return -1;
   qllg_cg_scalars *sc = W->sc;
   if(qllg_k_scg_init(ps, ps, xs, r, p, bp, ps == QLLG_F64 ? NULL : x64,
