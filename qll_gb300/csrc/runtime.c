@@ -272,7 +272,10 @@ static struct { const char *name; double value; } g_params[] = {
                                       sloppy iterations keep the CG recurrence
                                       over two decades (measured: 455
                                       iterations at 32^3x64, m=0.01, for 0.1
-                                      and 0.01; 464 at 0.003, 623 at 0.001) */
+                                      and 0.01; 464 at 0.003, 623 at 0.001;
+                                      Wilson CGNR at 16^3x32: 52 iterations
+                                      for both, 13.0 ms per solve at 0.01
+                                      against 14.8 ms at 0.1) */
   {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
   {"graph", 1},              /* run solver iterations as one CUDA graph launch */
   {"poll", 8},               /* first batch of iterations between host checks */
@@ -298,8 +301,9 @@ static struct { const char *name; double value; } g_params[] = {
   {"wilson_ru_df", 0},       /* intermediate reliable updates of the Wilson mixed
                                 CGNR in double-float.  Off: the double-float
                                 Wilson kernel is about as slow as the FP64 one,
-                                and its extra launches cost more (C2 15.1 against
-                                14.8 ms per solve, 32^3x64 139 against 128 ms) */
+                                and its extra launches cost more (updates at each
+                                10x fall of |r|: C2 15.1 against 14.8 ms per
+                                solve, 32^3x64 139 against 128 ms) */
   {"wilson_df_c3", 1},       /* three threads per site in the small double-float
                                 Wilson launches, whose one-thread kernel holds one
                                 block of 256 threads per SM */
