@@ -151,11 +151,17 @@ int qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, vo
  * allocate: a serving loop holding a fixed HBM budget for admitted solves,
  * or one whose concurrent streams a device-synchronising cudaMalloc/cudaFree
  * would stall.  Limits: nrhs in {1,2,4,8,16}; anything else, or links of
- * prec missing, returns -1 with qllg_last_error() saying why.  The first
- * call on each device looks up the scratch's address (cudaGetSymbolAddress
- * with that device current): make it before any stream capture.  The
- * scratch is one per device, so calls that overlap in time (other host
- * threads, other streams) race: serialise them. */
+ * prec missing, returns -1 with qllg_last_error() saying why.  The set-up
+ * happens when the operator's links of precision prec are made (at create
+ * time for the precision the operator was created in, else at the first
+ * call that derives them, e.g. one qllg_stag_dslash_device of that
+ * precision): the scratch's address is looked up (cudaGetSymbolAddress with
+ * that device current) and every kernel the call can launch is loaded, so
+ * that CUDA's lazy module loading allocates nothing during the call itself.
+ * The address is kept for the life of the process; do not use the library
+ * across a cudaDeviceReset.  The scratch is one per device, so calls that
+ * overlap in time (other host threads, other streams) race: serialise
+ * them. */
 int qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
                                    void *out_dev, const void *in_dev, double *norm2_dev);
 size_t qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs);
@@ -297,6 +303,9 @@ int qllg_autotune_report(char *buf, size_t len);
 void qllg_timing_enable(int on);
 /* number of kernels the library has launched since load */
 unsigned long long qllg_launch_count(void);
+/* number of device allocations (cudaMalloc) the library has made since
+ * load */
+unsigned long long qllg_device_alloc_count(void);
 void qllg_timing_reset(void);
 int qllg_timing_read(const char *name, int *count, double *ms);
 

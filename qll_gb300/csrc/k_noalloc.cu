@@ -7,8 +7,14 @@
 // work, and a library allocation would either exceed that budget or fail in
 // the middle of serving; and cudaMalloc/cudaFree may synchronise the whole
 // device, which would stall the other streams' solves that such a loop keeps
-// in flight.  Those callers need a call whose device footprint is fixed when
-// the library is loaded.
+// in flight.  Those callers need a call that adds nothing to the device
+// footprint once the operator is set up.
+//
+// CUDA loads modules lazily by default: the first cudaGetSymbolAddress of
+// the scratch loads it (262,400 B), and a kernel's first launch loads its
+// code.  Both happen when an operator's links of a precision are made
+// (noalloc_preload in stag.c), an allocating step anyway, so the
+// no-allocation call itself only finds them there.
 //
 // The scratch is the block-partial array and last-block counter of the
 // deterministic grid reduction (grid_reduce / grid_reduce_mr): partial
@@ -30,7 +36,9 @@
 static __device__ __align__(256) unsigned char noalloc_scratch[NOALLOC_PARTIAL_BYTES + 256];
 
 // device address of the scratch, looked up once per device with that
-// device current (the first call made while it is current does it)
+// device current (at the first link set-up on it).  Kept for the life of
+// the process: after cudaDeviceReset the module is reloaded and the
+// address may move, so the library must not be used across a device reset.
 static void *g_scratch_base[NOALLOC_MAXDEV];
 
 extern "C" int

@@ -631,6 +631,7 @@ int launch_compact(const qllg_stag_args *a)
          &blocks_per_sm, stag_dslash_compact<PS,PL,NS,NR,MINB>, kThreads, 0), "occupancy")) return -1;
     if(blocks_per_sm < 1) blocks_per_sm = 1;
   }
+  if(a->preload) return 0;
   // sized for one flagged rhs: with more, the grid-stride loop takes them
   size_t need = ((size_t)a->g.Vh + kThreads - 1)/kThreads;
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
@@ -663,11 +664,17 @@ int launch_mr(const qllg_stag_args *a)
     else { (void)vec; return stag_dslash_mr<PS,PL,NS,NR,R,true,CFG>; }
   };
   static int blocks_per_sm[2] = {0, 0};
-  if(!blocks_per_sm[v4]) {
-    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm[v4], kern(v4), TB, 0), "occupancy")) return -1;
-    if(blocks_per_sm[v4] < 1) blocks_per_sm[v4] = 1;
+  for(int k=0; k<2; k++) {
+    // a preload loads both access widths of CFG 0
+    const bool vk = a->preload ? (CFG != 0 || k == 1) : v4;
+    if(!a->preload && k) break;
+    if(!blocks_per_sm[vk]) {
+      if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+           &blocks_per_sm[vk], kern(vk), TB, 0), "occupancy")) return -1;
+      if(blocks_per_sm[vk] < 1) blocks_per_sm[vk] = 1;
+    }
   }
+  if(a->preload) return 0;
   size_t work = (size_t)a->g.Vh * (NR/R);
   size_t need = (work + TB - 1)/TB;
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm[v4];
@@ -691,6 +698,7 @@ int launch_plain(const qllg_stag_args *a)
          &blocks_per_sm, stag_dslash<PS,PL,NS,NR>, kThreads, 0), "occupancy")) return -1;
     if(blocks_per_sm < 1) blocks_per_sm = 1;
   }
+  if(a->preload) return 0;
   size_t total = (size_t)a->g.Vh * NR;
   size_t need = (total + kThreads - 1)/kThreads;
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
@@ -991,6 +999,7 @@ int launch_tile(const qllg_stag_args *a)
          &blocks_per_sm, stag_dslash_tile<NR_>, kThreads, kTileSmem), "occupancy")) return -1;
     if(blocks_per_sm < 1) blocks_per_sm = 1;
   }
+  if(a->preload) return 0;
   size_t ntiles = (size_t)a->g.Vh/kTileSites;
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
@@ -1165,6 +1174,11 @@ int tuned_variant(const qllg_stag_args *a)
 template <int PS, int PL, int NS, int NR>
 int launch_t(const qllg_stag_args *a)
 {
+  if(a->preload) {
+    // every launch shape the dispatch can reach for this rhs count
+    for(int v=0; v<kNumVariants; v++) if(launch_variant<PS,PL,NS,NR>(a, v)) return -1;
+    return launch_compact<PS,PL,NS,NR>(a);
+  }
   if(a->compact) return launch_compact<PS,PL,NS,NR>(a);
   int v = tuned_variant<PS,PL,NS,NR>(a);
   if(v < 0) return -1;
@@ -1174,6 +1188,9 @@ int launch_t(const qllg_stag_args *a)
 template <int PS, int PL, int NS>
 int launch_nr(const qllg_stag_args *a)
 {
+  if(a->preload)
+    return launch_t<PS,PL,NS,1>(a) || launch_t<PS,PL,NS,2>(a) || launch_t<PS,PL,NS,4>(a) ||
+           launch_t<PS,PL,NS,8>(a) || launch_t<PS,PL,NS,16>(a) ? -1 : 0;
   switch(a->nrhs) {
   case 1: return launch_t<PS,PL,NS,1>(a);
   case 2: return launch_t<PS,PL,NS,2>(a);

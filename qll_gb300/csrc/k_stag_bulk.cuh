@@ -324,6 +324,7 @@ int launch_bulk(const qllg_stag_args *a)
          &blocks_per_sm, stag_dslash_bulk<NR_>, kBkThreads, kBkSmem), "occupancy")) return -1;
     if(blocks_per_sm < 1) blocks_per_sm = 1;
   }
+  if(a->preload) return 0;
   size_t ntiles = (size_t)a->g.Vh/kBkSites;
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;

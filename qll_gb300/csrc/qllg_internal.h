@@ -166,6 +166,10 @@ typedef struct {
   int one_path;          /* multi-rhs Dslash: always the slot loop with the
                             active checks (one code path) */
   int no_tune;           /* caller must not allocate: no autotuning */
+  int preload;           /* load every launch shape's kernel of these
+                            precisions and slot count (each launcher's
+                            occupancy query loads its kernel) and launch
+                            nothing; nrhs and the pointers are ignored */
   int fb;                /* single-stored links: forward slots only, [nslots/2][9][V];
                             backward links made from them in the kernel */
   int dag;               /* Wilson only: gamma5 D gamma5 (projector signs flipped) */

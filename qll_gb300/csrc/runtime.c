@@ -169,12 +169,23 @@ qllg_get_stream(void)
   return (void *)g_stream;
 }
 
+/* device allocations made through qllg_dmalloc since load (every device
+ * allocation of the library goes through it) */
+static unsigned long long g_dallocs = 0;
+
+unsigned long long
+qllg_device_alloc_count(void)
+{
+  return g_dallocs;
+}
+
 void *
 qllg_dmalloc(size_t bytes)
 {
   if(qllg_runtime_init()) return NULL;
   void *p = NULL;
   if(bytes == 0) bytes = 16;
+  g_dallocs++;
   cudaError_t e = cudaMalloc(&p, bytes);
   if(e != cudaSuccess) {
     qllg_set_error("cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));

@@ -163,10 +163,46 @@ f32_links(qllg_stag *S)
   return QLLG_F32;
 }
 
+static int ensure_links_make(qllg_stag *S, int prec);
+
+/* Links of precision prec (FP64, FP32 or 16-bit) now exist for S, so
+ * qllg_stag_dslash_norm2_noalloc can take S at that precision.  That call
+ * must not allocate device memory, but with CUDA's lazy module loading
+ * (the default) the first launch of a kernel loads its code into device
+ * memory, and the first look-up of the fixed scratch loads the scratch.
+ * This, an allocating call anyway, does both ahead of it: it resolves the
+ * scratch's address on the current device and loads every Dslash kernel
+ * the no-allocation call can reach at this precision and slot count. */
+static int
+noalloc_preload(qllg_stag *S, int prec)
+{
+  if(prec < QLLG_F64 || prec > QLLG_I16 || !S->links[prec]) return 0;
+  qllg_redbuf rb;
+  if(qllg_noalloc_redbuf(&rb)) return -1;
+  qllg_stag_args A;
+  memset(&A, 0, sizeof(A));
+  A.g = S->g;
+  A.nrhs = 1;
+  A.nslots = S->nslots;
+  A.fb = S->fb;
+  A.links = S->links[prec];
+  A.rb = &rb;
+  A.preload = 1;
+  return qllg_k_stag_dslash(prec, prec, &A);
+}
+
 static int
 ensure_links(qllg_stag *S, int prec)
 {
   if(S->links[prec]) return 0;
+  int rc = ensure_links_make(S, prec);
+  if(!rc) rc = noalloc_preload(S, prec);
+  return rc;
+}
+
+static int
+ensure_links_make(qllg_stag *S, int prec)
+{
   if(prec == QLLG_F32R) {
     if(S->recon_bad) {
       qllg_set_error("reconstruct-12: Naik links are not real multiples of SU(3) matrices");
@@ -228,6 +264,7 @@ stag_create(const int dims[4], void *const fat[8], void *const lng[8], int dbl)
     }
     if(qllg_sync()) goto fail;
   }
+  if(noalloc_preload(S, S->master)) goto fail;
   return S;
 fail:
   qllg_stag_destroy(S);
@@ -266,7 +303,7 @@ qllg_stag_attach_links(qllg_stag *S, int prec, void *links)
 {
   if(S->links[prec]) qllg_dfree(S->links[prec]);
   S->links[prec] = links;
-  return 0;
+  return noalloc_preload(S, prec);
 }
 
 qllg_stag *
@@ -1209,9 +1246,9 @@ qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, void *
  * (deriving them allocates).  For callers with a fixed device-memory budget
  * (a serving loop that admits solves against HBM) or with other streams in
  * flight that a device-synchronising cudaMalloc/cudaFree would stall.
- * The first call on a device looks up the scratch's address; make it
- * before any stream capture.  Calls that overlap in time share the scratch
- * and race. */
+ * The scratch's address and the kernels the call launches were resolved
+ * and loaded when S's links of precision prec were made (noalloc_preload).
+ * Calls that overlap in time share the scratch and race. */
 int
 qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
                                void *out_dev, const void *in_dev, double *norm2_dev)

@@ -9,7 +9,9 @@ allocating call, so it must be bit-identical; the per-rhs norms must match
 1e-6 for FP32 spinors (each thread sums its squares in FP32 with Kahan
 compensation before the FP64 grid reduction) and to 2e-4 for the 16-bit
 layout (the kernel sums the values before they are rounded to 16 bits).  Two calls in a row are checked, so a counter or
-partial left over by the first call would show in the second.
+partial left over by the first call would show in the second.  Every call
+is also checked to allocate nothing: the library's count of device
+allocations stays put and the device's free memory does not drop.
 
 The file sorts last so it runs after every other test; it also passes
 alone in a fresh process."""
@@ -36,7 +38,22 @@ def _lib():
     L.qllg_stag_vec_bytes.argtypes = [VP, I, I]
     L.qllg_stag_dslash_device.argtypes = [VP, I, I, I, VP, VP]
     L.qllg_stag_dslash_norm2_noalloc.argtypes = [VP, I, I, I, VP, VP, VP]
+    L.qllg_device_alloc_count.restype = ctypes.c_ulonglong
     return L
+
+
+def _call_without_allocating(L, *args):
+    """one no-allocation call, checked to allocate nothing: the library's
+    own allocation count stays put, and so does the device's free memory
+    (which would drop if the call loaded a kernel or the scratch)"""
+    torch.cuda.synchronize()
+    n0 = L.qllg_device_alloc_count()
+    free0 = torch.cuda.mem_get_info()[0]
+    rc = L.qllg_stag_dslash_norm2_noalloc(*args)
+    torch.cuda.synchronize()
+    assert L.qllg_device_alloc_count() == n0, "the no-allocation call allocated device memory"
+    assert torch.cuda.mem_get_info()[0] >= free0, "device free memory dropped during the call"
+    return rc
 
 
 @pytest.fixture(scope="module")
@@ -97,9 +114,8 @@ def test_noalloc_matches_dslash_device(op, prec, nrhs):
         for call in range(2):
             out = torch.full_like(src, float("nan"))
             nrm = torch.full((nrhs,), float("nan"), dtype=torch.float64, device="cuda")
-            torch.cuda.synchronize()
-            rc = L.qllg_stag_dslash_norm2_noalloc(S, prec, nrhs, parity, VP(out.data_ptr()),
-                                                  VP(src.data_ptr()), VP(nrm.data_ptr()))
+            rc = _call_without_allocating(L, S, prec, nrhs, parity, VP(out.data_ptr()),
+                                          VP(src.data_ptr()), VP(nrm.data_ptr()))
             assert rc == 0, qll.last_error()
             torch.cuda.synchronize()
             assert torch.equal(out.view(torch.uint8), ref.view(torch.uint8)), \
@@ -129,10 +145,9 @@ def test_noalloc_with_the_grid_at_its_block_cap():
             for call in range(2):
                 out = torch.full_like(src, float("nan"))
                 nrm = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
-                torch.cuda.synchronize()
-                assert L.qllg_stag_dslash_norm2_noalloc(S, prec, 1, 1, VP(out.data_ptr()),
-                                                        VP(src.data_ptr()),
-                                                        VP(nrm.data_ptr())) == 0, qll.last_error()
+                assert _call_without_allocating(L, S, prec, 1, 1, VP(out.data_ptr()),
+                                                VP(src.data_ptr()),
+                                                VP(nrm.data_ptr())) == 0, qll.last_error()
                 torch.cuda.synchronize()
                 assert torch.equal(out.view(torch.uint8), ref.view(torch.uint8))
                 assert abs(nrm.item() - want.item())/want.item() < (1e-12 if prec == 0 else 1e-6)
