@@ -1,8 +1,12 @@
 /*
  * qll.h -- QLL's public C API served by libqll_gb300 (drop-in for the
  * reference's include/qll.h:1-58).  Code written against the reference
- * includes this header instead and links -lqll_gb300.
- * Every symbol exists in a ..F (float) and a ..D (double) variant.
+ * includes this header instead and links -lqll_gb300 (and the CUDA
+ * runtime, -lcudart); it needs no QMP.  Every symbol exists in a ..F
+ * (float) and a ..D (double) variant.  Differences from the reference:
+ * links live on the GPU (copied at create time), errors return a failure
+ * value with the message in qllg_last_error() instead of calling exit(),
+ * and the geometry is one process's whole lattice (no QMP ranks).
  */
 #ifndef QLLG_QLL_H
 #define QLLG_QLL_H

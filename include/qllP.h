@@ -4,8 +4,8 @@
  * include/qllP.h:1-110, plus the entry points that the reference declares
  * in its internal include/common.h:50-60 and defines in lib/stagDslash.c).
  *
- * Semantics that differ from the reference are stated per function; the
- * full list is in INTEGRATION.md.  Common to all: arrays are host arrays in
+ * Semantics that differ from the reference are stated per function.
+ * Common to all: arrays are host arrays in
  * the one-lane layout of layout.h; links are copied to GPU memory when the
  * link or solver object is created (the reference keeps the caller's
  * pointers and re-reads them on every call, lib/stagDslash.c:441-447), so a

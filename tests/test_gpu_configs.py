@@ -1,0 +1,247 @@
+"""GPU parity at the benchmarked configurations themselves, not only on
+small test lattices: the inputs are exactly the ones the benchmark legs
+solve (same lattices, eps, masses, gauge and source seeds), the GPU builds
+its own fat7 links from the thin links as in production, and the CPU oracle
+builds its own from the same thin links.
+
+  C1  8^4, eps 0.3, m 0.1, FP64 and mixed CG to true residual 1e-8
+  C2  16^3x32 Wilson even-odd CGNR, kappa 0.12, FP64 and mixed
+  C3  24^3x48, m 0.02, 12 shifts log-spaced over 1e-4..1 (one rhs of the
+      mixed multi-rhs multishift against the oracle's solveMulti2)
+  C4  32^3x64, eps 0.4, m 0.01, the 16-rhs FP32-mixed block (one rhs
+      against the oracle's FP64 solve2); fat7 links and one half Dslash
+      checked directly
+
+Tolerances: fat7 links and FP64 Dslash 1e-12 relative, FP32 Dslash 1e-5;
+every solution reaches its FP64 true residual (|r|^2 < rsq |b|^2 measured
+by the library in FP64) and agrees with the oracle's FP64 solution within
+10x the solver tolerance (relative 1e-7 for tolerance 1e-8) unless stated.
+FP64 CG iteration counts equal the oracle's within 1.
+"""
+import ctypes
+from ctypes import POINTER, byref, c_double, c_float, c_int, c_void_p
+
+import numpy as np
+import pytest
+
+import oracle_lib as orc
+from inputs import relerr, wilson_links
+from qll_gb300 import qll
+
+pytestmark = pytest.mark.gpu
+
+MAXITS = 20000
+
+
+def _lib():
+    L = qll.load()
+    L.qllg_stag_create_asqtad.restype = c_void_p
+    L.qllg_stag_create_asqtad.argtypes = [POINTER(c_int), POINTER(c_void_p),
+                                          POINTER(qll.Fat7Coeffs)]
+    L.qllg_stag_get_links.argtypes = [c_void_p, POINTER(c_void_p)]
+    L.qllg_stag_solve.argtypes = [c_void_p, c_int, POINTER(c_void_p), POINTER(c_void_p),
+                                  POINTER(c_double), c_double, c_int, c_int,
+                                  POINTER(qll.SolveInfo)]
+    L.qllg_stag_destroy.argtypes = [c_void_p]
+    return L
+
+
+def _oracle_links(dims, thin):
+    """fat7 and Naik links by the oracle from the thin links, with the
+    negative-adjoint backward links: (u, u3) in createStaggeredLinks order"""
+    fl, ll = orc.smear_fat7(dims, thin, qll.asqtad_coeffs())
+    u, u3 = [None]*8, [None]*8
+    for mu in range(4):
+        u[2*mu] = fl[mu]
+        u[2*mu + 1] = orc.negadj_back(dims, fl[mu], mu, 1)
+        u3[2*mu] = ll[mu]
+        u3[2*mu + 1] = orc.negadj_back(dims, ll[mu], mu, 3)
+    return u, u3
+
+
+def _gpu_operator(L, dims, seed, eps):
+    thin = qll.gen_gauge(dims, seed, eps, ks=True)
+    S = L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(thin),
+                                  byref(qll.asqtad_coeffs()))
+    assert S, qll.last_error()
+    return c_void_p(S), thin
+
+
+def _gpu_links(L, S, dims):
+    """the operator's 16 FP64 link slots, slot 4mu+2b+naik"""
+    V = int(np.prod(dims))
+    links = [np.zeros((V, 18)) for _ in range(16)]
+    assert L.qllg_stag_get_links(S, qll.vp_array(links)) == 0, qll.last_error()
+    return links
+
+
+def _solve(L, S, xs, bs, masses, rsq, mode):
+    n = len(bs)
+    info = qll.SolveInfo()
+    its = L.qllg_stag_solve(S, n, qll.vp_array(xs), qll.vp_array(bs), (c_double*n)(*masses), rsq,
+                            MAXITS, mode, byref(info))
+    assert its > 0, qll.last_error()
+    return its, info
+
+
+def test_c1_8x8x8x8_fp64_and_mixed_cg():
+    dims, mass, rsq = (8, 8, 8, 8), 0.1, 1e-16
+    L = _lib()
+    S, thin = _gpu_operator(L, dims, 1001, 0.3)
+    try:
+        u, u3 = _oracle_links(dims, thin)
+        gl = _gpu_links(L, S, dims)
+        for mu in range(4):
+            assert relerr(gl[4*mu], u[2*mu]) < 1e-12          # fat forward
+            assert relerr(gl[4*mu + 1], u3[2*mu]) < 1e-12     # Naik forward
+            assert relerr(gl[4*mu + 2], u[2*mu + 1]) < 1e-12  # fat backward
+            assert relerr(gl[4*mu + 3], u3[2*mu + 1]) < 1e-12
+        b = qll.gen_source(dims, 2100, 6, "even")
+        its_o, xo, _ = orc.solve2(dims, u, u3, mass, b, rsq, MAXITS, noscale=1)
+        Vh = b.shape[0]//2
+        for mode in (qll.SOLVE_DOUBLE, qll.SOLVE_MIXED_SINGLE):
+            x = np.zeros_like(b)
+            its, info = _solve(L, S, [x], [b], [mass], rsq, mode)
+            assert info.true_rsq[0] < rsq*1.0001, (mode, info.true_rsq[0])
+            assert relerr(x[:Vh], xo[:Vh]) < 1e-7, mode
+            if mode == qll.SOLVE_DOUBLE:
+                assert abs(its - its_o) <= 1, (its, its_o)
+    finally:
+        L.qllg_stag_destroy(S)
+
+
+@pytest.mark.parametrize("mode", [qll.SOLVE_DOUBLE, qll.SOLVE_MIXED_SINGLE])
+def test_c2_16x16x16x32_wilson_cgnr(mode):
+    """the Wilson e/o CGNR as the benchmark runs it: kappa 0.12 (QLL mass
+    1/(2 kappa) - 4), links c U with c = 1/2, normal-equation tolerance
+    1e-17 (true residual |b - S x|/|b| below 1e-8)"""
+    dims, kappa, rsq = (16, 16, 16, 32), 0.12, 1e-17
+    mass = 1/(2*kappa) - 4
+    L = qll.load()
+    L.qllg_wilson_create.restype = c_void_p
+    L.qllg_wilson_create.argtypes = [POINTER(c_int), POINTER(c_void_p)]
+    L.qllg_wilson_solve.restype = c_int
+    L.qllg_wilson_solve.argtypes = [c_void_p, c_void_p, c_void_p, c_double, c_double, c_int,
+                                    c_int, POINTER(qll.SolveInfo)]
+    u = list(wilson_links(dims, seed=1002, eps=0.3))
+    W = L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(u))
+    assert W, qll.last_error()
+    try:
+        b = qll.gen_source(dims, 2200, 24, "even")
+        x = np.zeros_like(b)
+        info = qll.SolveInfo()
+        its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, rsq, MAXITS, mode,
+                                  byref(info))
+        assert its > 0, qll.last_error()
+        its_o, xo, _ = orc.wilson_cgnr(dims, u, mass, b, rsq, MAXITS)
+        Vh = b.shape[0]//2
+        # the library's true residual is |b - S x|^2/|b|^2 in FP64
+        assert info.true_rsq[0] < 1e-16, info.true_rsq[0]
+        assert relerr(x[:Vh], xo[:Vh]) < 1e-7
+        if mode == qll.SOLVE_DOUBLE:
+            assert abs(its - its_o) <= 2, (its, its_o)
+    finally:
+        L.qllg_wilson_destroy(c_void_p(W))
+
+
+def test_c3_24x24x24x48_mixed_multishift():
+    """one rhs of the benchmark's mixed multishift solve (the first of its
+    8 sources) against the oracle's solveMulti2 on the oracle's links"""
+    dims, mass, rsq = (24, 24, 24, 48), 0.02, 1e-16
+    shifts = [10**(-4 + 4*k/11) for k in range(12)]
+    ns = len(shifts)
+    L = _lib()
+    L.qllg_stag_solve_multishift.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_double,
+                                             c_int, c_void_p, c_double, c_int, c_int, c_void_p,
+                                             c_void_p]
+    S, thin = _gpu_operator(L, dims, 1003, 0.3)
+    try:
+        b = qll.gen_source(dims, 2300, 6, "even")
+        xs = [np.zeros_like(b) for _ in range(ns)]
+        its = (c_int*ns)()
+        tr = (c_double*ns)()
+        rc = L.qllg_stag_solve_multishift(S, 1, qll.vp_array(xs), qll.vp_array([b]), mass, ns,
+                                          (c_double*ns)(*shifts), rsq, MAXITS,
+                                          qll.SOLVE_MIXED_SINGLE, its, tr)
+        assert rc > 0, qll.last_error()
+        u, u3 = _oracle_links(dims, thin)
+        _, xo = orc.solve_multi2(dims, u, u3, [np.sqrt(mass**2 + s) for s in shifts], b, rsq,
+                                 MAXITS, noscale=1)
+        Vh = b.shape[0]//2
+        for k in range(ns):
+            assert tr[k] < rsq*1.0001, (k, tr[k])
+            # the oracle's cgms stops on the base (smallest) shift's residual
+            # only; its larger shifts are solved more accurately than 1e-8
+            assert relerr(xs[k][:Vh], xo[k][:Vh]) < 1e-7, (k, relerr(xs[k][:Vh], xo[k][:Vh]))
+    finally:
+        L.qllg_stag_destroy(S)
+
+
+@pytest.fixture(scope="module")
+def c4():
+    """the headline lattice: 32^3x64, eps 0.4, gauge seed 1004; the GPU
+    operator (fat7 on the GPU) and the oracle's links from the same thin
+    links"""
+    dims = (32, 32, 32, 64)
+    L = _lib()
+    S, thin = _gpu_operator(L, dims, 1004, 0.4)
+    u, u3 = _oracle_links(dims, thin)
+    del thin
+    yield L, S, dims, u, u3
+    L.qllg_stag_destroy(S)
+
+
+def test_c4_32x32x32x64_fat7_links(c4):
+    L, S, dims, u, u3 = c4
+    gl = _gpu_links(L, S, dims)
+    for mu in range(4):
+        for slot, ref in ((4*mu, u[2*mu]), (4*mu + 1, u3[2*mu]), (4*mu + 2, u[2*mu + 1]),
+                          (4*mu + 3, u3[2*mu + 1])):
+            assert relerr(gl[slot], ref) < 1e-12, (slot, relerr(gl[slot], ref))
+
+
+@pytest.mark.parametrize("prec", ["D", "F"])
+def test_c4_32x32x32x64_dslash2(c4, prec):
+    """dslash2 through the drop-in API on the oracle's links, odd output
+    sites (the half Dslash of the solver) and all sites with the mass term:
+    FP64 within 1e-12 of the oracle, FP32 within 1e-5"""
+    L, S, dims, u, u3 = c4
+    dt, ct = (np.float64, c_double) if prec == "D" else (np.float32, c_float)
+    uu = [np.ascontiguousarray(a, dtype=dt) for a in u]
+    uu3 = [np.ascontiguousarray(a, dtype=dt) for a in u3]
+    lay = qll.setup_layout(dims, prec)
+    St = qll.D if prec == "D" else qll.F
+    y = qll.gen_source(dims, 2401, 6, "all").astype(dt)
+    Vh = y.shape[0]//2
+    for sub, mass in (("odd", 0.0), ("all", 0.01)):
+        sl = St["StaggeredLinks"]()
+        getattr(L, "createStaggeredLinks" + prec)(byref(sl), byref(lay), qll.ptr_array(uu, ct),
+                                                 qll.ptr_array(uu3, ct), sub.encode())
+        assert sl.t, qll.last_error()
+        try:
+            x = np.zeros_like(y)
+            getattr(L, "dslash2" + prec)(byref(sl), qll.ptr(x), ct(mass), qll.ptr(y))
+            assert not qll.last_error(), qll.last_error()
+            want = orc.dslash(dims, uu, uu3, mass, y, sub)
+            rng = slice(Vh, 2*Vh) if sub == "odd" else slice(0, 2*Vh)
+            err = relerr(x[rng], want[rng])
+            assert err < (1e-12 if prec == "D" else 1e-5), (sub, err)
+        finally:
+            getattr(L, "freeStaggeredLinks" + prec)(byref(sl))
+
+
+def test_c4_32x32x32x64_mixed_16rhs_block(c4):
+    """the benchmark's 16-rhs FP32-mixed solve (sources 2400..2415, m 0.01,
+    true residual 1e-8): every rhs reaches the FP64 true residual and the
+    first agrees with the oracle's FP64 solve2 of that rhs"""
+    L, S, dims, u, u3 = c4
+    mass, rsq, n = 0.01, 1e-16, 16
+    bs = [qll.gen_source(dims, 2400 + r, 6, "even") for r in range(n)]
+    xs = [np.zeros_like(bs[0]) for _ in range(n)]
+    its, info = _solve(L, S, xs, bs, [mass]*n, rsq, qll.SOLVE_MIXED_SINGLE)
+    for r in range(n):
+        assert info.true_rsq[r] < rsq*1.0001, (r, info.true_rsq[r])
+    its_o, xo, _ = orc.solve2(dims, u, u3, mass, bs[0], rsq, MAXITS, noscale=1)
+    Vh = bs[0].shape[0]//2
+    err = relerr(xs[0][:Vh], xo[:Vh])
+    assert err < 1e-7, (err, its, its_o)
