@@ -13,9 +13,9 @@ m = 0.01 its quantisation noise swamps the low modes and it needs about 3x
 the iterations, so FP32 sloppy storage is the faster choice here.
 
 --impl reference times the reference's algorithm on the host CPU cores: the
-reference cannot be compiled here, so it is the CPU oracle (a C restatement
-of QLL's FP64 solve2/cgSolveT), run for a bounded number of CG iterations
-and scaled to a full solve by the iteration count of the FP64 CG.
+CPU oracle (a C restatement of QLL's FP64 solve2/cgSolveT/dslash2, built
+for the host CPU), one converged solve of one source per step, on inputs
+made on the host without loading the GPU library.
 
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 For N > 1 each rank solves its own block (replicas; no collective in the
@@ -46,9 +46,10 @@ SEED_GAUGE = 1004
 SEED_SRC = 2400
 WORKLOAD = "asqtad_cg_32^3x64_m0.01_eps0.4_16rhs_mixed_fp32_fp64_tol1e-8"
 METRIC = "mixed-precision multi-RHS asqtad CG solves/s at 1e-8 true residual"
-# iterations of the FP64 CG (cgSolveT) on this workload, measured with the
-# library's FP64 solver on GB300 (same recurrence as the reference)
-FP64_ITERS_MEASURED = 454
+# the workload's description, identical in both arms
+CONFIG = {"workload": WORKLOAD, "lattice": list(DIMS), "mass": MASS, "eps": EPS, "nrhs": NRHS,
+          "tol_true_residual": 1e-8, "parallelism": "replicas (one process per GPU, no collective)",
+          "l2": "inputs larger than L2 (links 2.4 GB FP32 + 4.8 GB FP64)"}
 # DRAM bytes (read + write) per even site of one 16-rhs FP32 half Dslash
 # (the autotuned lean 64-register rolled launch shape), ncu capture at
 # 24^3x48: 554.7 MB + 121.5 MB over 331,776 sites
@@ -309,6 +310,7 @@ def run_gpu(args):
     pk = peaks()
     peak = pk.get("hbm_gbs")
     compulsory = (8*18*4 + 8*naik*4)/16 + 2*(6*4)
+    achieved_dram = compulsory*Vh*NRHS/(avg_ms*1e-3)/1e9
     # the fused D_eo + CG update: links + 16 neighbours + self + x and r
     # read and written
     fused_bytes = ((8*18*4 + 8*naik*4)/16 + 17*(6*4) + 4*(6*4))*Vh*NRHS
@@ -334,9 +336,7 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32 (sloppy vectors and links) / fp64 (reliable updates, solution)",
         "data": "synthetic (seeded SU(3) gauge, fat7 on GPU, Gaussian sources)",
-        "config": {"workload": WORKLOAD, "lattice": list(DIMS), "mass": MASS, "eps": EPS,
-                   "nrhs": NRHS, "tol_true_residual": 1e-8, "parallelism": "replicas",
-                   "l2": "inputs larger than L2 (links 1.2 GB 16-bit + 4.8 GB FP64)"},
+        "config": CONFIG,
         "iters_per_solve": iters, "max_true_rsq": max(truer),
         "mixed_16bit_storage": {"solves_per_s": ws*NRHS/t_h, "iters": its_half,
                                 "note": "16-bit Krylov vectors with per-site scale; slower at m=0.01"},
@@ -352,24 +352,32 @@ def run_gpu(args):
         "roofline": {"kernel": "stag_dslash_mr<f32,%s,16 slots,16 rhs>, %s"
                                % ("f32 reconstruct-12" if recon else "f32", tuned_choice(L)),
                      "bound": "hbm",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved/peak if peak else None,
+                     "achieved": achieved_dram, "peak": peak, "unit": "GB/s",
+                     "frac": achieved_dram/peak if peak else None,
+                     "basis": "compulsory DRAM bytes per launch: the links (shared by the 16 rhs) "
+                              "plus one load and one store of each spinor (%.0f B per site and "
+                              "rhs), over the event-timed launch duration" % compulsory,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else None,
-                     "algorithmic_bytes_per_launch": launch_bytes,
+                     "bytes_per_launch": compulsory*Vh*NRHS,
                      "avg_launch_ms": avg_ms, "launches_event_timed": cnt.value,
                      "timing_note": "avg launch time from CUDA events over one extra 16-rhs solve after the timed region",
-                     "compulsory_frac": compulsory*Vh*NRHS/(avg_ms*1e-3)/1e9/peak if peak else None,
                      # dram read+write of one launch from an ncu capture at
-                     # 24^3x48 (650 MB), scaled by sites to this lattice
+                     # 24^3x48, scaled by sites to this lattice
                      "traffic": TRAFFIC_PER_SITE_BYTES*Vh,
-                     "traffic_source": "ncu dram__bytes_read+write at 24^3x48, scaled by sites"},
+                     "traffic_source": "ncu dram__bytes_read+write of one launch at 24^3x48, "
+                                       "scaled by sites (captured separately; not measured in this run)",
+                     "lattice_convention": {
+                         "gbs": achieved, "bytes_per_launch": launch_bytes,
+                         "note": "16 neighbour spinor loads + 1 store per site and rhs, links "
+                                 "shared by the 16 rhs (%.0f B): neighbour reuse through L1/L2 "
+                                 "is what lets this figure exceed the HBM peak" % per_site_rhs}},
         "autotune": autotune_report(L),
         "gpu_launches": nlaunch,
         "clocks": clk.summary(local),
         "device_bytes": int(L.qllg_stag_device_bytes(S)),
     }
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(L, S, its64, bounded_iters=args.cpu_iters)
+        out["cpu_baseline"] = cpu_baseline(L, S)
     L.qllg_stag_vec_free(b_dev)
     L.qllg_stag_vec_free(x_dev)
     L.qllg_stag_vec_free(b1)
@@ -519,18 +527,8 @@ def run_c1(args):
     if L.qllg_stag_get_links(S, qll.vp_array(links)):
         raise RuntimeError(qll.last_error())
     L.qllg_stag_destroy(S)
-    lib, _ = _oracle()
-    PA = (POINTER(ctypes.c_double)*8)
-    u = PA(*[links[2*i].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
-    u3 = PA(*[links[2*i + 1].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
-    x = np.zeros_like(src)
-    fr = ctypes.c_double()
-    t = time.time()
-    its = lib.or_solve2D((ctypes.c_int*4)(*dims), x.ctypes.data_as(POINTER(ctypes.c_double)), u, u3,
-                         ctypes.c_double(mass), src.ctypes.data_as(POINTER(ctypes.c_double)),
-                         ctypes.c_double(rsq), MAXITS, 1, ctypes.byref(fr))
-    out["cpu_oracle_fp64"] = {"seconds": time.time() - t, "iters": its, "cores": lib.or_num_threads(),
-                              "kind": "port"}
+    sec, its, cores = cpu_solve(links, src, dims=dims, mass=mass, rsq=rsq)
+    out["cpu_oracle_fp64"] = {"seconds": sec, "iters": its, "cores": cores, "kind": "port"}
     return out
 
 
@@ -664,89 +662,132 @@ def run_serving(args):
 
 
 # ---------------------------------------------------------- CPU baseline
-def _oracle():
+def host_threads():
+    """the host cores this process may run on"""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def _oracle(fast=True):
+    """the CPU oracle: the timing build (host-native flags) or the parity
+    build, with its thread count set to every host core this process may
+    use (an OpenMP runtime shared with other code in the process may have
+    been set to fewer)"""
     from ctypes import POINTER
-    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "liboracle.so"))
+    name = "liboracle_fast.so" if fast else "liboracle.so"
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", name))
     lib.or_solve2D.restype = ctypes.c_int
     lib.or_num_threads.restype = ctypes.c_int
+    lib.or_set_num_threads(host_threads())
     return lib, POINTER
 
 
-def cpu_time_iters(u16, src, iters):
-    """seconds per FP64 CG iteration of the oracle (cgSolveT restated) on
-    the host cores, from a bounded run of `iters` iterations"""
+def cpu_solve(u16, src, dims=DIMS, mass=MASS, rsq=RSQ, maxits=MAXITS):
+    """one converged FP64 CG solve (solve2D: cgSolveT with dslash2, the
+    reference's algorithm restated) of one source on the host cores, timed
+    whole; u16 are the 16 link slots 4mu+2b+naik.  Returns (seconds,
+    iterations, threads)."""
     lib, POINTER = _oracle()
     PA = (POINTER(ctypes.c_double)*8)
     u = PA(*[u16[2*i].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
     u3 = PA(*[u16[2*i+1].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
     x = np.zeros_like(src)
     fr = ctypes.c_double()
-    lib.or_solve2D((ctypes.c_int*4)(*DIMS), x.ctypes.data_as(POINTER(ctypes.c_double)), u, u3,
-                   ctypes.c_double(MASS), src.ctypes.data_as(POINTER(ctypes.c_double)),
-                   ctypes.c_double(RSQ), 2, 1, ctypes.byref(fr))       # warm caches
+    args = lambda its: (dims_ct(dims), x.ctypes.data_as(POINTER(ctypes.c_double)), u, u3,
+                        ctypes.c_double(mass), src.ctypes.data_as(POINTER(ctypes.c_double)),
+                        ctypes.c_double(rsq), its, 1, ctypes.byref(fr))
+    lib.or_solve2D(*args(2))                            # first touch, thread start-up
+    x[:] = 0
     t = time.time()
-    its = lib.or_solve2D((ctypes.c_int*4)(*DIMS), x.ctypes.data_as(POINTER(ctypes.c_double)),
-                         u, u3, ctypes.c_double(MASS),
-                         src.ctypes.data_as(POINTER(ctypes.c_double)), ctypes.c_double(RSQ),
-                         iters, 1, ctypes.byref(fr))
-    dt = time.time() - t
-    return dt/its, lib.or_num_threads()
+    its = lib.or_solve2D(*args(maxits))
+    return time.time() - t, its, lib.or_num_threads()
 
 
-def cpu_baseline(L, S, its64, bounded_iters=30):
+def dims_ct(dims):
+    return (ctypes.c_int*4)(*dims)
+
+
+def cpu_baseline(L, S):
+    """the GPU arm's CPU baseline: one converged FP64 solve of one source
+    by the oracle on the host cores, on the operator's own links"""
     from qll_gb300 import qll
     V = int(np.prod(DIMS))
     links = [np.zeros((V, 18)) for _ in range(16)]
     if L.qllg_stag_get_links(S, qll.vp_array(links)):
         raise RuntimeError(qll.last_error())
     src = qll.gen_source(DIMS, SEED_SRC, 6, "even")
-    per_it, cores = cpu_time_iters(links, src, bounded_iters)
-    return {"value": 1.0/(per_it*its64), "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": "%d FP64 CG iterations (oracle restatement of cgSolveT + dslash2) on the "
-                      "32^3x64 links, %.3f s/iteration, scaled by the %d iterations the FP64 CG "
-                      "needs to converge; one source per solve" % (bounded_iters, per_it, its64)}
+    sec, its, cores = cpu_solve(links, src)
+    return {"value": 1.0/sec, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": "one converged FP64 CG solve of one source (%d iterations, %.1f s; the "
+                      "oracle's restatement of solve2D/cgSolveT/dslash2, host-native build, "
+                      "OpenMP on %d threads) on the 32^3x64 links" % (its, sec, cores)}
 
 
-def run_reference(args):
-    ws, rank, _ = dist_env()
-    if rank != 0:
-        return
-    from qll_gb300 import qll
-    # host-only inputs: thin links, oracle fat7, negative-adjoint backward links
-    lib, POINTER = _oracle()
-    thin = qll.gen_gauge(DIMS, SEED_GAUGE, EPS, ks=True)
+def cpu_inputs():
+    """the headline inputs made on the host by the oracle alone (no GPU
+    library loaded): thin links by the shared generator, fat7 and Naik
+    links by the oracle's smearFat7, negative-adjoint backward links; in
+    slot order 4mu+2b+naik"""
+    lib, POINTER = _oracle(fast=False)
     V = int(np.prod(DIMS))
+    thin = [np.zeros((V, 18)) for _ in range(4)]
+    pa = (ctypes.c_void_p*4)(*[t.ctypes.data for t in thin])
+    if lib.or_gen_gauge(dims_ct(DIMS), ctypes.c_ulonglong(SEED_GAUGE), ctypes.c_double(EPS), 1, pa):
+        raise RuntimeError("or_gen_gauge failed")
+    src = np.zeros((V, 6))
+    lib.or_gen_source(dims_ct(DIMS), ctypes.c_ulonglong(SEED_SRC), 6, b"even",
+                      ctypes.c_void_p(src.ctypes.data))
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as orc
-    fl, ll = orc.smear_fat7(DIMS, thin, qll.asqtad_coeffs())
+
+    class Coef:
+        one_link, three_staple, five_staple = 5/8, -1/16, 1/64
+        seven_staple, lepage, naik = -1/384, -1/16, -1/24
+    fl, ll = orc.smear_fat7(DIMS, thin, Coef)
+    del thin
     links = []
     for mu in range(4):
         links += [fl[mu], ll[mu], orc.negadj_back(DIMS, fl[mu], mu, 1),
                   orc.negadj_back(DIMS, ll[mu], mu, 3)]
-    # links in slot order 4mu+2b+naik -> u[2mu+b], u3[2mu+b]
-    order = []
-    for mu in range(4):
-        order += [links[4*mu], links[4*mu+1], links[4*mu+2], links[4*mu+3]]
-    src = qll.gen_source(DIMS, SEED_SRC, 6, "even")
-    its64 = FP64_ITERS_MEASURED or args.fp64_iters
-    vals = []
-    for _ in range(args.warmup):
-        cpu_time_iters(order, src, args.cpu_iters)
-    for _ in range(args.steps):
-        per_it, cores = cpu_time_iters(order, src, args.cpu_iters)
-        vals.append(1.0/(per_it*its64))
-    value = statistics.median(vals)
+    return links, src
+
+
+def run_reference(args):
+    """the reference arm: the reference's algorithm for this path on the
+    host cores (the oracle's C restatement of solve2D/cgSolveT/dslash2,
+    host-native build), one converged FP64 solve of one source per step,
+    on inputs made on the host without the GPU library.  Timed steps are
+    capped so that the run stays within a few minutes; the line reports the
+    steps actually timed."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    links, src = cpu_inputs()
+    lib, _ = _oracle()
+    budget_s = args.cpu_budget
+    secs, its = [], 0
+    for _ in range(min(args.warmup, 1)):
+        cpu_solve(links, src, maxits=20)                 # warm-up: a short solve
+    t0 = time.time()
+    for k in range(args.steps):
+        sec, its, cores = cpu_solve(links, src)
+        secs.append(sec)
+        if time.time() - t0 + sec > budget_s:
+            break
+    value = len(secs)/sum(secs)
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
-           "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "n_gpus": ws, "steps": len(secs), "steps_requested": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3*sum(secs)/len(secs),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded SU(3) gauge, oracle fat7, Gaussian source)",
-           "config": {"workload": WORKLOAD, "lattice": list(DIMS), "mass": MASS, "eps": EPS,
-                      "nrhs": NRHS, "tol_true_residual": 1e-8, "parallelism": "host threads"},
+           "config": CONFIG,
            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                            "sample": "%d FP64 CG iterations per step (oracle restatement of "
-                                      "cgSolveT/dslash2; the reference needs Lua-generated "
-                                      "sources and QMP and does not compile here), scaled by "
-                                      "%d iterations to convergence" % (args.cpu_iters, its64)},
+                            "sample": "%d converged FP64 CG solves of one source (%d iterations "
+                                      "each; the oracle's restatement of solve2D/cgSolveT/dslash2, "
+                                      "host-native build, OpenMP on %d threads)"
+                                      % (len(secs), its, cores)},
            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -882,8 +923,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-iters", type=int, default=30)
-    ap.add_argument("--fp64-iters", type=int, default=2000)
+    ap.add_argument("--cpu-budget", type=float, default=150.0,
+                    help="--impl reference: stop timing further solves after this many seconds")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--dslash-only", action="store_true")
     ap.add_argument("--dims", default="32,32,32,64")

@@ -24,6 +24,18 @@ or_num_threads(void)
 #endif
 }
 
+/* the thread count of the oracle's parallel loops (a host process that
+ * also runs other OpenMP code may have changed it) */
+void
+or_set_num_threads(int n)
+{
+#ifdef _OPENMP
+  if(n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
 int
 or_nsites(const int dims[4])
 {

@@ -135,6 +135,9 @@ double or_fieldtest_kat(const int dims[4]);
 
 /* number of OpenMP threads the oracle uses */
 int or_num_threads(void);
+void or_set_num_threads(int n);
+int or_gen_gauge(const int dims[4], unsigned long long seed, double eps, int ks, double *u[4]);
+int or_gen_source(const int dims[4], unsigned long long seed, int nelem, const char *sub, double *v);
 
 #ifdef __cplusplus
 }
