@@ -14,8 +14,10 @@ builds its own from the same thin links.
 
 Tolerances: fat7 links and FP64 Dslash 1e-12 relative, FP32 Dslash 1e-5;
 every solution reaches its FP64 true residual (|r|^2 < rsq |b|^2 measured
-by the library in FP64) and agrees with the oracle's FP64 solution within
-10x the solver tolerance (relative 1e-7 for tolerance 1e-8) unless stated.
+by the library in FP64), reaches it too under the oracle's FP64 operator
+(|b - A x|/|b| < 1.01e-8), and agrees with the oracle's FP64 solution
+within 10x the solver tolerance (relative 1e-7 for tolerance 1e-8) except
+where the test states a condition-number bound.
 FP64 CG iteration counts equal the oracle's within 1.
 """
 import ctypes
@@ -57,6 +59,18 @@ def _oracle_links(dims, thin):
         u3[2*mu] = ll[mu]
         u3[2*mu + 1] = orc.negadj_back(dims, ll[mu], mu, 3)
     return u, u3
+
+
+def _oracle_residual(dims, u, u3, mass, b, x):
+    """|b - A x|/|b| with the oracle's FP64 operator A = m^2 - D_eo D_oe
+    (dslashp2) on the even sites: the true residual of a GPU solution
+    measured by the oracle, so a GPU operator that differed from the
+    reference's would show here"""
+    Vh = b.shape[0]//2
+    xx = np.zeros_like(b)
+    xx[:Vh] = x[:Vh]
+    Ax, _ = orc.dslashp2(dims, u, u3, mass, xx)
+    return np.linalg.norm(b[:Vh] - Ax[:Vh])/np.linalg.norm(b[:Vh])
 
 
 def _gpu_operator(L, dims, seed, eps):
@@ -103,6 +117,7 @@ def test_c1_8x8x8x8_fp64_and_mixed_cg():
             x = np.zeros_like(b)
             its, info = _solve(L, S, [x], [b], [mass], rsq, mode)
             assert info.true_rsq[0] < rsq*1.0001, (mode, info.true_rsq[0])
+            assert _oracle_residual(dims, u, u3, mass, b, x) < 1.01e-8, mode
             assert relerr(x[:Vh], xo[:Vh]) < 1e-7, mode
             if mode == qll.SOLVE_DOUBLE:
                 assert abs(its - its_o) <= 1, (its, its_o)
@@ -135,8 +150,13 @@ def test_c2_16x16x16x32_wilson_cgnr(mode):
         assert its > 0, qll.last_error()
         its_o, xo, _ = orc.wilson_cgnr(dims, u, mass, b, rsq, MAXITS)
         Vh = b.shape[0]//2
-        # the library's true residual is |b - S x|^2/|b|^2 in FP64
+        # the library's true residual is |b - S x|^2/|b|^2 in FP64; the same
+        # under the oracle's Schur operator S
         assert info.true_rsq[0] < 1e-16, info.true_rsq[0]
+        xe = np.zeros_like(x)
+        xe[:Vh] = x[:Vh]
+        Sx = orc.wilson_schur(dims, u, mass, xe, 0)
+        assert np.linalg.norm(b[:Vh] - Sx[:Vh])/np.linalg.norm(b[:Vh]) < 1.01e-8
         assert relerr(x[:Vh], xo[:Vh]) < 1e-7
         if mode == qll.SOLVE_DOUBLE:
             assert abs(its - its_o) <= 2, (its, its_o)
@@ -170,9 +190,14 @@ def test_c3_24x24x24x48_mixed_multishift():
         Vh = b.shape[0]//2
         for k in range(ns):
             assert tr[k] < rsq*1.0001, (k, tr[k])
-            # the oracle's cgms stops on the base (smallest) shift's residual
-            # only; its larger shifts are solved more accurately than 1e-8
-            assert relerr(xs[k][:Vh], xo[k][:Vh]) < 1e-7, (k, relerr(xs[k][:Vh], xo[k][:Vh]))
+            m = np.sqrt(mass**2 + shifts[k])
+            assert _oracle_residual(dims, u, u3, m, b, xs[k]) < 1.01e-8, k
+            # the smallest shifts have m^2 + sigma = 5e-4 (condition number
+            # about 5e4): two solutions that each meet 1e-8 can differ by more
+            # than 1e-7 there (2e-7 measured for the smallest); the residual
+            # under the oracle's operator above is the sharp check
+            tol = 1e-7 if mass**2 + shifts[k] > 2e-3 else 1e-6
+            assert relerr(xs[k][:Vh], xo[k][:Vh]) < tol, (k, relerr(xs[k][:Vh], xo[k][:Vh]))
     finally:
         L.qllg_stag_destroy(S)
 
@@ -241,6 +266,8 @@ def test_c4_32x32x32x64_mixed_16rhs_block(c4):
     its, info = _solve(L, S, xs, bs, [mass]*n, rsq, qll.SOLVE_MIXED_SINGLE)
     for r in range(n):
         assert info.true_rsq[r] < rsq*1.0001, (r, info.true_rsq[r])
+    for r in (0, n - 1):
+        assert _oracle_residual(dims, u, u3, mass, bs[r], xs[r]) < 1.01e-8, r
     its_o, xo, _ = orc.solve2(dims, u, u3, mass, bs[0], rsq, MAXITS, noscale=1)
     Vh = bs[0].shape[0]//2
     err = relerr(xs[0][:Vh], xo[:Vh])
