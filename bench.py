@@ -12,10 +12,11 @@ The 16-bit-storage mode (per-site scale) is also run once and reported: at
 m = 0.01 its quantisation noise swamps the low modes and it needs about 3x
 the iterations, so FP32 sloppy storage is the faster choice here.
 
---impl reference times the reference's algorithm on the host CPU cores: the
-CPU oracle (a C restatement of QLL's FP64 solve2/cgSolveT/dslash2, built
-for the host CPU), one converged solve of one source per step, on inputs
-made on the host without loading the GPU library.
+--impl reference times the reference's own FP64 solve2 on the host CPU
+cores: the reference library compiled from its sources (oracle/_ref, its
+4-site SIMD layout, host-native flags), or, where it was not built, the CPU
+oracle's C restatement of it; one converged solve of one source per step,
+on inputs made on the host without loading the GPU library.
 
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 For N > 1 each rank solves its own block (replicas; no collective in the
@@ -709,6 +710,64 @@ def dims_ct(dims):
     return (ctypes.c_int*4)(*dims)
 
 
+REF_FAST = os.path.join(ROOT, "oracle", "_ref", "libqllref_fast.so")
+
+
+def _aligned(shape):
+    """a zeroed float64 array on a 64-byte boundary (the reference's
+    vector loads assume its own 64-byte-aligned allocations)"""
+    n = int(np.prod(shape))
+    buf = np.zeros(n + 16)
+    off = (-buf.ctypes.data % 64)//8
+    return buf[off:off + n].reshape(shape)
+
+
+def ref_cpu_solve(u16, src, dims=DIMS, mass=MASS, rsq=RSQ, maxits=MAXITS):
+    """one converged FP64 solve2 of the reference library itself
+    (oracle/_ref/libqllref_fast.so: the reference's sources, its 4-site SIMD
+    layout, host-native flags) on the host cores, timed whole; the links and
+    the source are moved into the reference's layout first, untimed.
+    Returns (seconds, iterations, threads)."""
+    from ctypes import POINTER, c_double, c_int
+    R = ctypes.CDLL(REF_FAST)
+    R.refh_solve2D.restype = c_int
+    n = host_threads()
+    R.refh_set_threads(n)
+    if R.refh_setup(dims_ct(dims)):
+        raise RuntimeError("reference setup failed")
+    P = lambda a: a.ctypes.data_as(POINTER(c_double))
+
+    def to_layout(a):
+        out = _aligned(a.shape)
+        R.refh_convertD(P(out), P(np.ascontiguousarray(a)), a.shape[1], 1)
+        return out
+    # slot 4mu+2b+naik -> u[2mu+b] (fat), u3[2mu+b] (Naik)
+    u = [to_layout(u16[4*mu + 2*b]) for mu in range(4) for b in range(2)]
+    u3 = [to_layout(u16[4*mu + 2*b + 1]) for mu in range(4) for b in range(2)]
+    PA = lambda arrs: (POINTER(c_double)*8)(*[P(a) for a in arrs])
+    b = to_layout(src)
+    x = _aligned(src.shape)
+    R.refh_solve2D(P(x), PA(u), PA(u3), c_double(mass), P(b), c_double(rsq), 2, 1)   # warm
+    x[:] = 0
+    t = time.time()
+    its = R.refh_solve2D(P(x), PA(u), PA(u3), c_double(mass), P(b), c_double(rsq), maxits, 1)
+    return time.time() - t, its, n
+
+
+def timed_cpu_solve(u16, src, **kw):
+    """the CPU baseline's converged solve: the reference library itself
+    where it was built here (kind "reference"), else the oracle's
+    restatement of it (kind "port")"""
+    if os.path.exists(REF_FAST):
+        sec, its, cores = ref_cpu_solve(u16, src, **kw)
+        return sec, its, cores, "reference", ("the reference's own solve2D/cgSolveT/dslash2, "
+                                              "compiled from its sources with its 4-site SIMD "
+                                              "layout (-DC4) and host-native flags")
+    sec, its, cores = cpu_solve(u16, src, **kw)
+    return sec, its, cores, "port", ("the oracle's restatement of solve2D/cgSolveT/dslash2, "
+                                     "host-native build")
+
+
 def cpu_baseline(L, S):
     """the GPU arm's CPU baseline: one converged FP64 solve of one source
     by the oracle on the host cores, on the operator's own links"""
@@ -718,11 +777,10 @@ def cpu_baseline(L, S):
     if L.qllg_stag_get_links(S, qll.vp_array(links)):
         raise RuntimeError(qll.last_error())
     src = qll.gen_source(DIMS, SEED_SRC, 6, "even")
-    sec, its, cores = cpu_solve(links, src)
-    return {"value": 1.0/sec, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": "one converged FP64 CG solve of one source (%d iterations, %.1f s; the "
-                      "oracle's restatement of solve2D/cgSolveT/dslash2, host-native build, "
-                      "OpenMP on %d threads) on the 32^3x64 links" % (its, sec, cores)}
+    sec, its, cores, kind, what = timed_cpu_solve(links, src)
+    return {"value": 1.0/sec, "unit": "solves/s", "cores": cores, "kind": kind,
+            "sample": "one converged FP64 CG solve of one source (%d iterations, %.1f s; %s, "
+                      "OpenMP on %d threads) on the 32^3x64 links" % (its, sec, what, cores)}
 
 
 def cpu_inputs():
@@ -755,24 +813,24 @@ def cpu_inputs():
 
 
 def run_reference(args):
-    """the reference arm: the reference's algorithm for this path on the
-    host cores (the oracle's C restatement of solve2D/cgSolveT/dslash2,
-    host-native build), one converged FP64 solve of one source per step,
-    on inputs made on the host without the GPU library.  Timed steps are
+    """the reference arm: the reference's own CPU solve on the host cores
+    (the reference library compiled from its sources, SIMD layout,
+    host-native flags; the oracle's restatement of it where the reference
+    was not built), one converged FP64 solve of one source per step, on
+    inputs made on the host without the GPU library.  Timed steps are
     capped so that the run stays within a few minutes; the line reports the
     steps actually timed."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     links, src = cpu_inputs()
-    lib, _ = _oracle()
     budget_s = args.cpu_budget
     secs, its = [], 0
     for _ in range(min(args.warmup, 1)):
-        cpu_solve(links, src, maxits=20)                 # warm-up: a short solve
+        timed_cpu_solve(links, src, maxits=20)           # warm-up: a short solve
     t0 = time.time()
     for k in range(args.steps):
-        sec, its, cores = cpu_solve(links, src)
+        sec, its, cores, kind, what = timed_cpu_solve(links, src)
         secs.append(sec)
         if time.time() - t0 + sec > budget_s:
             break
@@ -783,11 +841,10 @@ def run_reference(args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded SU(3) gauge, oracle fat7, Gaussian source)",
            "config": CONFIG,
-           "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+           "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": kind,
                             "sample": "%d converged FP64 CG solves of one source (%d iterations "
-                                      "each; the oracle's restatement of solve2D/cgSolveT/dslash2, "
-                                      "host-native build, OpenMP on %d threads)"
-                                      % (len(secs), its, cores)},
+                                      "each; %s, OpenMP on %d threads)"
+                                      % (len(secs), its, what, cores)},
            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)

@@ -16,10 +16,14 @@ include/Makefile:1-2) and the QMP message-passing library
   3. links them with ref_harness.c (this repository's C entry points that
      drive the reference API the way its test programs do) into
      _ref/libqllref.so.
-Builds: -DC1 (one SIMD lane, the reference's one-lane layout, the same
-site order as the oracle and the GPU library), without floating-point
-contraction, for parity; and _ref/libqllref_fast.so, the same with the
-host-native flags of the timing build.
+Builds: _ref/libqllref.so with -DC1 (one SIMD lane: the reference's
+one-lane layout, the same site order as the oracle and the GPU library),
+without floating-point contraction, for parity; and _ref/libqllref_fast.so
+with -DC4 (four sites per vector, the reference's portable GCC-vector SIMD
+path) and host-native flags (-O3 -mcpu=native on aarch64, -march=native on
+x86_64), the reference's own kind of timing build (its make.inc:18-24),
+for the CPU timing arm; refh_convert moves fields between the one-lane
+order and its layout.
 
 The reference's sources are staged, with the generated ones, under
 _ref/src (git-ignored, never committed), so that a machine without the
@@ -77,7 +81,7 @@ def native_flags():
 def compile_lib(name, extra, jobs=None):
     obj = os.path.join(OUT, "obj_" + name)
     os.makedirs(obj, exist_ok=True)
-    base = ["gcc", "-std=gnu99", "-fPIC", "-fopenmp", "-w", "-DC1",
+    base = ["gcc", "-std=gnu99", "-fPIC", "-fopenmp", "-w",
             "-I" + STUB, "-I" + os.path.join(SRC, "include"), "-I" + os.path.join(SRC, "lib")]
     cmds = []
     objs = []
@@ -113,8 +117,8 @@ def build(ref=None):
         stage(ref)
     if not os.path.exists(os.path.join(SRC, "lib", "vla0.c")):
         return None
-    lib = compile_lib("libqllref", ["-O2", "-ffp-contract=off"])
-    compile_lib("libqllref_fast", ["-O3"] + native_flags())
+    lib = compile_lib("libqllref", ["-DC1", "-O2", "-ffp-contract=off"])
+    compile_lib("libqllref_fast", ["-DC4", "-O3"] + native_flags())
     return lib
 
 

@@ -80,6 +80,35 @@ refh_nsites(void)
   return lay[0].nSites;
 }
 
+/* SIMD lanes per vector of this build (1 for -DC1; -DC4 packs 4 sites) */
+int
+refh_vlen(void)
+{
+  return lay[0].nSitesInner;
+}
+
+/* position of one-lane site s (the order of layoutIndex with one lane:
+ * even sites first, each parity lexicographic with x0 fastest, halved) in
+ * this build's layout, whose arrays are [(outer*nelem + e)*VLEN + lane]
+ * with layoutIndex's index = outer*VLEN + lane */
+static void
+site_slot(int p, int s, int *outer, int *lane)
+{
+  const Layout *l = &lay[p];
+  int V = ls[0]*ls[1]*ls[2]*ls[3];
+  int par = s >= V/2;
+  int i = s - par*(V/2);
+  int x[4];
+  int x0h = i % (ls[0]/2), r = i / (ls[0]/2);
+  x[1] = r % ls[1]; r /= ls[1];
+  x[2] = r % ls[2]; x[3] = r / ls[2];
+  x[0] = 2*x0h + ((par + x[1] + x[2] + x[3]) & 1);
+  LayoutIndex li;
+  layoutIndex((Layout *)l, &li, x);
+  *outer = li.index / l->nSitesInner;
+  *lane = li.index % l->nSitesInner;
+}
+
 #define REAL double
 #define SFX(x) x ## D
 #define LAYOUT (&lay[0])

@@ -3,6 +3,25 @@
  * included once with REAL double and once with float.
  */
 
+/* a field of nelem reals per site from the one-lane site order into this
+ * build's layout (to_layout 1) or back (0) */
+void
+SFX(refh_convert)(REAL *dst, const REAL *src, int nelem, int to_layout)
+{
+  const int p = sizeof(REAL) == sizeof(double) ? 0 : 1;
+  const int V = ls[0]*ls[1]*ls[2]*ls[3];
+  const int vl = lay[p].nSitesInner;
+  for(int s=0; s<V; s++) {
+    int o, ln;
+    site_slot(p, s, &o, &ln);
+    for(int e=0; e<nelem; e++) {
+      long k = ((long)o*nelem + e)*vl + ln;
+      if(to_layout) dst[k] = src[(long)s*nelem + e];
+      else dst[(long)s*nelem + e] = src[k];
+    }
+  }
+}
+
 /* defined in lib/stagDslash.c:522 and lib/wilsonDslash.c:263, not
  * declared in the reference's public headers */
 void SFX(freeStaggeredLinks)(SFX(StaggeredLinks) *sl);
