@@ -12,7 +12,9 @@ include/Makefile:1-2) and the QMP message-passing library
      own sources, with refstub/qmp.h standing in for QMP (one rank: no
      message is ever exchanged, the global sum is the identity) and
      refstub/rdtsc.h for the x86/PowerPC tick counter of
-     include/rdtsc.h, which has no aarch64 branch;
+     include/rdtsc.h, which has no aarch64 branch; the staged
+     include/thread.h takes the reference's own PowerPC memory barrier on
+     aarch64 as well (stage() says why);
   3. links them with ref_harness.c (this repository's C entry points that
      drive the reference API the way its test programs do) into
      _ref/libqllref.so.
@@ -66,6 +68,19 @@ def stage(ref):
             if name == "rdtsc.h" or not name.endswith((".c", ".h", ".lua")):
                 continue
             shutil.copyfile(f, os.path.join(SRC, sub, name))
+    # include/thread.h:83-88 makes its thread-reduction fence SYNC a full
+    # memory barrier on PowerPC only and empty elsewhere, which relies on
+    # x86's store and load ordering: on aarch64 the threads of its global
+    # sums (lib/common.c:30-72) can read a partner's partial sum before it
+    # is visible, and the sums come out wrong (observed on the aarch64 GPU
+    # host: the 16-thread CG at 32^3x64 did not converge).  The staged copy
+    # takes the reference's own PowerPC barrier on aarch64 too.
+    th = os.path.join(SRC, "include", "thread.h")
+    with open(th) as fh:
+        text = fh.read()
+    text = text.replace("#ifdef __powerpc__", "#if defined(__powerpc__) || defined(__aarch64__)", 1)
+    with open(th, "w") as fh:
+        fh.write(text)
     for script, out in GENERATED:
         path = os.path.join(SRC, script)
         tmp = os.path.join(SRC, out + ".tmp")
