@@ -165,6 +165,9 @@ int qllg_stag_dslash_device(qllg_stag *S, int prec, int nrhs, int out_parity, vo
 int qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
                                    void *out_dev, const void *in_dev, double *norm2_dev);
 size_t qllg_stag_vec_bytes(const qllg_stag *S, int prec, int nrhs);
+/* 1 when the last solve on S ran as one persistent cooperative launch
+ * (parameter "persistent"), 0 when it ran the multi-launch loop */
+int qllg_stag_last_solve_persistent(const qllg_stag *S);
 /* 1 when the mixed FP32 solves of S use reconstruct-12 links: the 8 Naik
  * slots held as rows 0 and 1 (48 of 72 bytes) and row 2 rebuilt in the
  * kernel as s conj(r0 x r1)/|r0|, which holds for a real multiple of an
@@ -266,6 +269,14 @@ void qllg_server_destroy(qllg_server *V);
  *    CGNR): a reliable update when |r| falls by this factor;
  *  "reortho" (1), "graph" (1: the solver loop as one CUDA-graph launch),
  *    "poll" (8: first batch of host-polled iterations);
+ *  "persistent" (1: on small lattices the whole CG loop as one cooperative
+ *    launch, for FP64 solves and FP32 mixed solves with FP64 reliable
+ *    updates), "persistent_max" (65536: ... when even sites x rhs is at most
+ *    this), "wait_polls" (2e7: polls, about 64 ns apart, a grid-barrier
+ *    wait of the persistent CG takes before the solve fails with an error
+ *    instead of hanging), "cg_barrier_extra" (0: arrivals its barriers
+ *    expect beyond the grid; nonzero only to make the waits run out in a
+ *    test);
  *  "ru_compact" (1: reliable updates over the flagged rhs only), "ru_df" (1:
  *    intermediate reliable updates in double-float, final ones in FP64),
  *    "df_blocks" (3: register cap of the double-float kernel);
@@ -275,7 +286,7 @@ void qllg_server_destroy(qllg_server *V);
  *  "autotune" (1: time the Dslash launch shapes of each new shape and keep
  *    the fastest), "dslash_tile" (1) and "dslash_bulk" (1): the staged and
  *    the bulk-copy candidates may be chosen; "dslash_variant" (-1: autotuned;
- *    0-14 forces a candidate where it applies, qllg_autotune_report names
+ *    0-17 forces a candidate where it applies, qllg_autotune_report names
  *    them);
  *  "links_recon12" (0; 1: reconstruct-12 Naik links in the FP32 solves),
  *  "solve2_mixed" (0; 1: the drop-in solve2D runs FP32 iterations with FP64

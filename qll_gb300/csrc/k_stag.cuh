@@ -210,14 +210,24 @@ stag_dslash(qllg_stag_args a)
 // 64 registers).  (Candidates measured slower and dropped: 56 and 48
 // registers, every slot loop rolled, 32-byte spinor loads, lean 2 rhs per
 // thread.)
+// 16 and 17: 8 and 15 with the rhs of a thread taken in interleaved pairs
+// (thread q of a site holds rhs 2q, 2q+1, 2Q+2q, 2Q+2q+1 for Q threads per
+// site instead of 4q..4q+3): the four threads of a site then read 64
+// contiguous bytes (two whole 32-byte sectors) of a neighbour's colour
+// vector per 16-byte load instead of four half sectors, halving the
+// sectors the L1 moves for spinor loads; 18: 16 with the complex FMAs on
+// packed FP32 pairs.
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int threads = (CFG == 14 || CFG == 15) ? 128 : 256;
-  static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 : (CFG == 3 || CFG == 8) ? 4 :
-                              CFG == 14 ? 7 : CFG == 15 ? 8 : (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
-  static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
+  static constexpr int threads = (CFG == 14 || CFG == 15 || CFG == 17) ? 128 : 256;
+  static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 :
+                              (CFG == 3 || CFG == 8 || CFG == 16 || CFG == 18) ? 4 :
+                              CFG == 14 ? 7 : (CFG == 15 || CFG == 17) ? 8 :
+                              (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
+  static constexpr bool f2 = (CFG == 1 || CFG == 18) && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
   static constexpr bool pf = CFG == 5 || CFG == 6;
   static constexpr bool roll = CFG == 7 || CFG == 8 || CFG == 9 || CFG >= 14;   // direction loop rolled
+  static constexpr bool pairs = CFG >= 16 && R == 4;
 };
 
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
@@ -244,6 +254,9 @@ stag_dslash_mr(qllg_stag_args a)
   const size_t loff = p ? (size_t)G.Vh : 0;
   const bool skip = a.done && *(volatile const int *)a.done;
   const int q = threadIdx.x % Q;
+  constexpr bool PAIRS = MrCfg<PS,R,CFG>::pairs;
+  // the rhs held in slot j of this thread
+  auto rix = [&](int j) -> int { return PAIRS ? (j >> 1)*2*Q + 2*q + (j & 1) : q*R + j; };
   bool act[R];
   T ca[R], alpha[R];
   bool anyact = false, allact = true;
@@ -256,7 +269,7 @@ stag_dslash_mr(qllg_stag_args a)
   if(a.active) for(int r=0; r<NR; r++) allrhs &= a.active[r] != 0;
 #pragma unroll
   for(int j=0; j<R; j++) {
-    const int rhs = q*R + j;
+    const int rhs = rix(j);
     act[j] = !a.active || a.active[rhs];
     anyact |= act[j];
     allact &= act[j];
@@ -278,8 +291,8 @@ stag_dslash_mr(qllg_stag_args a)
     }
     __syncthreads();
   }
-  auto cav = [&](int j) -> T { if constexpr (LEAN) return s_ca[q*R + j]; else return ca[j]; };
-  auto alv = [&](int j) -> T { if constexpr (LEAN) return s_alpha[q*R + j]; else return alpha[j]; };
+  auto cav = [&](int j) -> T { if constexpr (LEAN) return s_ca[rix(j)]; else return ca[j]; };
+  auto alv = [&](int j) -> T { if constexpr (LEAN) return s_alpha[rix(j)]; else return alpha[j]; };
   Acc<T> acc0r[LEAN ? 1 : R], acc1r[LEAN ? 1 : R];
   Acc<T> *accs = reinterpret_cast<Acc<T> *>(shm);
   static_assert(sizeof(Acc<T>) <= sizeof(double), "norm sums in shm");
@@ -299,7 +312,7 @@ stag_dslash_mr(qllg_stag_args a)
     for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < nwork;
         w += (size_t)gridDim.x*blockDim.x) {
       const int site = (int)(w / Q);
-      const size_t t0 = (size_t)site*NR + q*R;
+      const size_t sb = (size_t)site*NR;
       int x[4];
       site_coords(G, p, site, x);
       Cx<T> acc[R][3];
@@ -307,7 +320,7 @@ stag_dslash_mr(qllg_stag_args a)
       for(int j=0; j<R; j++) {
         if(a.mode == 1 && a.self) {
           Cx<T> s[3];
-          SpinorIO<PS,3>::load(a.self, total, t0 + j, s);
+          SpinorIO<PS,3>::load(a.self, total, sb + rix(j), s);
 #pragma unroll
           for(int c=0; c<3; c++) { acc[j][c].r = cav(j)*s[c].r; acc[j][c].i = cav(j)*s[c].i; }
         } else {
@@ -329,7 +342,7 @@ stag_dslash_mr(qllg_stag_args a)
             for(int nk=0; nk<(NS == 16 ? 2 : 1); nk++) {
               const int d = (nk ? 3 : 1)*(back ? -1 : 1);
               const size_t nb = (size_t)nbr_index(G, x, mu, d);
-              const size_t kb = nb*NR + q*R;
+              const size_t kb = nb*NR;
               Cx<T> U[9];
               slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
               if constexpr (v4) {
@@ -338,7 +351,7 @@ stag_dslash_mr(qllg_stag_args a)
                 for(int h=0; h<R/2; h++) {
                   if constexpr (CK) { if(!act[2*h] && !act[2*h + 1]) continue; }
                   Cx<T> v[2][3];
-                  Spinor4<PS>::load_half(a.in, total, kb, h, v);
+                  Spinor4<PS>::load_pair(a.in, total, kb + rix(2*h), v);
 #pragma unroll
                   for(int jj=0; jj<2; jj++) {
 #pragma unroll
@@ -356,7 +369,7 @@ stag_dslash_mr(qllg_stag_args a)
                 for(int j=0; j<R; j++) {
                   if constexpr (CK) { if(!act[j]) continue; }
                   Cx<T> v[3];
-                  SpinorIO<PS,3>::load(a.in, total, kb + j, v);
+                  SpinorIO<PS,3>::load(a.in, total, kb + rix(j), v);
 #pragma unroll
                   for(int l=0; l<3; l++) {
 #pragma unroll
@@ -384,7 +397,7 @@ stag_dslash_mr(qllg_stag_args a)
 #pragma unroll
           for(int h=0; h<R/2; h++) {
             Cx<T> w[2][3];
-            Spinor4<PS>::load_half(a.in, total, nb*NR + q*R, h, w);
+            Spinor4<PS>::load_pair(a.in, total, nb*NR + rix(2*h), w);
 #pragma unroll
             for(int c=0; c<3; c++) { v[2*h][c] = w[0][c]; v[2*h + 1][c] = w[1][c]; }
           }
@@ -429,11 +442,12 @@ stag_dslash_mr(qllg_stag_args a)
 #pragma unroll
           for(int h=0; h<R/2; h++) {
             Cx<T> sv[2][3];
-            if(a.self) Spinor4<PS>::load_half(a.self, total, t0, h, sv);
+            const size_t tp = sb + rix(2*h);
+            if(a.self) Spinor4<PS>::load_pair(a.self, total, tp, sv);
             if(a.mode == 3) {
               Cx<T> xv[2][3], rv[2][3];
-              Spinor4<PX>::load_half(a.x, total, t0, h, xv);
-              Spinor4<PX>::load_half(a.r, total, t0, h, rv);
+              Spinor4<PX>::load_pair(a.x, total, tp, xv);
+              Spinor4<PX>::load_pair(a.r, total, tp, rv);
 #pragma unroll
               for(int jj=0; jj<2; jj++) {
                 const int j = 2*h + jj;
@@ -448,8 +462,8 @@ stag_dslash_mr(qllg_stag_args a)
                 }
                 norm0(j, rv[jj]);
               }
-              Spinor4<PX>::store_half(a.x, total, t0, h, xv);
-              Spinor4<PX>::store_half(a.r, total, t0, h, rv);
+              Spinor4<PX>::store_pair(a.x, total, tp, xv);
+              Spinor4<PX>::store_pair(a.r, total, tp, rv);
               continue;
             }
             Cx<T> ov[2][3];
@@ -469,7 +483,7 @@ stag_dslash_mr(qllg_stag_args a)
               if(a.norm_out) norm0(j, ov[jj]);
               if(a.norm_self && a.self) norm1(j, sv[jj]);
             }
-            Spinor4<PS>::store_half(a.out, total, t0, h, ov);
+            Spinor4<PS>::store_pair(a.out, total, tp, ov);
           }
           continue;
         }
@@ -477,7 +491,7 @@ stag_dslash_mr(qllg_stag_args a)
 #pragma unroll
       for(int j=0; j<R; j++) {
         if(!act[j]) continue;
-        const size_t t = t0 + j;
+        const size_t t = sb + rix(j);
         Cx<T> self[3];
         if(a.self && a.mode != 1) SpinorIO<PS,3>::load(a.self, total, t, self);
         if(a.mode == 3) {
@@ -528,7 +542,7 @@ stag_dslash_mr(qllg_stag_args a)
   if(a.mode == 3) {
     if(skip) return;
     double *res[2] = {a.sc->tmp, NULL};
-    if(grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res)) {
+    if(grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res, 0, PAIRS)) {
       __syncthreads();
       if(threadIdx.x == 0) {
         if(a.mixed) cg_finish_mixed(a.sc, NR);
@@ -537,7 +551,7 @@ stag_dslash_mr(qllg_stag_args a)
     }
   } else if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
-    grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res);
+    grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res, 0, PAIRS);
   }
 }
 
@@ -1018,10 +1032,10 @@ int launch_tile(const qllg_stag_args *a)
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15 as variants 4-10 and
-// 12-14) and 11 = the bulk-copy pipeline (FP32 links and spinors, 16 slots,
-// 16 rhs, k_stag_bulk.cuh)
-constexpr int kNumVariants = 15;
+// launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15, 16, 17, 18 as
+// variants 4-10 and 12-17) and 11 = the bulk-copy pipeline (FP32 links and
+// spinors, 16 slots, 16 rhs, k_stag_bulk.cuh)
+constexpr int kNumVariants = 18;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
@@ -1029,7 +1043,10 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "4 rhs/thread rolled", "4 rhs/thread lean 64 regs rolled",
                                                 "bulk-copy pipeline", "4 rhs/thread lean 80 regs rolled",
                                                 "4 rhs/thread lean 72 regs rolled (128 threads)",
-                                                "4 rhs/thread lean 64 regs rolled (128 threads)"};
+                                                "4 rhs/thread lean 64 regs rolled (128 threads)",
+                                                "4 rhs/thread lean 64 regs rolled, paired rhs",
+                                                "4 rhs/thread lean 64 regs rolled (128 threads), paired rhs",
+                                                "4 rhs/thread lean 64 regs rolled, paired rhs, packed FMA"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1066,7 +1083,10 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 10: return launch_mr<PS,PL,NS,NR,4,8>(a);
       case 12: return launch_mr<PS,PL,NS,NR,4,9>(a);
       case 13: return launch_mr<PS,PL,NS,NR,4,14>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,15>(a);
+      case 14: return launch_mr<PS,PL,NS,NR,4,15>(a);
+      case 15: return launch_mr<PS,PL,NS,NR,4,16>(a);
+      case 16: return launch_mr<PS,PL,NS,NR,4,17>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,18>(a);
       }
     }
   }

@@ -16,10 +16,13 @@
 // indices; the ring keeps kBkStages slots of copies in flight per block
 // without holding registers.
 //
-// Every wait is bounded (about a second of clock64 time); a wait that runs
-// out records an error in g_bulk_err, stops the pipeline and lets the block
-// finish (the producer first waits, again bounded, for its copies in
-// flight), so a broken launch returns garbage with an error, not a hang.
+// Every wait is bounded: the pipeline's waits by the library's wait limit
+// (parameter wait_polls, about a second by default), after which the wait
+// records an error in g_bulk_err, stops the pipeline and lets the block
+// finish; the producer first waits for its copies in flight to land, with
+// a fixed limit of 2e9 clock cycles whatever the pipeline's own, so that
+// no copy lands in the shared memory of a block that has left.  A broken
+// launch returns garbage with an error, not a hang.
 #pragma once
 
 // (included inside k_stag.cuh's anonymous namespace)
@@ -31,7 +34,7 @@ constexpr int kBkLk = 9*kBkSites*8;                 // link rows of a slot: 4608
 constexpr int kBkSpC = kBkSites*128;                // one colour of the spinors: 8192 B
 constexpr int kBkStage = kBkLk + 3*kBkSpC;          // 29184 B (a multiple of 128)
 constexpr int kBkSmem = kBkStages*kBkStage + 2*kBkStages*8;
-constexpr long long kBkWait = 2000000000ll;         // clock64 cycles before a wait gives up
+constexpr long long kBkWait = 2000000000ll;         // clock64 cycles the drain waits at most
 
 __device__ int g_bulk_err;                          // nonzero: a wait ran out
 
@@ -56,8 +59,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *b)
                :: "r"(smem_addr(b)) : "memory");
 }
 // wait for the completion of the phase of parity ph; false when it has not
-// completed within kBkWait cycles
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned ph)
+// completed within `limit` clock64 cycles
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned ph, long long limit)
 {
   const unsigned a = smem_addr(b);
   const long long t0 = clock64();
@@ -68,7 +71,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned ph)
                  "selp.u32 %0, 1, 0, p;\n\t}"
                  : "=r"(ok) : "r"(a), "r"(ph) : "memory");
     if(ok) return true;
-    if(clock64() - t0 > kBkWait) return false;
+    if(clock64() - t0 > limit) return false;
   }
 }
 // global -> shared bulk copy (16-byte aligned ends, size a multiple of 16)
@@ -133,7 +136,7 @@ stag_dslash_bulk(qllg_stag_args a)
         const unsigned use = cnt/kBkStages;
         // every lane waits (each takes the barrier's acquire); the outcome
         // is made warp-uniform so that the shuffles below stay converged
-        if(use > 0 && !__all_sync(0xffffffffu, mbar_wait(&empty[st], (use - 1) & 1))) {
+        if(use > 0 && !__all_sync(0xffffffffu, mbar_wait(&empty[st], (use - 1) & 1, a.wait_cycles))) {
           ok = false;
           break;
         }
@@ -176,9 +179,10 @@ stag_dslash_bulk(qllg_stag_args a)
     if(!ok) {
       atomicExch(&g_bulk_err, 1);
       // let the copies already issued (the last kBkStages uses) land before
-      // the block moves on
+      // the block moves on: this wait keeps the long fixed limit, whatever
+      // the pipeline's own (a copy in flight lands within microseconds)
       for(unsigned c = cnt > kBkStages ? cnt - kBkStages : 0; c < cnt; c++)
-        mbar_wait(&full[c % kBkStages], (c/kBkStages) & 1);
+        mbar_wait(&full[c % kBkStages], (c/kBkStages) & 1, kBkWait);
     }
   } else if(!skip) {
     // ----------------------------------------------------------- consumers
@@ -213,7 +217,7 @@ stag_dslash_bulk(qllg_stag_args a)
 #pragma unroll 1
       for(int sl=0; sl<16; sl++, cnt++) {
         const int st = cnt % kBkStages;
-        if(!__all_sync(0xffffffffu, mbar_wait(&full[st], (cnt/kBkStages) & 1))) { ok = false; break; }
+        if(!__all_sync(0xffffffffu, mbar_wait(&full[st], (cnt/kBkStages) & 1, a.wait_cycles))) { ok = false; break; }
         const unsigned char *stage = smem + st*kBkStage;
         Cx<T> U[9];
 #pragma unroll
@@ -333,6 +337,9 @@ int launch_bulk(const qllg_stag_args *a)
   qllg_stag_args A = *a;
   A.partial = a->rb ? a->rb->partial : NULL;
   A.counter = a->rb ? a->rb->counter : NULL;
+  // the pipeline's waits give up after the library's wait limit (polls of
+  // about 64 ns, so about 100 clock cycles each)
+  A.wait_cycles = (long long)(qllg_get_param("wait_polls")*100.0);
   stag_dslash_bulk<NR_><<<grid, kBkThreads, kBkSmem, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash_bulk launch");
 }

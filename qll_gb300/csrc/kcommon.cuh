@@ -242,6 +242,24 @@ template <int P> struct Spinor4 {
   }
 };
 template <> struct Spinor4<QLLG_F32> {
+  // the two consecutive rhs at idx (even): one 16-byte load per colour
+  template <typename T>
+  static __device__ __forceinline__ void load_pair(const void *b, size_t stride, size_t idx,
+                                                   Cx<T> v[2][3]) {
+#pragma unroll
+    for(int c=0; c<3; c++) {
+      float4 q = __ldg((const float4 *)((const float2 *)b + c*stride + idx));
+      v[0][c].r = q.x; v[0][c].i = q.y; v[1][c].r = q.z; v[1][c].i = q.w;
+    }
+  }
+  template <typename T>
+  static __device__ __forceinline__ void store_pair(void *b, size_t stride, size_t idx,
+                                                    const Cx<T> v[2][3]) {
+#pragma unroll
+    for(int c=0; c<3; c++)
+      *(float4 *)((float2 *)b + c*stride + idx) =
+        make_float4((float)v[0][c].r, (float)v[0][c].i, (float)v[1][c].r, (float)v[1][c].i);
+  }
   // rhs 2h and 2h+1 only: one 16-byte load per colour
   template <typename T>
   static __device__ __forceinline__ void load_half(const void *b, size_t stride, size_t idx0, int h,
@@ -481,7 +499,8 @@ template <int NRED, int R>
 __device__ __forceinline__ bool grid_reduce_mr(double (&val)[NRED][R], int nrhs, int Q,
                                                double *partial, unsigned *counter,
                                                double *shm /* NRED*R*blockDim */,
-                                               double *result[NRED], int ntr = 0) {
+                                               double *result[NRED], int ntr = 0,
+                                               bool pairs = false) {
   const int tid = threadIdx.x, nt = ntr ? ntr : blockDim.x;
   const bool in = tid < nt;
   if(in) {
@@ -493,7 +512,11 @@ __device__ __forceinline__ bool grid_reduce_mr(double (&val)[NRED][R], int nrhs,
   __syncthreads();
   {
     const int K = NRED*nrhs, J = nt/K, c = tid % K, l = tid / K;
-    const int n = c / nrhs, r = c % nrhs, j = r % R, qq = r / R;
+    const int n = c / nrhs, r = c % nrhs;
+    // thread q of a site holds rhs q*R + j, or with pairs the rhs pairs
+    // h*2Q + 2q (+1), j = 2h (+1)
+    const int j = pairs ? 2*(r/(2*Q)) + (r & 1) : r % R;
+    const int qq = pairs ? (r % (2*Q))/2 : r / R;
     double s = 0;
     if(in) for(int i=l; i<nt/Q; i+=J) s += shm[(n*R + j)*nt + qq + Q*i];
     __syncthreads();

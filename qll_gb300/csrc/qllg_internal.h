@@ -166,6 +166,8 @@ typedef struct {
   int one_path;          /* multi-rhs Dslash: always the slot loop with the
                             active checks (one code path) */
   int no_tune;           /* caller must not allocate: no autotuning */
+  long long wait_cycles; /* bulk-copy pipeline: clock cycles a wait takes
+                            before it gives up with an error */
   int preload;           /* load every launch shape's kernel of these
                             precisions and slot count (each launcher's
                             occupancy query loads its kernel) and launch
@@ -220,6 +222,33 @@ typedef struct qllg_cg_scalars_s {
   int loops;                    /* graph-loop trips (safety cap) */
   int loop_limit;
 } qllg_cg_scalars;
+
+/* ---------------------------------------------------- persistent CG */
+/* one cooperative launch runs the CG loop (k_cgp.cu) on a small lattice:
+ * FP64 iterations (mixed 0), or FP32 iterations with FP64 reliable updates
+ * (mixed 1); x, r, p, v in the iteration precision, x64, r64, w64 and b
+ * in FP64.  The scalars (sc) must hold an initialised solve (cg_init or
+ * mcg_init); on return they hold the result.  partial: at least
+ * qllg_cgp_partial_bytes(grid) bytes; bar: two unsigned words, zero at
+ * rest; err: set to 1 when a barrier wait ran out after poll_limit polls
+ * (extra: arrivals expected beyond the grid, nonzero only to make the
+ * waits run out in a test) */
+typedef struct {
+  qllg_geom g;
+  int nslots, fb, mixed, reortho, nrhs;
+  const void *links, *links64;
+  const float *lscale;
+  void *x, *r, *p, *v, *x64, *r64, *w64;
+  const void *b;
+  struct qllg_cg_scalars_s *sc;
+  double *partial;
+  unsigned *bar;
+  int *err;
+  long long poll_limit;
+  int extra, trips;
+} qllg_cgp_args;
+int qllg_k_cg_persistent(const qllg_cgp_args *a, int *grid_out);
+size_t qllg_cgp_partial_bytes(int grid);
 
 /* ------------------------------------------ mixed-precision CG kernels */
 /* start: r64 = b, x64 = 0, rs = b (sloppy prec ps), xs = 0 (prec px),

@@ -289,6 +289,14 @@ static struct { const char *name; double value; } g_params[] = {
                                       against 14.8 ms at 0.1) */
   {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
   {"graph", 1},              /* run solver iterations as one CUDA graph launch */
+  {"persistent", 1},         /* small lattices: the whole CG loop in one cooperative
+                                launch (FP64, or FP32 with FP64 reliable updates) */
+  {"persistent_max", 65536}, /* ... when even sites x rhs is at most this */
+  {"wait_polls", 2e7},       /* polls (about 64 ns apart) a grid-barrier wait takes
+                                before it gives up with an error: about a second */
+  {"cg_barrier_extra", 0},   /* arrivals a persistent-CG barrier expects beyond the
+                                grid: nonzero only in a test that makes the waits
+                                run out */
   {"poll", 8},               /* first batch of iterations between host checks */
   {"dslash_mr", 1},          /* multi-rhs Dslash: one thread per site and 4 rhs */
   {"ru_compact", 1},         /* reliable-update Dslash over the flagged rhs only */
@@ -320,7 +328,7 @@ static struct { const char *name; double value; } g_params[] = {
                                 block of 256 threads per SM */
   {"dslash_split", 1},       /* multi-rhs Dslash: a slot loop without the active
                                 checks for launches with every rhs active */
-  {"dslash_variant", -1},    /* force a Dslash variant (0-14, qllg_autotune_report names
+  {"dslash_variant", -1},    /* force a Dslash variant (0-17, qllg_autotune_report names
                                 them); -1: autotuned */
   {"multishift_guess_rsq", 1e-10}, /* mixed multishift: the FP32 multishift CG
                                        goes to |r|^2 < this |b|^2 before the

@@ -26,7 +26,7 @@ int qllg_geom_from_layout(qllg_geom *g, const Layout *l);
 Layout *qllg_current_layout(void);
 
 enum { WS_X, WS_R, WS_P, WS_AP, WS_V, WS_B, WS_IO, WS_X64, WS_R64, WS_T64, WS_V64,
-       WS_PS, WS_OUT, WS_XDF, WS_N };
+       WS_PS, WS_OUT, WS_XDF, WS_CGP, WS_N };
 
 /* what one solver iteration launches */
 typedef struct {
@@ -62,6 +62,7 @@ struct qllg_stag {
   } graphs[6];
   int ngraph_next;
   int graph_body;          /* body of the graph the current solve launched, 0: none */
+  int used_persistent;     /* the last solve ran the persistent CG */
   unsigned char shared[QLLG_NLINKP]; /* links[p] belong to another operator */
   int recon_bad;           /* the Naik links are not reconstructible (reconstruct-12 refused) */
   int fb;                  /* single-stored: the nslots/2 forward slots only */
@@ -728,10 +729,75 @@ count_graph_trips(qllg_stag *S)
   S->graph_body = 0;
 }
 
+/* the persistent CG (one cooperative launch for the whole loop) takes the
+ * solve when the lattice is small enough for launch latency to dominate
+ * (sites x rhs up to persistent_max) and the precisions are ones it has:
+ * FP64 iterations, or FP32 iterations and links with FP64 reliable
+ * updates (intermediate ones in FP64 too, not double-float) */
+static int
+persistent_ok(const qllg_stag *S, const iter_ctx *c)
+{
+  if(qllg_get_param("persistent") == 0) return 0;
+  if((double)S->g.Vh*c->nrhs > qllg_get_param("persistent_max")) return 0;
+  if(c->mixed) return c->ps == QLLG_F32 && c->pl == QLLG_F32 && S->links[QLLG_F64];
+  return c->ps == QLLG_F64 && c->pl == QLLG_F64;
+}
+
+static int
+run_persistent(qllg_stag *S, const iter_ctx *c, int maxits)
+{
+  /* control words: barrier arrivals and generation, the error flag */
+  unsigned *ctl = ws_get(S, WS_CGP, 4*sizeof(unsigned));
+  if(!ctl) return -1;
+  if(qllg_check_cuda(cudaMemsetAsync(ctl, 0, 4*sizeof(unsigned), qllg_stream()),
+                     "persistent CG: control words")) return -1;
+  qllg_cgp_args a;
+  memset(&a, 0, sizeof(a));
+  a.g = S->g;
+  a.nslots = S->nslots;
+  a.fb = S->fb;
+  a.mixed = c->mixed;
+  a.reortho = c->reortho;
+  a.nrhs = c->nrhs;
+  a.links = S->links[c->pl];
+  a.links64 = S->links[QLLG_F64];
+  a.lscale = S->lscale;
+  a.x = c->x; a.r = c->r; a.p = c->p; a.v = c->v;
+  a.x64 = c->x64; a.r64 = c->r64; a.w64 = c->w64;
+  a.b = c->b;
+  a.sc = S->sc;
+  a.partial = S->rb.partial;
+  a.bar = ctl;
+  a.err = (int *)(ctl + 2);
+  a.poll_limit = (long long)qllg_get_param("wait_polls");
+  a.extra = (int)qllg_get_param("cg_barrier_extra");
+  a.trips = maxits + 2;
+  /* the launch takes at most 128 blocks, whose partials fit the
+   * operator's reduction buffer (checked here, before the launch) */
+  if(qllg_cgp_partial_bytes(128) > sizeof(double)*2*QLLG_MAXRHS*(size_t)S->rb.maxblocks) {
+    qllg_set_error("persistent CG: the reduction buffer is too small");
+    return -1;
+  }
+  int grid = 0;
+  if(qllg_k_cg_persistent(&a, &grid)) return -1;
+  int err = 0;
+  if(qllg_check_cuda(cudaMemcpyAsync(&err, ctl + 2, sizeof(int), cudaMemcpyDeviceToHost,
+                                     qllg_stream()), "persistent CG: error flag") ||
+     qllg_sync()) return -1;
+  if(err) {
+    qllg_set_error("persistent CG: a grid barrier wait ran out (%lld polls)", a.poll_limit);
+    return -1;
+  }
+  S->used_persistent = 1;
+  return 0;
+}
+
 static int
 run_loop(qllg_stag *S, const iter_ctx *c, int maxits)
 {
   S->graph_body = 0;
+  S->used_persistent = 0;
+  if(persistent_ok(S, c)) return run_persistent(S, c, maxits);
   if(qllg_get_param("graph") != 0 && !qllg_timing_on()) {
     /* one iteration launched directly first: every kernel of the body is
      * then loaded before the capture starts */
@@ -1296,6 +1362,13 @@ qllg_stag_dslash_norm2_noalloc(qllg_stag *S, int prec, int nrhs, int out_parity,
   A.rb = &rb;
   A.no_tune = 1;              /* tuning would allocate a side buffer */
   return qllg_k_stag_dslash(prec, prec, &A);
+}
+
+/* 1 when the operator's last solve ran as one persistent launch */
+int
+qllg_stag_last_solve_persistent(const qllg_stag *S)
+{
+  return S ? S->used_persistent : 0;
 }
 
 /* bytes of a device vector of nrhs rhs in precision prec (one parity) */
