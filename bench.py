@@ -606,8 +606,8 @@ def run_serving(args):
 
     # capacity: all requests queued at t = 0
     V = server()
-    recs, t_sat = serve.poisson_load(V, SERVE_LATTICES, rate=1e9, nreq=args.serve_requests//2,
-                                     seed=11)
+    recs, t_sat = serve.poisson_load(V, SERVE_LATTICES, rate=1e9,
+                                     nreq=min(60, args.serve_requests//2), seed=11)
     cap = len(recs)/t_sat
     V.close()
     # Poisson arrivals at 70% of the capacity
@@ -652,6 +652,7 @@ def run_serving(args):
         "latency_p50_s": float(np.percentile(lat, 50)),
         "latency_p99_s": float(np.percentile(lat, 99)),
         "latency_max_s": float(lat.max()),
+        "failed_requests": int(sum(1 for r in recs if r["status"] != 2)),
         "max_true_rsq_over_tol2": worst,
         "hbm_budget_bytes": st.budget_bytes, "hbm_used_bytes_end": st.used_bytes,
         "chunk_iters": args.serve_chunk,
@@ -1000,7 +1001,7 @@ def main():
     ap.add_argument("--multishift", action="store_true", help="only the multishift benchmark")
     ap.add_argument("--wilson", action="store_true", help="only the Wilson benchmark")
     ap.add_argument("--wilson-dims", default="16,16,16,32", help="lattice of the Wilson benchmark")
-    ap.add_argument("--serve-requests", type=int, default=36)
+    ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--serve-budget", type=float, default=48.0, help="GiB")
     ap.add_argument("--serve-chunk", type=int, default=20)
     args = ap.parse_args()

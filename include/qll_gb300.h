@@ -231,7 +231,9 @@ int qllg_wilson_solve(qllg_wilson *W, void *x, const void *b, double mass, doubl
 typedef struct qllg_server qllg_server;
 
 typedef struct {
-  int status;              /* 0 queued, 1 running, 2 done */
+  int status;              /* 0 queued, 1 running, 2 done, 3 failed: a shift
+                              ended without meeting the tolerance (a source
+                              that is not a number, or the iteration limit) */
   int ncol;                /* shifts (columns) of the request */
   int iters[16];           /* iterations per shift */
   double true_rsq[16];     /* |b - A x|^2/|b|^2 per shift, FP64 */
@@ -256,7 +258,10 @@ int qllg_server_add_lattice(qllg_server *V, qllg_stag *S);
 int qllg_server_submit(qllg_server *V, int lattice, double mass, int nshift, const double *shifts,
                        double tol, const double *src, double *const out[]);
 /* one scheduling pass (retire, admit, launch); never waits for the GPU.
- * Returns the number of requests completed in this pass, or -1. */
+ * Returns the number of requests completed (done or failed) in this pass,
+ * or -1 with qllg_last_error() set.  A failure while creating a batch (a
+ * device allocation) leaves the queued requests queued: a later step
+ * admits them. */
 int qllg_server_step(qllg_server *V);
 int qllg_server_pending(const qllg_server *V);
 int qllg_server_request(const qllg_server *V, int id, qllg_request_info *info);
@@ -276,7 +281,9 @@ void qllg_server_destroy(qllg_server *V);
  *    wait of the persistent CG takes before the solve fails with an error
  *    instead of hanging), "cg_barrier_extra" (0: arrivals its barriers
  *    expect beyond the grid; nonzero only to make the waits run out in a
- *    test);
+ *    test); "fail_alloc_at" (0: off; n: the library's device allocation
+ *    number n, counted by qllg_device_alloc_count, fails as cudaMalloc
+ *    would, for tests of the failure paths);
  *  "ru_compact" (1: reliable updates over the flagged rhs only), "ru_df" (1:
  *    intermediate reliable updates in double-float, final ones in FP64),
  *    "df_blocks" (3: register cap of the double-float kernel);

@@ -186,6 +186,13 @@ qllg_dmalloc(size_t bytes)
   void *p = NULL;
   if(bytes == 0) bytes = 16;
   g_dallocs++;
+  /* a failure injected by tests (parameter fail_alloc_at): allocation
+   * number n fails as cudaMalloc would, without touching the device */
+  const double fail_at = qllg_get_param("fail_alloc_at");
+  if(fail_at > 0 && (double)g_dallocs == fail_at) {
+    qllg_set_error("cudaMalloc(%zu bytes): injected failure", bytes);
+    return NULL;
+  }
   cudaError_t e = cudaMalloc(&p, bytes);
   if(e != cudaSuccess) {
     qllg_set_error("cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
@@ -294,6 +301,9 @@ static struct { const char *name; double value; } g_params[] = {
   {"persistent_max", 65536}, /* ... when even sites x rhs is at most this */
   {"wait_polls", 2e7},       /* polls (about 64 ns apart) a grid-barrier wait takes
                                 before it gives up with an error: about a second */
+  {"fail_alloc_at", 0},      /* tests: the library's device allocation number n
+                                (qllg_device_alloc_count() + 1 = the next) fails
+                                as cudaMalloc would; 0: off */
   {"cg_barrier_extra", 0},   /* arrivals a persistent-CG barrier expects beyond the
                                 grid: nonzero only in a test that makes the waits
                                 run out */

@@ -40,10 +40,13 @@
 #define MAXLAT 16
 #define MAXBATCH 64
 
-enum { REQ_QUEUED = 0, REQ_RUNNING = 1, REQ_DONE = 2 };
+/* a request ends DONE when every shift met its tolerance, FAILED when one
+ * did not (a source or solution that is not a number, or the iteration
+ * limit); either way its columns are freed and its batch-mates go on */
+enum { REQ_QUEUED = 0, REQ_RUNNING = 1, REQ_DONE = 2, REQ_FAILED = 3 };
 
 typedef struct {
-  int lattice, ncol, state, batch, left;
+  int lattice, ncol, state, batch, left, failed;
   double mass[NCOL], tol;
   const double *src;
   double *out[NCOL];
@@ -224,11 +227,14 @@ batch_harvest(qllg_server *V, int i)
     int k = B->col_k[c];
     if(qllg_batch_retire(B->S, c, R->out[k])) return -1;
     R->iters[k] = h->iters[c];
-    R->true_rsq[k] = h->bsq[c] > 0 ? h->rsq[c]/h->bsq[c] : 0;
+    /* |b|^2 is 0 only for a zero source (x = 0 is exact); a source that is
+     * not a number leaves NaN here */
+    R->true_rsq[k] = h->bsq[c] > 0 || h->bsq[c] != h->bsq[c] ? h->rsq[c]/h->bsq[c] : 0;
+    if(!(R->true_rsq[k] < R->tol*R->tol)) R->failed = 1;
     B->col_req[c] = -1;
     B->nfree++;
     if(--R->left == 0) {
-      R->state = REQ_DONE;
+      R->state = R->failed ? REQ_FAILED : REQ_DONE;
       R->t_done = now_s();
       done++;
     }
@@ -288,7 +294,7 @@ qllg_server_step(qllg_server *V)
   {
     int blocked[MAXLAT] = {0};
     int starving = -1;
-    while(V->first_open < V->nreq && V->req[V->first_open].state == REQ_DONE) V->first_open++;
+    while(V->first_open < V->nreq && V->req[V->first_open].state >= REQ_DONE) V->first_open++;
     for(int r=V->first_open; r<V->nreq; r++) {
       req_t *R = &V->req[r];
       if(R->state != REQ_QUEUED || blocked[R->lattice]) continue;
@@ -330,7 +336,7 @@ int
 qllg_server_pending(const qllg_server *V)
 {
   int n = 0;
-  for(int r=V->first_open; r<V->nreq; r++) n += V->req[r].state != REQ_DONE;
+  for(int r=V->first_open; r<V->nreq; r++) n += V->req[r].state < REQ_DONE;
   return n;
 }
 
@@ -347,7 +353,7 @@ qllg_server_request(const qllg_server *V, int id, qllg_request_info *info)
     info->true_rsq[k] = R->true_rsq[k];
   }
   if(R->state != REQ_QUEUED) info->seconds_queued = R->t_start - R->t_submit;
-  if(R->state == REQ_DONE) info->seconds_total = R->t_done - R->t_submit;
+  if(R->state >= REQ_DONE) info->seconds_total = R->t_done - R->t_submit;
   return 0;
 }
 

@@ -172,6 +172,7 @@ def poisson_load(server, lattices, rate, nreq, seed=7, tol_choices=(1e-8, 1e-10)
         server.step()
     for r in recs:
         inf = server.info(r["id"])
+        r["status"] = inf.status
         r["latency_s"] = inf.seconds_total
         r["queued_s"] = inf.seconds_queued
         r["iters"] = max(inf.iters[:inf.ncol])

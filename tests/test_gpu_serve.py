@@ -7,6 +7,8 @@ involves another column, so a request must give exactly the same solution
 and iteration counts alone and in the mix (whatever column it lands in and
 whenever it is admitted).  Accuracy: every shift reaches the requested
 true residual, and one shift is compared with the oracle's FP64 CG."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -136,4 +138,61 @@ def test_refused_requests():
     qll.load().qllg_clear_error()
     assert V.submit(0, 0.0, [], 1e-8, src) == -1
     qll.load().qllg_clear_error()
+    _close(V, ops)
+
+
+def test_nan_request_fails_alone():
+    """a request whose host source holds a NaN ends FAILED (status 3) while
+    the request sharing its batch converges bitwise as it does alone"""
+    src = _src(LATS[1], 7100)
+    V, ops = _server()
+    rid = V.submit(PROBE["lattice"], PROBE["mass"], PROBE["shifts"], PROBE["tol"], src)
+    V.drain()
+    alone = [x.copy() for x in V.result(rid)]
+    its_alone = list(V.info(rid).iters[:V.info(rid).ncol])
+    _close(V, ops)
+
+    V, ops = _server()
+    bad = _src(LATS[1], 7101)
+    bad[17, 3] = np.nan
+    rbad = V.submit(PROBE["lattice"], 0.07, [0.0, 1e-2], 1e-8, bad)
+    rid = V.submit(PROBE["lattice"], PROBE["mass"], PROBE["shifts"], PROBE["tol"], src)
+    assert rbad >= 0 and rid >= 0, qll.last_error()
+    busy = []
+    V.drain(on_step=lambda s: busy.append(s.stats().busy_columns))
+    assert max(busy) >= len(PROBE["shifts"]) + 1         # they shared a batch
+    assert V.info(rbad).status == 3
+    inf = V.info(rid)
+    assert inf.status == 2
+    assert list(inf.iters[:inf.ncol]) == its_alone
+    for k, x in enumerate(V.result(rid)):
+        assert np.array_equal(x, alone[k]), k
+    _close(V, ops)
+
+
+def test_allocation_failure_at_batch_creation_keeps_the_queue():
+    """a device allocation that fails while the first batch is made (an
+    injected cudaMalloc failure) fails that scheduling pass with an error
+    and leaves every request queued; the next passes admit and finish them"""
+    L = serve._lib()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_device_alloc_count.restype = ctypes.c_ulonglong
+    V, ops = _server()
+    ids = [V.submit(j % 2, 0.05 + 0.01*j, [0.0, 1e-2], 1e-8, _src(LATS[j % 2], 7500 + j))
+           for j in range(3)]
+    L.qllg_set_param(b"fail_alloc_at", float(L.qllg_device_alloc_count() + 1))
+    try:
+        with pytest.raises(RuntimeError, match="injected failure"):
+            V.step()
+    finally:
+        L.qllg_set_param(b"fail_alloc_at", 0.0)
+    L.qllg_clear_error()
+    assert V.pending() == 3
+    assert all(V.info(i).status == 0 for i in ids)
+    assert V.stats().batches == 0
+    V.drain()
+    for i in ids:
+        inf = V.info(i)
+        assert inf.status == 2
+        assert all(inf.true_rsq[k] < 1e-16 for k in range(inf.ncol))
     _close(V, ops)
