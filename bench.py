@@ -427,10 +427,52 @@ def wilson_links_host(dims, seed, eps, c=0.5):
     return u
 
 
+def wilson_dslash_timing(L, W, dims, prec, launches=50):
+    """event-timed half Wilson Dslash (the hop term, odd output sites) on
+    random device vectors: ms per launch and GB/s on two byte bases per
+    output site, compulsory (8 links + 1 spinor load + 1 store: the bytes
+    DRAM must move when neighbours come from cache) and the lattice
+    convention (8 links + 8 neighbour loads + 1 store)"""
+    import torch
+    from qll_gb300 import qll
+    L.qllg_wilson_vec_bytes.restype = ctypes.c_size_t
+    L.qllg_wilson_vec_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.qllg_wilson_dslash_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.c_void_p]
+    stream = torch.cuda.current_stream()
+    L.qllg_set_stream(ctypes.c_void_p(stream.cuda_stream))
+    nb = L.qllg_wilson_vec_bytes(W, prec)
+    dt = torch.float64 if prec == 0 else torch.float32
+    src = torch.randn(nb//(8 if prec == 0 else 4), dtype=dt, device="cuda")
+    dst = torch.empty_like(src)
+    for _ in range(3):
+        if L.qllg_wilson_dslash_device(W, prec, 1, ctypes.c_void_p(dst.data_ptr()),
+                                       ctypes.c_void_p(src.data_ptr())):
+            raise RuntimeError(qll.last_error())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(launches):
+        L.qllg_wilson_dslash_device(W, prec, 1, ctypes.c_void_p(dst.data_ptr()),
+                                    ctypes.c_void_p(src.data_ptr()))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)/launches
+    b = 8 if prec == 0 else 4
+    Vh = int(np.prod(dims))//2
+    comp = (8*18*b + 2*24*b)*Vh
+    conv = (8*18*b + 9*24*b)*Vh
+    return {"dims": list(dims), "prec": "f64" if prec == 0 else "f32", "ms": ms,
+            "compulsory_gbs": comp/(ms*1e-3)/1e9, "lattice_convention_gbs": conv/(ms*1e-3)/1e9,
+            "gflops": 1344*Vh/(ms*1e-3)/1e9, "bytes_compulsory": comp}
+
+
 def run_wilson(args):
     """C2: Wilson even-odd CGNR at 16^3x32 (--wilson-dims for another lattice), eps=0.3, kappa=0.12 (QLL mass
     1/(2 kappa) - 4), Gaussian 4x3 source, tolerance 1e-8: FP32 iterations
-    with FP64 reliable updates against the plain FP64 CG"""
+    with FP64 reliable updates against the plain FP64 CG, each solve one
+    CUDA-graph launch; and the half Wilson Dslash timed alone at C2 and at
+    32^3x64, with its roofline"""
     from qll_gb300 import qll
     L = qll.load()
     apply_params(L, args)
@@ -447,40 +489,64 @@ def run_wilson(args):
     if not W.value:
         raise RuntimeError(qll.last_error())
     b = qll.gen_source(dims, 2200, 24, "even")
-    Vh = b.shape[0]//2
     out = {"workload": "C2: Wilson e/o CGNR %s, eps=0.3, kappa=0.12, true residual 1e-8 "
                        "(normal-equation rsq 1e-17)" % "x".join(map(str, dims))}
+
+    def solve(mode, timing):
+        x = np.zeros_like(b)
+        info = qll.SolveInfo()
+        L.qllg_timing_enable(1 if timing else 0)
+        L.qllg_timing_reset()
+        t = time.time()
+        # CGNR stops on the normal-equation residual |S^+ r|^2 < rsq |S^+ b|^2;
+        # 1e-17 there puts the true residual |b - S x|/|b| below 1e-8
+        its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, 1e-17, MAXITS, mode,
+                                  ctypes.byref(info))
+        dt = time.time() - t
+        cnt, tot = ctypes.c_int(), ctypes.c_double()
+        L.qllg_timing_read(b"wilson_dslash", ctypes.byref(cnt), ctypes.byref(tot))
+        L.qllg_timing_enable(0)
+        if its < 0:
+            raise RuntimeError(qll.last_error())
+        return dt, its, info, cnt.value, tot.value
+
     for name, mode in (("mixed", qll.SOLVE_MIXED_SINGLE), ("fp64", qll.SOLVE_DOUBLE)):
         best = None
-        for rep in range(2):
-            x = np.zeros_like(b)
-            info = qll.SolveInfo()
-            L.qllg_timing_enable(1)
-            L.qllg_timing_reset()
-            t = time.time()
-            # CGNR stops on the normal-equation residual |S^+ r|^2 < rsq |S^+ b|^2;
-            # 1e-17 there puts the true residual |b - S x|/|b| below 1e-8
-            its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, 1e-17, MAXITS, mode,
-                                      ctypes.byref(info))
-            dt = time.time() - t
-            cnt, tot = ctypes.c_int(), ctypes.c_double()
-            L.qllg_timing_read(b"wilson_dslash", ctypes.byref(cnt), ctypes.byref(tot))
-            L.qllg_timing_enable(0)
-            if its < 0:
-                raise RuntimeError(qll.last_error())
+        for rep in range(3):
+            dt, its, info, _, _ = solve(mode, False)
             if best is None or dt < best["seconds"]:
                 best = {"seconds": dt, "solves_per_s": 1/dt, "iters": its,
-                        "true_rsq": info.true_rsq[0], "dslash_launches": cnt.value,
-                        "dslash_avg_ms": tot.value/max(cnt.value, 1)}
+                        "true_rsq": info.true_rsq[0], "loop": "one CUDA-graph launch"}
+        # the half-Dslash launches of one more solve, event-timed (a host-
+        # polled loop: events cannot sit in a graph's conditional body)
+        _, _, _, cnt, tot = solve(mode, True)
+        best["dslash_launches"] = cnt
+        best["dslash_avg_ms"] = tot/max(cnt, 1)
         out[name] = best
-    # Wilson half-Dslash algorithmic bytes per output site (the lattice
-    # convention, no neighbour reuse): 8 links + 8 neighbour spinors + 1
-    # store; the mixed solve's launches are mostly FP32
-    f = out["mixed"]
-    f["dslash_note"] = "avg over the solve's FP32 and FP64 half-Dslash launches"
-    out["fp64"]["dslash_gbs"] = (8*18*8 + 9*24*8)*Vh/(out["fp64"]["dslash_avg_ms"]*1e-3)/1e9
+    out["mixed"]["dslash_note"] = "avg over the solve's FP32 and FP64 half-Dslash launches"
     out["speedup_mixed_over_fp64"] = out["fp64"]["seconds"]/out["mixed"]["seconds"]
+    # the half Dslash alone: C2 in FP32 and FP64, and FP32 at 32^3x64
+    out["dslash_c2_f32"] = wilson_dslash_timing(L, W, dims, 1)
+    out["dslash_c2_f64"] = wilson_dslash_timing(L, W, dims, 0)
     L.qllg_wilson_destroy(W)
+    big = (32, 32, 32, 64)
+    ub = wilson_links_host(big, 1004, 0.3)
+    W = ctypes.c_void_p(L.qllg_wilson_create(qll.dims_c(big), qll.vp_array(ub)))
+    del ub
+    if not W.value:
+        raise RuntimeError(qll.last_error())
+    d32 = wilson_dslash_timing(L, W, big, 1)
+    L.qllg_wilson_destroy(W)
+    out["dslash_32x32x32x64_f32"] = d32
+    pk = peaks().get("hbm_gbs")
+    out["roofline"] = {"kernel": "wilson_dslash<f32> half Dslash, 32^3x64 (inputs larger than L2)",
+                       "bound": "hbm", "achieved": d32["compulsory_gbs"], "peak": pk, "unit": "GB/s",
+                       "frac": d32["compulsory_gbs"]/pk if pk else None,
+                       "basis": "compulsory bytes per output site: 8 links + 1 spinor load + "
+                                "1 store (768 B in FP32)",
+                       "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else None,
+                       "c2_note": "at 16^3x32 the links and spinors (66 MB FP32) fit in L2, so "
+                                  "its GB/s are not an HBM figure"}
     return out
 
 

@@ -207,11 +207,19 @@ void qllg_wilson_destroy(qllg_wilson *W);
 /* x = massp*y + W y on sub (massp already massFac*(4+m)); dag: g5 W g5 */
 int qllg_wilson_dslash(qllg_wilson *W, void *x, double massp, const void *y, const char *sub,
                        int dag);
+/* the massless Wilson hop term of one parity, out = W in on the output
+ * sites of out_parity, on device vectors in the library layout ([12][Vh]
+ * complex, FP64 or FP32 by prec 0 or 1; qllg_wilson_vec_bytes gives the
+ * size); links of that precision are derived from FP64 on first use */
+int qllg_wilson_dslash_device(qllg_wilson *W, int prec, int out_parity, void *out_dev,
+                              const void *in_dev);
+size_t qllg_wilson_vec_bytes(const qllg_wilson *W, int prec);
 /* even-odd normal-equation solve of the Schur complement
  * S = (4+m) - W_eo W_oe/(4+m): CG on S^dagger S x = S^dagger b, stopping at
  * |r|^2 < rsq |S^dagger b|^2; mode QLLG_SOLVE_DOUBLE or
  * QLLG_SOLVE_MIXED_SINGLE; x, b host [V][24] FP64, even half; info->true_rsq
- * is |b - S x|^2/|b|^2 in FP64 */
+ * is |b - S x|^2/|b|^2 in FP64.  The iterations run as one CUDA-graph
+ * launch (parameter "graph"; kernel timing on: a host-polled loop) */
 int qllg_wilson_solve(qllg_wilson *W, void *x, const void *b, double mass, double rsq,
                       int maxits, int mode, qllg_solve_info *info);
 

@@ -31,6 +31,8 @@ Layout *qllg_current_layout(void);
 enum { WW_X, WW_R, WW_P, WW_AP, WW_S, WW_V, WW_B, WW_X64, WW_R64, WW_T64, WW_S64, WW_V64,
        WW_XDF, WW_IO, WW_N };
 
+#define WGRAPHS 4
+
 struct qllg_wilson {
   qllg_geom g;
   int master;
@@ -40,12 +42,19 @@ struct qllg_wilson {
   void *ws[WW_N];
   size_t ws_bytes[WW_N];
   cudaEvent_t ev0, ev1;
+  /* captured CGNR loops, by what their launches bake in */
+  struct { long key[6]; cudaGraphExec_t exec; int body; } graphs[WGRAPHS];
+  int ngraph_next;
 };
+
+static void wgraphs_drop(qllg_wilson *W);
 
 static void *
 wws(qllg_wilson *W, int id, size_t bytes)
 {
   if(bytes <= W->ws_bytes[id]) return W->ws[id];
+  /* captured loops hold the old buffer's address */
+  wgraphs_drop(W);
   if(W->ws[id]) { qllg_sync(); qllg_dfree(W->ws[id]); }
   W->ws[id] = qllg_dmalloc(bytes);
   W->ws_bytes[id] = W->ws[id] ? bytes : 0;
@@ -82,6 +91,7 @@ qllg_wilson_destroy(qllg_wilson *W)
   if(W->hsc) cudaFreeHost(W->hsc);
   qllg_redbuf_free(&W->rb);
   for(int i=0; i<WW_N; i++) qllg_dfree(W->ws[i]);
+  for(int i=0; i<WGRAPHS; i++) if(W->graphs[i].exec) cudaGraphExecDestroy(W->graphs[i].exec);
   if(W->ev0) cudaEventDestroy(W->ev0);
   if(W->ev1) cudaEventDestroy(W->ev1);
   free(W);
@@ -172,6 +182,32 @@ whalf(qllg_wilson *W, int prec, int out_parity, const void *in, const void *self
 {
   return whalf_eq(W, prec, out_parity, in, self, out, mode, a0, b, norm_out, norm_self, active, 0,
                   done, dag);
+}
+
+/* out = W in on the output parity (the massless hop term of wilsonDslash,
+ * lib/wilsonDslash.c:21-179), device vectors in the library layout
+ * ([12][Vh] complex) of precision prec (0 FP64, 1 FP32) */
+int
+qllg_wilson_dslash_device(qllg_wilson *W, int prec, int out_parity, void *out_dev,
+                          const void *in_dev)
+{
+  if(!W || !out_dev || !in_dev) { qllg_set_error("wilson_dslash_device: null argument"); return -1; }
+  if(prec != QLLG_F64 && prec != QLLG_F32) {
+    qllg_set_error("wilson_dslash_device: precision %d", prec);
+    return -1;
+  }
+  if(out_parity != 0 && out_parity != 1) {
+    qllg_set_error("wilson_dslash_device: parity %d", out_parity);
+    return -1;
+  }
+  return whalf(W, prec, out_parity, in_dev, NULL, out_dev, 0, 0, 1, NULL, NULL, NULL, NULL, 0);
+}
+
+/* bytes of one parity of a Wilson device vector in precision prec */
+size_t
+qllg_wilson_vec_bytes(const qllg_wilson *W, int prec)
+{
+  return (prec == QLLG_F64 || prec == QLLG_F32) ? wvec(W, prec) : 0;
 }
 
 static int
@@ -293,6 +329,117 @@ apply_schur(qllg_wilson *W, int prec, const void *in, void *out, void *tmp, doub
   return apply_schur_eq(W, prec, in, out, tmp, a, dag, norm, active, 0, done);
 }
 
+/* what one CGNR iteration launches */
+typedef struct {
+  int ps;
+  double a;
+  void *xs, *r, *p, *Ap, *Sp, *v;
+  void *x64, *r64, *bp, *s64, *vv64, *t64, *xdf;
+} witer;
+
+/* one iteration of the CGNR on S^dagger S (the standard-form CG update,
+ * with the FP32 mode's reliable update of the flagged rhs); every launch
+ * returns at once when the solve is done, the reliable-update ones when
+ * no update is flagged */
+static int
+wilson_iteration(qllg_wilson *W, const witer *c)
+{
+  qllg_cg_scalars *sc = W->sc;
+  const int Vh = W->g.Vh, ps = c->ps;
+  const double a = c->a;
+  if(apply_schur(W, ps, c->p, c->Sp, c->v, a, 0, sc->pnorm, sc->active, &sc->done)) return -1;
+  if(apply_schur(W, ps, c->Sp, c->Ap, c->v, a, 1, NULL, sc->active, &sc->done)) return -1;
+  if(qllg_k_scg_update_xr(ps, ps, c->xs, c->r, c->p, c->Ap, Vh, 12, 1, sc, &W->rb)) return -1;
+  if(ps != QLLG_F64) {
+    if(qllg_k_mcg_accum(ps, c->x64, c->xs, Vh, 12, 1, sc)) return -1;
+    /* the double-float pass reuses s64, vv64 and t64 (same size); t
+     * goes back to FP64 in place */
+    if(c->xdf && (qllg_k_spinor_df(1, c->xdf, c->x64, Vh, 12, 1, sc->ru, 1, &sc->no_ru) ||
+                  apply_schur_eq(W, QLLG_DF, c->xdf, c->s64, c->vv64, a, 0, NULL, sc->ru, 1,
+                                 &sc->no_ru) ||
+                  apply_schur_eq(W, QLLG_DF, c->s64, c->t64, c->vv64, a, 1, NULL, sc->ru, 1,
+                                 &sc->no_ru) ||
+                  qllg_k_spinor_df(0, c->t64, c->t64, Vh, 12, 1, sc->ru, 1, &sc->no_ru)))
+      return -1;
+    const int eq = c->xdf ? 2 : 0;
+    if(apply_schur_eq(W, QLLG_F64, c->x64, c->s64, c->vv64, a, 0, NULL, sc->ru, eq, &sc->no_ru) ||
+       apply_schur_eq(W, QLLG_F64, c->s64, c->t64, c->vv64, a, 1, NULL, sc->ru, eq, &sc->no_ru))
+      return -1;
+    if(qllg_k_mcg_residual(ps, c->r64, c->r, c->bp, c->t64, Vh, 12, 1, 1, sc, &W->rb)) return -1;
+  }
+  return qllg_k_scg_update_p(ps, c->p, c->r, Vh, 12, 1, sc);
+}
+
+static void
+wgraphs_drop(qllg_wilson *W)
+{
+  for(int i=0; i<WGRAPHS; i++) {
+    if(W->graphs[i].exec) cudaGraphExecDestroy(W->graphs[i].exec);
+    W->graphs[i].exec = NULL;
+  }
+}
+
+/* a CUDA graph whose conditional WHILE node repeats one captured CGNR
+ * iteration until the done flag is set or the trip cap is reached (the
+ * staggered solver's loop_graph, for the Wilson iteration); cached by what
+ * the launches bake in: precision, a = 4 + m, the solution buffers */
+static cudaGraphExec_t
+wilson_graph(qllg_wilson *W, const witer *c, int *body_out)
+{
+  long abits;
+  memcpy(&abits, &c->a, sizeof(abits));
+  long key[6] = {c->ps, abits, (long)c->xs, (long)c->x64, (long)c->xdf, (long)c->bp};
+  for(int i=0; i<WGRAPHS; i++)
+    if(W->graphs[i].exec && !memcmp(W->graphs[i].key, key, sizeof(key))) {
+      *body_out = W->graphs[i].body;
+      return W->graphs[i].exec;
+    }
+  unsigned long long n0 = qllg_launch_count();
+  cudaGraph_t g = NULL;
+  cudaGraphExec_t exec = NULL;
+  cudaGraphConditionalHandle h;
+  cudaGraphNode_t node;
+  struct cudaGraphNodeParams np;
+  if(qllg_check_cuda(cudaGraphCreate(&g, 0), "graph create")) return NULL;
+  if(qllg_check_cuda(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault),
+                     "conditional handle")) goto fail;
+  memset(&np, 0, sizeof(np));
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  if(qllg_check_cuda(cudaGraphAddNode(&node, g, NULL, NULL, 0, &np), "conditional node")) goto fail;
+  if(qllg_capture_begin(np.conditional.phGraph_out[0])) goto fail;
+  {
+    int rc = wilson_iteration(W, c);
+    rc |= qllg_k_loop_cond((unsigned long long)h, &W->sc->done, &W->sc->loops,
+                           &W->sc->loop_limit);
+    rc |= qllg_capture_end(np.conditional.phGraph_out[0]);
+    if(rc) goto fail;
+  }
+  if(qllg_check_cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate")) goto fail;
+  cudaGraphDestroy(g);
+  {
+    /* the capture counted the body's launches without running them */
+    int body = (int)(qllg_launch_count() - n0);
+    qllg_launch_adjust(-(long long)body);
+    int i = W->ngraph_next;
+    W->ngraph_next = (i + 1) % WGRAPHS;
+    if(W->graphs[i].exec) cudaGraphExecDestroy(W->graphs[i].exec);
+    memcpy(W->graphs[i].key, key, sizeof(key));
+    W->graphs[i].exec = exec;
+    W->graphs[i].body = body;
+    *body_out = body;
+  }
+  return exec;
+fail:
+  if(qllg_capturing()) qllg_capture_end(np.conditional.phGraph_out[0]);
+  if(g) cudaGraphDestroy(g);
+  return NULL;
+}
+
+int qllg_timing_on(void);
+
 static int
 wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq, int maxits,
             int mode)
@@ -320,34 +467,29 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   memset(W->hsc, 0, sizeof(qllg_cg_scalars));
   W->hsc->rsq_stop[0] = rsq;
   W->hsc->maxits = maxits;
+  W->hsc->loop_limit = maxits + 2;
   const double delta = qllg_get_param("reliable_delta_single");
   W->hsc->delta2 = (ps == QLLG_F64) ? 0 : delta*delta;
   if(wpush(W)) return -1;
   qllg_cg_scalars *sc = W->sc;
   if(qllg_k_scg_init(ps, ps, xs, r, p, bp, ps == QLLG_F64 ? NULL : x64,
                      ps == QLLG_F64 ? NULL : r64, Vh, 12, 1, sc, &W->rb)) return -1;
+  witer c = {ps, a, xs, r, p, Ap, Sp, v, x64, r64, bp, s64, vv64, t64, xdf};
+  if(qllg_get_param("graph") != 0 && !qllg_timing_on()) {
+    /* one iteration launched directly first (every kernel of the body is
+     * then loaded before the capture), then the rest as one graph launch */
+    if(wilson_iteration(W, &c)) return -1;
+    int body = 0;
+    cudaGraphExec_t exec = wilson_graph(W, &c, &body);
+    if(!exec || qllg_check_cuda(cudaGraphLaunch(exec, qllg_stream()), "graph launch")) return -1;
+    if(wpull(W, 1)) return -1;
+    qllg_launch_adjust((long long)body*W->hsc->loops);
+    return W->hsc->iters[0];
+  }
   int issued = 0, batch = 8;
   while(issued < maxits) {
     int k = maxits - issued < batch ? maxits - issued : batch;
-    for(int it=0; it<k; it++) {
-      if(apply_schur(W, ps, p, Sp, v, a, 0, sc->pnorm, sc->active, &sc->done)) return -1;
-      if(apply_schur(W, ps, Sp, Ap, v, a, 1, NULL, sc->active, &sc->done)) return -1;
-      if(qllg_k_scg_update_xr(ps, ps, xs, r, p, Ap, Vh, 12, 1, sc, &W->rb)) return -1;
-      if(ps != QLLG_F64) {
-        if(qllg_k_mcg_accum(ps, x64, xs, Vh, 12, 1, sc)) return -1;
-        /* the double-float pass reuses s64, vv64 and t64 (same size); t
-         * goes back to FP64 in place */
-        if(xdf && (qllg_k_spinor_df(1, xdf, x64, Vh, 12, 1, sc->ru, 1, &sc->no_ru) ||
-                   apply_schur_eq(W, QLLG_DF, xdf, s64, vv64, a, 0, NULL, sc->ru, 1, &sc->no_ru) ||
-                   apply_schur_eq(W, QLLG_DF, s64, t64, vv64, a, 1, NULL, sc->ru, 1, &sc->no_ru) ||
-                   qllg_k_spinor_df(0, t64, t64, Vh, 12, 1, sc->ru, 1, &sc->no_ru))) return -1;
-        const int eq = xdf ? 2 : 0;
-        if(apply_schur_eq(W, QLLG_F64, x64, s64, vv64, a, 0, NULL, sc->ru, eq, &sc->no_ru) ||
-           apply_schur_eq(W, QLLG_F64, s64, t64, vv64, a, 1, NULL, sc->ru, eq, &sc->no_ru)) return -1;
-        if(qllg_k_mcg_residual(ps, r64, r, bp, t64, Vh, 12, 1, 1, sc, &W->rb)) return -1;
-      }
-      if(qllg_k_scg_update_p(ps, p, r, Vh, 12, 1, sc)) return -1;
-    }
+    for(int it=0; it<k; it++) if(wilson_iteration(W, &c)) return -1;
     issued += k;
     if(wpull(W, 0)) return -1;
     if(W->hsc->done) break;

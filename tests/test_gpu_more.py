@@ -449,3 +449,36 @@ def test_single_stored_operator_matches_double_stored():
         assert np.array_equal(sol[0][1][k], sol[1][1][k])
     L.qllg_stag_destroy(S1)
     L.qllg_stag_destroy(S2)
+
+
+@pytest.mark.parametrize("mode", [qll.SOLVE_DOUBLE, qll.SOLVE_MIXED_SINGLE])
+def test_wilson_cgnr_graph_matches_host_loop(mode):
+    """the CGNR loop captured as one CUDA-graph launch runs the same kernels
+    in the same order as the host-polled loop: bitwise the same solution
+    and iteration count"""
+    L = qll.load()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    L.qllg_wilson_create.restype = ctypes.c_void_p
+    L.qllg_wilson_create.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_void_p)]
+    L.qllg_wilson_solve.restype = c_int
+    L.qllg_wilson_solve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double,
+                                    c_double, c_int, c_int, ctypes.POINTER(qll.SolveInfo)]
+    dims = (8, 8, 8, 8)
+    u = list(wilson_links(dims))
+    W = L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(u))
+    assert W, qll.last_error()
+    b = qll.gen_source(dims, 24, 24, "even")
+    mass = 1/(2*0.12) - 4
+    out = []
+    for graph in (1, 0, 1):
+        L.qllg_set_param(b"graph", graph)
+        x = np.zeros_like(b)
+        info = qll.SolveInfo()
+        its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, 1e-16, 5000, mode,
+                                  byref(info))
+        assert its > 0, qll.last_error()
+        out.append((its, x))
+    L.qllg_set_param(b"graph", 1)
+    assert out[0][0] == out[1][0] == out[2][0]
+    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][1], out[2][1])
+    L.qllg_wilson_destroy(ctypes.c_void_p(W))
