@@ -280,6 +280,8 @@ void qllg_server_destroy(qllg_server *V);
  *  "reliable_delta" (0.1, 16-bit mixed mode),
  *  "reliable_delta_single" (0.01, FP32 mixed mode, staggered CG and Wilson
  *    CGNR): a reliable update when |r| falls by this factor;
+ *  "half_split" (0: the 16-bit mixed mode stores the Dslash operands and
+ *    the links in 16 bits; 1: only the links; 2: only the operands),
  *  "reortho" (1), "graph" (1: the solver loop as one CUDA-graph launch),
  *    "poll" (8: first batch of host-polled iterations);
  *  "persistent" (1: on small lattices the whole CG loop as one cooperative
@@ -291,7 +293,9 @@ void qllg_server_destroy(qllg_server *V);
  *    expect beyond the grid; nonzero only to make the waits run out in a
  *    test); "fail_alloc_at" (0: off; n: the library's device allocation
  *    number n, counted by qllg_device_alloc_count, fails as cudaMalloc
- *    would, for tests of the failure paths);
+ *    would, for tests of the failure paths); "bulk_wait_test" (0; 1: the
+ *    bulk-copy Dslash issues no copies, so that its consumers' waits run
+ *    out: a test of that error path);
  *  "ru_compact" (1: reliable updates over the flagged rhs only), "ru_df" (1:
  *    intermediate reliable updates in double-float, final ones in FP64),
  *    "df_blocks" (3: register cap of the double-float kernel);

@@ -10,6 +10,7 @@ extern "C" int qllg_k_stag_dslash_f32(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_i16(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_f32r(const qllg_stag_args *a);
 extern "C" int qllg_k_stag_dslash_df(const qllg_stag_args *a);
+extern "C" int qllg_k_stag_dslash_split(int ps, int pl, const qllg_stag_args *a);
 
 namespace {
 
@@ -44,6 +45,8 @@ qllg_k_stag_dslash(int ps, int pl, const qllg_stag_args *a)
   if(ps == QLLG_I16 && pl == QLLG_I16) return qllg_k_stag_dslash_i16(a);
   if(ps == QLLG_F32 && pl == QLLG_F32R) return qllg_k_stag_dslash_f32r(a);
   if(ps == QLLG_DF && pl == QLLG_DF) return qllg_k_stag_dslash_df(a);
+  if((ps == QLLG_F32 && pl == QLLG_I16) || (ps == QLLG_I16 && pl == QLLG_F32))
+    return qllg_k_stag_dslash_split(ps, pl, a);
   qllg_set_error("stag_dslash: unsupported precision pair %d/%d", ps, pl);
   return -1;
 }

@@ -125,6 +125,9 @@ stag_dslash_bulk(qllg_stag_args a)
   if(!skip && producer) {
     // ------------------------------------------------------------ producer
     unsigned cnt = 0;
+    // a test of the waits' error path: the producer issues nothing (so no
+    // copy is ever in flight) and the consumers' first waits run out
+    if(a.wait_test) ok = false;
     for(int tile=blockIdx.x; tile<ntiles && ok; tile+=gridDim.x) {
       const int site0 = tile*kBkSites;
       int x0[4], x1[4];
@@ -340,6 +343,7 @@ int launch_bulk(const qllg_stag_args *a)
   // the pipeline's waits give up after the library's wait limit (polls of
   // about 64 ns, so about 100 clock cycles each)
   A.wait_cycles = (long long)(qllg_get_param("wait_polls")*100.0);
+  A.wait_test = qllg_get_param("bulk_wait_test") != 0;
   stag_dslash_bulk<NR_><<<grid, kBkThreads, kBkSmem, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash_bulk launch");
 }

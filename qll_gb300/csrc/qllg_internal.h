@@ -168,6 +168,8 @@ typedef struct {
   int no_tune;           /* caller must not allocate: no autotuning */
   long long wait_cycles; /* bulk-copy pipeline: clock cycles a wait takes
                             before it gives up with an error */
+  int wait_test;         /* bulk-copy pipeline, tests only: the producer
+                            issues no copy, so the consumers' waits run out */
   int preload;           /* load every launch shape's kernel of these
                             precisions and slot count (each launcher's
                             occupancy query loads its kernel) and launch

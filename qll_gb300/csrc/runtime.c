@@ -295,12 +295,17 @@ static struct { const char *name; double value; } g_params[] = {
                                       for both, 13.0 ms per solve at 0.01
                                       against 14.8 ms at 0.1) */
   {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
+  {"half_split", 0},         /* MIXED_HALF solves: 0 16-bit Dslash operands and
+                                links, 1 16-bit links with FP32 operands, 2 FP32
+                                links with 16-bit operands */
   {"graph", 1},              /* run solver iterations as one CUDA graph launch */
   {"persistent", 1},         /* small lattices: the whole CG loop in one cooperative
                                 launch (FP64, or FP32 with FP64 reliable updates) */
   {"persistent_max", 65536}, /* ... when even sites x rhs is at most this */
   {"wait_polls", 2e7},       /* polls (about 64 ns apart) a grid-barrier wait takes
                                 before it gives up with an error: about a second */
+  {"bulk_wait_test", 0},     /* tests: the bulk-copy Dslash's producer issues no copy,
+                                so its consumers' bounded waits run out */
   {"fail_alloc_at", 0},      /* tests: the library's device allocation number n
                                 (qllg_device_alloc_count() + 1 = the next) fails
                                 as cudaMalloc would; 0: off */

@@ -1119,10 +1119,15 @@ solve_dev(qllg_stag *S, int nrhs, void *x, const void *b, const double mass[], d
   case QLLG_SOLVE_SINGLE:
     its = cg_plain(S, QLLG_F32, nrhs, x, b, mass, rsq, maxits);
     break;
-  case QLLG_SOLVE_MIXED_HALF:
-    its = cg_mixed(S, QLLG_I16, QLLG_F32, QLLG_I16, nrhs, x, b, mass, rsq, maxits,
-                   qllg_get_param("reliable_delta"), 0);
+  case QLLG_SOLVE_MIXED_HALF: {
+    /* half_split: 0 16-bit Dslash operands and links, 1 16-bit links with
+     * FP32 operands, 2 FP32 links with 16-bit operands */
+    const int split = (int)qllg_get_param("half_split");
+    const int ps = split == 1 ? QLLG_F32 : QLLG_I16, pl = split == 2 ? QLLG_F32 : QLLG_I16;
+    its = cg_mixed(S, ps, QLLG_F32, pl, nrhs, x, b, mass, rsq, maxits,
+                   qllg_get_param(split == 1 ? "reliable_delta_single" : "reliable_delta"), 0);
     break;
+  }
   case QLLG_SOLVE_MIXED_SINGLE:
     its = cg_mixed(S, QLLG_F32, QLLG_F32, f32_links(S), nrhs, x, b, mass, rsq, maxits,
                    qllg_get_param("reliable_delta_single"), 0);

@@ -94,10 +94,11 @@ def test_barrier_wait_runs_out_with_an_error():
 
 
 def test_bulk_pipeline_wait_runs_out_with_an_error():
-    """the bulk-copy pipeline's waits take the same limit: at zero the first
-    wait gives up at once, the launch records the error flag and returns,
-    and with the default limit the same launch is bitwise the register
-    kernel's"""
+    """the bulk-copy pipeline's waits take the same limit: with its
+    producer told to issue no copy (bulk_wait_test) the consumers' first
+    waits run out after the limit, the launch records the error flag and
+    returns; with copies issued again the same launch is bitwise the
+    register kernel's"""
     torch = pytest.importorskip("torch")
     L, S, u, u3 = _op()
     try:
@@ -110,19 +111,21 @@ def test_bulk_pipeline_wait_runs_out_with_an_error():
         src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
         outs = []
         assert L.qllg_k_bulk_error(1) >= 0
-        for variant, polls in ((11, 0), (11, 2e7), (10, 2e7)):
+        for variant, test in ((11, 1), (11, 0), (10, 0)):
             L.qllg_set_param(b"dslash_variant", variant)
-            L.qllg_set_param(b"wait_polls", polls)
+            L.qllg_set_param(b"bulk_wait_test", test)
+            L.qllg_set_param(b"wait_polls", 2e5 if test else 2e7)
             dst = torch.zeros_like(src)
             torch.cuda.synchronize()
             rc = L.qllg_stag_dslash_device(S, 1, 16, 1, ctypes.c_void_p(dst.data_ptr()),
                                            ctypes.c_void_p(src.data_ptr()))
             torch.cuda.synchronize()
             L.qllg_set_param(b"dslash_variant", -1)
+            L.qllg_set_param(b"bulk_wait_test", 0)
             L.qllg_set_param(b"wait_polls", 2e7)
             assert rc == 0, qll.last_error()
             outs.append((L.qllg_k_bulk_error(1), dst))
-        assert outs[0][0] == 1           # the zero limit ran out
+        assert outs[0][0] == 1           # the waits ran out
         assert outs[1][0] == 0 and outs[2][0] == 0
         assert torch.equal(outs[1][1], outs[2][1])
     finally:
