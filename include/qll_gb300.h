@@ -280,8 +280,9 @@ void qllg_server_destroy(qllg_server *V);
  *  "reliable_delta" (0.1, 16-bit mixed mode),
  *  "reliable_delta_single" (0.01, FP32 mixed mode, staggered CG and Wilson
  *    CGNR): a reliable update when |r| falls by this factor;
- *  "half_split" (0: the 16-bit mixed mode stores the Dslash operands and
- *    the links in 16 bits; 1: only the links; 2: only the operands),
+ *  "half_split" (2: the 16-bit mixed mode stores the Dslash operands in 16
+ *    bits and keeps FP32 links; 1: 16-bit links and FP32 operands; 0: both
+ *    in 16 bits),
  *  "reortho" (1), "graph" (1: the solver loop as one CUDA-graph launch),
  *    "poll" (8: first batch of host-polled iterations);
  *  "persistent" (1: on small lattices the whole CG loop as one cooperative

@@ -37,6 +37,7 @@ struct CgpArgs {
   const void *links64;            // FP64 links of the reliable updates (mixed)
   const float *lscale;
   void *x, *r, *p, *v;            // iteration vectors (FP64, or FP32 when mixed)
+  void *v2;                       // the second p buffer
   void *x64, *r64, *w64;          // mixed: FP64 solution, residual, odd temporary
   const void *b;                  // FP64 source
   qllg_cg_scalars *sc;
@@ -88,11 +89,11 @@ __device__ bool grid_barrier(const CgpArgs &a)
   return ok != 0;
 }
 
-// per-rhs sums of Q quantities over the grid: each thread holds val[q] for
-// its rhs (threadIdx.x % NR); the block folds them per rhs, writes one
-// partial per (quantity, rhs), and after the barrier every block folds the
-// partials of all blocks in block order into s.red.  false: a barrier
-// wait ran out.
+// per-rhs sums of Q quantities over the grid: each thread holds val[q]
+// for its rhs ((threadIdx.x/4) % NR); the block folds them per rhs in
+// thread order, writes one partial per (quantity, rhs), and after the
+// barrier every block folds the partials of all blocks in block order into
+// s.red.  false: a barrier wait ran out.
 template <int Q, int NR>
 __device__ bool grid_sum(const CgpArgs &a, Sc &s, const double (&val)[Q], int &phase)
 {
@@ -100,12 +101,11 @@ __device__ bool grid_sum(const CgpArgs &a, Sc &s, const double (&val)[Q], int &p
 #pragma unroll
   for(int q=0; q<Q; q++) buf[q][threadIdx.x] = val[q];
   __syncthreads();
-  // block fold: thread (q, r) adds the block's threads of rhs r in order
   double *part = a.partial + (size_t)(phase & 1)*gridDim.x*kQmax*QLLG_MAXRHS;
   if(threadIdx.x < Q*NR) {
     const int q = threadIdx.x / NR, r = threadIdx.x % NR;
     double t = 0;
-    for(int i=r; i<kPT; i+=NR) t += buf[q][i];
+    for(int i=0; i<kPT; i++) if(((i >> 2) % NR) == r) t += buf[q][i];
     part[((size_t)blockIdx.x*kQmax + q)*QLLG_MAXRHS + r] = t;
   }
   phase++;
@@ -121,43 +121,68 @@ __device__ bool grid_sum(const CgpArgs &a, Sc &s, const double (&val)[Q], int &p
   return true;
 }
 
-// acc = sum over the slots of U_s(x) psi(x + d_s) for output site `site`
-// of parity p and rhs `rhs` (slot order and arithmetic of stag_dslash)
+// The hop sum of one (site, rhs) item on four lanes of a warp, lane mu
+// taking the four slots of direction mu, then a butterfly over the four
+// lanes: every lane ends with the full sum.  The input of the slots is
+// in + beta*add (add NULL: in alone), formed at each neighbour as it is
+// loaded, so that a p update needs no pass (and no barrier) of its own.
 template <int PL, typename T, int NR>
-__device__ __forceinline__ void hop_sum(const qllg_stag_args &sa, const Geo &G, int p, int site, int rhs,
-                                        const void *in, Cx<T> acc[3])
+__device__ __forceinline__ void hop_sum4(const qllg_stag_args &sa, const Geo &G, int p, int site, int rhs,
+                                         const void *in, const void *add, T beta, Cx<T> acc[3])
 {
+  constexpr int PS = std::is_same<T, double>::value ? QLLG_F64 : QLLG_F32;
   const size_t V = (size_t)sa.g.V, total = (size_t)G.Vh*NR;
   const size_t loff = p ? (size_t)G.Vh : 0;
+  const int mu = threadIdx.x & 3;
   int x[4];
   site_coords(G, p, site, x);
 #pragma unroll
   for(int c=0; c<3; c++) { acc[c].r = 0; acc[c].i = 0; }
-  constexpr int PS = std::is_same<T, double>::value ? QLLG_F64 : QLLG_F32;
-#pragma unroll 1
-  for(int mu=0; mu<4; mu++) {
 #pragma unroll
-    for(int back=0; back<2; back++) {
+  for(int back=0; back<2; back++) {
 #pragma unroll
-      for(int nk=0; nk<2; nk++) {
-        if(nk && sa.nslots != 16) continue;
-        const int d = (nk ? 3 : 1)*(back ? -1 : 1);
-        const int k = nbr_index(G, x, mu, d);
-        Cx<T> U[9], v[3];
-        if(sa.nslots == 16)
-          slot_link<PL,16>(sa, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, (size_t)k, U);
-        else
-          slot_link<PL,8>(sa, mu, back, 0, V, (size_t)G.Vh, loff, (size_t)site, (size_t)k, U);
-        SpinorIO<PS,3>::load(in, total, (size_t)k*NR + rhs, v);
+    for(int nk=0; nk<2; nk++) {
+      if(nk && sa.nslots != 16) continue;
+      const int d = (nk ? 3 : 1)*(back ? -1 : 1);
+      const int k = nbr_index(G, x, mu, d);
+      Cx<T> U[9], v[3];
+      if(sa.nslots == 16)
+        slot_link<PL,16>(sa, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, (size_t)k, U);
+      else
+        slot_link<PL,8>(sa, mu, back, 0, V, (size_t)G.Vh, loff, (size_t)site, (size_t)k, U);
+      SpinorIO<PS,3>::load(in, total, (size_t)k*NR + rhs, v);
+      if(add) {
+        Cx<T> w[3];
+        SpinorIO<PS,3>::load(add, total, (size_t)k*NR + rhs, w);
 #pragma unroll
-        for(int l=0; l<3; l++) {
+        for(int c=0; c<3; c++) { v[c].r = fma(beta, w[c].r, v[c].r); v[c].i = fma(beta, w[c].i, v[c].i); }
+      }
 #pragma unroll
-          for(int j=0; j<3; j++) cmac(acc[j], U[3*l + j], v[l]);
-        }
+      for(int l=0; l<3; l++) {
+#pragma unroll
+        for(int j=0; j<3; j++) cmac(acc[j], U[3*l + j], v[l]);
       }
     }
   }
+#pragma unroll
+  for(int c=0; c<3; c++) {
+#pragma unroll
+    for(int o=1; o<4; o<<=1) {
+      acc[c].r += __shfl_xor_sync(0xffffffffu, acc[c].r, o);
+      acc[c].i += __shfl_xor_sync(0xffffffffu, acc[c].i, o);
+    }
+  }
 }
+
+// Items are (site, rhs) pairs, rhs fastest, four lanes each; a warp holds
+// eight consecutive items and the grid stride is a multiple of eight, so a
+// warp runs its loop trips together (the butterflies need every lane).
+#define ITEM_LOOP(item, valid, n)                                                              \
+  const size_t n##_round = ((size_t)(n) + 7)/8*8;                                              \
+  for(size_t item##_ = ((size_t)blockIdx.x*kPT + threadIdx.x) >> 2; item##_ < n##_round;       \
+      item##_ += ((size_t)gridDim.x*kPT) >> 2)                                                 \
+    for(bool valid = item##_ < (size_t)(n), once_ = true; once_; once_ = false)                \
+      for(size_t item = valid ? item##_ : (size_t)(n) - 1, once2_ = 1; once2_; once2_ = 0)
 
 template <int NR, bool MIXED>
 __global__ void __launch_bounds__(kPT)
@@ -169,7 +194,8 @@ cg_persistent(CgpArgs a)
   __shared__ Sc s;
   const Geo G = make_geo(a.g);
   const size_t total = (size_t)G.Vh*NR;
-  const int rhs = threadIdx.x % NR;
+  const int rhs = (threadIdx.x >> 2) % NR;
+  const bool lead = (threadIdx.x & 3) == 0;
   qllg_stag_args sa;
   memset(&sa, 0, sizeof(sa));
   sa.g = a.g;
@@ -183,13 +209,17 @@ cg_persistent(CgpArgs a)
     for(int q=0; q<NR; q++) {
       s.rsq[q] = a.sc->rsq[q]; s.stop[q] = a.sc->rsq_stop[q]; s.m2[q] = a.sc->mass2[q];
       s.maxr2[q] = a.sc->maxr2[q]; s.act[q] = a.sc->active[q]; s.iters[q] = a.sc->iters[q];
-      s.nru[q] = a.sc->nru[q]; s.ru[q] = 0;
+      s.nru[q] = a.sc->nru[q]; s.ru[q] = 0; s.pn[q] = 0; s.vn[q] = 0;
     }
     s.delta2 = a.sc->delta2;
     s.maxits = a.sc->maxits;
     s.failed = 0;
   }
   __syncthreads();
+  // p is double-buffered: the p update of an iteration writes the other
+  // buffer while the hop sums read the current one at the neighbours
+  void *pb[2] = {a.p, a.v2};
+  int cur = 0;
   int phase = 0, trip = 0;
   for(;;) {
     if(threadIdx.x == 0) {
@@ -201,62 +231,64 @@ cg_persistent(CgpArgs a)
     if(!s.any || trip >= a.trips) break;
     trip++;
     const bool act = s.act[rhs] != 0;
-    // p += r/|r|^2 with |p|^2
+    void *pc = pb[cur], *pn = pb[cur ^ 1];
+    const T beta = act ? (T)(1.0/s.rsq[rhs]) : (T)0;
+    // p' = p + r/|r|^2 with |p'|^2 (even sites), and v = D_oe p' with |v|^2
+    // (odd sites), p' formed at each neighbour from p and r
     {
-      Acc<T> acc;
-      if(act) {
-        const T beta = (T)(1.0/s.rsq[rhs]);
-        for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
-          Cx<T> pv[3], rv[3];
-          SpinorIO<P,3>::load(a.p, total, t, pv);
-          SpinorIO<P,3>::load(a.r, total, t, rv);
+      Acc<T> accp, accv;
+      {
+        // every lane of a warp runs every trip (the butterflies need them
+        // all); the rhs that are done only skip their stores
+        ITEM_LOOP(t, valid, total) {
+          if(lead && valid && act) {
+            Cx<T> pv[3], rv[3];
+            SpinorIO<P,3>::load(pc, total, t, pv);
+            SpinorIO<P,3>::load(a.r, total, t, rv);
 #pragma unroll
-          for(int c=0; c<3; c++) { pv[c].r = fma(beta, rv[c].r, pv[c].r); pv[c].i = fma(beta, rv[c].i, pv[c].i); }
-          SpinorIO<P,3>::store(a.p, total, t, pv);
-          acc.norm(pv);
-        }
-      }
-      const double val[1] = {acc.get()};
-      if(!grid_sum<1,NR>(a, s, val, phase)) return;
-      if(threadIdx.x < NR) s.pn[threadIdx.x] = s.red[0][threadIdx.x];
-    }
-    // v = D_oe p with |v|^2
-    {
-      Acc<T> acc;
-      if(act) {
-        for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
+            for(int c=0; c<3; c++) { pv[c].r = fma(beta, rv[c].r, pv[c].r); pv[c].i = fma(beta, rv[c].i, pv[c].i); }
+            SpinorIO<P,3>::store(pn, total, t, pv);
+            accp.norm(pv);
+          }
           Cx<T> o[3];
-          hop_sum<PL,T,NR>(sa, G, 1, (int)(t/NR), rhs, a.p, o);
-          SpinorIO<P,3>::store(a.v, total, t, o);
-          acc.norm(o);
+          hop_sum4<PL,T,NR>(sa, G, 1, (int)(t/NR), rhs, pc, a.r, beta, o);
+          if(lead && valid && act) {
+            SpinorIO<P,3>::store(a.v, total, t, o);
+            accv.norm(o);
+          }
         }
       }
-      const double val[1] = {acc.get()};
-      if(!grid_sum<1,NR>(a, s, val, phase)) return;
-      if(threadIdx.x < NR) s.vn[threadIdx.x] = s.red[0][threadIdx.x];
+      const double val[2] = {accp.get(), accv.get()};
+      if(!grid_sum<2,NR>(a, s, val, phase)) return;
+      if(threadIdx.x < NR) { s.pn[threadIdx.x] = s.red[0][threadIdx.x]; s.vn[threadIdx.x] = s.red[1][threadIdx.x]; }
       __syncthreads();
     }
-    // Ap = m^2 p - D_eo v in registers; x += a p, r -= a Ap with |r|^2
+    cur ^= 1;
+    pc = pb[cur];
+    // Ap = m^2 p - D_eo v; x += a p, r -= a Ap with |r|^2
     {
       Acc<T> acc;
-      if(act) {
-        const T alpha = (T)(1.0/(s.m2[rhs]*s.pn[rhs] + s.vn[rhs]));
+      {
+        const T alpha = act ? (T)(1.0/(s.m2[rhs]*s.pn[rhs] + s.vn[rhs])) : (T)0;
         const T ca = (T)s.m2[rhs];
-        for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
-          Cx<T> hs[3], pv[3], xv[3], rv[3];
-          hop_sum<PL,T,NR>(sa, G, 0, (int)(t/NR), rhs, a.v, hs);
-          SpinorIO<P,3>::load(a.p, total, t, pv);
-          SpinorIO<P,3>::load(a.x, total, t, xv);
-          SpinorIO<P,3>::load(a.r, total, t, rv);
+        ITEM_LOOP(t, valid, total) {
+          Cx<T> hs[3];
+          hop_sum4<PL,T,NR>(sa, G, 0, (int)(t/NR), rhs, a.v, NULL, (T)0, hs);
+          if(lead && valid && act) {
+            Cx<T> pv[3], xv[3], rv[3];
+            SpinorIO<P,3>::load(pc, total, t, pv);
+            SpinorIO<P,3>::load(a.x, total, t, xv);
+            SpinorIO<P,3>::load(a.r, total, t, rv);
 #pragma unroll
-          for(int c=0; c<3; c++) {
-            T apr = fma((T)-1, hs[c].r, ca*pv[c].r), api = fma((T)-1, hs[c].i, ca*pv[c].i);
-            xv[c].r = fma(alpha, pv[c].r, xv[c].r); xv[c].i = fma(alpha, pv[c].i, xv[c].i);
-            rv[c].r = fma(-alpha, apr, rv[c].r); rv[c].i = fma(-alpha, api, rv[c].i);
+            for(int c=0; c<3; c++) {
+              T apr = fma((T)-1, hs[c].r, ca*pv[c].r), api = fma((T)-1, hs[c].i, ca*pv[c].i);
+              xv[c].r = fma(alpha, pv[c].r, xv[c].r); xv[c].i = fma(alpha, pv[c].i, xv[c].i);
+              rv[c].r = fma(-alpha, apr, rv[c].r); rv[c].i = fma(-alpha, api, rv[c].i);
+            }
+            SpinorIO<P,3>::store(a.x, total, t, xv);
+            SpinorIO<P,3>::store(a.r, total, t, rv);
+            acc.norm(rv);
           }
-          SpinorIO<P,3>::store(a.x, total, t, xv);
-          SpinorIO<P,3>::store(a.r, total, t, rv);
-          acc.norm(rv);
         }
       }
       const double val[1] = {acc.get()};
@@ -285,47 +317,52 @@ cg_persistent(CgpArgs a)
     // reliable update of the flagged rhs: x64 += x, x = 0
     const bool fl = s.ru[rhs] != 0;
     if(fl) {
-      for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
-        Cx<double> xv[3];
-        Cx<float> sv[3], z[3];
-        SpinorIO<QLLG_F64,3>::load(a.x64, total, t, xv);
-        SpinorIO<QLLG_F32,3>::load(a.x, total, t, sv);
+      ITEM_LOOP(t, valid, total) {
+        if(lead && valid) {
+          Cx<double> xv[3];
+          Cx<float> sv[3], z[3];
+          SpinorIO<QLLG_F64,3>::load(a.x64, total, t, xv);
+          SpinorIO<QLLG_F32,3>::load(a.x, total, t, sv);
 #pragma unroll
-        for(int c=0; c<3; c++) { xv[c].r += sv[c].r; xv[c].i += sv[c].i; z[c].r = 0; z[c].i = 0; }
-        SpinorIO<QLLG_F64,3>::store(a.x64, total, t, xv);
-        SpinorIO<QLLG_F32,3>::store(a.x, total, t, z);
+          for(int c=0; c<3; c++) { xv[c].r += sv[c].r; xv[c].i += sv[c].i; z[c].r = 0; z[c].i = 0; }
+          SpinorIO<QLLG_F64,3>::store(a.x64, total, t, xv);
+          SpinorIO<QLLG_F32,3>::store(a.x, total, t, z);
+        }
       }
     }
     if(!grid_barrier(a)) return;
     // w64 = D_oe x64 (FP64)
-    if(fl) {
-      for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
+    {
+      ITEM_LOOP(t, valid, total) {
         Cx<double> o[3];
-        hop_sum<QLLG_F64,double,NR>(sa64, G, 1, (int)(t/NR), rhs, a.x64, o);
-        SpinorIO<QLLG_F64,3>::store(a.w64, total, t, o);
+        hop_sum4<QLLG_F64,double,NR>(sa64, G, 1, (int)(t/NR), rhs, a.x64, NULL, 0.0, o);
+        if(lead && valid && fl) SpinorIO<QLLG_F64,3>::store(a.w64, total, t, o);
       }
     }
     if(!grid_barrier(a)) return;
     // r64 = b - (m^2 x64 - D_eo w64), r = r64 in FP32, |r64|^2
     {
       double r2 = 0;
-      if(fl) {
+      {
         const double m2 = s.m2[rhs];
-        for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
-          Cx<double> hs[3], xv[3], bv[3];
-          Cx<float> f[3];
-          hop_sum<QLLG_F64,double,NR>(sa64, G, 0, (int)(t/NR), rhs, a.w64, hs);
-          SpinorIO<QLLG_F64,3>::load(a.x64, total, t, xv);
-          SpinorIO<QLLG_F64,3>::load(a.b, total, t, bv);
+        ITEM_LOOP(t, valid, total) {
+          Cx<double> hs[3];
+          hop_sum4<QLLG_F64,double,NR>(sa64, G, 0, (int)(t/NR), rhs, a.w64, NULL, 0.0, hs);
+          if(lead && valid && fl) {
+            Cx<double> xv[3], bv[3];
+            Cx<float> f[3];
+            SpinorIO<QLLG_F64,3>::load(a.x64, total, t, xv);
+            SpinorIO<QLLG_F64,3>::load(a.b, total, t, bv);
 #pragma unroll
-          for(int c=0; c<3; c++) {
-            const double tr = fma(-1.0, hs[c].r, m2*xv[c].r), ti = fma(-1.0, hs[c].i, m2*xv[c].i);
-            bv[c].r = bv[c].r - tr; bv[c].i = bv[c].i - ti;
-            r2 += bv[c].r*bv[c].r + bv[c].i*bv[c].i;
-            f[c].r = (float)bv[c].r; f[c].i = (float)bv[c].i;
+            for(int c=0; c<3; c++) {
+              const double tr = fma(-1.0, hs[c].r, m2*xv[c].r), ti = fma(-1.0, hs[c].i, m2*xv[c].i);
+              bv[c].r = bv[c].r - tr; bv[c].i = bv[c].i - ti;
+              r2 += bv[c].r*bv[c].r + bv[c].i*bv[c].i;
+              f[c].r = (float)bv[c].r; f[c].i = (float)bv[c].i;
+            }
+            SpinorIO<QLLG_F64,3>::store(a.r64, total, t, bv);
+            SpinorIO<QLLG_F32,3>::store(a.r, total, t, f);
           }
-          SpinorIO<QLLG_F64,3>::store(a.r64, total, t, bv);
-          SpinorIO<QLLG_F32,3>::store(a.r, total, t, f);
         }
       }
       const double val[1] = {r2};
@@ -344,22 +381,24 @@ cg_persistent(CgpArgs a)
     }
     if(!a.reortho) continue;
     // p -= (<r,p>/|r|^2) r for the flagged rhs (FP32, as mcg_orth_dot_k and
-    // mcg_orth_axpy_k)
+    // mcg_orth_axpy_k), on the current p buffer
     {
       Acc<float> are, aim;
       if(fl) {
-        for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
-          Cx<float> pv[3], rv[3];
-          SpinorIO<QLLG_F32,3>::load(a.p, total, t, pv);
-          SpinorIO<QLLG_F32,3>::load(a.r, total, t, rv);
-          float re = 0, im = 0;
+        ITEM_LOOP(t, valid, total) {
+          if(lead && valid) {
+            Cx<float> pv[3], rv[3];
+            SpinorIO<QLLG_F32,3>::load(pc, total, t, pv);
+            SpinorIO<QLLG_F32,3>::load(a.r, total, t, rv);
+            float re = 0, im = 0;
 #pragma unroll
-          for(int c=0; c<3; c++) {
-            re = fmaf(rv[c].r, pv[c].r, re); re = fmaf(rv[c].i, pv[c].i, re);
-            im = fmaf(rv[c].r, pv[c].i, im); im = fmaf(-rv[c].i, pv[c].r, im);
+            for(int c=0; c<3; c++) {
+              re = fmaf(rv[c].r, pv[c].r, re); re = fmaf(rv[c].i, pv[c].i, re);
+              im = fmaf(rv[c].r, pv[c].i, im); im = fmaf(-rv[c].i, pv[c].r, im);
+            }
+            are.add(re);
+            aim.add(im);
           }
-          are.add(re);
-          aim.add(im);
         }
       }
       const double val[2] = {are.get(), aim.get()};
@@ -368,21 +407,35 @@ cg_persistent(CgpArgs a)
         const double r2 = s.rsq[rhs];
         const float cr = (float)(r2 > 0 ? s.red[0][rhs]/r2 : 0);
         const float ci = (float)(r2 > 0 ? s.red[1][rhs]/r2 : 0);
-        for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
-          Cx<float> pv[3], rv[3];
-          SpinorIO<QLLG_F32,3>::load(a.p, total, t, pv);
-          SpinorIO<QLLG_F32,3>::load(a.r, total, t, rv);
+        ITEM_LOOP(t, valid, total) {
+          if(lead && valid) {
+            Cx<float> pv[3], rv[3];
+            SpinorIO<QLLG_F32,3>::load(pc, total, t, pv);
+            SpinorIO<QLLG_F32,3>::load(a.r, total, t, rv);
 #pragma unroll
-          for(int c=0; c<3; c++) {
-            pv[c].r -= cr*rv[c].r - ci*rv[c].i;
-            pv[c].i -= cr*rv[c].i + ci*rv[c].r;
+            for(int c=0; c<3; c++) {
+              pv[c].r -= cr*rv[c].r - ci*rv[c].i;
+              pv[c].i -= cr*rv[c].i + ci*rv[c].r;
+            }
+            SpinorIO<QLLG_F32,3>::store(pc, total, t, pv);
           }
-          SpinorIO<QLLG_F32,3>::store(a.p, total, t, pv);
         }
       }
     }
   }
-  // the scalars back to the host's struct (every block holds the same)
+  // the current p back where the caller keeps it (the double buffer may
+  // end on the other one); the scalars to the host's struct (every block
+  // holds the same)
+  if(cur) {
+    // every block's last p writes (a re-orthogonalisation ends without a
+    // barrier) before any block copies
+    if(!grid_barrier(a)) return;
+    for(size_t t = (size_t)blockIdx.x*kPT + threadIdx.x; t < total; t += (size_t)gridDim.x*kPT) {
+      Cx<T> pv[3];
+      SpinorIO<P,3>::load(pb[1], total, t, pv);
+      SpinorIO<P,3>::store(pb[0], total, t, pv);
+    }
+  }
   if(blockIdx.x == 0 && threadIdx.x == 0) {
     int any = 0;
     for(int q=0; q<NR; q++) {
@@ -407,7 +460,7 @@ int launch_cgp(const CgpArgs &a0, int *grid_out)
     if(per_sm < 1) { qllg_set_error("persistent CG: no resident block"); return -1; }
   }
   const size_t total = (size_t)a0.g.Vh*NR;
-  size_t want = (total + kPT - 1)/kPT;
+  size_t want = (4*total + kPT - 1)/kPT;          // four lanes per (site, rhs)
   // few blocks: the barriers and the partial folds cost per block
   const size_t cap = (size_t)qllg_num_sms()*per_sm;
   if(want > cap) want = cap;
@@ -436,7 +489,7 @@ qllg_k_cg_persistent(const qllg_cgp_args *h, int *grid_out)
   a.links = h->links;
   a.links64 = h->links64;
   a.lscale = h->lscale;
-  a.x = h->x; a.r = h->r; a.p = h->p; a.v = h->v;
+  a.x = h->x; a.r = h->r; a.p = h->p; a.v = h->v; a.v2 = h->p2;
   a.x64 = h->x64; a.r64 = h->r64; a.w64 = h->w64;
   a.b = h->b;
   a.sc = h->sc;

@@ -241,6 +241,7 @@ typedef struct {
   const void *links, *links64;
   const float *lscale;
   void *x, *r, *p, *v, *x64, *r64, *w64;
+  void *p2;                 /* a second buffer the size of p */
   const void *b;
   struct qllg_cg_scalars_s *sc;
   double *partial;

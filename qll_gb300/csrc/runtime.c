@@ -295,9 +295,13 @@ static struct { const char *name; double value; } g_params[] = {
                                       for both, 13.0 ms per solve at 0.01
                                       against 14.8 ms at 0.1) */
   {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
-  {"half_split", 0},         /* MIXED_HALF solves: 0 16-bit Dslash operands and
+  {"half_split", 2},         /* MIXED_HALF solves: 0 16-bit Dslash operands and
                                 links, 1 16-bit links with FP32 operands, 2 FP32
-                                links with 16-bit operands */
+                                links with 16-bit operands.  At 32^3x64, m = 0.01,
+                                16 rhs: 1382, 996 and 455 iterations (4.96, 2.81
+                                and 1.30 s; FP32 operands and links: 455, 1.04 s):
+                                the 16-bit links, one scale per slot, cost the
+                                iterations, the 16-bit operands do not */
   {"graph", 1},              /* run solver iterations as one CUDA graph launch */
   {"persistent", 1},         /* small lattices: the whole CG loop in one cooperative
                                 launch (FP64, or FP32 with FP64 reliable updates) */

@@ -748,7 +748,10 @@ run_persistent(qllg_stag *S, const iter_ctx *c, int maxits)
 {
   /* control words: barrier arrivals and generation, the error flag */
   unsigned *ctl = ws_get(S, WS_CGP, 4*sizeof(unsigned));
-  if(!ctl) return -1;
+  /* the second p buffer of the persistent loop (the Ap workspace, unused
+   * by this path) */
+  void *p2 = ws_get(S, WS_AP, vec_bytes(S, c->ps, c->nrhs));
+  if(!ctl || !p2) return -1;
   if(qllg_check_cuda(cudaMemsetAsync(ctl, 0, 4*sizeof(unsigned), qllg_stream()),
                      "persistent CG: control words")) return -1;
   qllg_cgp_args a;
@@ -764,6 +767,7 @@ run_persistent(qllg_stag *S, const iter_ctx *c, int maxits)
   a.lscale = S->lscale;
   a.x = c->x; a.r = c->r; a.p = c->p; a.v = c->v;
   a.x64 = c->x64; a.r64 = c->r64; a.w64 = c->w64;
+  a.p2 = p2;
   a.b = c->b;
   a.sc = S->sc;
   a.partial = S->rb.partial;

@@ -15,6 +15,19 @@ from qll_gb300 import qll
 
 pytestmark = pytest.mark.gpu
 
+
+@pytest.fixture(autouse=True)
+def _multi_launch_loop():
+    """these tests are about the multi-launch solver loop (fused Dslash
+    epilogues, graph capture, reliable-update kernels, launch shapes): on
+    their small lattices the persistent CG would take the solves, so it is
+    off here (tests/test_gpu_persistent.py covers it)"""
+    L = qll.load()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_set_param(b"persistent", 0)
+    yield
+    L.qllg_set_param(b"persistent", 1)
+
 DIMS = (4, 4, 6, 8)
 TOL = {"D": 1e-12, "F": 1e-5}
 DT = {"D": np.float64, "F": np.float32}
