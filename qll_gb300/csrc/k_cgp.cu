@@ -101,21 +101,35 @@ __device__ bool grid_sum(const CgpArgs &a, Sc &s, const double (&val)[Q], int &p
 #pragma unroll
   for(int q=0; q<Q; q++) buf[q][threadIdx.x] = val[q];
   __syncthreads();
+  // block fold, a fixed tree: threads t and t + w hold the same rhs while
+  // w is a multiple of 4*NR; the last four entries of a rhs are its lanes
+  for(int w = kPT/2; w >= 4*NR; w >>= 1) {
+    if(threadIdx.x < w) {
+#pragma unroll
+      for(int q=0; q<Q; q++) buf[q][threadIdx.x] += buf[q][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
   double *part = a.partial + (size_t)(phase & 1)*gridDim.x*kQmax*QLLG_MAXRHS;
   if(threadIdx.x < Q*NR) {
     const int q = threadIdx.x / NR, r = threadIdx.x % NR;
-    double t = 0;
-    for(int i=0; i<kPT; i++) if(((i >> 2) % NR) == r) t += buf[q][i];
+    const double t = (buf[q][4*r] + buf[q][4*r + 1]) + (buf[q][4*r + 2] + buf[q][4*r + 3]);
     part[((size_t)blockIdx.x*kQmax + q)*QLLG_MAXRHS + r] = t;
   }
   phase++;
   if(!grid_barrier(a)) return false;
-  if(threadIdx.x < Q*NR) {
-    const int q = threadIdx.x / NR, r = threadIdx.x % NR;
+  // fold of the blocks' partials: warp k takes the sums k, k + 8, ...; its
+  // lanes read blocks lane, lane + 32, ... in order and a butterfly adds
+  // the lanes, the same fixed order in every block
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for(int c = warp; c < Q*NR; c += kPT/32) {
+    const int q = c / NR, r = c % NR;
     double t = 0;
-    for(int b=0; b<(int)gridDim.x; b++)
+    for(int b = lane; b < (int)gridDim.x; b += 32)
       t += ((volatile double *)part)[((size_t)b*kQmax + q)*QLLG_MAXRHS + r];
-    s.red[q][r] = t;
+#pragma unroll
+    for(int o=16; o>0; o>>=1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if(lane == 0) s.red[q][r] = t;
   }
   __syncthreads();
   return true;
