@@ -97,6 +97,9 @@ class GpuOp:
         self.L = qll.load()
         self.L.qllg_stag_dslash_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                    ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        # the library's kernels on torch's current stream, in order with the
+        # face copies and vector updates made through torch
+        self.L.qllg_set_stream(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
         ul = [slab.local_field(a) for a in u]
         u3l = [slab.local_field(a) for a in u3]
         S = self.L.qllg_stag_create(qll.dims_c(slab.pdims), qll.vp_array(ul), qll.vp_array(u3l))
