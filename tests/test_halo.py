@@ -151,6 +151,7 @@ def test_decomposed_on_one_gpu_matches_global():
         og = torch.zeros_like(yg)
         assert L.qllg_stag_dslash_device(G, 0, 1, 1, ctypes.c_void_p(og.data_ptr()),
                                          ctypes.c_void_p(yg.data_ptr())) == 0
+        torch.cuda.synchronize()
         want = ops[0].to_host(og)
         ins = []
         for s, op in zip(slabs, ops):
