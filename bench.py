@@ -752,11 +752,12 @@ def _oracle(fast=True):
     return lib, POINTER
 
 
-def cpu_solve(u16, src, dims=DIMS, mass=MASS, rsq=RSQ, maxits=MAXITS):
+def cpu_solve(u16, src, dims=None, mass=MASS, rsq=RSQ, maxits=MAXITS):
     """one converged FP64 CG solve (solve2D: cgSolveT with dslash2, the
     reference's algorithm restated) of one source on the host cores, timed
     whole; u16 are the 16 link slots 4mu+2b+naik.  Returns (seconds,
     iterations, threads)."""
+    dims = tuple(dims or DIMS)
     lib, POINTER = _oracle()
     PA = (POINTER(ctypes.c_double)*8)
     u = PA(*[u16[2*i].ctypes.data_as(POINTER(ctypes.c_double)) for i in range(8)])
@@ -789,13 +790,14 @@ def _aligned(shape):
     return buf[off:off + n].reshape(shape)
 
 
-def ref_cpu_solve(u16, src, dims=DIMS, mass=MASS, rsq=RSQ, maxits=MAXITS):
+def ref_cpu_solve(u16, src, dims=None, mass=MASS, rsq=RSQ, maxits=MAXITS):
     """one converged FP64 solve2 of the reference library itself
     (oracle/_ref/libqllref_fast.so: the reference's sources, its 4-site SIMD
     layout, host-native flags) on the host cores, timed whole; the links and
     the source are moved into the reference's layout first, untimed.
     Returns (seconds, iterations, threads)."""
     from ctypes import POINTER, c_double, c_int
+    dims = tuple(dims or DIMS)
     R = ctypes.CDLL(REF_FAST)
     R.refh_solve2D.restype = c_int
     n = host_threads()

@@ -216,19 +216,27 @@ stag_dslash(qllg_stag_args a)
 // contiguous bytes (two whole 32-byte sectors) of a neighbour's colour
 // vector per 16-byte load instead of four half sectors, halving the
 // sectors the L1 moves for spinor loads; 18: 16 with the complex FMAs on
-// packed FP32 pairs.
+// packed FP32 pairs; 19 and 20: 8 and 15 with the next slot's neighbour
+// spinors and link rows prefetched into L1 (prefetch.global.L1, no
+// registers held) while the current slot computes.
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int threads = (CFG == 14 || CFG == 15 || CFG == 17) ? 128 : 256;
+  static constexpr int threads = (CFG == 14 || CFG == 15 || CFG == 17 || CFG == 20) ? 128 : 256;
   static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 :
-                              (CFG == 3 || CFG == 8 || CFG == 16 || CFG == 18) ? 4 :
-                              CFG == 14 ? 7 : (CFG == 15 || CFG == 17) ? 8 :
+                              (CFG == 3 || CFG == 8 || CFG == 16 || CFG == 18 || CFG == 19) ? 4 :
+                              CFG == 14 ? 7 : (CFG == 15 || CFG == 17 || CFG == 20) ? 8 :
                               (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = (CFG == 1 || CFG == 18) && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
   static constexpr bool pf = CFG == 5 || CFG == 6;
   static constexpr bool roll = CFG == 7 || CFG == 8 || CFG == 9 || CFG >= 14;   // direction loop rolled
-  static constexpr bool pairs = CFG >= 16 && R == 4;
+  static constexpr bool pairs = CFG >= 16 && CFG <= 18 && R == 4;
+  static constexpr bool pfl = CFG >= 19;                               // L1 prefetch
 };
+
+__device__ __forceinline__ void prefetch_l1(const void *p)
+{
+  asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
+}
 
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
 // sides, so each link is loaded and converted once per R rhs and the R
@@ -343,6 +351,29 @@ stag_dslash_mr(qllg_stag_args a)
               const int d = (nk ? 3 : 1)*(back ? -1 : 1);
               const size_t nb = (size_t)nbr_index(G, x, mu, d);
               const size_t kb = nb*NR;
+              if constexpr (MrCfg<PS,R,CFG>::pfl && PS == QLLG_F32 && PL == QLLG_F32 && NR == 16) {
+                // the next slot (nk, then back, then mu): lane q < 3 of a
+                // site prefetches colour q of that slot's neighbour (one
+                // 128-byte line: its 16 rhs); the lanes of site offset e in
+                // the warp prefetch link entry e (and 8) of the warp's eight
+                // sites, one 64-byte run
+                int nnk = nk + 1, nback = back, nmu = mu;
+                if(nnk == (NS == 16 ? 2 : 1)) { nnk = 0; nback++; }
+                if(nback == 2) { nback = 0; nmu++; }
+                if(nmu < 4) {
+                  const int nd = (nnk ? 3 : 1)*(nback ? -1 : 1);
+                  const size_t nbn = (size_t)nbr_index(G, x, nmu, nd);
+                  if(q < 3) prefetch_l1((const float2 *)a.in + (size_t)q*total + nbn*NR);
+                  if(!a.fb) {
+                    const int nslot = (NS == 16) ? (4*nmu + 2*nback + nnk) : (2*nmu + nback);
+                    const int e = (threadIdx.x & 31) >> 2;
+                    const size_t s0 = loff + ((size_t)site & ~(size_t)7);
+                    const float2 *lb = (const float2 *)a.links + (size_t)nslot*9*V + s0;
+                    if(q == 0) prefetch_l1(lb + (size_t)e*V);
+                    if(q == 1 && e == 0) prefetch_l1(lb + 8*V);
+                  }
+                }
+              }
               Cx<T> U[9];
               slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
               if constexpr (v4) {
@@ -1032,10 +1063,10 @@ int launch_tile(const qllg_stag_args *a)
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15, 16, 17, 18 as
-// variants 4-10 and 12-17) and 11 = the bulk-copy pipeline (FP32 links and
+// launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15, 16, 17, 18, 19, 20
+// as variants 4-10 and 12-19) and 11 = the bulk-copy pipeline (FP32 links and
 // spinors, 16 slots, 16 rhs, k_stag_bulk.cuh)
-constexpr int kNumVariants = 18;
+constexpr int kNumVariants = 20;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
@@ -1046,7 +1077,9 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "4 rhs/thread lean 64 regs rolled (128 threads)",
                                                 "4 rhs/thread lean 64 regs rolled, paired rhs",
                                                 "4 rhs/thread lean 64 regs rolled (128 threads), paired rhs",
-                                                "4 rhs/thread lean 64 regs rolled, paired rhs, packed FMA"};
+                                                "4 rhs/thread lean 64 regs rolled, paired rhs, packed FMA",
+                                                "4 rhs/thread lean 64 regs rolled, L1 prefetch",
+                                                "4 rhs/thread lean 64 regs rolled (128 threads), L1 prefetch"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1086,7 +1119,9 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 14: return launch_mr<PS,PL,NS,NR,4,15>(a);
       case 15: return launch_mr<PS,PL,NS,NR,4,16>(a);
       case 16: return launch_mr<PS,PL,NS,NR,4,17>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,18>(a);
+      case 17: return launch_mr<PS,PL,NS,NR,4,18>(a);
+      case 18: return launch_mr<PS,PL,NS,NR,4,19>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,20>(a);
       }
     }
   }

@@ -335,7 +335,7 @@ def test_dslash_variants_agree(nrhs):
     g = torch.Generator(device="cuda").manual_seed(91 + nrhs)
     src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
     outs = []
-    for v in range(18):
+    for v in range(20):
         L.qllg_set_param(b"dslash_variant", v)
         for parity in (0, 1):
             dst = torch.full_like(src, float("nan"))
@@ -352,7 +352,7 @@ def test_dslash_variants_agree(nrhs):
     L.qllg_stag_destroy(S)
 
 
-@pytest.mark.parametrize("variant", range(18))
+@pytest.mark.parametrize("variant", range(20))
 def test_mixed_solve_with_each_dslash_variant(variant):
     """the fused CG epilogue and the norms of every variant: the 16-rhs
     mixed solve reaches the FP64 true residual and matches the oracle"""
