@@ -919,6 +919,26 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_wilson_dslash_only(args):
+    """launches of the Wilson half Dslash alone on a chosen lattice (FP32,
+    random device input), for profiling"""
+    from qll_gb300 import qll
+    L = qll.load()
+    L.qllg_wilson_create.restype = ctypes.c_void_p
+    L.qllg_wilson_create.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]
+    L.qllg_wilson_destroy.argtypes = [ctypes.c_void_p]
+    dims = tuple(int(v) for v in args.dims.split(","))
+    u = wilson_links_host(dims, 1004, 0.3)
+    W = ctypes.c_void_p(L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(u)))
+    del u
+    if not W.value:
+        raise SystemExit(qll.last_error())
+    prec = {"f64": 0, "f32": 1}[args.prec]
+    out = wilson_dslash_timing(L, W, dims, prec, launches=args.launches)
+    L.qllg_wilson_destroy(W)
+    print(json.dumps({"wilson_dslash_only": out}), flush=True)
+
+
 def run_dslash_only(args):
     """a few launches of the headline Dslash kernel on a chosen lattice, for
     profiling: FP32, 16 rhs, device-resident random input"""
@@ -1053,6 +1073,8 @@ def main():
                     help="--impl reference: stop timing further solves after this many seconds")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--dslash-only", action="store_true")
+    ap.add_argument("--wilson-dslash-only", action="store_true",
+                    help="the Wilson half Dslash alone on --dims, --prec f32 or f64")
     ap.add_argument("--dims", default="32,32,32,64")
     ap.add_argument("--prec", default="f32", choices=["f64", "f32", "i16", "f32r", "df"])
     ap.add_argument("--nrhs", type=int, default=16)
@@ -1073,7 +1095,9 @@ def main():
     ap.add_argument("--serve-budget", type=float, default=48.0, help="GiB")
     ap.add_argument("--serve-chunk", type=int, default=20)
     args = ap.parse_args()
-    if args.dslash_only:
+    if args.wilson_dslash_only:
+        run_wilson_dslash_only(args)
+    elif args.dslash_only:
         run_dslash_only(args)
     elif args.solve_only:
         run_solve_only(args)

@@ -215,32 +215,60 @@ stag_dslash(qllg_stag_args a)
 // site instead of 4q..4q+3): the four threads of a site then read 64
 // contiguous bytes (two whole 32-byte sectors) of a neighbour's colour
 // vector per 16-byte load instead of four half sectors, halving the
-// sectors the L1 moves for spinor loads; 18: 16 with the complex FMAs on
-// packed FP32 pairs; 19 and 20: 8 and 15 with the next slot's neighbour
-// spinors and link rows prefetched into L1 (prefetch.global.L1, no
-// registers held) while the current slot computes.
+// sectors the L1 moves for spinor loads.  (Also measured slower and
+// dropped: 16 with packed FP32 FMAs, 1.3x the time of 8 at 32^3x64; 8 and
+// 15 with the next slot's neighbour spinors and link rows prefetched into
+// L1 by prefetch.global.L1, 1.6x.)
+// 18-22: the per-warp asynchronous pipeline (FP32 links and spinors,
+// double-stored links): each warp copies the links and neighbour spinors
+// of its eight sites for a slot ST - 1 slots ahead with cp.async into a
+// ring of ST shared-memory stages of its own, and computes the current
+// slot from shared memory, so that no register holds a load in flight and
+// a slot costs one wait instead of the two or three dependent load round
+// trips of the register shapes.  128-thread blocks; (ST, blocks/SM):
+// 18 (2, 6), 19 (3, 4), 20 (4, 3), and 21 and 22: 19 and 20 with packed
+// FP32 FMAs (the pipeline issues more instructions than the register
+// shapes and no longer waits on loads, so halving the FMA instructions
+// pays here).  The 3-stage ring at 5 blocks/SM (102 registers) spilled
+// and measured 1.03 ms at 32^3x64 against 0.78 at 4 blocks; dropped.
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int threads = (CFG == 14 || CFG == 15 || CFG == 17 || CFG == 20) ? 128 : 256;
+  static constexpr int pipe = (CFG >= 18 && CFG <= 22 && PS == QLLG_F32 && R == 4)
+                              ? ((CFG == 18) ? 2 : (CFG == 20 || CFG == 22) ? 4 : 3) : 0;
+  static constexpr int threads = (CFG == 14 || CFG == 15 || CFG == 17 || CFG >= 18) ? 128 : 256;
   static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 :
-                              (CFG == 3 || CFG == 8 || CFG == 16 || CFG == 18 || CFG == 19) ? 4 :
-                              CFG == 14 ? 7 : (CFG == 15 || CFG == 17 || CFG == 20) ? 8 :
+                              (CFG == 3 || CFG == 8 || CFG == 16) ? 4 :
+                              CFG == 14 ? 7 : (CFG == 15 || CFG == 17) ? 8 :
+                              CFG == 18 ? 6 : (CFG == 19 || CFG == 21) ? 4 : (CFG == 20 || CFG == 22) ? 3 :
                               (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
-  static constexpr bool f2 = (CFG == 1 || CFG == 18) && PS == QLLG_F32;
-  static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7;
+  static constexpr bool f2 = (CFG == 1 || CFG == 21 || CFG == 22) && PS == QLLG_F32;
+  static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7 && !pipe;
   static constexpr bool pf = CFG == 5 || CFG == 6;
   static constexpr bool roll = CFG == 7 || CFG == 8 || CFG == 9 || CFG >= 14;   // direction loop rolled
-  static constexpr bool pairs = CFG >= 16 && CFG <= 18 && R == 4;
-  static constexpr bool pfl = CFG >= 19;                               // L1 prefetch
+  static constexpr bool pairs = (CFG == 16 || CFG == 17) && R == 4;
 };
-
-__device__ __forceinline__ void prefetch_l1(const void *p)
-{
-  asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
-}
 
 // Multi-rhs variant: a thread owns one site and R consecutive right-hand
 // sides, so each link is loaded and converted once per R rhs and the R
 // accumulator sets give independent FMA chains.  Same epilogues as above.
+// one stage of the per-warp pipeline: the neighbour spinors of the warp's
+// eight sites, [colour][pair half h][lane ^ 4h] 16 bytes (lane 4e + q
+// holds rhs 4q + 2h, 4q + 2h + 1 of site e, so a stage is read with
+// conflict-free 16-byte loads; the XOR puts the two halves of a 32-byte
+// sector, which one copy writes, in different banks), then the links,
+// [entry][site] 8 bytes
+constexpr int kPipeSpinor = 3*1024;
+constexpr int kPipeStage = kPipeSpinor + 9*8*8;              // 3648
+
+__device__ __forceinline__ void cp_async16_ca(unsigned s, const void *gmem)
+{
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait()
+{
+  asm volatile("cp.async.wait_group %0;\n" :: "n"(N) : "memory");
+}
+
 template <int PS, int PL, int NS, int NR, int R, bool V4, int CFG>
 __global__ void __launch_bounds__(MrCfg<PS,R,CFG>::threads, MrCfg<PS,R,CFG>::minb)
 stag_dslash_mr(qllg_stag_args a)
@@ -252,7 +280,12 @@ stag_dslash_mr(qllg_stag_args a)
   constexpr bool PF = MrCfg<PS,R,CFG>::pf;
   constexpr int TB = MrCfg<PS,R,CFG>::threads;
   constexpr bool LEAN = MrCfg<PS,R,CFG>::lean;
-  __shared__ double shm[2*R*TB];
+  constexpr int ST = MrCfg<PS,R,CFG>::pipe;
+  constexpr bool PIPE = ST > 0 && PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && V4;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  // the pipeline's ring takes the reduction's scratch once the slot loop is done
+  __shared__ double shm_s[PIPE ? 1 : 2*R*TB];
+  double *shm = PIPE ? reinterpret_cast<double *>(dsm) : shm_s;
   __shared__ T s_ca[LEAN ? NR : 1], s_alpha[LEAN ? NR : 1];
   const Geo G = make_geo(a.g);
   const size_t V = (size_t)a.g.V;
@@ -316,7 +349,69 @@ stag_dslash_mr(qllg_stag_args a)
     if constexpr (LEAN) { Acc<T> t = accs[(R + j)*TB + threadIdx.x]; t.norm(v); accs[(R + j)*TB + threadIdx.x] = t; }
     else acc1r[j].norm(v);
   };
-  if(!skip && anyact) {
+  // the per-warp pipeline's issue pointer: the work item, slot and site
+  // coordinates of the next slot to copy, and the ring stage it goes to
+  const int lane = threadIdx.x & 31;
+  const unsigned wring = (unsigned)__cvta_generic_to_shared(dsm) + (threadIdx.x >> 5)*(ST ? ST : 1)*kPipeStage;
+  const unsigned char *wring_p = dsm + (threadIdx.x >> 5)*(ST ? ST : 1)*kPipeStage;
+  size_t iw = (size_t)blockIdx.x*blockDim.x + threadIdx.x;
+  int isl = 0, ibuf = 0, cbuf = 0;
+  // copy the next slot (or commit an empty group past the end of the
+  // warp's work, so that the group count stays uniform): lane L copies the
+  // 16-byte pieces L & 7 of the colour vectors of sites L >> 3 and
+  // 4 + (L >> 3), whose neighbours come from the lanes computing them, and
+  // link piece L (and 32 + L): entry L >> 2 of sites 2(L & 3), 2(L & 3) + 1
+  // the neighbours of the warp's eight sites for the sixteen slots of the
+  // issue pointer's site, [slot][site], after the ring: filled when the
+  // issue pointer reaches a site, lane 4e + q taking the four slots of
+  // direction q of site e; read by the copies of each slot
+  int *wnb = reinterpret_cast<int *>(dsm + (TB/32)*(ST ? ST : 1)*kPipeStage) + (threadIdx.x >> 5)*8*NS;
+  const char *ilk = nullptr, *ilk8 = nullptr;   // this lane's link pieces of slot 0 at the issue site
+  const char *const isp = (const char *)a.in + (lane & 7)*16;
+  const size_t cst = total*8;                   // bytes between colours
+  auto pipe_issue = [&]() {
+    if constexpr (PIPE) {
+      if(iw < nwork) {
+        if(isl == 0) {
+          const int isite = (int)(iw / Q);
+          const int e = lane >> 2, qd = lane & 3;
+          int xs[4];
+          site_coords(G, p, isite, xs);
+#pragma unroll
+          for(int k=0; k<4; k++)
+            wnb[(4*qd + k)*8 + e] = nbr_index(G, xs, qd, (k & 1 ? 3 : 1)*(k & 2 ? -1 : 1));
+          const float2 *lk = (const float2 *)a.links + loff + (size_t)(isite - e) + 2*qd;
+          ilk = (const char *)(lk + (size_t)e*V);
+          ilk8 = (const char *)(lk + 8*V);
+          __syncwarp();
+        }
+        const int n0 = wnb[isl*8 + (lane >> 3)], n1 = wnb[isl*8 + 4 + (lane >> 3)];
+        const int b = lane & 7;
+        const unsigned dst = wring + ibuf*kPipeStage + ((b & 1) << 9) +
+                             (((((lane >> 3) ^ (b & 1)) << 2) + (b >> 1)) << 4);
+        const char *src0 = isp + (size_t)n0*(NR*8), *src1 = isp + (size_t)n1*(NR*8);
+#pragma unroll
+        for(int c=0; c<3; c++) {
+          cp_async16_ca(dst + c*1024, src0 + c*cst);
+          cp_async16_ca(dst + c*1024 + 256, src1 + c*cst);
+        }
+        const size_t so = (size_t)isl*9*V*8;
+        const unsigned ldst = wring + ibuf*kPipeStage + kPipeSpinor;
+        cp_async16_ca(ldst + lane*16, ilk + so);
+        if(lane < 4) cp_async16_ca(ldst + 512 + lane*16, ilk8 + so);
+        if(++isl == NS) { isl = 0; iw += (size_t)gridDim.x*blockDim.x; }
+      }
+      cp_async_commit();
+      ibuf = ibuf + 1 == ST ? 0 : ibuf + 1;
+    }
+  };
+  // the pipeline runs whole warps (its copies and shuffles are warp-wide):
+  // a thread whose rhs are all inactive computes along and stores nothing
+  if(!skip && (PIPE || anyact)) {
+    if constexpr (PIPE) {
+#pragma unroll
+      for(int i=0; i<ST-1; i++) pipe_issue();
+    }
     for(size_t w = (size_t)blockIdx.x*blockDim.x + threadIdx.x; w < nwork;
         w += (size_t)gridDim.x*blockDim.x) {
       const int site = (int)(w / Q);
@@ -351,29 +446,6 @@ stag_dslash_mr(qllg_stag_args a)
               const int d = (nk ? 3 : 1)*(back ? -1 : 1);
               const size_t nb = (size_t)nbr_index(G, x, mu, d);
               const size_t kb = nb*NR;
-              if constexpr (MrCfg<PS,R,CFG>::pfl && PS == QLLG_F32 && PL == QLLG_F32 && NR == 16) {
-                // the next slot (nk, then back, then mu): lane q < 3 of a
-                // site prefetches colour q of that slot's neighbour (one
-                // 128-byte line: its 16 rhs); the lanes of site offset e in
-                // the warp prefetch link entry e (and 8) of the warp's eight
-                // sites, one 64-byte run
-                int nnk = nk + 1, nback = back, nmu = mu;
-                if(nnk == (NS == 16 ? 2 : 1)) { nnk = 0; nback++; }
-                if(nback == 2) { nback = 0; nmu++; }
-                if(nmu < 4) {
-                  const int nd = (nnk ? 3 : 1)*(nback ? -1 : 1);
-                  const size_t nbn = (size_t)nbr_index(G, x, nmu, nd);
-                  if(q < 3) prefetch_l1((const float2 *)a.in + (size_t)q*total + nbn*NR);
-                  if(!a.fb) {
-                    const int nslot = (NS == 16) ? (4*nmu + 2*nback + nnk) : (2*nmu + nback);
-                    const int e = (threadIdx.x & 31) >> 2;
-                    const size_t s0 = loff + ((size_t)site & ~(size_t)7);
-                    const float2 *lb = (const float2 *)a.links + (size_t)nslot*9*V + s0;
-                    if(q == 0) prefetch_l1(lb + (size_t)e*V);
-                    if(q == 1 && e == 0) prefetch_l1(lb + 8*V);
-                  }
-                }
-              }
               Cx<T> U[9];
               slot_link<PL,NS>(a, mu, back, nk, V, (size_t)G.Vh, loff, (size_t)site, nb, U);
               if constexpr (v4) {
@@ -412,7 +484,52 @@ stag_dslash_mr(qllg_stag_args a)
           }
         }
       };
-      if constexpr (PF && v4) {
+      // the per-warp pipeline: per slot, copy the slot ST - 1 ahead, wait
+      // for this one, compute it from the ring.  The warp barriers order
+      // the ring: every lane's copies are visible before the stage is
+      // read, and every lane has read a stage before it is refilled
+      auto pipe_slots = [&]() {
+        if constexpr (PIPE) {
+#pragma unroll 1
+          for(int sl=0; sl<NS; sl++) {
+            pipe_issue();
+            cp_async_wait<ST - 1>();
+            __syncwarp();
+            const unsigned char *sb = wring_p + cbuf*kPipeStage;
+            Cx<T> U[9];
+            const float2 *ls = (const float2 *)(sb + kPipeSpinor) + (lane >> 2);
+#pragma unroll
+            for(int k=0; k<9; k++) { const float2 t = ls[8*k]; U[k].r = t.x; U[k].i = t.y; }
+#pragma unroll
+            for(int h=0; h<R/2; h++) {
+              Cx<T> v[2][3];
+#pragma unroll
+              for(int c=0; c<3; c++) {
+                const float4 t = ((const float4 *)(sb + c*1024 + h*512))[lane ^ (h << 2)];
+                v[0][c].r = t.x; v[0][c].i = t.y; v[1][c].r = t.z; v[1][c].i = t.w;
+              }
+#pragma unroll
+              for(int jj=0; jj<2; jj++) {
+#pragma unroll
+                for(int l=0; l<3; l++) {
+#pragma unroll
+                  for(int c=0; c<3; c++) {
+                    if constexpr (F2) cmac_f2(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
+                    else cmac(acc[2*h + jj][c], U[3*l + c], v[jj][l]);
+                  }
+                }
+              }
+            }
+            __syncwarp();
+            cbuf = cbuf + 1 == ST ? 0 : cbuf + 1;
+          }
+        }
+      };
+      if constexpr (PIPE) {
+        // inactive rhs are computed too (their sums are neither stored nor
+        // reduced), so that one copy of the slot loop serves every launch
+        pipe_slots();
+      } else if constexpr (PF && v4) {
         // software pipeline, one slot ahead: the links and neighbour
         // spinors of slot s+1 are loaded before the FMAs of slot s.  The
         // run-time branch on a.fb in slot_link keeps the compiler from
@@ -557,6 +674,10 @@ stag_dslash_mr(qllg_stag_args a)
         if(a.norm_self && a.self) norm1(j, self);
       }
     }
+  }
+  if constexpr (PIPE) {
+    cp_async_wait<0>();              // only empty groups are left
+    __syncthreads();                 // the reduction reuses the ring
   }
   double red[2][R];
   if constexpr (LEAN) {
@@ -708,14 +829,20 @@ int launch_mr(const qllg_stag_args *a)
     if constexpr (CFG == 0) return vec ? stag_dslash_mr<PS,PL,NS,NR,R,true,0> : stag_dslash_mr<PS,PL,NS,NR,R,false,0>;
     else { (void)vec; return stag_dslash_mr<PS,PL,NS,NR,R,true,CFG>; }
   };
+  // the per-warp pipeline's ring: dynamic shared memory
+  constexpr int ST = MrCfg<PS,R,CFG>::pipe;
+  constexpr size_t DSM = (ST && PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16)
+                         ? (size_t)(TB/32)*(ST*kPipeStage + 8*NS*sizeof(int)) : 0;
   static int blocks_per_sm[2] = {0, 0};
   for(int k=0; k<2; k++) {
     // a preload loads both access widths of CFG 0
     const bool vk = a->preload ? (CFG != 0 || k == 1) : v4;
     if(!a->preload && k) break;
     if(!blocks_per_sm[vk]) {
+      if(DSM > 48*1024 && qllg_check_cuda(cudaFuncSetAttribute(kern(vk),
+           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DSM), "shared memory")) return -1;
       if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-           &blocks_per_sm[vk], kern(vk), TB, 0), "occupancy")) return -1;
+           &blocks_per_sm[vk], kern(vk), TB, DSM), "occupancy")) return -1;
       if(blocks_per_sm[vk] < 1) blocks_per_sm[vk] = 1;
     }
   }
@@ -730,7 +857,7 @@ int launch_mr(const qllg_stag_args *a)
   A.partial = a->rb ? a->rb->partial : NULL;
   A.counter = a->rb ? a->rb->counter : NULL;
   A.one_path = qllg_get_param("dslash_split") == 0;
-  kern(v4)<<<grid, TB, 0, qllg_stream()>>>(A);
+  kern(v4)<<<grid, TB, DSM, qllg_stream()>>>(A);
   return qllg_launched("stag_dslash_mr launch");
 }
 
@@ -1063,10 +1190,11 @@ int launch_tile(const qllg_stag_args *a)
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
-// launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15, 16, 17, 18, 19, 20
-// as variants 4-10 and 12-19) and 11 = the bulk-copy pipeline (FP32 links and
+// launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15, 16, 17 as variants
+// 4-10 and 12-16), and 17-21 the per-warp pipeline (MrCfg 18-22: FP32
+// links too, double-stored, Vh a multiple of 8) and 11 = the bulk-copy pipeline (FP32 links and
 // spinors, 16 slots, 16 rhs, k_stag_bulk.cuh)
-constexpr int kNumVariants = 20;
+constexpr int kNumVariants = 22;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
@@ -1077,9 +1205,9 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "4 rhs/thread lean 64 regs rolled (128 threads)",
                                                 "4 rhs/thread lean 64 regs rolled, paired rhs",
                                                 "4 rhs/thread lean 64 regs rolled (128 threads), paired rhs",
-                                                "4 rhs/thread lean 64 regs rolled, paired rhs, packed FMA",
-                                                "4 rhs/thread lean 64 regs rolled, L1 prefetch",
-                                                "4 rhs/thread lean 64 regs rolled (128 threads), L1 prefetch"};
+                                                "warp pipeline, 2 stages", "warp pipeline, 3 stages",
+                                                "warp pipeline, 4 stages", "warp pipeline, 3 stages, packed FMA",
+                                                "warp pipeline, 4 stages, packed FMA"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1090,6 +1218,10 @@ bool variant_ok(const qllg_stag_args *a, int v)
   if(v == 11)
     return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
            a->g.Vh % kBkSites == 0 && vec4_ok(a) && qllg_get_param("dslash_bulk") != 0;
+  if(v >= 17)
+    return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
+           a->g.Vh % 8 == 0 && ((uintptr_t)a->links & 15u) == 0 && vec4_ok(a) &&
+           qllg_get_param("dslash_vec4") != 0 && qllg_get_param("dslash_pipe") != 0;
   if(v >= 4)
     return PS == QLLG_F32 && NR == 16 && vec4_ok(a) && qllg_get_param("dslash_vec4") != 0;
   return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
@@ -1121,7 +1253,9 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 16: return launch_mr<PS,PL,NS,NR,4,17>(a);
       case 17: return launch_mr<PS,PL,NS,NR,4,18>(a);
       case 18: return launch_mr<PS,PL,NS,NR,4,19>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,20>(a);
+      case 19: return launch_mr<PS,PL,NS,NR,4,20>(a);
+      case 20: return launch_mr<PS,PL,NS,NR,4,21>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,22>(a);
       }
     }
   }

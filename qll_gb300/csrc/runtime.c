@@ -330,6 +330,7 @@ static struct { const char *name; double value; } g_params[] = {
   {"autotune", 1},           /* time the Dslash variants of a new launch shape */
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
+  {"dslash_pipe", 1},        /* allow the per-warp cp.async pipeline Dslash variants */
   {"solve2_mixed", 0},       /* solve2D (drop-in): FP32 iterations with FP64 reliable
                                 updates instead of the reference's FP64 CG */
   {"wilson_c3", 0},          /* small one-rhs FP32 Wilson launches: three threads
@@ -347,7 +348,7 @@ static struct { const char *name; double value; } g_params[] = {
                                 block of 256 threads per SM */
   {"dslash_split", 1},       /* multi-rhs Dslash: a slot loop without the active
                                 checks for launches with every rhs active */
-  {"dslash_variant", -1},    /* force a Dslash variant (0-19, qllg_autotune_report names
+  {"dslash_variant", -1},    /* force a Dslash variant (0-21, qllg_autotune_report names
                                 them); -1: autotuned */
   {"multishift_guess_rsq", 1e-10}, /* mixed multishift: the FP32 multishift CG
                                        goes to |r|^2 < this |b|^2 before the

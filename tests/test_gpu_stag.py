@@ -335,7 +335,7 @@ def test_dslash_variants_agree(nrhs):
     g = torch.Generator(device="cuda").manual_seed(91 + nrhs)
     src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
     outs = []
-    for v in range(20):
+    for v in range(22):
         L.qllg_set_param(b"dslash_variant", v)
         for parity in (0, 1):
             dst = torch.full_like(src, float("nan"))
@@ -352,7 +352,62 @@ def test_dslash_variants_agree(nrhs):
     L.qllg_stag_destroy(S)
 
 
-@pytest.mark.parametrize("variant", range(20))
+def test_warp_pipeline_over_several_passes():
+    """the per-warp cp.async pipeline (variants 17-21) on a lattice where
+    every warp takes several groups of sites, so that its ring prefetches
+    across the site boundary: bitwise the register kernel's Dslash, and a
+    16-rhs mixed solve (fused CG epilogue, norms, rhs dropping out as they
+    converge) to the same FP64 true residual in the same iterations"""
+    torch = pytest.importorskip("torch")
+    from ctypes import POINTER, c_void_p
+    dims = (16, 16, 16, 32)
+    L = qll.load()
+    L.qllg_stag_create_asqtad.restype = c_void_p
+    L.qllg_stag_create_asqtad.argtypes = [POINTER(c_int), POINTER(c_void_p), POINTER(qll.Fat7Coeffs)]
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    L.qllg_stag_vec_bytes.restype = ctypes.c_size_t
+    L.qllg_stag_vec_bytes.argtypes = [ctypes.c_void_p, c_int, c_int]
+    L.qllg_stag_dslash_device.argtypes = [ctypes.c_void_p, c_int, c_int, c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    thin = qll.gen_gauge(dims, 1005, 0.3, ks=True)
+    S = c_void_p(L.qllg_stag_create_asqtad(qll.dims_c(dims), qll.vp_array(thin),
+                                           byref(qll.asqtad_coeffs())))
+    assert S.value, qll.last_error()
+    n = L.qllg_stag_vec_bytes(S, 1, 16)//4
+    g = torch.Generator(device="cuda").manual_seed(77)
+    src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
+    want = {}
+    for v in (10, 17, 18, 19, 20, 21):
+        L.qllg_set_param(b"dslash_variant", v)
+        for parity in (0, 1):
+            dst = torch.full_like(src, float("nan"))
+            torch.cuda.synchronize()
+            assert L.qllg_stag_dslash_device(S, 1, 16, parity, ctypes.c_void_p(dst.data_ptr()),
+                                             ctypes.c_void_p(src.data_ptr())) == 0, qll.last_error()
+            torch.cuda.synchronize()
+            if parity not in want:
+                want[parity] = dst
+            assert torch.equal(dst, want[parity]), (v, parity)
+    nrhs = 16
+    masses = [0.02 + 0.01*k for k in range(nrhs)]
+    bs = [qll.gen_source(dims, 8100 + k, 6, "even") for k in range(nrhs)]
+    iters = {}
+    for v in (10, 19):
+        L.qllg_set_param(b"dslash_variant", v)
+        xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
+        info = qll.SolveInfo()
+        its = L.qllg_stag_solve(S, nrhs, qll.vp_array(xs), qll.vp_array(bs), (c_double*nrhs)(*masses),
+                                1e-16, 5000, qll.SOLVE_MIXED_SINGLE, byref(info))
+        assert its > 0, qll.last_error()
+        assert max(info.true_rsq[k] for k in range(nrhs)) < 1e-16*1.0001, v
+        iters[v] = [info.iters[k] for k in range(nrhs)]
+    L.qllg_set_param(b"dslash_variant", -1)
+    # the per-rhs sums are folded in a different order: iterations within 2
+    assert all(abs(a - b) <= 2 for a, b in zip(iters[10], iters[19])), iters
+    L.qllg_stag_destroy(S)
+
+
+@pytest.mark.parametrize("variant", range(22))
 def test_mixed_solve_with_each_dslash_variant(variant):
     """the fused CG epilogue and the norms of every variant: the 16-rhs
     mixed solve reaches the FP64 true residual and matches the oracle"""
