@@ -52,9 +52,9 @@ CONFIG = {"workload": WORKLOAD, "lattice": list(DIMS), "mass": MASS, "eps": EPS,
           "tol_true_residual": 1e-8, "parallelism": "replicas (one process per GPU, no collective)",
           "l2": "inputs larger than L2 (links 2.4 GB FP32 + 4.8 GB FP64)"}
 # DRAM bytes (read + write) per even site of one 16-rhs FP32 half Dslash
-# (the autotuned lean 64-register rolled launch shape), ncu capture at
-# 24^3x48: 554.7 MB + 121.5 MB over 331,776 sites
-TRAFFIC_PER_SITE_BYTES = (554.6688e6 + 121.459712e6)/331776
+# (the autotuned launch shape, the per-warp cp.async pipeline with 4
+# stages), ncu capture at 24^3x48: 531.2 MB + 112.1 MB over 331,776 sites
+TRAFFIC_PER_SITE_BYTES = (531.186176e6 + 112.13824e6)/331776
 
 
 def apply_params(L, args):

@@ -305,8 +305,9 @@ void qllg_server_destroy(qllg_server *V);
  *    checks when every rhs of a launch is active);
  *  "autotune" (1: time the Dslash launch shapes of each new shape and keep
  *    the fastest), "dslash_tile" (1) and "dslash_bulk" (1): the staged and
- *    the bulk-copy candidates may be chosen, "dslash_pipe" (1): the per-warp
- *    cp.async pipeline candidates may be chosen; "dslash_variant" (-1: autotuned;
+ *    the bulk-copy candidates may be chosen, "dslash_pipe" (1) and
+ *    "dslash_tma" (1): the per-warp cp.async and tensor-copy pipeline
+ *    candidates may be chosen; "dslash_variant" (-1: autotuned;
  *    0-21 forces a candidate where it applies, qllg_autotune_report names
  *    them);
  *  "links_recon12" (0; 1: reconstruct-12 Naik links in the FP32 solves),

@@ -13,6 +13,7 @@
 #pragma once
 #include <stdio.h>
 #include <type_traits>
+#include <cuda.h>                 // CUtensorMap (the encoder is reached through the runtime)
 #include "kcommon.cuh"
 
 using namespace qk;
@@ -226,21 +227,22 @@ stag_dslash(qllg_stag_args a)
 // slot from shared memory, so that no register holds a load in flight and
 // a slot costs one wait instead of the two or three dependent load round
 // trips of the register shapes.  128-thread blocks; (ST, blocks/SM):
-// 18 (2, 6), 19 (3, 4), 20 (4, 3), and 21 and 22: 19 and 20 with packed
-// FP32 FMAs (the pipeline issues more instructions than the register
-// shapes and no longer waits on loads, so halving the FMA instructions
-// pays here).  The 3-stage ring at 5 blocks/SM (102 registers) spilled
-// and measured 1.03 ms at 32^3x64 against 0.78 at 4 blocks; dropped.
+// 18 (2, 6), 19 (3, 4), 20 (4, 3).  Dropped: the 3-stage ring at 5
+// blocks/SM (102 registers) spilled and measured 1.03 ms at 32^3x64
+// against 0.73 at 4 blocks; 19 and 20 with packed FP32 FMAs measured 0.75
+// and 0.72 against 0.73 and 0.72 (fma.rn.f32x2 wants its operands as
+// register pairs, and the complex MAC's v.r and v.i broadcast into pairs
+// costs the moves that the halved FMA count saves).
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int pipe = (CFG >= 18 && CFG <= 22 && PS == QLLG_F32 && R == 4)
-                              ? ((CFG == 18) ? 2 : (CFG == 20 || CFG == 22) ? 4 : 3) : 0;
+  static constexpr int pipe = (CFG >= 18 && CFG <= 20 && PS == QLLG_F32 && R == 4)
+                              ? (CFG == 18 ? 2 : CFG == 20 ? 4 : 3) : 0;
   static constexpr int threads = (CFG == 14 || CFG == 15 || CFG == 17 || CFG >= 18) ? 128 : 256;
   static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 :
                               (CFG == 3 || CFG == 8 || CFG == 16) ? 4 :
                               CFG == 14 ? 7 : (CFG == 15 || CFG == 17) ? 8 :
-                              CFG == 18 ? 6 : (CFG == 19 || CFG == 21) ? 4 : (CFG == 20 || CFG == 22) ? 3 :
+                              CFG == 18 ? 6 : CFG == 19 ? 4 : CFG == 20 ? 3 :
                               (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
-  static constexpr bool f2 = (CFG == 1 || CFG == 21 || CFG == 22) && PS == QLLG_F32;
+  static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7 && !pipe;
   static constexpr bool pf = CFG == 5 || CFG == 6;
   static constexpr bool roll = CFG == 7 || CFG == 8 || CFG == 9 || CFG >= 14;   // direction loop rolled
@@ -1185,14 +1187,17 @@ int launch_tile(const qllg_stag_args *a)
 }
 
 #include "k_stag_bulk.cuh"
+#include "k_stag_tma.cuh"
 
 // variants of one launch shape, in the order the autotuner tries them:
 // 0 = 4 rhs per thread, 1 = 2 rhs per thread, 2 = one thread per (site,
 // rhs), 3 = shared-memory staging (FP32, 16 slots, 16 rhs only); FP32
 // spinors at 16 rhs with 16-byte access also the 4-rhs kernel's other
 // launch shapes (MrCfg 1, 2, 3, 5, 6, 7, 8, 9, 14, 15, 16, 17 as variants
-// 4-10 and 12-16), and 17-21 the per-warp pipeline (MrCfg 18-22: FP32
-// links too, double-stored, Vh a multiple of 8) and 11 = the bulk-copy pipeline (FP32 links and
+// 4-10 and 12-16), 17-19 the per-warp cp.async pipeline (MrCfg 18-20:
+// FP32 links too, double-stored, Vh a multiple of 8), and 20-21 the
+// per-warp tensor-copy pipeline (k_stag_tma.cuh, 3 and 4 stages; the same
+// conditions) and 11 = the bulk-copy pipeline (FP32 links and
 // spinors, 16 slots, 16 rhs, k_stag_bulk.cuh)
 constexpr int kNumVariants = 22;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
@@ -1206,8 +1211,8 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "4 rhs/thread lean 64 regs rolled, paired rhs",
                                                 "4 rhs/thread lean 64 regs rolled (128 threads), paired rhs",
                                                 "warp pipeline, 2 stages", "warp pipeline, 3 stages",
-                                                "warp pipeline, 4 stages", "warp pipeline, 3 stages, packed FMA",
-                                                "warp pipeline, 4 stages, packed FMA"};
+                                                "warp pipeline, 4 stages", "warp tensor-copy pipeline, 3 stages",
+                                                "warp tensor-copy pipeline, 4 stages"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1218,6 +1223,9 @@ bool variant_ok(const qllg_stag_args *a, int v)
   if(v == 11)
     return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
            a->g.Vh % kBkSites == 0 && vec4_ok(a) && qllg_get_param("dslash_bulk") != 0;
+  if(v >= 20)
+    return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && tma_ok(a) && vec4_ok(a) &&
+           qllg_get_param("dslash_tma") != 0;
   if(v >= 17)
     return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
            a->g.Vh % 8 == 0 && ((uintptr_t)a->links & 15u) == 0 && vec4_ok(a) &&
@@ -1235,6 +1243,8 @@ int launch_variant(const qllg_stag_args *a, int v)
   if constexpr (PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16) {
     if(v == 3) return launch_tile<NR>(a);
     if(v == 11) return launch_bulk<NR>(a);
+    if(v == 20) return launch_tma<NR,3,4>(a);
+    if(v == 21) return launch_tma<NR,4,3>(a);
   }
   if constexpr (PS == QLLG_F32 && NR == 16) {
     if(v >= 4) {
@@ -1253,9 +1263,7 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 16: return launch_mr<PS,PL,NS,NR,4,17>(a);
       case 17: return launch_mr<PS,PL,NS,NR,4,18>(a);
       case 18: return launch_mr<PS,PL,NS,NR,4,19>(a);
-      case 19: return launch_mr<PS,PL,NS,NR,4,20>(a);
-      case 20: return launch_mr<PS,PL,NS,NR,4,21>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,22>(a);
+      default: return launch_mr<PS,PL,NS,NR,4,20>(a);
       }
     }
   }

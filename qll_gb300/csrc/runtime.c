@@ -331,6 +331,7 @@ static struct { const char *name; double value; } g_params[] = {
   {"dslash_tile", 1},        /* allow the shared-memory-staged Dslash variant */
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
   {"dslash_pipe", 1},        /* allow the per-warp cp.async pipeline Dslash variants */
+  {"dslash_tma", 1},         /* allow the per-warp tensor-copy (TMA) pipeline Dslash variants */
   {"solve2_mixed", 0},       /* solve2D (drop-in): FP32 iterations with FP64 reliable
                                 updates instead of the reference's FP64 CG */
   {"wilson_c3", 0},          /* small one-rhs FP32 Wilson launches: three threads

@@ -93,12 +93,13 @@ def test_barrier_wait_runs_out_with_an_error():
         L.qllg_stag_destroy(S)
 
 
-def test_bulk_pipeline_wait_runs_out_with_an_error():
-    """the bulk-copy pipeline's waits take the same limit: with its
-    producer told to issue no copy (bulk_wait_test) the consumers' first
-    waits run out after the limit, the launch records the error flag and
-    returns; with copies issued again the same launch is bitwise the
-    register kernel's"""
+@pytest.mark.parametrize("pipeline", [11, 20])
+def test_bulk_pipeline_wait_runs_out_with_an_error(pipeline):
+    """the copy pipelines' waits (the bulk-copy kernel, variant 11, and the
+    per-warp tensor-copy kernel, variant 20) take the same limit: with
+    their copies not issued (bulk_wait_test) the first waits run out after
+    the limit, the launch records the error flag and returns; with copies
+    issued again the same launch is bitwise the register kernel's"""
     torch = pytest.importorskip("torch")
     L, S, u, u3 = _op()
     try:
@@ -111,7 +112,7 @@ def test_bulk_pipeline_wait_runs_out_with_an_error():
         src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
         outs = []
         assert L.qllg_k_bulk_error(1) >= 0
-        for variant, test in ((11, 1), (11, 0), (10, 0)):
+        for variant, test in ((pipeline, 1), (pipeline, 0), (10, 0)):
             L.qllg_set_param(b"dslash_variant", variant)
             L.qllg_set_param(b"bulk_wait_test", test)
             L.qllg_set_param(b"wait_polls", 2e5 if test else 2e7)

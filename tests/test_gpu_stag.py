@@ -353,11 +353,12 @@ def test_dslash_variants_agree(nrhs):
 
 
 def test_warp_pipeline_over_several_passes():
-    """the per-warp cp.async pipeline (variants 17-21) on a lattice where
-    every warp takes several groups of sites, so that its ring prefetches
-    across the site boundary: bitwise the register kernel's Dslash, and a
-    16-rhs mixed solve (fused CG epilogue, norms, rhs dropping out as they
-    converge) to the same FP64 true residual in the same iterations"""
+    """the per-warp cp.async pipelines (variants 17-19) and tensor-copy
+    pipelines (20, 21) on a lattice where every warp takes several groups
+    of sites, so that its ring prefetches across the group boundary:
+    bitwise the register kernel's Dslash, and a 16-rhs mixed solve (fused
+    CG epilogue, norms, rhs dropping out as they converge) to the same FP64
+    true residual in the same iterations"""
     torch = pytest.importorskip("torch")
     from ctypes import POINTER, c_void_p
     dims = (16, 16, 16, 32)
@@ -392,7 +393,7 @@ def test_warp_pipeline_over_several_passes():
     masses = [0.02 + 0.01*k for k in range(nrhs)]
     bs = [qll.gen_source(dims, 8100 + k, 6, "even") for k in range(nrhs)]
     iters = {}
-    for v in (10, 19):
+    for v in (10, 19, 20):
         L.qllg_set_param(b"dslash_variant", v)
         xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
         info = qll.SolveInfo()
@@ -403,7 +404,9 @@ def test_warp_pipeline_over_several_passes():
         iters[v] = [info.iters[k] for k in range(nrhs)]
     L.qllg_set_param(b"dslash_variant", -1)
     # the per-rhs sums are folded in a different order: iterations within 2
-    assert all(abs(a - b) <= 2 for a, b in zip(iters[10], iters[19])), iters
+    for v in (19, 20):
+        assert all(abs(a - b) <= 2 for a, b in zip(iters[10], iters[v])), iters
+    assert L.qllg_k_bulk_error(1) == 0
     L.qllg_stag_destroy(S)
 
 
