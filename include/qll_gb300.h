@@ -308,7 +308,7 @@ void qllg_server_destroy(qllg_server *V);
  *    the bulk-copy candidates may be chosen, "dslash_pipe" (1) and
  *    "dslash_tma" (1): the per-warp cp.async and tensor-copy pipeline
  *    candidates may be chosen; "dslash_variant" (-1: autotuned;
- *    0-21 forces a candidate where it applies, qllg_autotune_report names
+ *    0-23 forces a candidate where it applies, qllg_autotune_report names
  *    them);
  *  "links_recon12" (0; 1: reconstruct-12 Naik links in the FP32 solves),
  *  "solve2_mixed" (0; 1: the drop-in solve2D runs FP32 iterations with FP64

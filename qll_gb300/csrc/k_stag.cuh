@@ -356,21 +356,26 @@ stag_dslash_mr(qllg_stag_args a)
   const int lane = threadIdx.x & 31;
   const unsigned wring = (unsigned)__cvta_generic_to_shared(dsm) + (threadIdx.x >> 5)*(ST ? ST : 1)*kPipeStage;
   const unsigned char *wring_p = dsm + (threadIdx.x >> 5)*(ST ? ST : 1)*kPipeStage;
+  // the issue pointer: this lane's work item and slot of the next slot to
+  // copy; the byte offsets of the issue and the consume stages in the ring
   size_t iw = (size_t)blockIdx.x*blockDim.x + threadIdx.x;
-  int isl = 0, ibuf = 0, cbuf = 0;
-  // copy the next slot (or commit an empty group past the end of the
-  // warp's work, so that the group count stays uniform): lane L copies the
-  // 16-byte pieces L & 7 of the colour vectors of sites L >> 3 and
-  // 4 + (L >> 3), whose neighbours come from the lanes computing them, and
-  // link piece L (and 32 + L): entry L >> 2 of sites 2(L & 3), 2(L & 3) + 1
+  int isl = 0;
+  unsigned ioff = 0, coff = 0;
   // the neighbours of the warp's eight sites for the sixteen slots of the
-  // issue pointer's site, [slot][site], after the ring: filled when the
-  // issue pointer reaches a site, lane 4e + q taking the four slots of
+  // issue pointer's site group, [slot][site], after the ring: filled when
+  // the issue pointer reaches a group, lane 4e + q taking the four slots of
   // direction q of site e; read by the copies of each slot
   int *wnb = reinterpret_cast<int *>(dsm + (TB/32)*(ST ? ST : 1)*kPipeStage) + (threadIdx.x >> 5)*8*NS;
-  const char *ilk = nullptr, *ilk8 = nullptr;   // this lane's link pieces of slot 0 at the issue site
-  const char *const isp = (const char *)a.in + (lane & 7)*16;
+  // lane L copies the 16-byte pieces b = L & 7 of the colour vectors of
+  // sites L >> 3 and 4 + (L >> 3) (the neighbours come from the table), to
+  // [colour][b & 1][(L >> 3) ^ (b & 1)][b >> 1], and link piece L (and 32 +
+  // L): entry L >> 2 of sites 2(L & 3), 2(L & 3) + 1 of the group
+  const unsigned dlane = ((lane & 1) << 9) + ((((lane >> 3) ^ (lane & 1)) << 2) << 4) + (((lane & 7) >> 1) << 4);
   const size_t cst = total*8;                   // bytes between colours
+  const char *const isp0 = (const char *)a.in + (lane & 7)*16;
+  const char *const isp1 = isp0 + cst, *const isp2 = isp1 + cst;
+  const size_t lstride = (size_t)9*V*8;         // bytes between slots' link blocks
+  const char *ilk = nullptr, *ilk8 = nullptr;   // this lane's link pieces of the next slot
   auto pipe_issue = [&]() {
     if constexpr (PIPE) {
       if(iw < nwork) {
@@ -387,24 +392,23 @@ stag_dslash_mr(qllg_stag_args a)
           ilk8 = (const char *)(lk + 8*V);
           __syncwarp();
         }
-        const int n0 = wnb[isl*8 + (lane >> 3)], n1 = wnb[isl*8 + 4 + (lane >> 3)];
-        const int b = lane & 7;
-        const unsigned dst = wring + ibuf*kPipeStage + ((b & 1) << 9) +
-                             (((((lane >> 3) ^ (b & 1)) << 2) + (b >> 1)) << 4);
-        const char *src0 = isp + (size_t)n0*(NR*8), *src1 = isp + (size_t)n1*(NR*8);
-#pragma unroll
-        for(int c=0; c<3; c++) {
-          cp_async16_ca(dst + c*1024, src0 + c*cst);
-          cp_async16_ca(dst + c*1024 + 256, src1 + c*cst);
-        }
-        const size_t so = (size_t)isl*9*V*8;
-        const unsigned ldst = wring + ibuf*kPipeStage + kPipeSpinor;
-        cp_async16_ca(ldst + lane*16, ilk + so);
-        if(lane < 4) cp_async16_ca(ldst + 512 + lane*16, ilk8 + so);
+        const unsigned n0 = (unsigned)wnb[isl*8 + (lane >> 3)], n1 = (unsigned)wnb[isl*8 + 4 + (lane >> 3)];
+        const unsigned dst = wring + ioff + dlane;
+        cp_async16_ca(dst, isp0 + (size_t)n0*(NR*8));
+        cp_async16_ca(dst + 256, isp0 + (size_t)n1*(NR*8));
+        cp_async16_ca(dst + 1024, isp1 + (size_t)n0*(NR*8));
+        cp_async16_ca(dst + 1024 + 256, isp1 + (size_t)n1*(NR*8));
+        cp_async16_ca(dst + 2048, isp2 + (size_t)n0*(NR*8));
+        cp_async16_ca(dst + 2048 + 256, isp2 + (size_t)n1*(NR*8));
+        const unsigned ldst = wring + ioff + kPipeSpinor + lane*16;
+        cp_async16_ca(ldst, ilk);
+        if(lane < 4) cp_async16_ca(ldst + 512, ilk8);
+        ilk += lstride;
+        ilk8 += lstride;
         if(++isl == NS) { isl = 0; iw += (size_t)gridDim.x*blockDim.x; }
       }
       cp_async_commit();
-      ibuf = ibuf + 1 == ST ? 0 : ibuf + 1;
+      ioff = ioff + kPipeStage == (unsigned)(ST*kPipeStage) ? 0u : ioff + kPipeStage;
     }
   };
   // the pipeline runs whole warps (its copies and shuffles are warp-wide):
@@ -497,7 +501,7 @@ stag_dslash_mr(qllg_stag_args a)
             pipe_issue();
             cp_async_wait<ST - 1>();
             __syncwarp();
-            const unsigned char *sb = wring_p + cbuf*kPipeStage;
+            const unsigned char *sb = wring_p + coff;
             Cx<T> U[9];
             const float2 *ls = (const float2 *)(sb + kPipeSpinor) + (lane >> 2);
 #pragma unroll
@@ -523,7 +527,7 @@ stag_dslash_mr(qllg_stag_args a)
               }
             }
             __syncwarp();
-            cbuf = cbuf + 1 == ST ? 0 : cbuf + 1;
+            coff = coff + kPipeStage == (unsigned)(ST*kPipeStage) ? 0u : coff + kPipeStage;
           }
         }
       };
@@ -1197,9 +1201,9 @@ int launch_tile(const qllg_stag_args *a)
 // 4-10 and 12-16), 17-19 the per-warp cp.async pipeline (MrCfg 18-20:
 // FP32 links too, double-stored, Vh a multiple of 8), and 20-21 the
 // per-warp tensor-copy pipeline (k_stag_tma.cuh, 3 and 4 stages; the same
-// conditions) and 11 = the bulk-copy pipeline (FP32 links and
+// conditions), 22-23 the same in one-warp blocks and 11 = the bulk-copy pipeline (FP32 links and
 // spinors, 16 slots, 16 rhs, k_stag_bulk.cuh)
-constexpr int kNumVariants = 22;
+constexpr int kNumVariants = 24;
 const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", "1 rhs/thread",
                                                 "smem-staged 4 rhs/thread", "4 rhs/thread packed FMA",
                                                 "4 rhs/thread lean 80 regs", "4 rhs/thread lean 64 regs",
@@ -1212,7 +1216,9 @@ const char *const kVariantName[kNumVariants] = {"4 rhs/thread", "2 rhs/thread", 
                                                 "4 rhs/thread lean 64 regs rolled (128 threads), paired rhs",
                                                 "warp pipeline, 2 stages", "warp pipeline, 3 stages",
                                                 "warp pipeline, 4 stages", "warp tensor-copy pipeline, 3 stages",
-                                                "warp tensor-copy pipeline, 4 stages"};
+                                                "warp tensor-copy pipeline, 4 stages",
+                                                "one-warp tensor-copy pipeline, 3 stages",
+                                                "one-warp tensor-copy pipeline, 4 stages"};
 
 template <int PS, int PL, int NS, int NR>
 bool variant_ok(const qllg_stag_args *a, int v)
@@ -1243,8 +1249,10 @@ int launch_variant(const qllg_stag_args *a, int v)
   if constexpr (PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16) {
     if(v == 3) return launch_tile<NR>(a);
     if(v == 11) return launch_bulk<NR>(a);
-    if(v == 20) return launch_tma<NR,3,4>(a);
-    if(v == 21) return launch_tma<NR,4,3>(a);
+    if(v == 20) return launch_tma<NR,3,4,4>(a);
+    if(v == 21) return launch_tma<NR,4,3,4>(a);
+    if(v == 22) return launch_tma<NR,3,16,1>(a);
+    if(v == 23) return launch_tma<NR,4,13,1>(a);
   }
   if constexpr (PS == QLLG_F32 && NR == 16) {
     if(v >= 4) {

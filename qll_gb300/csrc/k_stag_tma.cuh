@@ -19,6 +19,16 @@
 // in the bulk-copy kernel), so that the 8 lanes of an access phase, two sites,
 // hit distinct banks.
 //
+// With one warp per block (W = 1) the group index comes from blockIdx alone,
+// so the first site's coordinates and its neighbour in each slot are
+// block-uniform values, which the copies take as operands directly: when the
+// eight neighbours of a slot are consecutive sites (every slot but the
+// x-direction ones at a row's end, when the row holds a whole number of
+// groups) the slot's spinors are one tiled 3-D copy of 3 x 8 rows instead of
+// six gathers.  (With four warps a block, each copy's operands come from
+// per-lane registers, and the issuing lane pays for moving them into
+// uniform registers: about 120 instructions a slot.)
+//
 // Waits are bounded as in the bulk-copy kernel: a wait that runs out records
 // an error in g_bulk_err and stops the warp's pipeline; the warp then lets the
 // copies it has issued land (each wait bounded by the fixed drain limit) and
@@ -27,22 +37,22 @@
 #pragma once
 
 // (included inside k_stag.cuh's anonymous namespace)
-constexpr int kTmW = 4;                         // warps per block
-constexpr int kTmThreads = 32*kTmW;
 constexpr int kTmSp = 3*8*128;                  // spinor rows of a stage: 3072 B
 constexpr int kTmLk = 9*8*8;                    // link block of a stage: 576 B
 constexpr int kTmLkPad = 640;                   // link stages 128-byte aligned
 
-// per block: [warp][stage] spinor rows, [warp][stage] link blocks, [warp]
-// [stage] barriers, [warp] tables of the neighbours' spinor rows
-// ([slot][colour][site]: colour*Vh + neighbour), the per-rhs scalars
-template <int ST> struct TmaLayout {
+// per block of W warps: [warp][stage] spinor rows, [warp][stage] link
+// blocks, [warp][stage] barriers, [warp] tables of the neighbours' spinor
+// rows ([slot][colour][site]: colour*Vh + neighbour), the per-rhs scalars,
+// and room for the norm reduction (2 x 4 rhs doubles a thread)
+template <int ST, int W> struct TmaLayout {
   static constexpr int sp = 0;
-  static constexpr int lk = kTmW*ST*kTmSp;
-  static constexpr int bar = lk + kTmW*ST*kTmLkPad;
-  static constexpr int nbt = bar + kTmW*ST*8;
-  static constexpr int scal = nbt + kTmW*16*3*8*4;
-  static constexpr int bytes = scal + 2*16*4;
+  static constexpr int lk = W*ST*kTmSp;
+  static constexpr int bar = lk + W*ST*kTmLkPad;
+  static constexpr int nbt = (bar + W*ST*8 + 127)/128*128;   // read as 16-byte vectors
+  static constexpr int scal = nbt + W*16*3*8*4;
+  static constexpr int end = scal + 2*16*4;
+  static constexpr int bytes = end > 2*4*32*W*8 ? end : 2*4*32*W*8;
 };
 
 // four 128-byte rows of a 2-D tensor (rows r.x..r.w, from column 0) into
@@ -53,6 +63,13 @@ __device__ __forceinline__ void tma_gather4(unsigned dst, const CUtensorMap *m, 
   asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
                " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
                :: "r"(dst), "l"(m), "r"(0), "r"(r.x), "r"(r.y), "r"(r.z), "r"(r.w), "r"(b) : "memory");
+}
+// the box of a 3-D tensor at (0, y, 0) into shared memory, completing on b
+__device__ __forceinline__ void tma_tile3d_y(unsigned dst, const CUtensorMap *m, int y, unsigned b)
+{
+  asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+               " [%0], [%1, {%2, %3, %4}], [%5];"
+               :: "r"(dst), "l"(m), "r"(0), "r"(y), "r"(0), "r"(b) : "memory");
 }
 // the box of a 2-D tensor at (x, y) into shared memory, completing on b
 __device__ __forceinline__ void tma_tile2d(unsigned dst, const CUtensorMap *m, int x, int y, unsigned b)
@@ -81,23 +98,25 @@ __device__ __forceinline__ bool mbar_wait_sleep(unsigned a, unsigned ph, long lo
 
 // FP32 spinors and links (double-stored), 16 slots, 16 rhs; modes 0-3 and the
 // norms as stag_dslash_mr.  tm_in: the input spinors as rows of 32 floats,
-// [colour*Vh + site]; tm_lk: the links as [slot*9 + entry][2V floats], box 16
-// floats x 9 rows.  Needs Vh a multiple of 8 (the launcher checks).
-template <int NR_, int ST, int MINB>
-__global__ void __launch_bounds__(kTmThreads, MINB)
+// [colour*Vh + site], box one row; tm_in3: the same as [colour][site][32
+// floats], box 3 x 8 x 32; tm_lk: the links as [slot*9 + entry][2V floats],
+// box 16 floats x 9 rows.  Needs Vh a multiple of 8 (the launcher checks).
+template <int NR_, int ST, int MINB, int W>
+__global__ void __launch_bounds__(32*W, MINB)
 stag_dslash_tma(qllg_stag_args a, const __grid_constant__ CUtensorMap tm_in,
-                const __grid_constant__ CUtensorMap tm_lk)
+                const __grid_constant__ CUtensorMap tm_in3, const __grid_constant__ CUtensorMap tm_lk)
 {
   extern __shared__ __align__(128) unsigned char tsm[];
   typedef float T;
-  typedef TmaLayout<ST> Lo;
+  typedef TmaLayout<ST,W> Lo;
+  constexpr int TB = 32*W;
   constexpr int NR = 16, R = 4, Q = 4, PS = QLLG_F32, PX = QLLG_F32;
   T *s_ca = (T *)(tsm + Lo::scal), *s_alpha = s_ca + NR;
   const Geo G = make_geo(a.g);
   const size_t total = (size_t)G.Vh*NR;
   const int p = a.out_parity;
   const int loff = p ? G.Vh : 0;
-  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, w = W == 1 ? 0 : tid >> 5, lane = tid & 31;
   const int e = lane >> 2, q = lane & 3, sw = e & 1;
   const bool skip = a.done && *(volatile const int *)a.done;     // uniform
   uint64_t *bars = (uint64_t *)(tsm + Lo::bar) + w*ST;
@@ -126,11 +145,13 @@ stag_dslash_tma(qllg_stag_args a, const __grid_constant__ CUtensorMap tm_in,
   for(int jp=0; jp<R; jp++) if(!a.active || a.active[q*R + jp]) actm |= 1u << jp;
   const bool allact = actm == (1u << R) - 1;
   const int ngroups = G.Vh/8;
-  const int gstride = gridDim.x*kTmW;
+  const int gstride = gridDim.x*W;
   // the issue pointer: group, slot and stage of the next slot to copy
-  int ig = blockIdx.x*kTmW + w, isl = 0, ibuf = 0, cbuf = 0;
+  int ig = blockIdx.x*W + w, isl = 0, ibuf = 0, cbuf = 0;
   unsigned ph = 0;                       // bit s: parity of stage s's next phase
   unsigned issued = 0, consumed = 0;
+  unsigned cmask = 0;                    // W == 1: bit s: slot s's 8 neighbours consecutive
+  int xf[4];                             // W == 1: coordinates of the group's first site
   auto issue = [&]() {
     if(ig < ngroups && ok) {
       if(isl == 0) {
@@ -138,25 +159,49 @@ stag_dslash_tma(qllg_stag_args a, const __grid_constant__ CUtensorMap tm_in,
         // takes the four slots of direction q of site e
         int xs[4];
         site_coords(G, p, ig*8 + e, xs);
+        unsigned ball[4];
 #pragma unroll
         for(int k=0; k<4; k++) {
           const int n = nbr_index(G, xs, q, (k & 1 ? 3 : 1)*(k & 2 ? -1 : 1));
 #pragma unroll
           for(int c=0; c<3; c++) nbt[((4*q + k)*3 + c)*8 + e] = c*G.Vh + n;
+          if constexpr (W == 1) {
+            // site e's neighbour follows site e - 1's (lane 4(e - 1) + q)
+            const int prev = __shfl_up_sync(0xffffffffu, n, 4);
+            ball[k] = __ballot_sync(0xffffffffu, e == 0 || n == prev + 1);
+          }
+        }
+        if constexpr (W == 1) {
+          cmask = 0;
+#pragma unroll
+          for(int qq=0; qq<4; qq++)
+#pragma unroll
+            for(int k=0; k<4; k++)
+              if(((ball[k] >> qq) & 0x11111111u) == 0x11111111u) cmask |= 1u << (4*qq + k);
+          site_coords(G, p, ig*8, xf);
         }
         __syncwarp();
       }
+      // W == 1: the first site's neighbour in this slot, from block-uniform
+      // values only
+      int nf = 0;
+      if constexpr (W == 1)
+        nf = nbr_index(G, xf, isl >> 2, (isl & 1 ? 3 : 1)*(isl & 2 ? -1 : 1));
       if(lane == 0 && !a.wait_test) {
-        const int4 *rows = (const int4 *)(nbt + isl*24);
         const unsigned bar = bars_s + ibuf*8, sp = spw_s + ibuf*kTmSp;
         // the lanes' reads of this stage (ordered by the warp barrier after
         // them) come before the copies' writes
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_expect_tx(&bars[ibuf], kTmSp + kTmLk);
+        if(W == 1 && ((cmask >> isl) & 1)) {
+          tma_tile3d_y(sp, &tm_in3, nf, bar);
+        } else {
+          const int4 *rows = (const int4 *)(nbt + isl*24);
 #pragma unroll
-        for(int c=0; c<3; c++) {
-          tma_gather4(sp + c*1024, &tm_in, rows[2*c], bar);
-          tma_gather4(sp + c*1024 + 512, &tm_in, rows[2*c + 1], bar);
+          for(int c=0; c<3; c++) {
+            tma_gather4(sp + c*1024, &tm_in, rows[2*c], bar);
+            tma_gather4(sp + c*1024 + 512, &tm_in, rows[2*c + 1], bar);
+          }
         }
         tma_tile2d(lkw_s + ibuf*kTmLkPad, &tm_lk, 2*(loff + ig*8), isl*9, bar);
       }
@@ -168,7 +213,7 @@ stag_dslash_tma(qllg_stag_args a, const __grid_constant__ CUtensorMap tm_in,
   if(!skip) {
 #pragma unroll
     for(int i=0; i<ST-1; i++) issue();
-    for(int g = blockIdx.x*kTmW + w; g < ngroups && ok; g += gstride) {
+    for(int g = blockIdx.x*W + w; g < ngroups && ok; g += gstride) {
       const int site = g*8 + e;
       const size_t t0 = (size_t)site*NR + q*R;
       Cx<T> acc[R][3];
@@ -290,7 +335,7 @@ stag_dslash_tma(qllg_stag_args a, const __grid_constant__ CUtensorMap tm_in,
   if(a.mode == 3) {
     if(skip) return;
     double *res[2] = {a.sc->tmp, NULL};
-    if(grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res, kTmThreads)) {
+    if(grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res, TB)) {
       __syncthreads();
       if(threadIdx.x == 0) {
         if(a.mixed) cg_finish_mixed(a.sc, NR);
@@ -299,7 +344,7 @@ stag_dslash_tma(qllg_stag_args a, const __grid_constant__ CUtensorMap tm_in,
     }
   } else if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
-    grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res, kTmThreads);
+    grid_reduce_mr<2,R>(red, NR, Q, a.partial, a.counter, shm, res, TB);
   }
 }
 
@@ -328,37 +373,40 @@ TmaEncodeFn tma_encoder()
   return fn;
 }
 
-// a 2-D FP32 tensor map (inner extent n0 floats, n1 rows of `pitch` bytes,
-// box b0 x b1), cached by address and shape: the solvers reuse a handful of
-// vectors and one link buffer per operator
-int tma_map(CUtensorMap *out, const void *base, uint64_t n0, uint64_t n1, uint64_t pitch,
-            uint32_t b0, uint32_t b1)
+// an FP32 tensor map of rank 2 or 3 (extents n[] from the innermost, byte
+// pitches pitch[] of the outer dimensions, box[]), cached by address and
+// shape: the solvers reuse a handful of vectors and one link buffer per
+// operator
+int tma_map(CUtensorMap *out, const void *base, int rank, const uint64_t *n, const uint64_t *pitch,
+            const uint32_t *box)
 {
-  struct Ent { const void *base; uint64_t n0, n1; uint32_t b0; CUtensorMap m; };
-  static Ent cache[16];
+  struct Ent { const void *base; int rank; uint64_t n[3]; uint32_t box[3]; CUtensorMap m; };
+  static Ent cache[24];
   static int used = 0, next = 0;
-  for(int i=0; i<used; i++)
-    if(cache[i].base == base && cache[i].n0 == n0 && cache[i].n1 == n1 && cache[i].b0 == b0) {
-      *out = cache[i].m;
-      return 0;
-    }
+  for(int i=0; i<used; i++) {
+    const Ent &E = cache[i];
+    bool same = E.base == base && E.rank == rank;
+    for(int d=0; d<rank && same; d++) same = E.n[d] == n[d] && E.box[d] == box[d];
+    if(same) { *out = E.m; return 0; }
+  }
   TmaEncodeFn enc = tma_encoder();
   if(!enc) { qllg_set_error("tensor-map encoder not available"); return -1; }
-  const cuuint64_t dims[2] = {n0, n1};
-  const cuuint64_t strides[1] = {pitch};
-  const cuuint32_t box[2] = {b0, b1};
-  const cuuint32_t estr[2] = {1, 1};
+  cuuint64_t dims[3], strides[2];
+  cuuint32_t bx[3], estr[3] = {1, 1, 1};
+  for(int d=0; d<rank; d++) { dims[d] = n[d]; bx[d] = box[d]; }
+  for(int d=0; d<rank-1; d++) strides[d] = pitch[d];
   Ent &E = cache[next];
-  if(enc(&E.m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, estr,
+  if(enc(&E.m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, (void *)base, dims, strides, bx, estr,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
     qllg_set_error("cuTensorMapEncodeTiled failed");
     return -1;
   }
-  E.base = base; E.n0 = n0; E.n1 = n1; E.b0 = b0;
+  E.base = base; E.rank = rank;
+  for(int d=0; d<rank; d++) { E.n[d] = n[d]; E.box[d] = box[d]; }
   *out = E.m;
-  next = (next + 1) % 16;
-  if(used < 16) used++;
+  next = (next + 1) % 24;
+  if(used < 24) used++;
   return 0;
 }
 
@@ -368,27 +416,34 @@ bool tma_ok(const qllg_stag_args *a)
          ((uintptr_t)a->in & 15u) == 0 && tma_encoder() != NULL;
 }
 
-template <int NR_, int ST, int MINB>
+template <int NR_, int ST, int MINB, int W>
 int launch_tma(const qllg_stag_args *a)
 {
-  constexpr int smem = TmaLayout<ST>::bytes;
+  constexpr int smem = TmaLayout<ST,W>::bytes;
   static int blocks_per_sm = 0;
   if(!blocks_per_sm) {
-    if(qllg_check_cuda(cudaFuncSetAttribute(stag_dslash_tma<NR_,ST,MINB>,
+    if(qllg_check_cuda(cudaFuncSetAttribute(stag_dslash_tma<NR_,ST,MINB,W>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "tma smem") ||
        qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &blocks_per_sm, stag_dslash_tma<NR_,ST,MINB>, kTmThreads, smem), "occupancy")) return -1;
+         &blocks_per_sm, stag_dslash_tma<NR_,ST,MINB,W>, 32*W, smem), "occupancy")) return -1;
     if(blocks_per_sm < 1) blocks_per_sm = 1;
   }
   if(a->preload) return 0;
   const uint64_t Vh = (uint64_t)a->g.Vh, V = (uint64_t)a->g.V;
-  CUtensorMap tin, tlk;
-  // spinors: rows of 16 rhs x 2 floats, [colour*Vh + site]; links: rows of
-  // the full lattice's V sites x 2 floats, [slot*9 + entry]
-  if(tma_map(&tin, a->in, 32, 3*Vh, 128, 32, 1) ||
-     tma_map(&tlk, a->links, 2*V, 16*9, 8*V, 16, 9)) return -1;
+  CUtensorMap tin, tin3, tlk;
+  // spinors: rows of 16 rhs x 2 floats, [colour*Vh + site] (one row a box)
+  // and [colour][site][32 floats] (3 x 8 rows a box); links: rows of the
+  // full lattice's V sites x 2 floats, [slot*9 + entry] (16 floats x 9 rows)
+  const uint64_t n_in[2] = {32, 3*Vh}, p_in[1] = {128};
+  const uint32_t b_in[2] = {32, 1};
+  const uint64_t n_in3[3] = {32, Vh, 3}, p_in3[2] = {128, 128*Vh};
+  const uint32_t b_in3[3] = {32, 8, 3};
+  const uint64_t n_lk[2] = {2*V, 16*9}, p_lk[1] = {8*V};
+  const uint32_t b_lk[2] = {16, 9};
+  if(tma_map(&tin, a->in, 2, n_in, p_in, b_in) || tma_map(&tin3, a->in, 3, n_in3, p_in3, b_in3) ||
+     tma_map(&tlk, a->links, 2, n_lk, p_lk, b_lk)) return -1;
   const size_t ngroups = Vh/8;
-  const size_t need = (ngroups + kTmW - 1)/kTmW;
+  const size_t need = (ngroups + W - 1)/W;
   size_t maxg = (size_t)qllg_num_sms()*blocks_per_sm;
   if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
   int grid = (int)(need < maxg ? need : maxg);
@@ -398,6 +453,6 @@ int launch_tma(const qllg_stag_args *a)
   A.counter = a->rb ? a->rb->counter : NULL;
   A.wait_cycles = (long long)(qllg_get_param("wait_polls")*100.0);
   A.wait_test = qllg_get_param("bulk_wait_test") != 0;
-  stag_dslash_tma<NR_,ST,MINB><<<grid, kTmThreads, smem, qllg_stream()>>>(A, tin, tlk);
+  stag_dslash_tma<NR_,ST,MINB,W><<<grid, 32*W, smem, qllg_stream()>>>(A, tin, tin3, tlk);
   return qllg_launched("stag_dslash_tma launch");
 }

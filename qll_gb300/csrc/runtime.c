@@ -349,7 +349,7 @@ static struct { const char *name; double value; } g_params[] = {
                                 block of 256 threads per SM */
   {"dslash_split", 1},       /* multi-rhs Dslash: a slot loop without the active
                                 checks for launches with every rhs active */
-  {"dslash_variant", -1},    /* force a Dslash variant (0-21, qllg_autotune_report names
+  {"dslash_variant", -1},    /* force a Dslash variant (0-23, qllg_autotune_report names
                                 them); -1: autotuned */
   {"multishift_guess_rsq", 1e-10}, /* mixed multishift: the FP32 multishift CG
                                        goes to |r|^2 < this |b|^2 before the

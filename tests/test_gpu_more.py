@@ -418,7 +418,7 @@ def test_single_stored_operator_matches_double_stored():
     L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
     n = L.qllg_stag_vec_bytes(S2, 1, 16)
     src = torch.randn(n//4, dtype=torch.float32, device="cuda", generator=g)
-    for v in range(22):
+    for v in range(24):
         L.qllg_set_param(b"dslash_variant", v)
         o2, o1 = torch.zeros_like(src), torch.zeros_like(src)
         torch.cuda.synchronize()

@@ -93,10 +93,10 @@ def test_barrier_wait_runs_out_with_an_error():
         L.qllg_stag_destroy(S)
 
 
-@pytest.mark.parametrize("pipeline", [11, 20])
+@pytest.mark.parametrize("pipeline", [11, 20, 22])
 def test_bulk_pipeline_wait_runs_out_with_an_error(pipeline):
     """the copy pipelines' waits (the bulk-copy kernel, variant 11, and the
-    per-warp tensor-copy kernel, variant 20) take the same limit: with
+    per-warp tensor-copy kernels, variants 20 and 22) take the same limit: with
     their copies not issued (bulk_wait_test) the first waits run out after
     the limit, the launch records the error flag and returns; with copies
     issued again the same launch is bitwise the register kernel's"""

@@ -335,7 +335,7 @@ def test_dslash_variants_agree(nrhs):
     g = torch.Generator(device="cuda").manual_seed(91 + nrhs)
     src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
     outs = []
-    for v in range(22):
+    for v in range(24):
         L.qllg_set_param(b"dslash_variant", v)
         for parity in (0, 1):
             dst = torch.full_like(src, float("nan"))
@@ -354,7 +354,7 @@ def test_dslash_variants_agree(nrhs):
 
 def test_warp_pipeline_over_several_passes():
     """the per-warp cp.async pipelines (variants 17-19) and tensor-copy
-    pipelines (20, 21) on a lattice where every warp takes several groups
+    pipelines (20-23) on a lattice where every warp takes several groups
     of sites, so that its ring prefetches across the group boundary:
     bitwise the register kernel's Dslash, and a 16-rhs mixed solve (fused
     CG epilogue, norms, rhs dropping out as they converge) to the same FP64
@@ -378,7 +378,7 @@ def test_warp_pipeline_over_several_passes():
     g = torch.Generator(device="cuda").manual_seed(77)
     src = torch.randn(n, dtype=torch.float32, device="cuda", generator=g)
     want = {}
-    for v in (10, 17, 18, 19, 20, 21):
+    for v in (10, 17, 18, 19, 20, 21, 22, 23):
         L.qllg_set_param(b"dslash_variant", v)
         for parity in (0, 1):
             dst = torch.full_like(src, float("nan"))
@@ -393,7 +393,7 @@ def test_warp_pipeline_over_several_passes():
     masses = [0.02 + 0.01*k for k in range(nrhs)]
     bs = [qll.gen_source(dims, 8100 + k, 6, "even") for k in range(nrhs)]
     iters = {}
-    for v in (10, 19, 20):
+    for v in (10, 19, 20, 22):
         L.qllg_set_param(b"dslash_variant", v)
         xs = [np.zeros_like(bs[0]) for _ in range(nrhs)]
         info = qll.SolveInfo()
@@ -404,13 +404,13 @@ def test_warp_pipeline_over_several_passes():
         iters[v] = [info.iters[k] for k in range(nrhs)]
     L.qllg_set_param(b"dslash_variant", -1)
     # the per-rhs sums are folded in a different order: iterations within 2
-    for v in (19, 20):
+    for v in (19, 20, 22):
         assert all(abs(a - b) <= 2 for a, b in zip(iters[10], iters[v])), iters
     assert L.qllg_k_bulk_error(1) == 0
     L.qllg_stag_destroy(S)
 
 
-@pytest.mark.parametrize("variant", range(22))
+@pytest.mark.parametrize("variant", range(24))
 def test_mixed_solve_with_each_dslash_variant(variant):
     """the fused CG epilogue and the norms of every variant: the 16-rhs
     mixed solve reaches the FP64 true residual and matches the oracle"""
