@@ -265,6 +265,10 @@ __device__ __forceinline__ void cp_async16_ca(unsigned s, const void *gmem)
 {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async8_ca(unsigned s, const void *gmem)
+{
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" :: "r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_async_wait()
 {
@@ -375,7 +379,13 @@ stag_dslash_mr(qllg_stag_args a)
   const char *const isp0 = (const char *)a.in + (lane & 7)*16;
   const char *const isp1 = isp0 + cst, *const isp2 = isp1 + cst;
   const size_t lstride = (size_t)9*V*8;         // bytes between slots' link blocks
-  const char *ilk = nullptr, *ilk8 = nullptr;   // this lane's link pieces of the next slot
+  const char *ilk = nullptr, *ilk8 = nullptr;   // this lane's link pieces of slot 0 of the group
+  // single-stored links (createStaggeredLinksFb): a forward slot's block is
+  // stored slot 2mu + naik; a backward slot reads the forward link of each
+  // neighbour site, -F(y)^dagger, so its 72 entries are gathered one 8-byte
+  // piece at a time (lane L: entries L >> 3, 4 + (L >> 3) and, for L < 8,
+  // 8, of site L & 7) and the transpose and sign are applied when it is read
+  const bool fbl = a.fb != 0;
   auto pipe_issue = [&]() {
     if constexpr (PIPE) {
       if(iw < nwork) {
@@ -400,11 +410,22 @@ stag_dslash_mr(qllg_stag_args a)
         cp_async16_ca(dst + 1024 + 256, isp1 + (size_t)n1*(NR*8));
         cp_async16_ca(dst + 2048, isp2 + (size_t)n0*(NR*8));
         cp_async16_ca(dst + 2048 + 256, isp2 + (size_t)n1*(NR*8));
-        const unsigned ldst = wring + ioff + kPipeSpinor + lane*16;
-        cp_async16_ca(ldst, ilk);
-        if(lane < 4) cp_async16_ca(ldst + 512, ilk8);
-        ilk += lstride;
-        ilk8 += lstride;
+        const unsigned lbase = wring + ioff + kPipeSpinor;
+        const int bk = (isl >> 1) & 1;
+        const int lslot = fbl ? 2*(isl >> 2) + (isl & 1) : isl;
+        if(!fbl || !bk) {
+          const size_t so = (size_t)lslot*lstride;
+          cp_async16_ca(lbase + lane*16, ilk + so);
+          if(lane < 4) cp_async16_ca(lbase + 512 + lane*16, ilk8 + so);
+        } else {
+          const int e8 = lane & 7, k0 = lane >> 3;
+          const unsigned nbe = (unsigned)wnb[isl*8 + e8];
+          const char *f = (const char *)a.links +
+                          ((size_t)lslot*9*V + (size_t)(G.Vh - (int)loff) + nbe)*8;
+          cp_async8_ca(lbase + k0*64 + e8*8, f + (size_t)k0*V*8);
+          cp_async8_ca(lbase + (4 + k0)*64 + e8*8, f + (size_t)(4 + k0)*V*8);
+          if(lane < 8) cp_async8_ca(lbase + 8*64 + e8*8, f + (size_t)8*V*8);
+        }
         if(++isl == NS) { isl = 0; iw += (size_t)gridDim.x*blockDim.x; }
       }
       cp_async_commit();
@@ -504,8 +525,19 @@ stag_dslash_mr(qllg_stag_args a)
             const unsigned char *sb = wring_p + coff;
             Cx<T> U[9];
             const float2 *ls = (const float2 *)(sb + kPipeSpinor) + (lane >> 2);
+            if(fbl && ((sl >> 1) & 1)) {
+              // -F^dagger of the neighbour's forward link
 #pragma unroll
-            for(int k=0; k<9; k++) { const float2 t = ls[8*k]; U[k].r = t.x; U[k].i = t.y; }
+              for(int l=0; l<3; l++)
+#pragma unroll
+                for(int c=0; c<3; c++) {
+                  const float2 t = ls[8*(3*c + l)];
+                  U[3*l + c].r = -t.x; U[3*l + c].i = t.y;
+                }
+            } else {
+#pragma unroll
+              for(int k=0; k<9; k++) { const float2 t = ls[8*k]; U[k].r = t.x; U[k].i = t.y; }
+            }
 #pragma unroll
             for(int h=0; h<R/2; h++) {
               Cx<T> v[2][3];
@@ -1233,7 +1265,7 @@ bool variant_ok(const qllg_stag_args *a, int v)
     return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && tma_ok(a) && vec4_ok(a) &&
            qllg_get_param("dslash_tma") != 0;
   if(v >= 17)
-    return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 && !a->fb &&
+    return PS == QLLG_F32 && PL == QLLG_F32 && NS == 16 && NR == 16 &&
            a->g.Vh % 8 == 0 && ((uintptr_t)a->links & 15u) == 0 && vec4_ok(a) &&
            qllg_get_param("dslash_vec4") != 0 && qllg_get_param("dslash_pipe") != 0;
   if(v >= 4)
