@@ -233,14 +233,19 @@ stag_dslash(qllg_stag_args a)
 // and 0.72 against 0.73 and 0.72 (fma.rn.f32x2 wants its operands as
 // register pairs, and the complex MAC's v.r and v.i broadcast into pairs
 // costs the moves that the halved FMA count saves).
+// 23, 24 and 25: 18, 19 and 20 for single-stored links (a separate
+// instantiation, so that the double-stored one carries no run-time branch
+// on the link storage in its slot loop).
 template <int PS, int R, int CFG> struct MrCfg {
-  static constexpr int pipe = (CFG >= 18 && CFG <= 20 && PS == QLLG_F32 && R == 4)
-                              ? (CFG == 18 ? 2 : CFG == 20 ? 4 : 3) : 0;
+  static constexpr int pc = CFG >= 23 ? CFG - 5 : CFG;          // the pipeline shape
+  static constexpr bool fbp = CFG >= 23 && CFG <= 25;           // single-stored links
+  static constexpr int pipe = (((CFG >= 18 && CFG <= 20) || fbp) && PS == QLLG_F32 && R == 4)
+                              ? (pc == 18 ? 2 : pc == 20 ? 4 : 3) : 0;
   static constexpr int threads = (CFG == 14 || CFG == 15 || CFG == 17 || CFG >= 18) ? 128 : 256;
   static constexpr int minb = (CFG == 2 || CFG == 9) ? 3 :
                               (CFG == 3 || CFG == 8 || CFG == 16) ? 4 :
                               CFG == 14 ? 7 : (CFG == 15 || CFG == 17) ? 8 :
-                              CFG == 18 ? 6 : CFG == 19 ? 4 : CFG == 20 ? 3 :
+                              pc == 18 ? 6 : pc == 19 ? 4 : pc == 20 ? 3 :
                               (PS == QLLG_F64 ? 1 : (R <= 2 ? 3 : 2));
   static constexpr bool f2 = CFG == 1 && PS == QLLG_F32;
   static constexpr bool lean = CFG != 0 && CFG != 1 && CFG != 5 && CFG != 7 && !pipe;
@@ -253,11 +258,11 @@ template <int PS, int R, int CFG> struct MrCfg {
 // sides, so each link is loaded and converted once per R rhs and the R
 // accumulator sets give independent FMA chains.  Same epilogues as above.
 // one stage of the per-warp pipeline: the neighbour spinors of the warp's
-// eight sites, [colour][pair half h][lane ^ 4h] 16 bytes (lane 4e + q
-// holds rhs 4q + 2h, 4q + 2h + 1 of site e, so a stage is read with
-// conflict-free 16-byte loads; the XOR puts the two halves of a 32-byte
-// sector, which one copy writes, in different banks), then the links,
-// [entry][site] 8 bytes
+// eight sites, [colour][site half e >> 2][pair half h][((e & 3) ^ h)][q] 16
+// bytes, where lane 4e + q holds rhs 4q + 2h, 4q + 2h + 1 of site e: each
+// copy instruction writes 512 contiguous bytes, the two halves of a
+// 32-byte sector land in different banks, and a stage is read with
+// conflict-free 16-byte loads; then the links, [entry][site] 8 bytes
 constexpr int kPipeSpinor = 3*1024;
 constexpr int kPipeStage = kPipeSpinor + 9*8*8;              // 3648
 
@@ -372,9 +377,9 @@ stag_dslash_mr(qllg_stag_args a)
   int *wnb = reinterpret_cast<int *>(dsm + (TB/32)*(ST ? ST : 1)*kPipeStage) + (threadIdx.x >> 5)*8*NS;
   // lane L copies the 16-byte pieces b = L & 7 of the colour vectors of
   // sites L >> 3 and 4 + (L >> 3) (the neighbours come from the table), to
-  // [colour][b & 1][(L >> 3) ^ (b & 1)][b >> 1], and link piece L (and 32 +
-  // L): entry L >> 2 of sites 2(L & 3), 2(L & 3) + 1 of the group
-  const unsigned dlane = ((lane & 1) << 9) + ((((lane >> 3) ^ (lane & 1)) << 2) << 4) + (((lane & 7) >> 1) << 4);
+  // [colour][0 or 1][b & 1][(L >> 3) ^ (b & 1)][b >> 1], and link piece L
+  // (and 32 + L): entry L >> 2 of sites 2(L & 3), 2(L & 3) + 1 of the group
+  const unsigned dlane = ((lane & 1) << 8) + ((((lane >> 3) ^ (lane & 1)) << 2) << 4) + (((lane & 7) >> 1) << 4);
   const size_t cst = total*8;                   // bytes between colours
   const char *const isp0 = (const char *)a.in + (lane & 7)*16;
   const char *const isp1 = isp0 + cst, *const isp2 = isp1 + cst;
@@ -385,7 +390,7 @@ stag_dslash_mr(qllg_stag_args a)
   // neighbour site, -F(y)^dagger, so its 72 entries are gathered one 8-byte
   // piece at a time (lane L: entries L >> 3, 4 + (L >> 3) and, for L < 8,
   // 8, of site L & 7) and the transpose and sign are applied when it is read
-  const bool fbl = a.fb != 0;
+  constexpr bool fbl = MrCfg<PS,R,CFG>::fbp;
   auto pipe_issue = [&]() {
     if constexpr (PIPE) {
       if(iw < nwork) {
@@ -405,11 +410,11 @@ stag_dslash_mr(qllg_stag_args a)
         const unsigned n0 = (unsigned)wnb[isl*8 + (lane >> 3)], n1 = (unsigned)wnb[isl*8 + 4 + (lane >> 3)];
         const unsigned dst = wring + ioff + dlane;
         cp_async16_ca(dst, isp0 + (size_t)n0*(NR*8));
-        cp_async16_ca(dst + 256, isp0 + (size_t)n1*(NR*8));
+        cp_async16_ca(dst + 512, isp0 + (size_t)n1*(NR*8));
         cp_async16_ca(dst + 1024, isp1 + (size_t)n0*(NR*8));
-        cp_async16_ca(dst + 1024 + 256, isp1 + (size_t)n1*(NR*8));
+        cp_async16_ca(dst + 1024 + 512, isp1 + (size_t)n1*(NR*8));
         cp_async16_ca(dst + 2048, isp2 + (size_t)n0*(NR*8));
-        cp_async16_ca(dst + 2048 + 256, isp2 + (size_t)n1*(NR*8));
+        cp_async16_ca(dst + 2048 + 512, isp2 + (size_t)n1*(NR*8));
         const unsigned lbase = wring + ioff + kPipeSpinor;
         const int bk = (isl >> 1) & 1;
         const int lslot = fbl ? 2*(isl >> 2) + (isl & 1) : isl;
@@ -543,7 +548,8 @@ stag_dslash_mr(qllg_stag_args a)
               Cx<T> v[2][3];
 #pragma unroll
               for(int c=0; c<3; c++) {
-                const float4 t = ((const float4 *)(sb + c*1024 + h*512))[lane ^ (h << 2)];
+                const float4 t = *(const float4 *)(sb + c*1024 + h*256 + ((lane >> 4) << 9) +
+                                                   (((lane ^ (h << 2)) & 15) << 4));
                 v[0][c].r = t.x; v[0][c].i = t.y; v[1][c].r = t.z; v[1][c].i = t.w;
               }
 #pragma unroll
@@ -1301,9 +1307,9 @@ int launch_variant(const qllg_stag_args *a, int v)
       case 14: return launch_mr<PS,PL,NS,NR,4,15>(a);
       case 15: return launch_mr<PS,PL,NS,NR,4,16>(a);
       case 16: return launch_mr<PS,PL,NS,NR,4,17>(a);
-      case 17: return launch_mr<PS,PL,NS,NR,4,18>(a);
-      case 18: return launch_mr<PS,PL,NS,NR,4,19>(a);
-      default: return launch_mr<PS,PL,NS,NR,4,20>(a);
+      case 17: return a->fb ? launch_mr<PS,PL,NS,NR,4,23>(a) : launch_mr<PS,PL,NS,NR,4,18>(a);
+      case 18: return a->fb ? launch_mr<PS,PL,NS,NR,4,24>(a) : launch_mr<PS,PL,NS,NR,4,19>(a);
+      default: return a->fb ? launch_mr<PS,PL,NS,NR,4,25>(a) : launch_mr<PS,PL,NS,NR,4,20>(a);
       }
     }
   }
