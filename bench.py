@@ -924,6 +924,7 @@ def run_wilson_dslash_only(args):
     random device input), for profiling"""
     from qll_gb300 import qll
     L = qll.load()
+    apply_params(L, args)
     L.qllg_wilson_create.restype = ctypes.c_void_p
     L.qllg_wilson_create.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]
     L.qllg_wilson_destroy.argtypes = [ctypes.c_void_p]

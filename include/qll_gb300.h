@@ -278,8 +278,9 @@ void qllg_server_destroy(qllg_server *V);
 
 /* solver parameters (name, default):
  *  "reliable_delta" (0.1, 16-bit mixed mode),
- *  "reliable_delta_single" (0.01, FP32 mixed mode, staggered CG and Wilson
- *    CGNR): a reliable update when |r| falls by this factor;
+ *  "reliable_delta_single" (0.01, FP32 mixed mode of the staggered CG) and
+ *    "wilson_delta" (0.001, the Wilson CGNR's FP32 mode): a reliable update
+ *    when |r| falls by this factor;
  *  "half_split" (2: the 16-bit mixed mode stores the Dslash operands in 16
  *    bits and keeps FP32 links; 1: 16-bit links and FP32 operands; 0: both
  *    in 16 bits),
@@ -319,7 +320,7 @@ void qllg_server_destroy(qllg_server *V);
  *    in small one-rhs FP32 Wilson launches), "wilson_ru_df" (0; 1: the
  *    Wilson mixed CGNR's intermediate reliable updates in double-float),
  *    "wilson_df_c3" (1: three threads per site in the small double-float
- *    Wilson launches).
+ *    Wilson launches), "wilson_f64_c3" (0: the same for the FP64 ones).
  * Returns -1 for an unknown name. */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);

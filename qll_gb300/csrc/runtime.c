@@ -290,10 +290,13 @@ static struct { const char *name; double value; } g_params[] = {
                                       sloppy iterations keep the CG recurrence
                                       over two decades (measured: 455
                                       iterations at 32^3x64, m=0.01, for 0.1
-                                      and 0.01; 464 at 0.003, 623 at 0.001;
-                                      Wilson CGNR at 16^3x32: 52 iterations
-                                      for both, 13.0 ms per solve at 0.01
-                                      against 14.8 ms at 0.1) */
+                                      and 0.01; 464 at 0.003, 623 at 0.001) */
+  {"wilson_delta", 0.001},   /* the same for the Wilson CGNR's FP32 mode
+                                (measured at 16^3x32, kappa 0.12: 52
+                                iterations and the same true residual for
+                                0.01 down to 0.0003; 9.6 ms per solve at
+                                0.01, 9.0 at 0.003, 8.4 at 0.001: fewer
+                                FP64 updates) */
   {"reortho", 1},            /* restore p orthogonal to r after a reliable update */
   {"half_split", 2},         /* MIXED_HALF solves: 0 16-bit Dslash operands and
                                 links, 1 16-bit links with FP32 operands, 2 FP32
@@ -334,6 +337,8 @@ static struct { const char *name; double value; } g_params[] = {
   {"dslash_tma", 1},         /* allow the per-warp tensor-copy (TMA) pipeline Dslash variants */
   {"solve2_mixed", 0},       /* solve2D (drop-in): FP32 iterations with FP64 reliable
                                 updates instead of the reference's FP64 CG */
+  {"wilson_f64_c3", 0},      /* the same for the FP64 launches (the reliable
+                                updates of the mixed CGNR, and the FP64 CGNR) */
   {"wilson_c3", 0},          /* small one-rhs FP32 Wilson launches: three threads
                                 per site, one per output colour (C2 at 16^3x32:
                                 17.8 ms per mixed solve against 14.7 ms with one

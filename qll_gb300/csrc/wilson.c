@@ -468,7 +468,7 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   W->hsc->rsq_stop[0] = rsq;
   W->hsc->maxits = maxits;
   W->hsc->loop_limit = maxits + 2;
-  const double delta = qllg_get_param("reliable_delta_single");
+  const double delta = qllg_get_param("wilson_delta");
   W->hsc->delta2 = (ps == QLLG_F64) ? 0 : delta*delta;
   if(wpush(W)) return -1;
   qllg_cg_scalars *sc = W->sc;
