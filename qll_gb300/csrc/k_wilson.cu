@@ -281,8 +281,8 @@ int launch_t(const qllg_stag_args *a)
   // one rhs, fewer sites than half the GPU's resident threads: three
   // threads per site (FP32 on request; double-float by default, whose
   // one-thread kernel holds one block of 256 threads per SM)
-  if constexpr (NR == 1 && (PS == QLLG_F32 || PS == QLLG_DF)) {
-    const char *knob = PS == QLLG_DF ? "wilson_df_c3" : "wilson_c3";
+  if constexpr (NR == 1 && (PS == QLLG_F32 || PS == QLLG_DF || PS == QLLG_F64)) {
+    const char *knob = PS == QLLG_DF ? "wilson_df_c3" : PS == QLLG_F64 ? "wilson_f64_c3" : "wilson_c3";
     if(qllg_get_param(knob) != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
       return launch_c3<PS,PL>(a);
   }
