@@ -245,28 +245,30 @@ def test_wilson_dslash_matches_oracle(prec, sub):
     getattr(L, "freeWilsonLinks" + prec)(byref(wl))
 
 
+@pytest.mark.parametrize("prec", ["F", "D"])
 @pytest.mark.parametrize("sub", ["all", "even", "odd"])
-def test_wilson_three_threads_per_site(sub):
-    """the small-launch FP32 Wilson kernel (three threads per site, one per
-    output colour) against the one-thread-per-site kernel: the same sums in
-    another order, so FP32 rounding apart"""
+def test_wilson_three_threads_per_site(sub, prec):
+    """the small-launch Wilson kernel (three threads per site, one per output
+    colour; FP32 wilson_c3, FP64 wilson_f64_c3) against the one-thread-per-
+    site kernel: the same sums in another order, so rounding apart"""
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
-    lay = qll.setup_layout(DIMS, "F")
-    u = as_dtype(wilson_links(DIMS), DT["F"])
-    wl = qll.F["WilsonLinks"]()
-    L.createWilsonLinksF(byref(wl), byref(lay), _ptrs(u, "F"), sub.encode())
+    knob = b"wilson_c3" if prec == "F" else b"wilson_f64_c3"
+    lay = qll.setup_layout(DIMS, prec)
+    u = as_dtype(wilson_links(DIMS), DT[prec])
+    wl = qll.F["WilsonLinks"]() if prec == "F" else qll.D["WilsonLinks"]()
+    getattr(L, "createWilsonLinks" + prec)(byref(wl), byref(lay), _ptrs(u, prec), sub.encode())
     assert wl.t, qll.last_error()
-    y = qll.gen_source(DIMS, 24, 24, "all").astype(np.float32)
+    y = qll.gen_source(DIMS, 24, 24, "all").astype(DT[prec])
     outs = []
     for c3 in (1, 0):
-        L.qllg_set_param(b"wilson_c3", c3)
+        L.qllg_set_param(knob, c3)
         x = np.full_like(y, 3.0)
-        L.wilsonDslashF(byref(wl), qll.ptr(x), CT["F"](0.1667), 1, qll.ptr(y))
+        getattr(L, "wilsonDslash" + prec)(byref(wl), qll.ptr(x), CT[prec](0.1667), 1, qll.ptr(y))
         outs.append(x)
-    L.qllg_set_param(b"wilson_c3", 0)
-    assert relerr(outs[0], outs[1]) < 1e-6
-    L.freeWilsonLinksF(byref(wl))
+    L.qllg_set_param(knob, 0)
+    assert relerr(outs[0], outs[1]) < (1e-6 if prec == "F" else 1e-14)
+    getattr(L, "freeWilsonLinks" + prec)(byref(wl))
 
 
 def test_wilson_reference_solve_iterates_match():
