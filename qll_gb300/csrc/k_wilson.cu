@@ -132,6 +132,127 @@ wilson_dslash(qllg_stag_args a)
   }
 }
 
+// Small one-rhs launches split by direction: a block is 64 sites and two
+// halves of two warps; half 0 takes the x and y hops (slots 0-3), half 1
+// the z and t hops (slots 4-7), each with wilson_dslash's arithmetic, and
+// half 1 hands its partial sums to half 0 through shared memory, which adds
+// them and finishes the site.  Twice the threads of the one-thread kernel
+// with no repeated work (the FP64 launches are bound by the FP64 pipe, so
+// the three-threads-per-colour form, which repeats the spin projections,
+// is slower).  The two partial sums are added at the end, so the result
+// differs from the one-thread kernel's in rounding only.
+constexpr int kDir2Threads = 128;
+
+template <int PS, int PL>
+__global__ void __launch_bounds__(kDir2Threads, 3)
+wilson_dslash_dir2(qllg_stag_args a)
+{
+  typedef typename Calc<PS, PL>::T T;
+  constexpr int SB = kDir2Threads/2;            // sites a block
+  __shared__ double shm[2*kDir2Threads];
+  __shared__ T part[24][SB];
+  const Geo G = make_geo(a.g);
+  const size_t V = (size_t)a.g.V;
+  const size_t total = (size_t)G.Vh;
+  const int p = a.out_parity;
+  const size_t loff = p ? (size_t)G.Vh : 0;
+  const bool skip = a.done && *(volatile const int *)a.done;
+  const int half = threadIdx.x / SB, ls = threadIdx.x % SB;
+  Acc<T> acc0, acc1;
+  const bool act = !a.active || (a.active[0] && (!a.active_eq || a.active[0] == a.active_eq));
+  const T ca = (T)(a.a ? a.a[0] : a.a0);
+  const T cb = (T)a.b;
+  if(!skip && act) {
+    for(size_t base = (size_t)blockIdx.x*SB; base < total; base += (size_t)gridDim.x*SB) {
+      const size_t t = base + ls;
+      const bool valid = t < total;
+      Cx<T> acc[12], self[12];
+#pragma unroll
+      for(int c=0; c<12; c++) { acc[c].r = 0; acc[c].i = 0; }
+      auto hops = [&](auto mu0) {
+        constexpr int M0 = decltype(mu0)::value;
+        int x[4];
+        site_coords(G, p, (int)t, x);
+#pragma unroll
+        for(int mu=M0; mu<M0+2; mu++) {
+#pragma unroll
+          for(int back=0; back<2; back++) {
+            const int sgn = (back ? 1 : -1)*(a.dag ? -1 : 1);
+            const int k = nbr_index(G, x, mu, back ? -1 : 1);
+            Cx<T> U[9], f[12];
+            LinkIO<PL>::load(a.links, 2*mu + back, V, loff + t, a.lscale, U);
+            SpinorIO<PS,12>::load(a.in, total, (size_t)k, f);
+#pragma unroll
+            for(int hk=0; hk<2; hk++) {
+              const int col = gcol(mu, hk);
+              const int ph = gph(mu, hk) + (sgn < 0 ? 2 : 0);
+              Cx<T> h[3], tt[3];
+#pragma unroll
+              for(int c=0; c<3; c++) {
+                Cx<T> y = phase(f[3*col + c], ph);
+                h[c].r = f[3*hk + c].r + y.r; h[c].i = f[3*hk + c].i + y.i;
+                tt[c].r = 0; tt[c].i = 0;
+              }
+#pragma unroll
+              for(int l=0; l<3; l++) {
+#pragma unroll
+                for(int j=0; j<3; j++) cmac(tt[j], U[3*l + j], h[l]);
+              }
+#pragma unroll
+              for(int c=0; c<3; c++) { acc[3*hk + c].r -= tt[c].r; acc[3*hk + c].i -= tt[c].i; }
+#pragma unroll
+              for(int ar=2; ar<4; ar++) {
+                if(gcol(mu, ar) == hk) {
+                  const int pa = gph(mu, ar) + (sgn < 0 ? 0 : 2);
+#pragma unroll
+                  for(int c=0; c<3; c++) {
+                    Cx<T> y = phase(tt[c], pa);
+                    acc[3*ar + c].r += y.r; acc[3*ar + c].i += y.i;
+                  }
+                }
+              }
+            }
+          }
+        }
+      };
+      if(valid) {
+        if(half == 0) hops(std::integral_constant<int, 0>());
+        else hops(std::integral_constant<int, 2>());
+      }
+      if(half == 1 && valid) {
+#pragma unroll
+        for(int c=0; c<12; c++) { part[2*c][ls] = acc[c].r; part[2*c + 1][ls] = acc[c].i; }
+      }
+      __syncthreads();
+      if(half == 0 && valid) {
+        if(a.self) SpinorIO<PS,12>::load(a.self, total, t, self);
+        Cx<T> out[12];
+#pragma unroll
+        for(int c=0; c<12; c++) {
+          Cx<T> s;
+          s.r = acc[c].r + part[2*c][ls]; s.i = acc[c].i + part[2*c + 1][ls];
+          if(a.mode == 1) {
+            s.r = kfma(ca, self[c].r, s.r); s.i = kfma(ca, self[c].i, s.i);
+            out[c] = s;
+          } else if(a.mode == 2) {
+            T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
+            out[c].r = kfma(cb, s.r, sr); out[c].i = kfma(cb, s.i, si);
+          } else out[c] = s;
+        }
+        SpinorIO<PS,12>::store(a.out, total, t, out);
+        if(a.norm_out) acc0.norm(out);
+        if(a.norm_self && a.self) acc1.norm(self);
+      }
+      __syncthreads();
+    }
+  }
+  double red[2] = {acc0.get(), acc1.get()};
+  if(a.norm_out || a.norm_self) {
+    double *res[2] = {a.norm_out, a.norm_self};
+    grid_reduce<2>(red, 1, 0, a.partial, a.counter, shm, res);
+  }
+}
+
 // one component of a spinor, one row of a link (the layouts of SpinorIO and
 // LinkIO: component-major spinors, [slot][9][V] links, entry 3*col + row)
 template <int P, typename T>
@@ -275,9 +396,36 @@ int launch_c3(const qllg_stag_args *a)
   return qllg_launched("wilson_dslash_c3 launch");
 }
 
+template <int PS, int PL>
+int launch_dir2(const qllg_stag_args *a)
+{
+  static int bps = 0;
+  if(!bps) {
+    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &bps, wilson_dslash_dir2<PS,PL>, kDir2Threads, 0), "occupancy")) return -1;
+    if(bps < 1) bps = 1;
+  }
+  size_t need = ((size_t)a->g.Vh + kDir2Threads/2 - 1)/(kDir2Threads/2);
+  size_t maxg = (size_t)qllg_num_sms()*bps;
+  if(a->rb && maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
+  int grid = (int)(need < maxg ? need : maxg);
+  if(grid < 1) grid = 1;
+  qllg_stag_args A = *a;
+  A.partial = a->rb ? a->rb->partial : NULL;
+  A.counter = a->rb ? a->rb->counter : NULL;
+  wilson_dslash_dir2<PS,PL><<<grid, kDir2Threads, 0, qllg_stream()>>>(A);
+  return qllg_launched("wilson_dslash_dir2 launch");
+}
+
 template <int PS, int PL, int NR>
 int launch_t(const qllg_stag_args *a)
 {
+  // one rhs in FP64, fewer sites than the GPU's resident threads: two
+  // threads per site, split by direction
+  if constexpr (NR == 1 && PS == QLLG_F64 && PL == QLLG_F64) {
+    if(qllg_get_param("wilson_f64_dir2") != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
+      return launch_dir2<PS,PL>(a);
+  }
   // one rhs, fewer sites than half the GPU's resident threads: three
   // threads per site (FP32 on request; double-float by default, whose
   // one-thread kernel holds one block of 256 threads per SM)

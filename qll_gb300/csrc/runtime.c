@@ -337,6 +337,8 @@ static struct { const char *name; double value; } g_params[] = {
   {"dslash_tma", 1},         /* allow the per-warp tensor-copy (TMA) pipeline Dslash variants */
   {"solve2_mixed", 0},       /* solve2D (drop-in): FP32 iterations with FP64 reliable
                                 updates instead of the reference's FP64 CG */
+  {"wilson_f64_dir2", 1},    /* small one-rhs FP64 Wilson launches: two threads
+                                per site, split by direction */
   {"wilson_f64_c3", 0},      /* the same for the FP64 launches (the reliable
                                 updates of the mixed CGNR, and the FP64 CGNR) */
   {"wilson_c3", 0},          /* small one-rhs FP32 Wilson launches: three threads
