@@ -322,7 +322,8 @@ void qllg_server_destroy(qllg_server *V);
  *    "wilson_df_c3" (1: three threads per site in the small double-float
  *    Wilson launches), "wilson_f64_c3" (0: the same for the FP64 ones),
  *    "wilson_f64_dir2" (1: two threads per site, split by direction, in the
- *    small one-rhs FP64 Wilson launches).
+ *    small one-rhs FP64 Wilson launches), "wilson_f32_dir2" (0: the same for
+ *    the FP32 ones).
  * Returns -1 for an unknown name. */
 int qllg_set_param(const char *name, double value);
 double qllg_get_param(const char *name);

@@ -422,8 +422,9 @@ int launch_t(const qllg_stag_args *a)
 {
   // one rhs in FP64, fewer sites than the GPU's resident threads: two
   // threads per site, split by direction
-  if constexpr (NR == 1 && PS == QLLG_F64 && PL == QLLG_F64) {
-    if(qllg_get_param("wilson_f64_dir2") != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
+  if constexpr (NR == 1 && ((PS == QLLG_F64 && PL == QLLG_F64) || (PS == QLLG_F32 && PL == QLLG_F32))) {
+    if(qllg_get_param(PS == QLLG_F64 ? "wilson_f64_dir2" : "wilson_f32_dir2") != 0 &&
+       (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
       return launch_dir2<PS,PL>(a);
   }
   // one rhs, fewer sites than half the GPU's resident threads: three

@@ -339,6 +339,7 @@ static struct { const char *name; double value; } g_params[] = {
                                 updates instead of the reference's FP64 CG */
   {"wilson_f64_dir2", 1},    /* small one-rhs FP64 Wilson launches: two threads
                                 per site, split by direction */
+  {"wilson_f32_dir2", 0},    /* the same for the FP32 ones */
   {"wilson_f64_c3", 0},      /* the same for the FP64 launches (the reliable
                                 updates of the mixed CGNR, and the FP64 CGNR) */
   {"wilson_c3", 0},          /* small one-rhs FP32 Wilson launches: three threads
