@@ -247,28 +247,39 @@ def test_wilson_dslash_matches_oracle(prec, sub):
 
 @pytest.mark.parametrize("prec", ["F", "D"])
 @pytest.mark.parametrize("sub", ["all", "even", "odd"])
-def test_wilson_three_threads_per_site(sub, prec):
-    """the small-launch Wilson kernel (three threads per site, one per output
-    colour; FP32 wilson_c3, FP64 wilson_f64_c3) against the one-thread-per-
-    site kernel: the same sums in another order, so rounding apart"""
+def test_wilson_small_launch_kernels(sub, prec):
+    """the small-launch Wilson kernels (three threads per site, one per
+    output colour: wilson_c3, wilson_f64_c3; two threads per site split by
+    direction: wilson_f32_dir2, wilson_f64_dir2) each against the one-
+    thread-per-site kernel: the same sums in another order, so rounding
+    apart"""
     L = qll.load()
     L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
-    knob = b"wilson_c3" if prec == "F" else b"wilson_f64_c3"
+    L.qllg_get_param.argtypes = [ctypes.c_char_p]
+    L.qllg_get_param.restype = c_double
+    knobs = [b"wilson_c3", b"wilson_f32_dir2"] if prec == "F" else [b"wilson_f64_c3", b"wilson_f64_dir2"]
+    saved = {k: L.qllg_get_param(k) for k in knobs}
     lay = qll.setup_layout(DIMS, prec)
     u = as_dtype(wilson_links(DIMS), DT[prec])
     wl = qll.F["WilsonLinks"]() if prec == "F" else qll.D["WilsonLinks"]()
     getattr(L, "createWilsonLinks" + prec)(byref(wl), byref(lay), _ptrs(u, prec), sub.encode())
     assert wl.t, qll.last_error()
     y = qll.gen_source(DIMS, 24, 24, "all").astype(DT[prec])
-    outs = []
-    for c3 in (1, 0):
-        L.qllg_set_param(knob, c3)
+
+    def run(on):
+        for k in knobs:
+            L.qllg_set_param(k, 1 if k == on else 0)
         x = np.full_like(y, 3.0)
         getattr(L, "wilsonDslash" + prec)(byref(wl), qll.ptr(x), CT[prec](0.1667), 1, qll.ptr(y))
-        outs.append(x)
-    L.qllg_set_param(knob, 0)
-    assert relerr(outs[0], outs[1]) < (1e-6 if prec == "F" else 1e-14)
-    getattr(L, "freeWilsonLinks" + prec)(byref(wl))
+        return x
+    try:
+        base = run(None)
+        for k in knobs:
+            assert relerr(run(k), base) < (1e-6 if prec == "F" else 1e-14), k
+    finally:
+        for k in knobs:
+            L.qllg_set_param(k, saved[k])
+        getattr(L, "freeWilsonLinks" + prec)(byref(wl))
 
 
 def test_wilson_reference_solve_iterates_match():
