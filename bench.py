@@ -315,6 +315,8 @@ def run_gpu(args):
     # the fused D_eo + CG update: links + 16 neighbours + self + x and r
     # read and written
     fused_bytes = ((8*18*4 + 8*naik*4)/16 + 17*(6*4) + 4*(6*4))*Vh*NRHS
+    # its compulsory DRAM bytes: links, v in, p (self) in, x and r in and out
+    fused_compulsory = ((8*18*4 + 8*naik*4)/16 + 6*(6*4))*Vh*NRHS
     favg = ftot.value/max(fcnt.value, 1)
 
     # the 16-bit-storage mode, once (not timed in the headline)
@@ -349,7 +351,11 @@ def run_gpu(args):
                 "d2h_bytes_per_step": bytes_io, "host_memory": "pinned",
                 "api": "qllg_stag_solve (host arrays)"},
         "fused_cg_kernel": {"avg_launch_ms": favg, "launches": fcnt.value,
-                            "gbs": fused_bytes/(favg*1e-3)/1e9 if favg > 0 else None},
+                            "gbs": fused_bytes/(favg*1e-3)/1e9 if favg > 0 else None,
+                            "compulsory_gbs": fused_compulsory/(favg*1e-3)/1e9 if favg > 0 else None,
+                            "frac_of_hbm": (fused_compulsory/(favg*1e-3)/1e9/peak) if (favg > 0 and peak) else None,
+                            "basis": "compulsory DRAM bytes per launch: links, v, p (the mass term), x and r "
+                                     "read, x and r written (216 B per site and rhs)"},
         "roofline": {"kernel": "stag_dslash_mr<f32,%s,16 slots,16 rhs>, %s"
                                % ("f32 reconstruct-12" if recon else "f32", tuned_choice(L)),
                      "bound": "hbm",
