@@ -311,6 +311,10 @@ void qllg_server_destroy(qllg_server *V);
  *    candidates may be chosen; "dslash_variant" (-1: autotuned;
  *    0-23 forces a candidate where it applies, qllg_autotune_report names
  *    them);
+ *  "host_copy_sm" (1: copies of at least 1 MiB between page-locked host
+ *    arrays and the device, such as the sources and solutions of the
+ *    host-array solves, run on the SMs through the arrays' mapped device
+ *    addresses instead of on a copy engine; 0: copy engine always),
  *  "links_recon12" (0; 1: reconstruct-12 Naik links in the FP32 solves),
  *  "solve2_mixed" (0; 1: the drop-in solve2D runs FP32 iterations with FP64
  *    reliable updates, to the same true residual, instead of the reference's

@@ -909,3 +909,28 @@ qllg_k_loop_cond(unsigned long long handle, int *done, int *loops, const int *li
   loop_cond_k<<<1, 32, 0, qllg_stream()>>>((cudaGraphConditionalHandle)handle, done, loops, limit);
   return done_check("loop_cond");
 }
+
+// ------------------------------------------------ host <-> device copies
+// A copy between device memory and page-locked host memory done by the SMs,
+// which reach the host buffer through its mapped device address over the
+// CPU-GPU link, instead of by a copy engine.  On GB300 (805 MB, 64 KB host
+// pages) a copy-engine transfer of a host buffer that the GPU has not
+// touched for a while (after a one-second solve, or after 0.5 s idle) took
+// 35-90 ms against 3.9 ms when repeated at once; the SM copy takes 3.9-4.0
+// ms in both cases.  16-byte accesses: the caller checks that both ends are
+// 16-byte aligned and the size a multiple of 16.
+__global__ void copy16_k(const int4 *__restrict__ src, int4 *__restrict__ dst, size_t n)
+{
+  GRID_LOOP(t, n) dst[t] = src[t];
+}
+
+extern "C" int
+qllg_k_copy16(void *dst, const void *src, size_t bytes)
+{
+  const size_t n = bytes/16;
+  size_t g = (n + kT - 1)/kT, m = (size_t)qllg_num_sms()*32;
+  if(g > m) g = m;
+  if(g < 1) g = 1;
+  copy16_k<<<(int)g, kT, 0, qllg_stream()>>>((const int4 *)src, (int4 *)dst, n);
+  return done_check("copy16");
+}

@@ -75,8 +75,14 @@ void qllg_tune_store(const char *key, int choice, int ncand, const float *ms,
 int   qllg_check_cuda(cudaError_t e, const char *what);   /* 0 ok */
 void *qllg_dmalloc(size_t bytes);              /* NULL + error on failure */
 void  qllg_dfree(void *p);
+/* host <-> device copies on the library stream: at least 1 MiB between
+   page-locked host memory and device memory, 16-byte aligned, runs on the
+   SMs (qllg_k_copy16); anything else on a copy engine.  qllg_d2h waits for
+   the copy, qllg_d2h_async does not */
 int   qllg_h2d(void *d, const void *h, size_t bytes);
 int   qllg_d2h(void *h, const void *d, size_t bytes);
+int   qllg_d2h_async(void *h, const void *d, size_t bytes);
+int   qllg_k_copy16(void *dst, const void *src, size_t bytes);
 int   qllg_sync(void);
 int   qllg_num_sms(void);
 /* CUDA graph capture of library launches (graph bodies) */

@@ -1032,8 +1032,7 @@ qllg_batch_admit(qllg_stag *S, int ncol, const int cols[], const double mass[], 
   for(int i=0; i<ncol; i++) {
     int col = cols[i];
     if(col < 0 || col >= QLLG_MAXRHS) { qllg_set_error("batch_admit: column %d", col); return -1; }
-    if(qllg_check_cuda(cudaMemcpyAsync(S->bstage, src[i], 48*(size_t)Vh, cudaMemcpyHostToDevice,
-                                       qllg_stream()), "batch source")) return -1;
+    if(qllg_h2d(S->bstage, src[i], 48*(size_t)Vh)) return -1;
     if(qllg_k_column_from_aos((void *)c->b, S->bstage, Vh, QLLG_MAXRHS, col)) return -1;
     ad.mask[col] = 1;
     ad.mass2[col] = mass[i]*mass[i];
@@ -1087,9 +1086,7 @@ qllg_batch_retire(qllg_stag *S, int col, double *out)
 {
   const int Vh = S->g.Vh;
   if(qllg_k_column_to_aos(S->bctx.x64, S->bstage, Vh, QLLG_MAXRHS, col)) return -1;
-  if(qllg_check_cuda(cudaMemcpyAsync(out, S->bstage, 48*(size_t)Vh, cudaMemcpyDeviceToHost,
-                                     qllg_stream()), "batch solution")) return -1;
-  return qllg_check_cuda(cudaStreamSynchronize(qllg_stream()), "batch retire");
+  return qllg_d2h(out, S->bstage, 48*(size_t)Vh);
 }
 
 static int
@@ -1219,8 +1216,7 @@ vec_download(qllg_stag *S, int prec, const void *v_dev, int nrhs, void *const h[
   if(!stage) return -1;
   if(qllg_k_spinor_to_aos(prec, v_dev, stage, dbl, Vh, 3, nrhs, 6*(size_t)Vh)) return -1;
   for(int r=0; r<nrhs; r++)
-    if(qllg_check_cuda(cudaMemcpyAsync(h[r], stage + blk*r, blk, cudaMemcpyDeviceToHost,
-                                       qllg_stream()), "copy device to host")) return -1;
+    if(qllg_d2h_async(h[r], stage + blk*r, blk)) return -1;
   return qllg_sync();
 }
 
