@@ -311,6 +311,10 @@ void qllg_server_destroy(qllg_server *V);
  *    candidates may be chosen; "dslash_variant" (-1: autotuned;
  *    0-23 forces a candidate where it applies, qllg_autotune_report names
  *    them);
+ *  "graph_ru_if" (1: in the graph-captured mixed solver loops the
+ *    reliable-update launches are the body of a conditional IF node, taken
+ *    only in the iterations that flag an update; 0: they are launched every
+ *    iteration and return at once when nothing is flagged),
  *  "host_copy_sm" (1: copies of at least 1 MiB between page-locked host
  *    arrays and the device, such as the sources and solutions of the
  *    host-array solves, run on the SMs through the arrays' mapped device

@@ -910,6 +910,24 @@ qllg_k_loop_cond(unsigned long long handle, int *done, int *loops, const int *li
   return done_check("loop_cond");
 }
 
+// the IF condition of a graph's reliable-update block: taken when some rhs
+// is flagged for an update (*no_ru clear); *trips counts the times taken
+__global__ void ru_cond_k(cudaGraphConditionalHandle h, const int *no_ru, int *trips)
+{
+  if(threadIdx.x == 0) {
+    const int take = !*(volatile const int *)no_ru;
+    if(take) ++*trips;
+    cudaGraphSetConditional(h, take ? 1u : 0u);
+  }
+}
+
+extern "C" int
+qllg_k_ru_cond(unsigned long long handle, const int *no_ru, int *trips)
+{
+  ru_cond_k<<<1, 32, 0, qllg_stream()>>>((cudaGraphConditionalHandle)handle, no_ru, trips);
+  return done_check("ru_cond");
+}
+
 // ------------------------------------------------ host <-> device copies
 // A copy between device memory and page-locked host memory done by the SMs,
 // which reach the host buffer through its mapped device address over the

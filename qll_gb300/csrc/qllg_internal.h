@@ -89,8 +89,17 @@ int   qllg_num_sms(void);
 int   qllg_capturing(void);
 int   qllg_capture_begin(cudaGraph_t body);
 int   qllg_capture_end(cudaGraph_t body);
+/* a conditional IF block inside a capture: the handle (default 0 at each
+ * launch of the captured graph), then the node, whose body takes the
+ * launches up to qllg_capture_if_end */
+int   qllg_capture_cond(unsigned long long *handle);
+int   qllg_capture_if_begin(unsigned long long handle);
+int   qllg_capture_if_end(void);
 /* last kernel of a graph-loop body: keep looping while work remains */
 int   qllg_k_loop_cond(unsigned long long handle, int *done, int *loops, const int *limit);
+/* the IF condition of a captured reliable-update block: set when *no_ru is
+ * clear, counting the times in *trips */
+int   qllg_k_ru_cond(unsigned long long handle, const int *no_ru, int *trips);
 /* after a kernel launch: count it and check the launch error */
 int   qllg_launched(const char *what);
 double qllg_get_param(const char *name);
@@ -229,6 +238,7 @@ typedef struct qllg_cg_scalars_s {
   int count;                    /* iterations issued */
   int loops;                    /* graph-loop trips (safety cap) */
   int loop_limit;
+  int ru_trips;                 /* graph-loop trips that took the reliable-update block */
 } qllg_cg_scalars;
 
 /* ---------------------------------------------------- persistent CG */

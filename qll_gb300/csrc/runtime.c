@@ -107,11 +107,13 @@ qllg_num_sms(void)
  * stream instead of the library stream */
 static cudaStream_t g_cap = 0;
 static int g_capturing = 0;
+static cudaStream_t g_cap_if = 0;   /* capture of a conditional IF body inside g_cap's */
+static int g_nested = 0;
 
 cudaStream_t
 qllg_stream(void)
 {
-  return g_capturing ? g_cap : g_stream;
+  return g_capturing ? (g_nested ? g_cap_if : g_cap) : g_stream;
 }
 
 int
@@ -136,8 +138,68 @@ int
 qllg_capture_end(cudaGraph_t body)
 {
   cudaGraph_t out = body;
+  int rc = qllg_capture_if_end();
   g_capturing = 0;
-  return qllg_check_cuda(cudaStreamEndCapture(g_cap, &out), "end capture");
+  return qllg_check_cuda(cudaStreamEndCapture(g_cap, &out), "end capture") || rc;
+}
+
+/* inside a capture: a conditional handle of the graph being captured,
+ * reset to 0 at each launch of that graph (a kernel sets it) */
+int
+qllg_capture_cond(unsigned long long *handle)
+{
+  enum cudaStreamCaptureStatus st;
+  cudaGraph_t g = NULL;
+  cudaGraphConditionalHandle h;
+  if(!g_capturing || g_nested) { qllg_set_error("conditional handle outside a capture"); return -1; }
+  if(qllg_check_cuda(cudaStreamGetCaptureInfo(g_cap, &st, NULL, &g, NULL, NULL, NULL), "capture info") ||
+     qllg_check_cuda(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault),
+                     "conditional handle")) return -1;
+  *handle = (unsigned long long)h;
+  return 0;
+}
+
+/* inside a capture: an IF node on handle, after everything captured so far;
+ * the launches up to qllg_capture_if_end are captured into its body, and
+ * the capture goes on after the node */
+int
+qllg_capture_if_begin(unsigned long long handle)
+{
+  enum cudaStreamCaptureStatus st;
+  cudaGraph_t g = NULL;
+  const cudaGraphNode_t *deps = NULL;
+  const cudaGraphEdgeData *edges = NULL;
+  size_t nd = 0;
+  cudaGraphNode_t node;
+  struct cudaGraphNodeParams np;
+  if(!g_capturing || g_nested) { qllg_set_error("conditional node outside a capture"); return -1; }
+  if(!g_cap_if && qllg_check_cuda(cudaStreamCreateWithFlags(&g_cap_if, cudaStreamNonBlocking),
+                                  "conditional capture stream")) return -1;
+  if(qllg_check_cuda(cudaStreamGetCaptureInfo(g_cap, &st, NULL, &g, &deps, &edges, &nd), "capture info"))
+    return -1;
+  memset(&np, 0, sizeof(np));
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = (cudaGraphConditionalHandle)handle;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  if(qllg_check_cuda(cudaGraphAddNode(&node, g, deps, edges, nd, &np), "conditional IF node") ||
+     qllg_check_cuda(cudaStreamUpdateCaptureDependencies(g_cap, &node, NULL, 1,
+                                                         cudaStreamSetCaptureDependencies),
+                     "capture dependencies") ||
+     qllg_check_cuda(cudaStreamBeginCaptureToGraph(g_cap_if, np.conditional.phGraph_out[0], NULL, NULL,
+                                                   0, cudaStreamCaptureModeRelaxed),
+                     "begin conditional capture")) return -1;
+  g_nested = 1;
+  return 0;
+}
+
+int
+qllg_capture_if_end(void)
+{
+  cudaGraph_t out = NULL;
+  if(!g_nested) return 0;
+  g_nested = 0;
+  return qllg_check_cuda(cudaStreamEndCapture(g_cap_if, &out), "end conditional capture");
 }
 
 int
@@ -363,6 +425,10 @@ static struct { const char *name; double value; } g_params[] = {
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
   {"dslash_pipe", 1},        /* allow the per-warp cp.async pipeline Dslash variants */
   {"dslash_tma", 1},         /* allow the per-warp tensor-copy (TMA) pipeline Dslash variants */
+  {"graph_ru_if", 1},        /* graph-captured mixed solver loops: the reliable-update
+                                launches sit in a conditional IF node taken only in
+                                the iterations that flag an update (else they are
+                                launched every iteration and return at once) */
   {"host_copy_sm", 1},       /* copies of at least 1 MiB between page-locked host
                                 memory and the device run on the SMs instead of
                                 a copy engine (805 MB on GB300 after a solve: 4 ms

@@ -59,9 +59,12 @@ struct qllg_stag {
     long key[11];
     cudaGraphExec_t exec;
     int body;              /* kernels in one trip of the loop body */
+    int ifbody;            /* ... of it in the conditional reliable-update block */
   } graphs[6];
   int ngraph_next;
   int graph_body;          /* body of the graph the current solve launched, 0: none */
+  int graph_ifbody;
+  int cap_ifbody;          /* while capturing: kernels of the reliable-update block */
   int used_persistent;     /* the last solve ran the persistent CG */
   unsigned char shared[QLLG_NLINKP]; /* links[p] belong to another operator */
   int recon_bad;           /* the Naik links are not reconstructible (reconstruct-12 refused) */
@@ -639,7 +642,16 @@ issue_iteration(qllg_stag *S, const iter_ctx *c)
   if(cg_iteration(S, c->ps, c->pl, c->nrhs, c->x, c->r, c->p, c->v, c->mixed)) return -1;
   if(!c->mixed) return 0;
   /* reliable update of the flagged rhs; every launch returns at once when
-   * no rhs is flagged */
+   * no rhs is flagged.  In a captured loop the block is the body of a
+   * conditional IF node, taken only in the iterations that flag an update */
+  const int cond = qllg_capturing() && qllg_get_param("graph_ru_if") != 0;
+  unsigned long long n1 = 0;
+  if(cond) {
+    unsigned long long h;
+    if(qllg_capture_cond(&h) || qllg_k_ru_cond(h, &sc->no_ru, &sc->ru_trips) ||
+       qllg_capture_if_begin(h)) return -1;
+    n1 = qllg_launch_count();
+  }
   if(qllg_k_mcg_accum(QLLG_F32, c->x64, c->x, Vh, 3, c->nrhs, sc)) return -1;
   if(qllg_get_param("ru_compact") != 0) {
     if(c->xdf) {
@@ -657,6 +669,10 @@ issue_iteration(qllg_stag *S, const iter_ctx *c)
   if(qllg_k_mcg_residual(QLLG_F32, c->r64, c->r, c->b, c->t64, Vh, 3, c->nrhs, 0, sc, &S->rb))
     return -1;
   if(c->reortho && qllg_k_mcg_reortho(c->ps, c->p, c->r, Vh, c->nrhs, sc, &S->rb)) return -1;
+  if(cond) {
+    S->cap_ifbody = (int)(qllg_launch_count() - n1);
+    if(qllg_capture_if_end()) return -1;
+  }
   return 0;
 }
 
@@ -666,12 +682,15 @@ static cudaGraphExec_t
 loop_graph(qllg_stag *S, const iter_ctx *c)
 {
   long key[11] = {c->mixed, c->ps, c->pl, c->nrhs, c->reortho, (long)c->x, (long)c->b,
-                  (long)c->x64, (long)S->ws_gen, (long)c->xdf, 1};
+                  (long)c->x64, (long)S->ws_gen, (long)c->xdf,
+                  2 + (qllg_get_param("graph_ru_if") != 0)};
   for(int i=0; i<6; i++)
     if(S->graphs[i].exec && !memcmp(S->graphs[i].key, key, sizeof(key))) {
       S->graph_body = S->graphs[i].body;
+      S->graph_ifbody = S->graphs[i].ifbody;
       return S->graphs[i].exec;
     }
+  S->cap_ifbody = 0;
   unsigned long long n0 = qllg_launch_count();
   cudaGraph_t g = NULL;
   cudaGraphExec_t exec = NULL;
@@ -698,16 +717,19 @@ loop_graph(qllg_stag *S, const iter_ctx *c)
   if(qllg_check_cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate")) goto fail;
   cudaGraphDestroy(g);
   {
-    /* the capture counted the body's launches without running them */
-    int body = (int)(qllg_launch_count() - n0);
-    qllg_launch_adjust(-(long long)body);
+    /* the capture counted the body's launches without running them; those
+     * of the conditional block run only in the trips that take it */
+    int all = (int)(qllg_launch_count() - n0);
+    qllg_launch_adjust(-(long long)all);
     int i = S->ngraph_next;
     S->ngraph_next = (i + 1) % 6;
     if(S->graphs[i].exec) cudaGraphExecDestroy(S->graphs[i].exec);
     memcpy(S->graphs[i].key, key, sizeof(key));
     S->graphs[i].exec = exec;
-    S->graphs[i].body = body;
-    S->graph_body = body;
+    S->graphs[i].body = all - S->cap_ifbody;
+    S->graphs[i].ifbody = S->cap_ifbody;
+    S->graph_body = all - S->cap_ifbody;
+    S->graph_ifbody = S->cap_ifbody;
   }
   return exec;
 fail:
@@ -725,8 +747,11 @@ int qllg_timing_on(void);
 static void
 count_graph_trips(qllg_stag *S)
 {
-  if(S->graph_body) qllg_launch_adjust((long long)S->graph_body*S->hsc->loops);
+  if(S->graph_body)
+    qllg_launch_adjust((long long)S->graph_body*S->hsc->loops +
+                       (long long)S->graph_ifbody*S->hsc->ru_trips);
   S->graph_body = 0;
+  S->graph_ifbody = 0;
 }
 
 /* the persistent CG (one cooperative launch for the whole loop) takes the

@@ -43,8 +43,9 @@ struct qllg_wilson {
   size_t ws_bytes[WW_N];
   cudaEvent_t ev0, ev1;
   /* captured CGNR loops, by what their launches bake in */
-  struct { long key[6]; cudaGraphExec_t exec; int body; } graphs[WGRAPHS];
+  struct { long key[7]; cudaGraphExec_t exec; int body, ifbody; } graphs[WGRAPHS];
   int ngraph_next;
+  int cap_ifbody;        /* while capturing: kernels of the reliable-update block */
 };
 
 static void wgraphs_drop(qllg_wilson *W);
@@ -351,6 +352,16 @@ wilson_iteration(qllg_wilson *W, const witer *c)
   if(apply_schur(W, ps, c->Sp, c->Ap, c->v, a, 1, NULL, sc->active, &sc->done)) return -1;
   if(qllg_k_scg_update_xr(ps, ps, c->xs, c->r, c->p, c->Ap, Vh, 12, 1, sc, &W->rb)) return -1;
   if(ps != QLLG_F64) {
+    /* in a captured loop the reliable-update block is the body of a
+     * conditional IF node, taken only in the iterations that flag one */
+    const int cond = qllg_capturing() && qllg_get_param("graph_ru_if") != 0;
+    unsigned long long n1 = 0;
+    if(cond) {
+      unsigned long long h;
+      if(qllg_capture_cond(&h) || qllg_k_ru_cond(h, &sc->no_ru, &sc->ru_trips) ||
+         qllg_capture_if_begin(h)) return -1;
+      n1 = qllg_launch_count();
+    }
     if(qllg_k_mcg_accum(ps, c->x64, c->xs, Vh, 12, 1, sc)) return -1;
     /* the double-float pass reuses s64, vv64 and t64 (same size); t
      * goes back to FP64 in place */
@@ -366,6 +377,10 @@ wilson_iteration(qllg_wilson *W, const witer *c)
        apply_schur_eq(W, QLLG_F64, c->s64, c->t64, c->vv64, a, 1, NULL, sc->ru, eq, &sc->no_ru))
       return -1;
     if(qllg_k_mcg_residual(ps, c->r64, c->r, c->bp, c->t64, Vh, 12, 1, 1, sc, &W->rb)) return -1;
+    if(cond) {
+      W->cap_ifbody = (int)(qllg_launch_count() - n1);
+      if(qllg_capture_if_end()) return -1;
+    }
   }
   return qllg_k_scg_update_p(ps, c->p, c->r, Vh, 12, 1, sc);
 }
@@ -384,16 +399,19 @@ wgraphs_drop(qllg_wilson *W)
  * staggered solver's loop_graph, for the Wilson iteration); cached by what
  * the launches bake in: precision, a = 4 + m, the solution buffers */
 static cudaGraphExec_t
-wilson_graph(qllg_wilson *W, const witer *c, int *body_out)
+wilson_graph(qllg_wilson *W, const witer *c, int *body_out, int *ifbody_out)
 {
   long abits;
   memcpy(&abits, &c->a, sizeof(abits));
-  long key[6] = {c->ps, abits, (long)c->xs, (long)c->x64, (long)c->xdf, (long)c->bp};
+  long key[7] = {c->ps, abits, (long)c->xs, (long)c->x64, (long)c->xdf, (long)c->bp,
+                 qllg_get_param("graph_ru_if") != 0};
   for(int i=0; i<WGRAPHS; i++)
     if(W->graphs[i].exec && !memcmp(W->graphs[i].key, key, sizeof(key))) {
       *body_out = W->graphs[i].body;
+      *ifbody_out = W->graphs[i].ifbody;
       return W->graphs[i].exec;
     }
+  W->cap_ifbody = 0;
   unsigned long long n0 = qllg_launch_count();
   cudaGraph_t g = NULL;
   cudaGraphExec_t exec = NULL;
@@ -420,16 +438,19 @@ wilson_graph(qllg_wilson *W, const witer *c, int *body_out)
   if(qllg_check_cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate")) goto fail;
   cudaGraphDestroy(g);
   {
-    /* the capture counted the body's launches without running them */
-    int body = (int)(qllg_launch_count() - n0);
-    qllg_launch_adjust(-(long long)body);
+    /* the capture counted the body's launches without running them; those
+     * of the conditional block run only in the trips that take it */
+    int all = (int)(qllg_launch_count() - n0);
+    qllg_launch_adjust(-(long long)all);
     int i = W->ngraph_next;
     W->ngraph_next = (i + 1) % WGRAPHS;
     if(W->graphs[i].exec) cudaGraphExecDestroy(W->graphs[i].exec);
     memcpy(W->graphs[i].key, key, sizeof(key));
     W->graphs[i].exec = exec;
-    W->graphs[i].body = body;
-    *body_out = body;
+    W->graphs[i].body = all - W->cap_ifbody;
+    W->graphs[i].ifbody = W->cap_ifbody;
+    *body_out = all - W->cap_ifbody;
+    *ifbody_out = W->cap_ifbody;
   }
   return exec;
 fail:
@@ -479,11 +500,11 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
     /* one iteration launched directly first (every kernel of the body is
      * then loaded before the capture), then the rest as one graph launch */
     if(wilson_iteration(W, &c)) return -1;
-    int body = 0;
-    cudaGraphExec_t exec = wilson_graph(W, &c, &body);
+    int body = 0, ifbody = 0;
+    cudaGraphExec_t exec = wilson_graph(W, &c, &body, &ifbody);
     if(!exec || qllg_check_cuda(cudaGraphLaunch(exec, qllg_stream()), "graph launch")) return -1;
     if(wpull(W, 1)) return -1;
-    qllg_launch_adjust((long long)body*W->hsc->loops);
+    qllg_launch_adjust((long long)body*W->hsc->loops + (long long)ifbody*W->hsc->ru_trips);
     return W->hsc->iters[0];
   }
   int issued = 0, batch = 8;
