@@ -503,12 +503,16 @@ def run_wilson(args):
     W = ctypes.c_void_p(L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(u)))
     if not W.value:
         raise RuntimeError(qll.last_error())
-    b = qll.gen_source(dims, 2200, 24, "even")
+    b = pinned_like(qll.gen_source(dims, 2200, 24, "even"))
     out = {"workload": "C2: Wilson e/o CGNR %s, eps=0.3, kappa=0.12, true residual 1e-8 "
-                       "(normal-equation rsq 1e-17)" % "x".join(map(str, dims))}
+                       "(normal-equation rsq 1e-17)" % "x".join(map(str, dims)),
+           "host_arrays": "pinned; seconds: host clock around qllg_wilson_solve (upload of b, the CGNR, the "
+                          "FP64 true residual of S x = b, download of x); device_seconds: the CGNR alone "
+                          "(CUDA events)"}
+    x = pinned_like(np.zeros_like(b))
 
     def solve(mode, timing):
-        x = np.zeros_like(b)
+        x[...] = 0
         info = qll.SolveInfo()
         L.qllg_timing_enable(1 if timing else 0)
         L.qllg_timing_reset()
@@ -531,6 +535,7 @@ def run_wilson(args):
             dt, its, info, _, _ = solve(mode, False)
             if best is None or dt < best["seconds"]:
                 best = {"seconds": dt, "solves_per_s": 1/dt, "iters": its,
+                        "device_seconds": info.seconds, "reliable_updates": info.reliable_updates,
                         "true_rsq": info.true_rsq[0], "loop": "one CUDA-graph launch"}
         # the half-Dslash launches of one more solve, event-timed (a host-
         # polled loop: events cannot sit in a graph's conditional body)
@@ -615,6 +620,15 @@ def run_c1(args):
 
 
 # ------------------------------------------------------------- multishift
+def pinned_like(a):
+    """a page-locked copy of host array a (the library moves page-locked
+    arrays of 1 MiB or more on the SMs rather than the copy engines)"""
+    import torch
+    t = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy().reshape(a.shape)
+    t[...] = a
+    return t
+
+
 def run_multishift(args):
     """C3: 24^3x48, m=0.02, 12 shifts log-spaced over 1e-4..1, 8 Gaussian
     rhs, tolerance 1e-8 on every shift: the mixed multi-rhs solve (FP32
@@ -632,11 +646,15 @@ def run_multishift(args):
     shifts = [10**(-4 + 4*k/11) for k in range(12)]
     ns = len(shifts)
     S = serve.asqtad_operator(dims, 1003, 0.3)
-    bs = [qll.gen_source(dims, 2300 + r, 6, "even") for r in range(nrhs)]
+    bs = [pinned_like(qll.gen_source(dims, 2300 + r, 6, "even")) for r in range(nrhs)]
     out = {"workload": "C3: asqtad multishift 24^3x48, m=0.02, eps=0.3, 12 shifts 1e-4..1, "
-                       "8 rhs, tolerance 1e-8 on every shift", "dims": list(dims)}
+                       "8 rhs, tolerance 1e-8 on every shift", "dims": list(dims),
+           "host_arrays": "pinned; seconds: host clock around qllg_stag_solve_multishift (sources in, "
+                          "96 solutions out)"}
+    xs = [pinned_like(np.zeros_like(bs[0])) for _ in range(nrhs*ns)]
     for name, mode in (("mixed", qll.SOLVE_MIXED_SINGLE), ("fp64_cgms", qll.SOLVE_DOUBLE)):
-        xs = [np.zeros_like(bs[0]) for _ in range(nrhs*ns)]
+        for x in xs:
+            x[...] = 0
         its = (ctypes.c_int*(nrhs*ns))()
         tr = (ctypes.c_double*(nrhs*ns))()
         reps = 1 if mode == qll.SOLVE_DOUBLE else 2

@@ -311,6 +311,9 @@ void qllg_server_destroy(qllg_server *V);
  *    candidates may be chosen; "dslash_variant" (-1: autotuned;
  *    0-23 forces a candidate where it applies, qllg_autotune_report names
  *    them);
+ *  "wilson_fused_update" (1: the FP32 iterations of the Wilson CGNR run
+ *    the CG update in the epilogue of their last half Dslash; 0: a separate
+ *    update kernel),
  *  "graph_ru_if" (1: in the graph-captured mixed solver loops the
  *    reliable-update launches are the body of a conditional IF node, taken
  *    only in the iterations that flag an update; 0: they are launched every

@@ -572,30 +572,7 @@ scg_xr_k(void *x, void *r, const void *p, const void *Ap, int nsites, qllg_cg_sc
   double *res[1] = {s->tmp};
   if(grid_reduce<1>(red, NR, rhs, partial, counter, shm, res)) {
     __syncthreads();
-    if(threadIdx.x == 0) {
-      int anyru = 0, any = 0;
-      const bool mixed = s->delta2 > 0;
-      for(int q=0; q<NR; q++) {
-        s->ru[q] = 0;
-        if(s->active[q]) {
-          double r2 = s->tmp[q];
-          s->iters[q]++;
-          s->prev[q] = s->rsq[q];
-          s->rsq[q] = r2;
-          s->alpha[q] = r2/s->prev[q];
-          if(mixed) {
-            s->ru[q] = ru_kind(s, q, r2);
-            anyru |= s->ru[q] != 0;
-          } else if(!(r2 >= s->rsq_stop[q] && s->iters[q] < s->maxits)) {
-            s->active[q] = 0;
-          }
-        }
-        any |= s->active[q];
-      }
-      s->no_ru = !anyru;
-      s->done = !any;
-      s->count++;
-    }
+    if(threadIdx.x == 0) cg_finish_std(s, NR);
   }
 }
 

@@ -38,9 +38,11 @@ __device__ __forceinline__ Cx<T> phase(const Cx<T> &z, int code) {
   return r;
 }
 
-template <int PS, int PL, int NR>
-__global__ void __launch_bounds__(kThreads)
-wilson_dslash(qllg_stag_args a)
+// UPD: the body of mode 4 (FP32 only), a kernel of its own
+// (wilson_dslash_upd) so that the fused update's registers do not cost
+// the other launches occupancy
+template <int PS, int PL, int NR, bool UPD>
+__device__ __forceinline__ void wilson_dslash_body(const qllg_stag_args &a)
 {
   typedef typename Calc<PS, PL>::T T;
   __shared__ double shm[2*kThreads];
@@ -55,6 +57,13 @@ wilson_dslash(qllg_stag_args a)
   const bool act = !a.active || (a.active[rhs] && (!a.active_eq || a.active[rhs] == a.active_eq));
   const T ca = (T)(a.a ? a.a[rhs] : a.a0);
   const T cb = (T)a.b;
+  // mode 4: the step length of the fused x, r update (read before any
+  // block's bookkeeping can change the scalars: the last block writes them
+  // only after every block has reduced)
+  static_assert(!UPD || (PS == QLLG_F32 && PL == QLLG_F32), "mode 4 is FP32 only");
+  constexpr bool F4 = UPD;
+  float alpha = 0;
+  if constexpr (F4) if(a.mode == 4 && act && !skip) alpha = (float)(a.sc->rsq[rhs]/a.sc->pnorm[rhs]);
   if(!skip && act) {
     for(size_t t = (size_t)blockIdx.x*blockDim.x + threadIdx.x; t < total;
         t += (size_t)gridDim.x*blockDim.x) {
@@ -115,21 +124,69 @@ wilson_dslash(qllg_stag_args a)
       Cx<T> out[12];
 #pragma unroll
       for(int c=0; c<12; c++) {
-        if(a.mode == 2) {
+        if(a.mode == 2 || (UPD && a.mode == 4)) {
           T sr = a.self ? ca*self[c].r : (T)0, si = a.self ? ca*self[c].i : (T)0;
           out[c].r = kfma(cb, acc[c].r, sr); out[c].i = kfma(cb, acc[c].i, si);
         } else out[c] = acc[c];
+      }
+      if constexpr (F4) if(a.mode == 4) {
+        // out is Ap: x += alpha p, r -= alpha Ap, |r|^2 (as scg_xr_k)
+        Cx<T> xv[12], rv[12], pv[12];
+        SpinorIO<PS,12>::load(a.x, total, t, xv);
+        SpinorIO<PS,12>::load(a.r, total, t, rv);
+        SpinorIO<PS,12>::load(a.pvec, total, t, pv);
+#pragma unroll
+        for(int c=0; c<12; c++) {
+          xv[c].r = fma(alpha, pv[c].r, xv[c].r); xv[c].i = fma(alpha, pv[c].i, xv[c].i);
+          rv[c].r = fma(-alpha, out[c].r, rv[c].r); rv[c].i = fma(-alpha, out[c].i, rv[c].i);
+        }
+        acc0.norm(rv);
+        SpinorIO<PS,12>::store(a.x, total, t, xv);
+        SpinorIO<PS,12>::store(a.r, total, t, rv);
+        continue;
       }
       SpinorIO<PS,12>::store(a.out, total, t, out);
       if(a.norm_out) acc0.norm(out);
       if(a.norm_self && a.self) acc1.norm(self);
     }
   }
+  if(F4 && a.mode == 4) {
+    if(skip) return;                   // uniform: the solve is done
+    double red1[1] = {acc0.get()};
+    double *res1[1] = {a.sc->tmp};
+    if(grid_reduce<1>(red1, NR, rhs, a.partial, a.counter, shm, res1)) {
+      __syncthreads();
+      if(threadIdx.x == 0) {
+        cg_finish_std(a.sc, NR);
+        if(a.cond) {
+          // the reliable-update block of a captured loop runs when flagged
+          const int take = !a.sc->no_ru;
+          if(take) a.sc->ru_trips++;
+          cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, take ? 1u : 0u);
+        }
+      }
+    }
+    return;
+  }
   double red[2] = {acc0.get(), acc1.get()};
   if(a.norm_out || a.norm_self) {
     double *res[2] = {a.norm_out, a.norm_self};
     grid_reduce<2>(red, NR, rhs, a.partial, a.counter, shm, res);
   }
+}
+
+template <int PS, int PL, int NR>
+__global__ void __launch_bounds__(kThreads)
+wilson_dslash(qllg_stag_args a)
+{
+  wilson_dslash_body<PS,PL,NR,false>(a);
+}
+
+// mode 4, two blocks of 256 a SM (128 registers)
+__global__ void __launch_bounds__(kThreads, 2)
+wilson_dslash_upd(qllg_stag_args a)
+{
+  wilson_dslash_body<QLLG_F32,QLLG_F32,1,true>(a);
 }
 
 // Small one-rhs launches split by direction: a block is 64 sites and two
@@ -417,13 +474,39 @@ int launch_dir2(const qllg_stag_args *a)
   return qllg_launched("wilson_dslash_dir2 launch");
 }
 
+// mode 4: the FP32 one-rhs kernel with the fused CG update
+int launch_upd(const qllg_stag_args *a)
+{
+  static int bps = 0;
+  if(!bps) {
+    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &bps, wilson_dslash_upd, kThreads, 0), "occupancy")) return -1;
+    if(bps < 1) bps = 1;
+  }
+  size_t need = ((size_t)a->g.Vh + kThreads - 1)/kThreads;
+  size_t maxg = (size_t)qllg_num_sms()*bps;
+  if(maxg > (size_t)a->rb->maxblocks) maxg = a->rb->maxblocks;
+  int grid = (int)(need < maxg ? need : maxg);
+  if(grid < 1) grid = 1;
+  qllg_stag_args A = *a;
+  A.partial = a->rb->partial;
+  A.counter = a->rb->counter;
+  wilson_dslash_upd<<<grid, kThreads, 0, qllg_stream()>>>(A);
+  return qllg_launched("wilson_dslash launch");
+}
+
 template <int PS, int PL, int NR>
 int launch_t(const qllg_stag_args *a)
 {
   // one rhs in FP64, fewer sites than the GPU's resident threads: two
   // threads per site, split by direction
+  if(a->mode == 4 && (PS != QLLG_F32 || PL != QLLG_F32 || NR != 1 || !a->rb || !a->sc || !a->x || !a->r ||
+                     !a->pvec)) {
+    qllg_set_error("wilson_dslash: the fused CG update (mode 4) takes FP32, a reduction workspace and x, r, p");
+    return -1;
+  }
   if constexpr (NR == 1 && ((PS == QLLG_F64 && PL == QLLG_F64) || (PS == QLLG_F32 && PL == QLLG_F32))) {
-    if(qllg_get_param(PS == QLLG_F64 ? "wilson_f64_dir2" : "wilson_f32_dir2") != 0 &&
+    if(a->mode != 4 && qllg_get_param(PS == QLLG_F64 ? "wilson_f64_dir2" : "wilson_f32_dir2") != 0 &&
        (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
       return launch_dir2<PS,PL>(a);
   }
@@ -432,9 +515,11 @@ int launch_t(const qllg_stag_args *a)
   // one-thread kernel holds one block of 256 threads per SM)
   if constexpr (NR == 1 && (PS == QLLG_F32 || PS == QLLG_DF || PS == QLLG_F64)) {
     const char *knob = PS == QLLG_DF ? "wilson_df_c3" : PS == QLLG_F64 ? "wilson_f64_c3" : "wilson_c3";
-    if(qllg_get_param(knob) != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
+    if(a->mode != 4 && qllg_get_param(knob) != 0 && (size_t)a->g.Vh < (size_t)qllg_num_sms()*1024)
       return launch_c3<PS,PL>(a);
   }
+  if constexpr (PS == QLLG_F32 && PL == QLLG_F32 && NR == 1)
+    if(a->mode == 4) return launch_upd(a);
   static int bps = 0;
   if(!bps) {
     if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(

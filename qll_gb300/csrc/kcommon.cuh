@@ -600,4 +600,32 @@ __device__ inline void cg_finish_mixed(qllg_cg_scalars *s, int nr) {
   s->count++;
 }
 
+// standard-form CG (r -= alpha Ap, then p = r + beta p with beta in
+// alpha[]): the bookkeeping after |r|^2 of the update is reduced into
+// tmp[]; mixed (delta2 > 0): reliable-update flags instead of stopping
+__device__ inline void cg_finish_std(qllg_cg_scalars *s, int nr) {
+  int anyru = 0, any = 0;
+  const bool mixed = s->delta2 > 0;
+  for(int q=0; q<nr; q++) {
+    s->ru[q] = 0;
+    if(s->active[q]) {
+      double r2 = s->tmp[q];
+      s->iters[q]++;
+      s->prev[q] = s->rsq[q];
+      s->rsq[q] = r2;
+      s->alpha[q] = r2/s->prev[q];
+      if(mixed) {
+        s->ru[q] = ru_kind(s, q, r2);
+        anyru |= s->ru[q] != 0;
+      } else if(!(r2 >= s->rsq_stop[q] && s->iters[q] < s->maxits)) {
+        s->active[q] = 0;
+      }
+    }
+    any |= s->active[q];
+  }
+  s->no_ru = !anyru;
+  s->done = !any;
+  s->count++;
+}
+
 } // namespace qk

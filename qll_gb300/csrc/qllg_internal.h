@@ -200,6 +200,13 @@ typedef struct {
   void *x, *r;
   struct qllg_cg_scalars_s *sc;
   int mixed;
+  /* mode 4 (Wilson standard-form CG, fused): Ap = a0*self + b*acc stays in
+   * registers, then x += alpha pvec, r -= alpha Ap with alpha = rsq/pnorm
+   * and |r|^2 reduced; the last block does the iteration's bookkeeping
+   * (cg_finish_std) and, when cond is a graph conditional handle, sets it
+   * to "a reliable update is flagged".  FP32 spinors, x and r FP32. */
+  const void *pvec;
+  unsigned long long cond;
 } qllg_stag_args;
 int qllg_k_stag_dslash(int prec_spinor, int prec_link, const qllg_stag_args *a);
 

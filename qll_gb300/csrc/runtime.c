@@ -425,6 +425,9 @@ static struct { const char *name; double value; } g_params[] = {
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
   {"dslash_pipe", 1},        /* allow the per-warp cp.async pipeline Dslash variants */
   {"dslash_tma", 1},         /* allow the per-warp tensor-copy (TMA) pipeline Dslash variants */
+  {"wilson_fused_update", 1}, /* FP32 Wilson CGNR: the CG update (x, r, |r|^2 and the
+                                iteration's bookkeeping) in the epilogue of the last
+                                half Dslash of the iteration */
   {"graph_ru_if", 1},        /* graph-captured mixed solver loops: the reliable-update
                                 launches sit in a conditional IF node taken only in
                                 the iterations that flag an update (else they are

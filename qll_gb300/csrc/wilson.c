@@ -338,28 +338,71 @@ typedef struct {
   void *x64, *r64, *bp, *s64, *vv64, *t64, *xdf;
 } witer;
 
+/* the last half Dslash of an FP32 iteration fused with the CG update:
+ * Ap = a Sp - W_eo^dagger v / a stays in registers, x += alpha p,
+ * r -= alpha Ap and |r|^2, then the iteration's bookkeeping; cond: the
+ * graph conditional the last block sets when an update is flagged */
+static int
+whalf_update(qllg_wilson *W, const witer *c, unsigned long long cond)
+{
+  if(wlinks(W, QLLG_F32)) return -1;
+  qllg_stag_args A;
+  memset(&A, 0, sizeof(A));
+  A.g = W->g;
+  A.out_parity = 0;
+  A.nrhs = 1;
+  A.nslots = 8;
+  A.links = W->links[QLLG_F32];
+  A.in = c->v;
+  A.self = c->Sp;
+  A.mode = 4;
+  A.a0 = c->a;
+  A.b = -1.0/c->a;
+  A.active = W->sc->active;
+  A.done = &W->sc->done;
+  A.rb = &W->rb;
+  A.dag = 1;
+  A.x = c->xs;
+  A.r = c->r;
+  A.pvec = c->p;
+  A.sc = W->sc;
+  A.cond = cond;
+  qllg_tm_begin("wilson_dslash");
+  int rc = qllg_k_wilson_dslash(QLLG_F32, QLLG_F32, &A);
+  qllg_tm_end();
+  return rc;
+}
+
 /* one iteration of the CGNR on S^dagger S (the standard-form CG update,
  * with the FP32 mode's reliable update of the flagged rhs); every launch
  * returns at once when the solve is done, the reliable-update ones when
- * no update is flagged */
+ * no update is flagged.  FP32: the CG update runs in the epilogue of the
+ * last half Dslash (parameter wilson_fused_update) */
 static int
 wilson_iteration(qllg_wilson *W, const witer *c)
 {
   qllg_cg_scalars *sc = W->sc;
   const int Vh = W->g.Vh, ps = c->ps;
   const double a = c->a;
+  const int fused = ps == QLLG_F32 && qllg_get_param("wilson_fused_update") != 0;
+  /* in a captured loop the reliable-update block is the body of a
+   * conditional IF node, taken only in the iterations that flag one */
+  const int cond = ps != QLLG_F64 && qllg_capturing() && qllg_get_param("graph_ru_if") != 0;
+  unsigned long long h = 0;
+  if(cond && qllg_capture_cond(&h)) return -1;
   if(apply_schur(W, ps, c->p, c->Sp, c->v, a, 0, sc->pnorm, sc->active, &sc->done)) return -1;
-  if(apply_schur(W, ps, c->Sp, c->Ap, c->v, a, 1, NULL, sc->active, &sc->done)) return -1;
-  if(qllg_k_scg_update_xr(ps, ps, c->xs, c->r, c->p, c->Ap, Vh, 12, 1, sc, &W->rb)) return -1;
+  if(fused) {
+    if(whalf(W, ps, 1, c->Sp, NULL, c->v, 0, 0, 1, NULL, NULL, sc->active, &sc->done, 1) ||
+       whalf_update(W, c, h)) return -1;
+  } else {
+    if(apply_schur(W, ps, c->Sp, c->Ap, c->v, a, 1, NULL, sc->active, &sc->done)) return -1;
+    if(qllg_k_scg_update_xr(ps, ps, c->xs, c->r, c->p, c->Ap, Vh, 12, 1, sc, &W->rb)) return -1;
+    if(cond && qllg_k_ru_cond(h, &sc->no_ru, &sc->ru_trips)) return -1;
+  }
   if(ps != QLLG_F64) {
-    /* in a captured loop the reliable-update block is the body of a
-     * conditional IF node, taken only in the iterations that flag one */
-    const int cond = qllg_capturing() && qllg_get_param("graph_ru_if") != 0;
     unsigned long long n1 = 0;
     if(cond) {
-      unsigned long long h;
-      if(qllg_capture_cond(&h) || qllg_k_ru_cond(h, &sc->no_ru, &sc->ru_trips) ||
-         qllg_capture_if_begin(h)) return -1;
+      if(qllg_capture_if_begin(h)) return -1;
       n1 = qllg_launch_count();
     }
     if(qllg_k_mcg_accum(ps, c->x64, c->xs, Vh, 12, 1, sc)) return -1;
@@ -404,7 +447,7 @@ wilson_graph(qllg_wilson *W, const witer *c, int *body_out, int *ifbody_out)
   long abits;
   memcpy(&abits, &c->a, sizeof(abits));
   long key[7] = {c->ps, abits, (long)c->xs, (long)c->x64, (long)c->xdf, (long)c->bp,
-                 qllg_get_param("graph_ru_if") != 0};
+                 (qllg_get_param("graph_ru_if") != 0) + 2*(qllg_get_param("wilson_fused_update") != 0)};
   for(int i=0; i<WGRAPHS; i++)
     if(W->graphs[i].exec && !memcmp(W->graphs[i].key, key, sizeof(key))) {
       *body_out = W->graphs[i].body;

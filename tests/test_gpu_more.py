@@ -495,3 +495,47 @@ def test_wilson_cgnr_graph_matches_host_loop(mode):
     assert out[0][0] == out[1][0] == out[2][0]
     assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][1], out[2][1])
     L.qllg_wilson_destroy(ctypes.c_void_p(W))
+
+
+def test_wilson_fused_update_matches_separate_kernels():
+    """the FP32 CGNR with the CG update in the last half Dslash's epilogue
+    (wilson_fused_update) against the separate update kernel: the |r|^2
+    sums are reduced in a different order, so the two agree to the solver's
+    accuracy (iterations within one, solutions within 1e-6), and both reach
+    the true residual target; the reliable-update block as a graph
+    conditional (graph_ru_if) changes nothing, bitwise"""
+    L = qll.load()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    L.qllg_wilson_create.restype = ctypes.c_void_p
+    L.qllg_wilson_create.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_void_p)]
+    L.qllg_wilson_solve.restype = c_int
+    L.qllg_wilson_solve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double,
+                                    c_double, c_int, c_int, ctypes.POINTER(qll.SolveInfo)]
+    dims = (8, 8, 8, 16)
+    u = list(wilson_links(dims))
+    W = L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(u))
+    assert W, qll.last_error()
+    b = qll.gen_source(dims, 31, 24, "even")
+    mass = 1/(2*0.12) - 4
+    runs = {}
+    for fused in (1, 0):
+        for ru_if in (1, 0):
+            L.qllg_set_param(b"wilson_fused_update", fused)
+            L.qllg_set_param(b"graph_ru_if", ru_if)
+            x = np.zeros_like(b)
+            info = qll.SolveInfo()
+            its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, mass, 1e-17, 5000,
+                                      qll.SOLVE_MIXED_SINGLE, byref(info))
+            assert its > 0, qll.last_error()
+            assert info.true_rsq[0] < 1e-16
+            runs[(fused, ru_if)] = (its, info.reliable_updates, x)
+    L.qllg_set_param(b"wilson_fused_update", 1)
+    L.qllg_set_param(b"graph_ru_if", 1)
+    # the IF node changes nothing: bitwise the same per fused setting
+    for fused in (1, 0):
+        a, c = runs[(fused, 1)], runs[(fused, 0)]
+        assert a[0] == c[0] and a[1] == c[1] and np.array_equal(a[2], c[2])
+    f, s = runs[(1, 1)], runs[(0, 1)]
+    assert abs(f[0] - s[0]) <= 1
+    assert relerr(f[2], s[2]) < 1e-6
+    L.qllg_wilson_destroy(ctypes.c_void_p(W))
