@@ -38,6 +38,59 @@ __device__ __forceinline__ Cx<T> phase(const Cx<T> &z, int code) {
   return r;
 }
 
+// acc -= the eight hops of site `site` (coordinates x) of the output
+// parity: per slot the neighbour spinor projected to two spin components,
+// multiplied by the link and reconstructed (dag: gamma5 D gamma5)
+template <int PS, int PL, int NR, typename T>
+__device__ __forceinline__ void wilson_hops(const void *links, const float *lscale, const void *in, int dag,
+                                            const Geo &G, size_t V, size_t loff, int site, const int x[4],
+                                            int rhs, size_t total, Cx<T> acc[12])
+{
+#pragma unroll
+  for(int mu=0; mu<4; mu++) {
+#pragma unroll
+    for(int back=0; back<2; back++) {
+      // slot 2mu: (1 - g_mu) from x+mu; slot 2mu+1: (1 + g_mu) from x-mu
+      const int sgn = (back ? 1 : -1)*(dag ? -1 : 1);
+      const int k = nbr_index(G, x, mu, back ? -1 : 1);
+      Cx<T> U[9], f[12];
+      LinkIO<PL>::load(links, 2*mu + back, V, loff + site, lscale, U);
+      SpinorIO<PS,12>::load(in, total, (size_t)k*NR + rhs, f);
+#pragma unroll
+      for(int hk=0; hk<2; hk++) {
+        const int col = gcol(mu, hk);
+        const int ph = gph(mu, hk) + (sgn < 0 ? 2 : 0);
+        Cx<T> h[3], tt[3];
+#pragma unroll
+        for(int c=0; c<3; c++) {
+          Cx<T> y = phase(f[3*col + c], ph);
+          h[c].r = f[3*hk + c].r + y.r; h[c].i = f[3*hk + c].i + y.i;
+          tt[c].r = 0; tt[c].i = 0;
+        }
+#pragma unroll
+        for(int l=0; l<3; l++) {
+#pragma unroll
+          for(int j=0; j<3; j++) cmac(tt[j], U[3*l + j], h[l]);
+        }
+        // r_hk -= t; r_a -= sgn*phase_a*t for the lower row a fed by hk
+#pragma unroll
+        for(int c=0; c<3; c++) { acc[3*hk + c].r -= tt[c].r; acc[3*hk + c].i -= tt[c].i; }
+#pragma unroll
+        for(int ar=2; ar<4; ar++) {
+          if(gcol(mu, ar) == hk) {
+            const int pa = gph(mu, ar) + (sgn < 0 ? 0 : 2);   // minus sign folded in
+#pragma unroll
+            for(int c=0; c<3; c++) {
+              Cx<T> y = phase(tt[c], pa);
+              acc[3*ar + c].r += y.r; acc[3*ar + c].i += y.i;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 // UPD: the body of mode 4 (FP32 only), a kernel of its own
 // (wilson_dslash_upd) so that the fused update's registers do not cost
 // the other launches occupancy
@@ -77,49 +130,7 @@ __device__ __forceinline__ void wilson_dslash_body(const qllg_stag_args &a)
         if(a.mode == 1) { acc[c].r = ca*self[c].r; acc[c].i = ca*self[c].i; }
         else { acc[c].r = 0; acc[c].i = 0; }
       }
-#pragma unroll
-      for(int mu=0; mu<4; mu++) {
-#pragma unroll
-        for(int back=0; back<2; back++) {
-          // slot 2mu: (1 - g_mu) from x+mu; slot 2mu+1: (1 + g_mu) from x-mu
-          const int sgn = (back ? 1 : -1)*(a.dag ? -1 : 1);
-          const int k = nbr_index(G, x, mu, back ? -1 : 1);
-          Cx<T> U[9], f[12];
-          LinkIO<PL>::load(a.links, 2*mu + back, V, loff + site, a.lscale, U);
-          SpinorIO<PS,12>::load(a.in, total, (size_t)k*NR + rhs, f);
-#pragma unroll
-          for(int hk=0; hk<2; hk++) {
-            const int col = gcol(mu, hk);
-            const int ph = gph(mu, hk) + (sgn < 0 ? 2 : 0);
-            Cx<T> h[3], tt[3];
-#pragma unroll
-            for(int c=0; c<3; c++) {
-              Cx<T> y = phase(f[3*col + c], ph);
-              h[c].r = f[3*hk + c].r + y.r; h[c].i = f[3*hk + c].i + y.i;
-              tt[c].r = 0; tt[c].i = 0;
-            }
-#pragma unroll
-            for(int l=0; l<3; l++) {
-#pragma unroll
-              for(int j=0; j<3; j++) cmac(tt[j], U[3*l + j], h[l]);
-            }
-            // r_hk -= t; r_a -= sgn*phase_a*t for the lower row a fed by hk
-#pragma unroll
-            for(int c=0; c<3; c++) { acc[3*hk + c].r -= tt[c].r; acc[3*hk + c].i -= tt[c].i; }
-#pragma unroll
-            for(int ar=2; ar<4; ar++) {
-              if(gcol(mu, ar) == hk) {
-                const int pa = gph(mu, ar) + (sgn < 0 ? 0 : 2);   // minus sign folded in
-#pragma unroll
-                for(int c=0; c<3; c++) {
-                  Cx<T> y = phase(tt[c], pa);
-                  acc[3*ar + c].r += y.r; acc[3*ar + c].i += y.i;
-                }
-              }
-            }
-          }
-        }
-      }
+      wilson_hops<PS,PL,NR,T>(a.links, a.lscale, a.in, a.dag, G, V, loff, site, x, rhs, total, acc);
       if(a.self && a.mode != 1) SpinorIO<PS,12>::load(a.self, total, t, self);
       Cx<T> out[12];
 #pragma unroll
@@ -187,6 +198,243 @@ __global__ void __launch_bounds__(kThreads, 2)
 wilson_dslash_upd(qllg_stag_args a)
 {
   wilson_dslash_body<QLLG_F32,QLLG_F32,1,true>(a);
+}
+
+// ------------------------------------------ persistent CGNR iterations
+// One cooperative launch runs the FP32 iterations of the mixed Wilson CGNR
+// (the standard-form CG on S^dagger S of wilson.c, one rhs) until a
+// reliable update is flagged, the solve is done or the trip cap is reached;
+// the host then takes the update with the FP64 kernels and launches again.
+// On a small lattice (C2, 16^3x32: 65,536 even sites) the graph loop's
+// half Dslashes are about 10 us of work each and the gaps between its
+// kernel nodes cost as much again.  Per iteration:
+//   v = W_oe p; Sp = a p - W_eo v / a with |Sp|^2; v = W_oe^+ Sp;
+//   Ap = a Sp - W_eo^+ v / a, x += alpha p, r -= alpha Ap with |r|^2
+//   (alpha = |r|^2/|Sp|^2); the bookkeeping of cg_finish_std; p = r + beta p
+// with a grid barrier after each step.  Each reduction writes one partial
+// per block, a barrier follows, and every block folds the partials in
+// block order itself, so all blocks hold bitwise the same scalars.  The
+// barrier is a counter and a generation word whose waits give up after
+// poll_limit polls: the block sets the error word and returns, and so do
+// the others at their next barrier.
+struct WcgpArgs {
+  qllg_geom g;
+  const void *links;              // FP32 links
+  void *x, *r, *p, *Sp, *v;       // FP32: x, r, p, S p (even sites), v (odd sites)
+  qllg_cg_scalars *sc;
+  double a;                       // 4 + m
+  double *partial;                // [2][gridDim]
+  unsigned *bar;                  // [0] arrivals, [1] generation
+  int *err;                       // 1: a barrier wait ran out
+  long long poll_limit;
+  int extra;                      // barrier arrivals expected beyond the grid (tests)
+  int trips;                      // iteration cap of this launch
+};
+
+__device__ bool wcg_barrier(const WcgpArgs &a)
+{
+  __shared__ int ok;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned *gen = a.bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned want = gridDim.x + (unsigned)a.extra;
+    if(atomicAdd(a.bar, 1u) == want - 1) {
+      a.bar[0] = 0;
+      __threadfence();
+      atomicAdd(a.bar + 1, 1u);
+    } else {
+      long long n = 0;
+      while(*gen == g) {
+        if(++n > a.poll_limit || *(volatile int *)a.err) {
+          atomicExch(a.err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// the grid's sum of val (one value a thread), the same in every block
+__device__ bool wcg_sum(const WcgpArgs &a, double val, double &out, int &phase)
+{
+  __shared__ double buf[kThreads];
+  __shared__ double res;
+  buf[threadIdx.x] = val;
+  __syncthreads();
+  for(int w = kThreads/2; w > 0; w >>= 1) {
+    if(threadIdx.x < w) buf[threadIdx.x] += buf[threadIdx.x + w];
+    __syncthreads();
+  }
+  double *part = a.partial + (size_t)(phase & 1)*gridDim.x;
+  if(threadIdx.x == 0) part[blockIdx.x] = buf[0];
+  phase++;
+  if(!wcg_barrier(a)) return false;
+  if(threadIdx.x < 32) {
+    double t = 0;
+    for(int b = threadIdx.x; b < (int)gridDim.x; b += 32) t += ((volatile double *)part)[b];
+#pragma unroll
+    for(int o=16; o>0; o>>=1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if(threadIdx.x == 0) res = t;
+  }
+  __syncthreads();
+  out = res;
+  return true;
+}
+
+// out = W_oe^(dag) in on the odd sites (mode 0 of the half Dslash)
+__device__ __forceinline__ void wcg_hop_odd(const WcgpArgs &a, const Geo &G, const void *in, int dag)
+{
+  const size_t V = (size_t)a.g.V, total = (size_t)G.Vh;
+  for(size_t t = (size_t)blockIdx.x*kThreads + threadIdx.x; t < total; t += (size_t)gridDim.x*kThreads) {
+    int x[4];
+    site_coords(G, 1, (int)t, x);
+    Cx<float> acc[12];
+#pragma unroll
+    for(int c=0; c<12; c++) { acc[c].r = 0; acc[c].i = 0; }
+    wilson_hops<QLLG_F32,QLLG_F32,1,float>(a.links, NULL, in, dag, G, V, (size_t)G.Vh, (int)t, x, 0, total,
+                                           acc);
+    SpinorIO<QLLG_F32,12>::store(a.v, total, t, acc);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 2)
+wilson_cgnr_persistent(WcgpArgs a)
+{
+  const Geo G = make_geo(a.g);
+  const size_t V = (size_t)a.g.V, total = (size_t)G.Vh;
+  const float ca = (float)a.a, cb = (float)(-1.0/a.a);
+  __shared__ double s_rsq, s_pn, s_beta, s_maxr2, s_stop, s_delta2, s_prev;
+  __shared__ int s_act, s_iters, s_maxits, s_ru, s_stop_loop;
+  if(threadIdx.x == 0) {
+    qllg_cg_scalars *sc = a.sc;
+    s_rsq = sc->rsq[0]; s_pn = sc->pnorm[0]; s_beta = sc->alpha[0]; s_maxr2 = sc->maxr2[0];
+    s_stop = sc->rsq_stop[0]; s_delta2 = sc->delta2; s_prev = sc->prev[0];
+    s_act = sc->active[0] && !sc->done; s_iters = sc->iters[0]; s_maxits = sc->maxits;
+    s_ru = 0; s_stop_loop = 0;
+  }
+  __syncthreads();
+  int phase = 0, trip = 0;
+  while(s_act && !s_stop_loop && trip < a.trips) {
+    trip++;
+    // v = W_oe p
+    wcg_hop_odd(a, G, a.p, 0);
+    if(!wcg_barrier(a)) return;
+    // Sp = a p - W_eo v / a, |Sp|^2
+    Acc<float> an;
+    for(size_t t = (size_t)blockIdx.x*kThreads + threadIdx.x; t < total; t += (size_t)gridDim.x*kThreads) {
+      int x[4];
+      site_coords(G, 0, (int)t, x);
+      Cx<float> acc[12], pv[12], o[12];
+#pragma unroll
+      for(int c=0; c<12; c++) { acc[c].r = 0; acc[c].i = 0; }
+      wilson_hops<QLLG_F32,QLLG_F32,1,float>(a.links, NULL, a.v, 0, G, V, 0, (int)t, x, 0, total, acc);
+      SpinorIO<QLLG_F32,12>::load(a.p, total, t, pv);
+#pragma unroll
+      for(int c=0; c<12; c++) { o[c].r = kfma(cb, acc[c].r, ca*pv[c].r); o[c].i = kfma(cb, acc[c].i, ca*pv[c].i); }
+      SpinorIO<QLLG_F32,12>::store(a.Sp, total, t, o);
+      an.norm(o);
+    }
+    double pn;
+    if(!wcg_sum(a, an.get(), pn, phase)) return;
+    // v = W_oe^+ Sp
+    wcg_hop_odd(a, G, a.Sp, 1);
+    if(!wcg_barrier(a)) return;
+    // Ap = a Sp - W_eo^+ v / a; x += alpha p, r -= alpha Ap, |r|^2
+    Acc<float> ar;
+    {
+      const float alpha = (float)(s_rsq/pn);
+      for(size_t t = (size_t)blockIdx.x*kThreads + threadIdx.x; t < total; t += (size_t)gridDim.x*kThreads) {
+        int x[4];
+        site_coords(G, 0, (int)t, x);
+        Cx<float> acc[12], sv[12], xv[12], rv[12], pv[12];
+#pragma unroll
+        for(int c=0; c<12; c++) { acc[c].r = 0; acc[c].i = 0; }
+        wilson_hops<QLLG_F32,QLLG_F32,1,float>(a.links, NULL, a.v, 1, G, V, 0, (int)t, x, 0, total, acc);
+        SpinorIO<QLLG_F32,12>::load(a.Sp, total, t, sv);
+        SpinorIO<QLLG_F32,12>::load(a.x, total, t, xv);
+        SpinorIO<QLLG_F32,12>::load(a.r, total, t, rv);
+        SpinorIO<QLLG_F32,12>::load(a.p, total, t, pv);
+#pragma unroll
+        for(int c=0; c<12; c++) {
+          const float apr = kfma(cb, acc[c].r, ca*sv[c].r), api = kfma(cb, acc[c].i, ca*sv[c].i);
+          xv[c].r = fmaf(alpha, pv[c].r, xv[c].r); xv[c].i = fmaf(alpha, pv[c].i, xv[c].i);
+          rv[c].r = fmaf(-alpha, apr, rv[c].r); rv[c].i = fmaf(-alpha, api, rv[c].i);
+        }
+        ar.norm(rv);
+        SpinorIO<QLLG_F32,12>::store(a.x, total, t, xv);
+        SpinorIO<QLLG_F32,12>::store(a.r, total, t, rv);
+      }
+    }
+    double r2;
+    if(!wcg_sum(a, ar.get(), r2, phase)) return;
+    // cg_finish_std's bookkeeping (every block the same)
+    if(threadIdx.x == 0) {
+      s_pn = pn;
+      s_iters++;
+      s_prev = s_rsq;
+      s_rsq = r2;
+      s_beta = r2/s_prev;
+      if(r2 < s_stop || s_iters >= s_maxits || !(r2 == r2)) s_ru = 2;
+      else s_ru = r2 < s_delta2*s_maxr2 ? 1 : 0;
+      s_stop_loop = s_ru != 0;       // the host takes the update, then p
+    }
+    __syncthreads();
+    if(s_stop_loop) break;
+    // p = r + beta p
+    {
+      const float beta = (float)s_beta;
+      for(size_t t = (size_t)blockIdx.x*kThreads + threadIdx.x; t < total; t += (size_t)gridDim.x*kThreads) {
+        Cx<float> pv[12], rv[12];
+        SpinorIO<QLLG_F32,12>::load(a.p, total, t, pv);
+        SpinorIO<QLLG_F32,12>::load(a.r, total, t, rv);
+#pragma unroll
+        for(int c=0; c<12; c++) { pv[c].r = fmaf(beta, pv[c].r, rv[c].r); pv[c].i = fmaf(beta, pv[c].i, rv[c].i); }
+        SpinorIO<QLLG_F32,12>::store(a.p, total, t, pv);
+      }
+    }
+    if(!wcg_barrier(a)) return;
+  }
+  if(blockIdx.x == 0 && threadIdx.x == 0) {
+    qllg_cg_scalars *sc = a.sc;
+    sc->rsq[0] = s_rsq; sc->prev[0] = s_prev; sc->alpha[0] = s_beta; sc->pnorm[0] = s_pn;
+    sc->iters[0] = s_iters;
+    sc->ru[0] = s_ru;
+    sc->no_ru = s_ru == 0;
+    sc->count += trip;
+  }
+}
+
+int launch_wcgp(const WcgpArgs &a0, size_t partial_len, int *grid_out)
+{
+  static int per_sm = 0;
+  if(!per_sm) {
+    if(qllg_check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wilson_cgnr_persistent,
+                                                                     kThreads, 0),
+                       "persistent CGNR occupancy")) return -1;
+    if(per_sm < 1) { qllg_set_error("persistent CGNR: no resident block"); return -1; }
+  }
+  size_t want = ((size_t)a0.g.Vh + kThreads - 1)/kThreads;
+  const size_t cap = (size_t)qllg_num_sms()*per_sm;
+  if(want > cap) want = cap;
+  const int grid = want < 1 ? 1 : (int)want;
+  *grid_out = grid;
+  if(2*(size_t)grid > partial_len) {
+    qllg_set_error("persistent CGNR: the reduction buffer is too small");
+    return -1;
+  }
+  WcgpArgs a = a0;
+  void *args[] = {&a};
+  return qllg_check_cuda(cudaLaunchCooperativeKernel((const void *)wilson_cgnr_persistent, dim3(grid),
+                                                     dim3(kThreads), args, 0, qllg_stream()),
+                         "persistent CGNR launch") || qllg_launched("wilson_cgnr_persistent launch");
 }
 
 // Small one-rhs launches split by direction: a block is 64 sites and two
@@ -552,6 +800,25 @@ int launch_nr(const qllg_stag_args *a)
 }
 
 } // namespace
+
+extern "C" int
+qllg_k_wilson_cgnr_persistent(const qllg_wcgp_args *h, int *grid_out)
+{
+  WcgpArgs a;
+  memset(&a, 0, sizeof(a));
+  a.g = h->g;
+  a.links = h->links;
+  a.x = h->x; a.r = h->r; a.p = h->p; a.Sp = h->Sp; a.v = h->v;
+  a.sc = h->sc;
+  a.a = h->a;
+  a.partial = h->partial;
+  a.bar = h->bar;
+  a.err = h->err;
+  a.poll_limit = h->poll_limit;
+  a.extra = h->extra;
+  a.trips = h->trips;
+  return launch_wcgp(a, h->partial_len, grid_out);
+}
 
 extern "C" int
 qllg_k_wilson_dslash(int ps, int pl, const qllg_stag_args *a)

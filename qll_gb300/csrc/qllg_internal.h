@@ -248,6 +248,29 @@ typedef struct qllg_cg_scalars_s {
   int ru_trips;                 /* graph-loop trips that took the reliable-update block */
 } qllg_cg_scalars;
 
+/* ------------------------------------------- persistent Wilson CGNR */
+/* one cooperative launch runs FP32 iterations of the mixed Wilson CGNR
+ * (k_wilson.cu) until a reliable update is flagged, the solve is done or
+ * `trips` iterations ran; the scalars (sc, one rhs) must hold the solve's
+ * state, p the current direction.  partial: partial_len doubles (at least
+ * two per block); bar: two control words and err one, zeroed before the
+ * first launch */
+typedef struct {
+  qllg_geom g;
+  const void *links;
+  void *x, *r, *p, *Sp, *v;
+  struct qllg_cg_scalars_s *sc;
+  double a;
+  double *partial;
+  size_t partial_len;
+  unsigned *bar;
+  int *err;
+  long long poll_limit;
+  int extra;
+  int trips;
+} qllg_wcgp_args;
+int qllg_k_wilson_cgnr_persistent(const qllg_wcgp_args *a, int *grid_out);
+
 /* ---------------------------------------------------- persistent CG */
 /* one cooperative launch runs the CG loop (k_cgp.cu) on a small lattice:
  * FP64 iterations (mixed 0), or FP32 iterations with FP64 reliable updates

@@ -29,7 +29,7 @@ int qllg_geom_from_layout(qllg_geom *g, const Layout *l);
 Layout *qllg_current_layout(void);
 
 enum { WW_X, WW_R, WW_P, WW_AP, WW_S, WW_V, WW_B, WW_X64, WW_R64, WW_T64, WW_S64, WW_V64,
-       WW_XDF, WW_IO, WW_N };
+       WW_XDF, WW_IO, WW_CTL, WW_N };
 
 #define WGRAPHS 4
 
@@ -338,6 +338,33 @@ typedef struct {
   void *x64, *r64, *bp, *s64, *vv64, *t64, *xdf;
 } witer;
 
+/* the reliable update of the mixed CGNR when one is flagged (every launch
+ * returns at once otherwise): x64 += x, t = S^+ S x64 (intermediate ones in
+ * double-float on request, the final candidates in FP64), r64 = b' - t and
+ * r = r64 rounded, with |r|^2 and beta for the p update that follows */
+static int
+wilson_ru_block(qllg_wilson *W, const witer *c)
+{
+  qllg_cg_scalars *sc = W->sc;
+  const int Vh = W->g.Vh, ps = c->ps;
+  const double a = c->a;
+  if(qllg_k_mcg_accum(ps, c->x64, c->xs, Vh, 12, 1, sc)) return -1;
+  /* the double-float pass reuses s64, vv64 and t64 (same size); t
+   * goes back to FP64 in place */
+  if(c->xdf && (qllg_k_spinor_df(1, c->xdf, c->x64, Vh, 12, 1, sc->ru, 1, &sc->no_ru) ||
+                apply_schur_eq(W, QLLG_DF, c->xdf, c->s64, c->vv64, a, 0, NULL, sc->ru, 1,
+                               &sc->no_ru) ||
+                apply_schur_eq(W, QLLG_DF, c->s64, c->t64, c->vv64, a, 1, NULL, sc->ru, 1,
+                               &sc->no_ru) ||
+                qllg_k_spinor_df(0, c->t64, c->t64, Vh, 12, 1, sc->ru, 1, &sc->no_ru)))
+    return -1;
+  const int eq = c->xdf ? 2 : 0;
+  if(apply_schur_eq(W, QLLG_F64, c->x64, c->s64, c->vv64, a, 0, NULL, sc->ru, eq, &sc->no_ru) ||
+     apply_schur_eq(W, QLLG_F64, c->s64, c->t64, c->vv64, a, 1, NULL, sc->ru, eq, &sc->no_ru))
+    return -1;
+  return qllg_k_mcg_residual(ps, c->r64, c->r, c->bp, c->t64, Vh, 12, 1, 1, sc, &W->rb);
+}
+
 /* the last half Dslash of an FP32 iteration fused with the CG update:
  * Ap = a Sp - W_eo^dagger v / a stays in registers, x += alpha p,
  * r -= alpha Ap and |r|^2, then the iteration's bookkeeping; cond: the
@@ -405,21 +432,7 @@ wilson_iteration(qllg_wilson *W, const witer *c)
       if(qllg_capture_if_begin(h)) return -1;
       n1 = qllg_launch_count();
     }
-    if(qllg_k_mcg_accum(ps, c->x64, c->xs, Vh, 12, 1, sc)) return -1;
-    /* the double-float pass reuses s64, vv64 and t64 (same size); t
-     * goes back to FP64 in place */
-    if(c->xdf && (qllg_k_spinor_df(1, c->xdf, c->x64, Vh, 12, 1, sc->ru, 1, &sc->no_ru) ||
-                  apply_schur_eq(W, QLLG_DF, c->xdf, c->s64, c->vv64, a, 0, NULL, sc->ru, 1,
-                                 &sc->no_ru) ||
-                  apply_schur_eq(W, QLLG_DF, c->s64, c->t64, c->vv64, a, 1, NULL, sc->ru, 1,
-                                 &sc->no_ru) ||
-                  qllg_k_spinor_df(0, c->t64, c->t64, Vh, 12, 1, sc->ru, 1, &sc->no_ru)))
-      return -1;
-    const int eq = c->xdf ? 2 : 0;
-    if(apply_schur_eq(W, QLLG_F64, c->x64, c->s64, c->vv64, a, 0, NULL, sc->ru, eq, &sc->no_ru) ||
-       apply_schur_eq(W, QLLG_F64, c->s64, c->t64, c->vv64, a, 1, NULL, sc->ru, eq, &sc->no_ru))
-      return -1;
-    if(qllg_k_mcg_residual(ps, c->r64, c->r, c->bp, c->t64, Vh, 12, 1, 1, sc, &W->rb)) return -1;
+    if(wilson_ru_block(W, c)) return -1;
     if(cond) {
       W->cap_ifbody = (int)(qllg_launch_count() - n1);
       if(qllg_capture_if_end()) return -1;
@@ -504,6 +517,48 @@ fail:
 
 int qllg_timing_on(void);
 
+/* the FP32 iterations as persistent launches (k_wilson.cu), each running
+ * until a reliable update is flagged; the host takes the update with the
+ * FP64 kernels, forms p and launches again */
+static int
+wilson_persistent_loop(qllg_wilson *W, const witer *c, int maxits)
+{
+  unsigned *ctl = wws(W, WW_CTL, 4*sizeof(unsigned));
+  if(!ctl || wlinks(W, QLLG_F32)) return -1;
+  if(qllg_check_cuda(cudaMemsetAsync(ctl, 0, 4*sizeof(unsigned), qllg_stream()),
+                     "persistent CGNR: control words")) return -1;
+  qllg_wcgp_args a;
+  memset(&a, 0, sizeof(a));
+  a.g = W->g;
+  a.links = W->links[QLLG_F32];
+  a.x = c->xs; a.r = c->r; a.p = c->p; a.Sp = c->Sp; a.v = c->v;
+  a.sc = W->sc;
+  a.a = c->a;
+  a.partial = W->rb.partial;
+  a.partial_len = 2*QLLG_MAXRHS*(size_t)W->rb.maxblocks;
+  a.bar = ctl;
+  a.err = (int *)(ctl + 2);
+  a.poll_limit = (long long)qllg_get_param("wait_polls");
+  a.extra = (int)qllg_get_param("cg_barrier_extra");
+  a.trips = maxits + 2;
+  for(int launch = 0; launch <= maxits + 2; launch++) {
+    int grid = 0, err = 0;
+    if(qllg_k_wilson_cgnr_persistent(&a, &grid) ||
+       qllg_check_cuda(cudaMemcpyAsync(&err, ctl + 2, sizeof(int), cudaMemcpyDeviceToHost,
+                                       qllg_stream()), "persistent CGNR: error flag") ||
+       wpull(W, 1)) return -1;
+    if(err) {
+      qllg_set_error("persistent CGNR: a grid barrier wait ran out (%lld polls)", a.poll_limit);
+      return -1;
+    }
+    if(W->hsc->done || W->hsc->no_ru) break;
+    if(wilson_ru_block(W, c) ||
+       qllg_k_scg_update_p(QLLG_F32, c->p, c->r, W->g.Vh, 12, 1, W->sc)) return -1;
+  }
+  if(wpull(W, 1)) return -1;
+  return W->hsc->iters[0];
+}
+
 static int
 wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq, int maxits,
             int mode)
@@ -539,6 +594,9 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   if(qllg_k_scg_init(ps, ps, xs, r, p, bp, ps == QLLG_F64 ? NULL : x64,
                      ps == QLLG_F64 ? NULL : r64, Vh, 12, 1, sc, &W->rb)) return -1;
   witer c = {ps, a, xs, r, p, Ap, Sp, v, x64, r64, bp, s64, vv64, t64, xdf};
+  if(ps == QLLG_F32 && qllg_get_param("wilson_persistent") != 0 && !qllg_timing_on() &&
+     (double)Vh <= qllg_get_param("persistent_max"))
+    return wilson_persistent_loop(W, &c, maxits);
   if(qllg_get_param("graph") != 0 && !qllg_timing_on()) {
     /* one iteration launched directly first (every kernel of the body is
      * then loaded before the capture), then the rest as one graph launch */

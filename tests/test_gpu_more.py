@@ -483,6 +483,7 @@ def test_wilson_cgnr_graph_matches_host_loop(mode):
     b = qll.gen_source(dims, 24, 24, "even")
     mass = 1/(2*0.12) - 4
     out = []
+    L.qllg_set_param(b"wilson_persistent", 0)     # the graph loop, not the persistent one
     for graph in (1, 0, 1):
         L.qllg_set_param(b"graph", graph)
         x = np.zeros_like(b)
@@ -492,6 +493,7 @@ def test_wilson_cgnr_graph_matches_host_loop(mode):
         assert its > 0, qll.last_error()
         out.append((its, x))
     L.qllg_set_param(b"graph", 1)
+    L.qllg_set_param(b"wilson_persistent", 1)
     assert out[0][0] == out[1][0] == out[2][0]
     assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][1], out[2][1])
     L.qllg_wilson_destroy(ctypes.c_void_p(W))
@@ -518,6 +520,7 @@ def test_wilson_fused_update_matches_separate_kernels():
     b = qll.gen_source(dims, 31, 24, "even")
     mass = 1/(2*0.12) - 4
     runs = {}
+    L.qllg_set_param(b"wilson_persistent", 0)     # the graph loop, not the persistent one
     for fused in (1, 0):
         for ru_if in (1, 0):
             L.qllg_set_param(b"wilson_fused_update", fused)
@@ -531,6 +534,7 @@ def test_wilson_fused_update_matches_separate_kernels():
             runs[(fused, ru_if)] = (its, info.reliable_updates, x)
     L.qllg_set_param(b"wilson_fused_update", 1)
     L.qllg_set_param(b"graph_ru_if", 1)
+    L.qllg_set_param(b"wilson_persistent", 1)
     # the IF node changes nothing: bitwise the same per fused setting
     for fused in (1, 0):
         a, c = runs[(fused, 1)], runs[(fused, 0)]

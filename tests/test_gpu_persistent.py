@@ -131,3 +131,74 @@ def test_bulk_pipeline_wait_runs_out_with_an_error(pipeline):
         assert torch.equal(outs[1][1], outs[2][1])
     finally:
         L.qllg_stag_destroy(S)
+
+
+def _wilson(dims):
+    from inputs import wilson_links
+    L = qll.load()
+    L.qllg_set_param.argtypes = [ctypes.c_char_p, c_double]
+    L.qllg_wilson_create.restype = ctypes.c_void_p
+    L.qllg_wilson_create.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]
+    L.qllg_wilson_solve.restype = ctypes.c_int
+    L.qllg_wilson_solve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double,
+                                    c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(qll.SolveInfo)]
+    L.qllg_wilson_destroy.argtypes = [ctypes.c_void_p]
+    W = L.qllg_wilson_create(qll.dims_c(dims), qll.vp_array(list(wilson_links(dims))))
+    assert W, qll.last_error()
+    return L, ctypes.c_void_p(W)
+
+
+def _wsolve(L, W, b, persistent):
+    L.qllg_set_param(b"wilson_persistent", persistent)
+    x = np.zeros_like(b)
+    info = qll.SolveInfo()
+    try:
+        its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, 1/(2*0.12) - 4, 1e-17, 5000,
+                                  qll.SOLVE_MIXED_SINGLE, byref(info))
+    finally:
+        L.qllg_set_param(b"wilson_persistent", 1)
+    return its, x, info
+
+
+@pytest.mark.parametrize("dims", [(8, 8, 8, 8), (8, 8, 8, 16)])
+def test_wilson_persistent_matches_graph_loop(dims):
+    """the persistent FP32 iterations of the mixed Wilson CGNR (cooperative
+    launches between the reliable updates) against the graph loop: their
+    sums are reduced in another order, so reliable updates and iterations
+    agree within one, solutions within 1e-6
+    of each other and the true residual of S x = b below 1e-8 in both"""
+    L, W = _wilson(dims)
+    try:
+        b = qll.gen_source(dims, 77, 24, "even")
+        itp, xp, ip = _wsolve(L, W, b, 1)
+        itg, xg, ig = _wsolve(L, W, b, 0)
+        assert itp > 0 and itg > 0, qll.last_error()
+        assert abs(itp - itg) <= 1, (itp, itg)
+        assert ip.reliable_updates >= 1 and abs(ip.reliable_updates - ig.reliable_updates) <= 1
+        assert ip.true_rsq[0] < 1e-16 and ig.true_rsq[0] < 1e-16
+        assert relerr(xp, xg) < 1e-6
+    finally:
+        L.qllg_wilson_destroy(W)
+
+
+def test_wilson_persistent_barrier_wait_runs_out_with_an_error():
+    """a barrier of the persistent CGNR that can never be passed ends the
+    solve with an error after the poll limit; the next solve works"""
+    dims = (8, 8, 8, 8)
+    L, W = _wilson(dims)
+    try:
+        b = qll.gen_source(dims, 78, 24, "even")
+        L.qllg_set_param(b"cg_barrier_extra", 1)
+        L.qllg_set_param(b"wait_polls", 2000)
+        try:
+            its, _, _ = _wsolve(L, W, b, 1)
+        finally:
+            L.qllg_set_param(b"cg_barrier_extra", 0)
+            L.qllg_set_param(b"wait_polls", 2e7)
+        assert its < 0
+        assert "barrier wait ran out" in qll.last_error()
+        L.qllg_clear_error()
+        its, _, info = _wsolve(L, W, b, 1)
+        assert its > 0 and info.true_rsq[0] < 1e-16
+    finally:
+        L.qllg_wilson_destroy(W)
