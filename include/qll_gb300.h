@@ -332,8 +332,9 @@ void qllg_server_destroy(qllg_server *V);
  *    FP64 CG);
  *  "multishift_guess_rsq" (1e-10: the mixed multishift's first stage
  *    stops at |r|^2 < this |b|^2), "wilson_c3" (0; 1: three threads per site
- *    in small one-rhs FP32 Wilson launches), "wilson_ru_df" (0; 1: the
- *    Wilson mixed CGNR's intermediate reliable updates in double-float),
+ *    in small one-rhs FP32 Wilson launches), "wilson_ru_df" (2: the
+ *    Wilson mixed CGNR's intermediate reliable updates in double-float
+ *    with the persistent iterations; 1: always; 0: never),
  *    "wilson_df_c3" (1: three threads per site in the small double-float
  *    Wilson launches), "wilson_f64_c3" (0: the same for the FP64 ones),
  *    "wilson_f64_dir2" (1: two threads per site, split by direction, in the

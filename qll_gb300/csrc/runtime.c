@@ -450,12 +450,13 @@ static struct { const char *name; double value; } g_params[] = {
                                 per site, one per output colour (C2 at 16^3x32:
                                 17.8 ms per mixed solve against 14.7 ms with one
                                 thread per site, so off) */
-  {"wilson_ru_df", 0},       /* intermediate reliable updates of the Wilson mixed
-                                CGNR in double-float.  Off: the double-float
-                                Wilson kernel is about as slow as the FP64 one,
-                                and its extra launches cost more (updates at each
-                                10x fall of |r|: C2 15.1 against 14.8 ms per
-                                solve, 32^3x64 139 against 128 ms) */
+  {"wilson_ru_df", 2},       /* intermediate reliable updates of the Wilson mixed
+                                CGNR in double-float: 1 always, 2 with the
+                                persistent iterations only (C2: 4.78 against 5.28
+                                ms per solve), 0 never.  In the graph loop their
+                                extra launches cost more than they save (updates
+                                at each 10x fall of |r|: C2 15.1 against 14.8 ms,
+                                32^3x64 139 against 128 ms) */
   {"wilson_df_c3", 1},       /* three threads per site in the small double-float
                                 Wilson launches, whose one-thread kernel holds one
                                 block of 256 threads per SM */

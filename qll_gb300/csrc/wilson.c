@@ -577,11 +577,16 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   void *r = wws(W, WW_R, vs), *p = wws(W, WW_P, vs), *Ap = wws(W, WW_AP, vs);
   void *Sp = wws(W, WW_S, vs), *v = wws(W, WW_V, vs);
   if(!xs || !r || !p || !Ap || !Sp || !v) return -1;
-  /* on request, intermediate reliable updates (ru 1) in double-float:
-   * S^+ S x in the FP32 pipes at about 44-bit precision; the final one
-   * (ru 2), whose residual may end the solve, in FP64 */
+  /* the FP32 iterations as persistent launches on small lattices */
+  const int persist = ps == QLLG_F32 && qllg_get_param("wilson_persistent") != 0 && !qllg_timing_on() &&
+                      (double)Vh <= qllg_get_param("persistent_max");
+  /* intermediate reliable updates (ru 1) in double-float (wilson_ru_df 1,
+   * or 2 with the persistent iterations): S^+ S x in the FP32 pipes at
+   * about 44-bit precision; the final one (ru 2), whose residual may end
+   * the solve, in FP64 */
   void *xdf = NULL;
-  if(ps != QLLG_F64 && qllg_get_param("wilson_ru_df") != 0 &&
+  const double rdf = qllg_get_param("wilson_ru_df");
+  if(ps != QLLG_F64 && (rdf == 1 || (rdf == 2 && persist)) &&
      (wlinks(W, QLLG_DF) || !(xdf = wws(W, WW_XDF, wvec(W, QLLG_DF))))) return -1;
   memset(W->hsc, 0, sizeof(qllg_cg_scalars));
   W->hsc->rsq_stop[0] = rsq;
@@ -594,9 +599,7 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   if(qllg_k_scg_init(ps, ps, xs, r, p, bp, ps == QLLG_F64 ? NULL : x64,
                      ps == QLLG_F64 ? NULL : r64, Vh, 12, 1, sc, &W->rb)) return -1;
   witer c = {ps, a, xs, r, p, Ap, Sp, v, x64, r64, bp, s64, vv64, t64, xdf};
-  if(ps == QLLG_F32 && qllg_get_param("wilson_persistent") != 0 && !qllg_timing_on() &&
-     (double)Vh <= qllg_get_param("persistent_max"))
-    return wilson_persistent_loop(W, &c, maxits);
+  if(persist) return wilson_persistent_loop(W, &c, maxits);
   if(qllg_get_param("graph") != 0 && !qllg_timing_on()) {
     /* one iteration launched directly first (every kernel of the body is
      * then loaded before the capture), then the rest as one graph launch */

@@ -362,7 +362,7 @@ def test_wilson_double_float_reliable_updates():
         assert its > 0, qll.last_error()
         assert info.reliable_updates > 1
         res[ru_df, c3] = (x, its, info.true_rsq[0])
-    L.qllg_set_param(b"wilson_ru_df", 0)
+    L.qllg_set_param(b"wilson_ru_df", 2)
     L.qllg_set_param(b"wilson_df_c3", 1)
     its_o, xo, _ = orc.wilson_cgnr(DIMS, u, mass, b, 1e-20, 5000)
     for key, (x, its, tr) in res.items():
