@@ -202,3 +202,28 @@ def test_wilson_persistent_barrier_wait_runs_out_with_an_error():
         assert its > 0 and info.true_rsq[0] < 1e-16
     finally:
         L.qllg_wilson_destroy(W)
+
+
+def test_wilson_persistent_stops_at_maxits():
+    """a solve capped below convergence stops at the cap in the persistent
+    loop as in the graph loop, with its FP64 residual reported"""
+    dims = (8, 8, 8, 8)
+    L, W = _wilson(dims)
+    try:
+        b = qll.gen_source(dims, 79, 24, "even")
+        out = {}
+        for persistent in (1, 0):
+            L.qllg_set_param(b"wilson_persistent", persistent)
+            x = np.zeros_like(b)
+            info = qll.SolveInfo()
+            try:
+                its = L.qllg_wilson_solve(W, x.ctypes.data, b.ctypes.data, 1/(2*0.12) - 4, 1e-17, 7,
+                                          qll.SOLVE_MIXED_SINGLE, byref(info))
+            finally:
+                L.qllg_set_param(b"wilson_persistent", 1)
+            assert its == 7, (persistent, its, qll.last_error())
+            assert info.true_rsq[0] > 1e-16
+            out[persistent] = x
+        assert relerr(out[1], out[0]) < 1e-5
+    finally:
+        L.qllg_wilson_destroy(W)
