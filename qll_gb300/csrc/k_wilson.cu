@@ -40,14 +40,11 @@ __device__ __forceinline__ Cx<T> phase(const Cx<T> &z, int code) {
 
 // acc -= the eight hops of site `site` (coordinates x) of the output
 // parity: per slot the neighbour spinor projected to two spin components,
-// multiplied by the link and reconstructed (dag: gamma5 D gamma5).  ADD:
-// the input is formed at each neighbour as add + beta*in (a CG direction
-// update that needs no pass of its own)
-template <int PS, int PL, int NR, typename T, bool ADD = false>
+// multiplied by the link and reconstructed (dag: gamma5 D gamma5)
+template <int PS, int PL, int NR, typename T>
 __device__ __forceinline__ void wilson_hops(const void *links, const float *lscale, const void *in, int dag,
                                             const Geo &G, size_t V, size_t loff, int site, const int x[4],
-                                            int rhs, size_t total, Cx<T> acc[12],
-                                            const void *add = nullptr, T beta = T(0))
+                                            int rhs, size_t total, Cx<T> acc[12])
 {
 #pragma unroll
   for(int mu=0; mu<4; mu++) {
@@ -59,12 +56,6 @@ __device__ __forceinline__ void wilson_hops(const void *links, const float *lsca
       Cx<T> U[9], f[12];
       LinkIO<PL>::load(links, 2*mu + back, V, loff + site, lscale, U);
       SpinorIO<PS,12>::load(in, total, (size_t)k*NR + rhs, f);
-      if constexpr (ADD) {
-        Cx<T> g[12];
-        SpinorIO<PS,12>::load(add, total, (size_t)k*NR + rhs, g);
-#pragma unroll
-        for(int c=0; c<12; c++) { f[c].r = fma(beta, f[c].r, g[c].r); f[c].i = fma(beta, f[c].i, g[c].i); }
-      }
 #pragma unroll
       for(int hk=0; hk<2; hk++) {
         const int col = gcol(mu, hk);
@@ -219,11 +210,8 @@ wilson_dslash_upd(qllg_stag_args a)
 // kernel nodes cost as much again.  Per iteration:
 //   v = W_oe p; Sp = a p - W_eo v / a with |Sp|^2; v = W_oe^+ Sp;
 //   Ap = a Sp - W_eo^+ v / a, x += alpha p, r -= alpha Ap with |r|^2
-//   (alpha = |r|^2/|Sp|^2); the bookkeeping of cg_finish_std
-// with a grid barrier after each step.  The update p = r + beta p is
-// formed at each neighbour by the next iteration's first half Dslash and
-// at each site (and stored) by its second, so it takes no pass or barrier
-// of its own.  Each reduction writes one partial
+//   (alpha = |r|^2/|Sp|^2); the bookkeeping of cg_finish_std; p = r + beta p
+// with a grid barrier after each step.  Each reduction writes one partial
 // per block, a barrier follows, and every block folds the partials in
 // block order itself, so all blocks hold bitwise the same scalars.  The
 // barrier is a counter and a generation word whose waits give up after
@@ -301,11 +289,8 @@ __device__ bool wcg_sum(const WcgpArgs &a, double val, double &out, int &phase)
   return true;
 }
 
-// v = W_oe^(dag) in on the odd sites (mode 0 of the half Dslash); ADD: the
-// input is add + beta*in, formed at each neighbour
-template <bool ADD>
-__device__ __forceinline__ void wcg_hop_odd(const WcgpArgs &a, const Geo &G, const void *in, int dag,
-                                            const void *add = nullptr, float beta = 0.f)
+// out = W_oe^(dag) in on the odd sites (mode 0 of the half Dslash)
+__device__ __forceinline__ void wcg_hop_odd(const WcgpArgs &a, const Geo &G, const void *in, int dag)
 {
   const size_t V = (size_t)a.g.V, total = (size_t)G.Vh;
   for(size_t t = (size_t)blockIdx.x*kThreads + threadIdx.x; t < total; t += (size_t)gridDim.x*kThreads) {
@@ -314,8 +299,8 @@ __device__ __forceinline__ void wcg_hop_odd(const WcgpArgs &a, const Geo &G, con
     Cx<float> acc[12];
 #pragma unroll
     for(int c=0; c<12; c++) { acc[c].r = 0; acc[c].i = 0; }
-    wilson_hops<QLLG_F32,QLLG_F32,1,float,ADD>(a.links, NULL, in, dag, G, V, (size_t)G.Vh, (int)t, x, 0,
-                                               total, acc, add, beta);
+    wilson_hops<QLLG_F32,QLLG_F32,1,float>(a.links, NULL, in, dag, G, V, (size_t)G.Vh, (int)t, x, 0, total,
+                                           acc);
     SpinorIO<QLLG_F32,12>::store(a.v, total, t, acc);
   }
 }
@@ -337,16 +322,10 @@ wilson_cgnr_persistent(WcgpArgs a)
   }
   __syncthreads();
   int phase = 0, trip = 0;
-  // the p update p = r + beta p of the previous iteration is pending from
-  // the second trip on: formed at each neighbour in the first half Dslash
-  // and at each site (and stored) in the second
-  bool pend = false;
   while(s_act && !s_stop_loop && trip < a.trips) {
     trip++;
-    const float beta = (float)s_beta;
     // v = W_oe p
-    if(pend) wcg_hop_odd<true>(a, G, a.p, 0, a.r, beta);
-    else wcg_hop_odd<false>(a, G, a.p, 0);
+    wcg_hop_odd(a, G, a.p, 0);
     if(!wcg_barrier(a)) return;
     // Sp = a p - W_eo v / a, |Sp|^2
     Acc<float> an;
@@ -358,23 +337,15 @@ wilson_cgnr_persistent(WcgpArgs a)
       for(int c=0; c<12; c++) { acc[c].r = 0; acc[c].i = 0; }
       wilson_hops<QLLG_F32,QLLG_F32,1,float>(a.links, NULL, a.v, 0, G, V, 0, (int)t, x, 0, total, acc);
       SpinorIO<QLLG_F32,12>::load(a.p, total, t, pv);
-      if(pend) {
-        Cx<float> rv[12];
-        SpinorIO<QLLG_F32,12>::load(a.r, total, t, rv);
-#pragma unroll
-        for(int c=0; c<12; c++) { pv[c].r = fmaf(beta, pv[c].r, rv[c].r); pv[c].i = fmaf(beta, pv[c].i, rv[c].i); }
-        SpinorIO<QLLG_F32,12>::store(a.p, total, t, pv);
-      }
 #pragma unroll
       for(int c=0; c<12; c++) { o[c].r = kfma(cb, acc[c].r, ca*pv[c].r); o[c].i = kfma(cb, acc[c].i, ca*pv[c].i); }
       SpinorIO<QLLG_F32,12>::store(a.Sp, total, t, o);
       an.norm(o);
     }
-    pend = false;
     double pn;
     if(!wcg_sum(a, an.get(), pn, phase)) return;
     // v = W_oe^+ Sp
-    wcg_hop_odd<false>(a, G, a.Sp, 1);
+    wcg_hop_odd(a, G, a.Sp, 1);
     if(!wcg_barrier(a)) return;
     // Ap = a Sp - W_eo^+ v / a; x += alpha p, r -= alpha Ap, |r|^2
     Acc<float> ar;
@@ -416,20 +387,20 @@ wilson_cgnr_persistent(WcgpArgs a)
       s_stop_loop = s_ru != 0;       // the host takes the update, then p
     }
     __syncthreads();
-    if(s_stop_loop) break;           // the host takes the update, then forms p
-    pend = true;
-  }
-  // a launch that ends on its trip cap leaves p formed, as the host expects
-  if(pend) {
-    const float beta = (float)s_beta;
-    for(size_t t = (size_t)blockIdx.x*kThreads + threadIdx.x; t < total; t += (size_t)gridDim.x*kThreads) {
-      Cx<float> pv[12], rv[12];
-      SpinorIO<QLLG_F32,12>::load(a.p, total, t, pv);
-      SpinorIO<QLLG_F32,12>::load(a.r, total, t, rv);
+    if(s_stop_loop) break;
+    // p = r + beta p
+    {
+      const float beta = (float)s_beta;
+      for(size_t t = (size_t)blockIdx.x*kThreads + threadIdx.x; t < total; t += (size_t)gridDim.x*kThreads) {
+        Cx<float> pv[12], rv[12];
+        SpinorIO<QLLG_F32,12>::load(a.p, total, t, pv);
+        SpinorIO<QLLG_F32,12>::load(a.r, total, t, rv);
 #pragma unroll
-      for(int c=0; c<12; c++) { pv[c].r = fmaf(beta, pv[c].r, rv[c].r); pv[c].i = fmaf(beta, pv[c].i, rv[c].i); }
-      SpinorIO<QLLG_F32,12>::store(a.p, total, t, pv);
+        for(int c=0; c<12; c++) { pv[c].r = fmaf(beta, pv[c].r, rv[c].r); pv[c].i = fmaf(beta, pv[c].i, rv[c].i); }
+        SpinorIO<QLLG_F32,12>::store(a.p, total, t, pv);
+      }
     }
+    if(!wcg_barrier(a)) return;
   }
   if(blockIdx.x == 0 && threadIdx.x == 0) {
     qllg_cg_scalars *sc = a.sc;
