@@ -529,6 +529,17 @@ def run_wilson(args):
             raise RuntimeError(qll.last_error())
         return dt, its, info, cnt.value, tot.value
 
+    L.qllg_get_param.restype = ctypes.c_double
+    L.qllg_get_param.argtypes = [ctypes.c_char_p]
+
+    def loop_kind(mode):
+        # the library's choice: persistent FP32 iterations on small lattices
+        vh = b.shape[0]//2
+        if (mode == qll.SOLVE_MIXED_SINGLE and L.qllg_get_param(b"wilson_persistent") != 0 and
+                vh <= L.qllg_get_param(b"persistent_max")):
+            return "persistent cooperative launches of the FP32 iterations between the reliable updates"
+        return "one CUDA-graph launch"
+
     for name, mode in (("mixed", qll.SOLVE_MIXED_SINGLE), ("fp64", qll.SOLVE_DOUBLE)):
         best = None
         for rep in range(3):
@@ -536,7 +547,7 @@ def run_wilson(args):
             if best is None or dt < best["seconds"]:
                 best = {"seconds": dt, "solves_per_s": 1/dt, "iters": its,
                         "device_seconds": info.seconds, "reliable_updates": info.reliable_updates,
-                        "true_rsq": info.true_rsq[0], "loop": "one CUDA-graph launch"}
+                        "true_rsq": info.true_rsq[0], "loop": loop_kind(mode)}
         # the half-Dslash launches of one more solve, event-timed (a host-
         # polled loop: events cannot sit in a graph's conditional body)
         _, _, _, cnt, tot = solve(mode, True)
