@@ -312,9 +312,9 @@ void qllg_server_destroy(qllg_server *V);
  *    0-23 forces a candidate where it applies, qllg_autotune_report names
  *    them);
  *  "wilson_persistent" (1: the FP32 Wilson CGNR on a lattice of at most
- *    persistent_max even sites runs its iterations as persistent
- *    cooperative launches, each until a reliable update is flagged, which
- *    the host then takes with the FP64 kernels),
+ *    "wilson_persistent_max" (4194304) even sites runs its iterations as
+ *    persistent cooperative launches, each until a reliable update is
+ *    flagged, which the host then takes with the FP64 kernels),
  *  "wilson_fused_update" (1: the FP32 iterations of the Wilson CGNR run
  *    the CG update in the epilogue of their last half Dslash; 0: a separate
  *    update kernel),

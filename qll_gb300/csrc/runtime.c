@@ -425,9 +425,13 @@ static struct { const char *name; double value; } g_params[] = {
   {"dslash_bulk", 1},        /* allow the bulk-copy pipeline Dslash variant */
   {"dslash_pipe", 1},        /* allow the per-warp cp.async pipeline Dslash variants */
   {"dslash_tma", 1},         /* allow the per-warp tensor-copy (TMA) pipeline Dslash variants */
-  {"wilson_persistent", 1},  /* FP32 Wilson CGNR with even sites up to persistent_max:
-                                the iterations as persistent cooperative launches,
-                                each until a reliable update is flagged */
+  {"wilson_persistent", 1},  /* FP32 Wilson CGNR with even sites up to
+                                wilson_persistent_max: the iterations as persistent
+                                cooperative launches, each until a reliable update
+                                is flagged */
+  {"wilson_persistent_max", 4194304}, /* ... (with double-float updates, against the
+                                graph loop with FP64 ones: 16^3x32 4.8 against 7.6 ms,
+                                24^3x48 24.1 against 27.7 ms, 32^3x64 71 against 76 ms) */
   {"wilson_fused_update", 1}, /* FP32 Wilson CGNR: the CG update (x, r, |r|^2 and the
                                 iteration's bookkeeping) in the epilogue of the last
                                 half Dslash of the iteration */

@@ -579,7 +579,7 @@ wilson_cgnr(qllg_wilson *W, void *x64, const void *b64, double mass, double rsq,
   if(!xs || !r || !p || !Ap || !Sp || !v) return -1;
   /* the FP32 iterations as persistent launches on small lattices */
   const int persist = ps == QLLG_F32 && qllg_get_param("wilson_persistent") != 0 && !qllg_timing_on() &&
-                      (double)Vh <= qllg_get_param("persistent_max");
+                      (double)Vh <= qllg_get_param("wilson_persistent_max");
   /* intermediate reliable updates (ru 1) in double-float (wilson_ru_df 1,
    * or 2 with the persistent iterations): S^+ S x in the FP32 pipes at
    * about 44-bit precision; the final one (ru 2), whose residual may end
