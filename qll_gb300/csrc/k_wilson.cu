@@ -204,10 +204,12 @@ wilson_dslash_upd(qllg_stag_args a)
 // One cooperative launch runs the FP32 iterations of the mixed Wilson CGNR
 // (the standard-form CG on S^dagger S of wilson.c, one rhs) until a
 // reliable update is flagged, the solve is done or the trip cap is reached;
-// the host then takes the update with the FP64 kernels and launches again.
-// On a small lattice (C2, 16^3x32: 65,536 even sites) the graph loop's
-// half Dslashes are about 10 us of work each and the gaps between its
-// kernel nodes cost as much again.  Per iteration:
+// the host then takes the update with the double-float and FP64 kernels and
+// launches again.  On a small lattice (C2, 16^3x32: 65,536 even sites) the
+// graph loop's half Dslashes are about 10 us of work each and the gaps
+// between its kernel nodes cost as much again; at 32^3x64 the launch is
+// still a few percent ahead.  The grid is the co-resident blocks at most,
+// each walking its sites with a grid stride.  Per iteration:
 //   v = W_oe p; Sp = a p - W_eo v / a with |Sp|^2; v = W_oe^+ Sp;
 //   Ap = a Sp - W_eo^+ v / a, x += alpha p, r -= alpha Ap with |r|^2
 //   (alpha = |r|^2/|Sp|^2); the bookkeeping of cg_finish_std; p = r + beta p
