@@ -17,6 +17,7 @@
 #include <cuda_runtime_api.h>
 #include "qll_gb300.h"
 #include "qllg_internal.h"
+#include "vla.h"
 
 void qllg_stag_set_single_store(qllg_stag *S);
 
@@ -350,3 +351,33 @@ gaugeDoublestore##S_(Field##S_ *ua[], Field##S_ *u[], int dirs[], int lens[], in
 
 DEFINE_GAUGE_DROPIN(D, double, QLLG_F64)
 DEFINE_GAUGE_DROPIN(F, float, QLLG_F32)
+
+/* ------------------------------------------------- makeU (drop-in) */
+/* makeU (include/vla.h:85, lib/vla.c:1635-1665): re-unitarise sites [i0, i1)
+ * of host matrices, 2 nc^2 reals a site in QLL's one-lane order, by
+ * Gram-Schmidt of the nc vectors (make_u_k on the GPU).  void, as the
+ * reference's: a failure leaves the matrices untouched and records the
+ * message (qllg_last_error). */
+static void
+make_u_host(int prec, void *mm, int nc, int i0, int i1)
+{
+  if(i1 <= i0) return;
+  if(nc < 1 || nc > 3) { qllg_set_error("makeU: nc %d (1 to 3)", nc); return; }
+  if(qllg_runtime_init()) return;
+  const size_t per = (prec == QLLG_F64 ? 8 : 4)*2*(size_t)nc*nc;
+  const size_t bytes = per*(size_t)(i1 - i0);
+  char *h = (char *)mm + per*(size_t)i0;
+  void *d = qllg_stage(bytes);
+  if(!d || qllg_h2d(d, h, bytes) || qllg_k_make_u(prec, d, nc, 0, (size_t)(i1 - i0))) {
+    qllg_sync();
+    return;
+  }
+  /* into a host copy first, so that a failed copy leaves mm as it was */
+  char *tmp = malloc(bytes);
+  if(!tmp) { qllg_set_error("makeU: host buffer of %zu bytes", bytes); qllg_sync(); return; }
+  if(qllg_d2h(tmp, d, bytes) == 0) memcpy(h, tmp, bytes);
+  free(tmp);
+}
+
+void makeUD(double *mm, int nc, int i0, int i1) { make_u_host(QLLG_F64, mm, nc, i0, i1); }
+void makeUF(float *mm, int nc, int i0, int i1) { make_u_host(QLLG_F32, mm, nc, i0, i1); }

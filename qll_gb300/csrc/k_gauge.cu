@@ -329,3 +329,66 @@ qllg_k_aos_sum(int prec, const void *x, int nelem, int s0, int s1, int sq, doubl
   else aos_sum_k<float><<<gr, kT, 0, qllg_stream()>>>((const float *)x, a, b, sq, out, rb->partial, rb->counter);
   return done("aos_sum");
 }
+
+// ------------------------------------------------------ re-unitarisation
+// makeU (lib/vla.c:1635-1665, makeUsite) on host-layout sites [s0, s1) of
+// nc x nc complex matrices, 2 nc^2 reals a site: vector i (2 nc reals from
+// 2 nc i) is normalised, then for each earlier vector j its projection
+// <v_j, v_i> v_j is removed and v_i normalised again -- the reference's
+// order, including the normalisation after every projection.  nc <= 3.
+namespace {
+template <typename T>
+__global__ void make_u_k(T *m, int nc, size_t s0, size_t s1)
+{
+  for(size_t s = s0 + (size_t)blockIdx.x*blockDim.x + threadIdx.x; s < s1; s += (size_t)gridDim.x*blockDim.x) {
+    T *ms = m + (size_t)2*nc*nc*s;
+    T v[18];
+    for(int k=0; k<2*nc*nc; k++) v[k] = ms[k];
+    for(int i=0; i<nc; i++) {
+      T *vi = v + 2*nc*i;
+      T n = vi[0]*vi[0];
+      for(int k=1; k<2*nc; k++) n = fma(vi[k], vi[k], n);
+      T ni = (T)1/sqrt(n);
+      for(int k=0; k<2*nc; k++) vi[k] = ni*vi[k];
+      for(int j=0; j<i; j++) {
+        const T *vj = v + 2*nc*j;
+        // d = <v_j, v_i> (conjugate on v_j)
+        T dr = vj[0]*vi[0], di = vj[0]*vi[1];
+        dr = fma(vj[1], vi[1], dr);
+        di = fma(-vj[1], vi[0], di);
+        for(int k=2; k<2*nc; k+=2) {
+          dr = fma(vj[k], vi[k], dr);
+          di = fma(vj[k], vi[k+1], di);
+          dr = fma(vj[k+1], vi[k+1], dr);
+          di = fma(-vj[k+1], vi[k], di);
+        }
+        // v_i -= d v_j
+        for(int k=0; k<2*nc; k+=2) {
+          T x0 = vi[k], x1 = vi[k+1];
+          x0 = fma(-dr, vj[k], x0);
+          x1 = fma(-dr, vj[k+1], x1);
+          x0 = fma(di, vj[k+1], x0);
+          x1 = fma(-di, vj[k], x1);
+          vi[k] = x0; vi[k+1] = x1;
+        }
+        n = vi[0]*vi[0];
+        for(int k=1; k<2*nc; k++) n = fma(vi[k], vi[k], n);
+        ni = (T)1/sqrt(n);
+        for(int k=0; k<2*nc; k++) vi[k] = ni*vi[k];
+      }
+    }
+    for(int k=0; k<2*nc*nc; k++) ms[k] = v[k];
+  }
+}
+} // namespace
+
+extern "C" int
+qllg_k_make_u(int prec, void *m, int nc, size_t s0, size_t s1)
+{
+  if(nc < 1 || nc > 3) { qllg_set_error("makeU: nc %d (1 to 3)", nc); return -1; }
+  if(s1 <= s0) return 0;
+  int gr = grid_for(s1 - s0);
+  if(prec == QLLG_F64) make_u_k<double><<<gr, kT, 0, qllg_stream()>>>((double *)m, nc, s0, s1);
+  else make_u_k<float><<<gr, kT, 0, qllg_stream()>>>((float *)m, nc, s0, s1);
+  return done("make_u");
+}

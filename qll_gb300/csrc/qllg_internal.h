@@ -248,6 +248,10 @@ typedef struct qllg_cg_scalars_s {
   int ru_trips;                 /* graph-loop trips that took the reliable-update block */
 } qllg_cg_scalars;
 
+/* makeU's Gram-Schmidt (lib/vla.c:1635-1665) on device sites [s0, s1) of
+ * nc x nc complex matrices, 2 nc^2 reals a site (nc <= 3) */
+int qllg_k_make_u(int prec, void *m, int nc, size_t s0, size_t s1);
+
 /* ------------------------------------------- persistent Wilson CGNR */
 /* one cooperative launch runs FP32 iterations of the mixed Wilson CGNR
  * (k_wilson.cu) until a reliable update is flagged, the solve is done or

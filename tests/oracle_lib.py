@@ -209,3 +209,10 @@ def gamma(d):
     lib().or_gamma(d, g)
     a = np.array(g[:]).reshape(4, 4, 2)
     return a[..., 0] + 1j*a[..., 1]
+
+
+def make_u(m):
+    """or_makeU (lib/vla.c:1635-1665) in place on [nsites][18] reals"""
+    s = "D" if m.dtype == np.float64 else "F"
+    getattr(lib(), "or_makeU" + s)(P(m), int(m.size//18))
+    return m
