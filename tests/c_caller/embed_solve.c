@@ -16,6 +16,12 @@
 #include <string.h>
 #include "qll.h"
 #include "qll_gb300.h"
+#include "vla.h"
+
+/* the test programs' re-unitarisation entry points link too (QLL's
+ * stress.c and fieldtest.c call makeU on their link fields) */
+void (*const reunitarise_d)(double *, int, int, int) = makeUD;
+void (*const reunitarise_f)(float *, int, int, int) = makeUF;
 
 /* x = -y^dagger for every 3x3 matrix of a [V][18] field (column-major
  * complex entries, entry 3*column + row) */

@@ -1,6 +1,7 @@
 """A C program written against the drop-in headers (tests/c_caller/
 embed_solve.c: layout setup, smearFat7, shift, createStaggeredSolver,
-solve2, dslash2, the embedqop.c pattern) compiles and links against
+solve2, dslash2, the embedqop.c pattern, and makeU's entry points)
+compiles and links against
 -lqll_gb300 on the CPU; on a GPU it runs and reaches the tolerance."""
 import os
 import subprocess
