@@ -137,3 +137,14 @@ SFX(refh_doublestore)(REAL *ua[], REAL *u[], int dirs[], int lens[], int n)
   }
   SFX(gaugeDoublestore)(ap, up, dirs, lens, n);
 }
+
+/* makeU of lib/vla.c:1656-1665 (declared in the reference's internal
+ * include/vla.h:85) on sites [0, n) of nc x nc matrices, 2 nc^2 reals a
+ * site.  Site-local, so the one-lane build takes the array as it is. */
+void SFX(makeU)(REAL *mm, int nc, int i0, int i1);
+
+void
+SFX(refh_makeU)(REAL *m, int nc, int n)
+{
+  SFX(makeU)(m, nc, 0, n);
+}

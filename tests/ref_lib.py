@@ -122,3 +122,9 @@ def doublestore(dims, u, mu, length):
     getattr(lib(), "refh_doublestore" + _sfx(u))(_PA([out]), _PA([u]), (c_int*1)(mu),
                                                  (c_int*1)(length), 1)
     return out
+
+
+def make_u(m, nc=3):
+    """the reference's makeU on every site of m ([nsites][2 nc^2] reals), in place"""
+    getattr(lib(), "refh_makeU" + _sfx(m))(_P(m), nc, int(m.size//(2*nc*nc)))
+    return m

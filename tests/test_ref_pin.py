@@ -123,3 +123,14 @@ def test_shift_doublestore_and_backward_links():
             want = ref.doublestore(dims, th[mu], mu, -ln)
             assert np.array_equal(orc.doublestore(dims, th[mu], mu, -ln), want)
             assert np.array_equal(orc.negadj_back(dims, th[mu], mu, ln), -want)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_make_u_bitwise(dtype):
+    """makeU (lib/vla.c:1635-1665) is site-local: the oracle's restatement
+    equals the reference's result bit for bit on seeded random matrices"""
+    rng = np.random.default_rng(1656)
+    m = rng.standard_normal((2048, 18)).astype(dtype)
+    want = ref.make_u(m.copy())
+    got = orc.make_u(m.copy())
+    assert np.array_equal(got, want), relerr(got, want)
